@@ -1,0 +1,182 @@
+/*
+ * latttmat.h -- C ABI of the GB300 transfer-matrix library (liblatttmat_gb300.so).
+ *
+ * A tm_op is one transfer-matrix operator, the GPU counterpart of one of the
+ * reference's MatVecProd classes.  Its tables live in HBM.  Each entry point
+ * names the reference interface it replaces (file:line in LattTMat).
+ *
+ * Conventions
+ *  - Every call returns a tm_status (0 = TM_OK).  No C++ exception crosses
+ *    this boundary.  tm_last_error() returns a message for the calling thread's
+ *    last failure.
+ *  - Buffers are owned by the caller.  Each argument says whether it is a host
+ *    or a device pointer.  Host vectors are FP64, as in the reference's
+ *    perform_op(const double*, double*).
+ *  - Vector order is the reference's: full operators index states 0..2^L-1.
+ *    Reduced operators index orbit representatives in ascending state order,
+ *    the reference's idxlist order.
+ *  - Operators are thread-compatible, not thread-safe: one call at a time per
+ *    tm_op.  The reference op is not reentrant either; its matvec counter is
+ *    a non-atomic static (TMat/utility.hpp:191-199).
+ */
+#ifndef LATTTMAT_GB300_H
+#define LATTTMAT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tm_op tm_op;
+typedef int tm_status;
+
+enum {
+  TM_OK = 0,
+  TM_ERR_ARG = 1,         /* invalid argument (reference: assert / int error codes) */
+  TM_ERR_UNSUPPORTED = 2, /* model/dim/axialdir not provided (reference: assert(false), TMat/pfunc.cpp:59) */
+  TM_ERR_CUDA = 3,        /* CUDA runtime failure */
+  TM_ERR_NOMEM = 4,       /* device allocation failed */
+  TM_ERR_NOCONV = 5,      /* eigensolver did not converge (reference: TMat/pfunc.hpp:110-114) */
+  TM_ERR_NONFINITE = 6,   /* NaN/Inf detected in an input or iterate */
+  TM_ERR_NOTRANSPOSE = 7, /* operator has no transpose form */
+  TM_ERR_LIMIT = 8        /* size outside an entry point's stated maximum */
+};
+
+typedef enum { TM_F64 = 0, TM_F32 = 1 } tm_dtype;
+
+/* Model parameters; mirrors MParameter (TMat/commondef.hpp:18-24).  For dim=3
+ * `size` is packed as (size1 << 16) | size2, as TMat/read_input.cpp:41 does. */
+typedef struct {
+  double betaJ;
+  double kappa;
+  double kappa2;
+  double h;
+  int size;
+} tm_params;
+
+/* Eigensolver precision modes for tm_eigs. */
+enum {
+  TM_EIGS_F64 = 0,   /* every matvec in FP64 */
+  TM_EIGS_MIXED = 1  /* FP32 matvec bulk + FP64 Rayleigh-Ritz refinement and residual check */
+};
+
+/* Diagnostics returned by tm_eigs. */
+typedef struct {
+  int nconv;          /* converged eigenvalues (Spectra compute() return value) */
+  int matvecs;        /* total operator applications (reference: OpCounter) */
+  int matvecs_f64;    /* of which FP64 */
+  int restarts;       /* restart cycles */
+  int ncv;            /* subspace size used */
+  double max_resid;   /* max relative residual ||T v - lambda v|| / |lambda| of the returned pairs (FP64) */
+  double seconds;     /* wall time inside tm_eigs */
+} tm_eigs_info;
+
+/* ---- operator lifetime ------------------------------------------------- */
+
+/* Build an operator.  Replaces the constructors dispatched by pfunc
+ * (TMat/pfunc.cpp:16-106): model 'A','B','D'; dim 2 or 3; axialdir as in the
+ * reference; extend_cond as the reference constructors take it (bit 0 open
+ * boundary, bit 1 disables the spin-flip reduction, TMat/tmatreduce.cpp:338-341).
+ * The reference driver passes extend_cond = (neigs > 1 ? 2 : 0) for reduced
+ * operators (TMat/pfunc.cpp:22).  Orbit tables and Boltzmann weights are built
+ * on the GPU.  Uses the current CUDA device. */
+tm_status tm_create(const tm_params* p, char model, int dim, int axialdir, int extend_cond,
+                    tm_op** out);
+
+/* Transpose operator T^T, sharing the parent's tables (the parent must outlive
+ * it).  Replaces get_t_instance() (e.g. TMat/tmatreduce.hpp:195-196,
+ * TMat/tmat.hpp:534-535).  Symmetric operators return a view of themselves. */
+tm_status tm_transpose(const tm_op* op, tm_op** out);
+
+/* Release an operator and its device memory. */
+tm_status tm_destroy(tm_op* op);
+
+/* ---- Spectra operator concept (TMat/tmat.hpp:82-120) ------------------- */
+
+int64_t tm_rows(const tm_op* op);          /* MatVecProd::rows() */
+int64_t tm_cols(const tm_op* op);          /* MatVecProd::cols() */
+double tm_normfactor(const tm_op* op);     /* MatVecProd::getnormfactor(); eigenvalues are lambda/normfactor */
+int tm_layer_size(const tm_op* op);        /* MatVecProd2D/3D::getLayerSize() */
+int tm_is_symmetric(const tm_op* op);      /* 1 if Scalar=double (SymEigsSolver path), 0 if general */
+int tm_suggested_ncv(const tm_op* op, int nev); /* MatVecProd::suggested_nev (TMat/tmat.hpp:88) */
+int64_t tm_matvec_count(const tm_op* op);  /* OpCounter::get() (TMat/utility.hpp:191-199), per operator */
+
+/* y = T x on host FP64 buffers of length cols(); drop-in for perform_op
+ * (TMat/tmat.hpp:89).  Copies in, computes in FP64 on the GPU, copies out. */
+tm_status tm_perform_op(const tm_op* op, const double* x_host, double* y_host);
+
+/* y = T x on device buffers (dtype TM_F64 or TM_F32, length cols()), on the
+ * given CUDA stream (cudaStream_t, or NULL for the library's stream).
+ * Asynchronous with respect to the host. */
+tm_status tm_perform_op_dev(const tm_op* op, const void* x_dev, void* y_dev, tm_dtype dtype,
+                            void* stream);
+
+/* Orbit table of a reduced operator: ascending representatives (idxlist) and
+ * orbit sizes (duplist), bit-exact with genX2DDuplist / genZ2DDuplist /
+ * genX3DDuplist (TMat/tmatreduce.cpp:19-111, 242-334; TMat/tmat3d.cpp:17-98).
+ * Host buffers of capacity `cap`; *n receives the table length.  Either
+ * buffer may be NULL to query the length only.  Full operators return
+ * TM_ERR_UNSUPPORTED. */
+tm_status tm_orbit_table(const tm_op* op, uint64_t* idx_host, uint16_t* dup_host, int64_t cap,
+                         int64_t* n);
+
+/* ---- eigensolver (replaces pfunc_inner, TMat/pfunc.hpp:79-202) ---------- */
+
+/* Largest-magnitude eigenpairs on the GPU: thick-restart Lanczos for symmetric
+ * operators, Krylov-Schur Arnoldi for general ones.  FP64 Gram-Schmidt and
+ * Rayleigh-Ritz on the device.
+ *   nev       wanted eigenvalues (reference `neigs`)
+ *   ncv       subspace size (0 = tm_suggested_ncv)
+ *   tol       relative residual tolerance
+ *   seed      start vector uniform(0,1) from splitmix64(seed)
+ *   mode      TM_EIGS_F64 or TM_EIGS_MIXED
+ *   vals_re/vals_im  host, nev each: eigenvalues / normfactor, in descending
+ *             magnitude (vals_im may be NULL for symmetric operators)
+ *   vecs      host or NULL: right eigenvectors, column-major rows x nev.
+ *             FP64 for symmetric operators; complex128 (re,im interleaved)
+ *             for general ones.
+ *   vecl      host or NULL: general operators only, the leading left
+ *             eigenvector (real part, length rows), from a second solve on the
+ *             transpose as getlefteigvec does (TMat/pfunc.hpp:47-68)
+ *   info      host or NULL: diagnostics */
+tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, int mode,
+                  double* vals_re, double* vals_im, double* vecs, double* vecl, tm_eigs_info* info);
+
+/* ---- observables ------------------------------------------------------- */
+
+/* Magnetisation moments <M^k>/L, k=1..4 (TMat/tmatphys.cpp:13-38, 71-98,
+ * reduced overrides TMat/tmatreduce.cpp:565-591, 882-909, 1261-1287,
+ * 1748-1775; TMat/tmat3d.cpp:137-163), from host eigenvectors ql, qr of
+ * length rows (ql may equal qr).  Returns the reference's status in *ref_status. */
+tm_status tm_moments(const tm_op* op, const double* ql_host, const double* qr_host, double out4[4],
+                     int* ref_status);
+
+/* Extended observables (phys_extend): <n_node>, <n_node^2> for X operators
+ * (TMat/tmatphys.cpp:40-59, TMat/tmatreduce.cpp:593-613), the four stripe /
+ * magnetisation averages for reduced DNNI (TMat/tmatreduce.cpp:1289-1320).
+ * *nout receives the count written (<= cap); *ref_status the reference's
+ * return status. */
+tm_status tm_phys_extend(const tm_op* op, const double* ql_host, const double* qr_host, double* out,
+                         int cap, int* nout, int* ref_status);
+
+/* ---- adjoint (no reference counterpart) -------------------------------- */
+
+/* d ln(lambda)/d(betaJ, kappa, kappa2, h) of the eigenvalue whose right
+ * eigenvector is qr (and left eigenvector ql, NULL for symmetric operators),
+ * host FP64 vectors of length rows.  lambda_internal is the operator's own
+ * eigenvalue (reported eigenvalue times normfactor).  The result includes the
+ * -d ln(normfactor) term, so it is the derivative of the reported eigenvalue. */
+tm_status tm_grad(const tm_op* op, const double* qr_host, const double* ql_host,
+                  double lambda_internal, double grad4[4]);
+
+/* ---- misc -------------------------------------------------------------- */
+
+const char* tm_last_error(void);
+const char* tm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LATTTMAT_GB300_H */

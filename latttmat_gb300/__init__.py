@@ -1,0 +1,267 @@
+"""latttmat_gb300 -- GB300 transfer-matrix operators and eigensolver.
+
+Python mirror of the reference's operator interface over the C ABI in
+``include/latttmat.h`` (liblatttmat_gb300.so, sm_103a).  ``TMatOp`` plays the
+part of one reference MatVecProd class (TMat/tmat.hpp:82-144):
+``rows()/cols()/perform_op(x, y)/getnormfactor()/getLayerSize()/moments()/
+phys_extend()/get_t_instance()``.  ``pfunc`` and ``read_input`` mirror
+TMat/pfunc.hpp / TMat/read_input.cpp (see ``latttmat_gb300.driver``).
+
+The CUDA library is required: there is no CPU fallback.  Importing works on a
+machine without a GPU (tests check the exported symbols there), but every
+compute call needs a CUDA device.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblatttmat_gb300.so")
+
+TM_OK = 0
+TM_ERR_ARG = 1
+TM_ERR_UNSUPPORTED = 2
+TM_ERR_CUDA = 3
+TM_ERR_NOMEM = 4
+TM_ERR_NOCONV = 5
+TM_ERR_NONFINITE = 6
+TM_ERR_NOTRANSPOSE = 7
+TM_ERR_LIMIT = 8
+
+TM_F64 = 0
+TM_F32 = 1
+TM_EIGS_F64 = 0
+TM_EIGS_MIXED = 1
+
+# every symbol include/latttmat.h declares
+EXPORTED_SYMBOLS = (
+    "tm_create", "tm_transpose", "tm_destroy", "tm_rows", "tm_cols", "tm_normfactor", "tm_layer_size",
+    "tm_is_symmetric", "tm_suggested_ncv", "tm_matvec_count", "tm_perform_op", "tm_perform_op_dev",
+    "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
+)
+
+
+class TMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class tm_params(ctypes.Structure):
+    _fields_ = [("betaJ", ctypes.c_double), ("kappa", ctypes.c_double), ("kappa2", ctypes.c_double),
+                ("h", ctypes.c_double), ("size", ctypes.c_int)]
+
+
+class tm_eigs_info(ctypes.Structure):
+    _fields_ = [("nconv", ctypes.c_int), ("matvecs", ctypes.c_int), ("matvecs_f64", ctypes.c_int),
+                ("restarts", ctypes.c_int), ("ncv", ctypes.c_int), ("max_resid", ctypes.c_double),
+                ("seconds", ctypes.c_double)]
+
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None) -> ctypes.CDLL:
+    """Load liblatttmat_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} not found; build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(p)
+    P = ctypes.c_void_p
+    lib.tm_create.argtypes = [ctypes.POINTER(tm_params), ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              ctypes.POINTER(P)]
+    lib.tm_transpose.argtypes = [P, ctypes.POINTER(P)]
+    lib.tm_destroy.argtypes = [P]
+    for f in ("tm_rows", "tm_cols", "tm_matvec_count"):
+        getattr(lib, f).argtypes = [P]
+        getattr(lib, f).restype = ctypes.c_int64
+    lib.tm_normfactor.argtypes = [P]
+    lib.tm_normfactor.restype = ctypes.c_double
+    lib.tm_layer_size.argtypes = [P]
+    lib.tm_is_symmetric.argtypes = [P]
+    lib.tm_suggested_ncv.argtypes = [P, ctypes.c_int]
+    lib.tm_perform_op.argtypes = [P, P, P]
+    lib.tm_perform_op_dev.argtypes = [P, P, P, ctypes.c_int, P]
+    lib.tm_orbit_table.argtypes = [P, P, P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    lib.tm_eigs.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, ctypes.c_int, P, P, P,
+                            P, ctypes.POINTER(tm_eigs_info)]
+    lib.tm_moments.argtypes = [P, P, P, P, ctypes.POINTER(ctypes.c_int)]
+    lib.tm_phys_extend.argtypes = [P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(ctypes.c_int)]
+    lib.tm_grad.argtypes = [P, P, P, ctypes.c_double, P]
+    lib.tm_last_error.restype = ctypes.c_char_p
+    lib.tm_version.restype = ctypes.c_char_p
+    for f in ("tm_create", "tm_transpose", "tm_destroy", "tm_perform_op", "tm_perform_op_dev", "tm_orbit_table",
+              "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad"):
+        getattr(lib, f).restype = ctypes.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(code: int):
+    if code != TM_OK:
+        msg = load_library().tm_last_error().decode(errors="replace")
+        raise TMError(code, msg)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class TMatOp:
+    """One transfer-matrix operator on the GPU (a reference MatVecProd).
+
+    model: 'A' (ANNNI), 'B' (BNNNI+3NN), 'D' (DNNI); dim 2 or 3; axialdir as
+    in the reference input file; extend_cond as the reference constructors take
+    it (bit 0 open boundary, bit 1 no spin-flip reduction).  For dim=3 pass
+    size=(size1, size2).
+    """
+
+    def __init__(self, model: str, dim: int, axialdir: int, betaJ: float, kappa: float, h: float = 0.0,
+                 size=12, kappa2: float = 0.0, extend_cond: int = 0, _handle=None, _parent=None):
+        lib = load_library()
+        self._lib = lib
+        self._parent = _parent
+        if _handle is not None:
+            self._h = _handle
+        else:
+            if dim == 3:
+                s1, s2 = size
+                packed = (int(s1) << 16) | int(s2)
+            else:
+                packed = int(size)
+            p = tm_params(float(betaJ), float(kappa), float(kappa2), float(h), packed)
+            h_ = ctypes.c_void_p()
+            _check(lib.tm_create(ctypes.byref(p), model.encode()[:1], int(dim), int(axialdir), int(extend_cond),
+                                 ctypes.byref(h_)))
+            self._h = h_
+        self.model, self.dim, self.axialdir = model, dim, axialdir
+
+    # --- Spectra operator concept -------------------------------------
+    def rows(self) -> int:
+        return int(self._lib.tm_rows(self._h))
+
+    def cols(self) -> int:
+        return int(self._lib.tm_cols(self._h))
+
+    def getnormfactor(self) -> float:
+        return float(self._lib.tm_normfactor(self._h))
+
+    def getLayerSize(self) -> int:
+        return int(self._lib.tm_layer_size(self._h))
+
+    def is_symmetric(self) -> bool:
+        return bool(self._lib.tm_is_symmetric(self._h))
+
+    def suggested_nev(self, neig: int) -> int:
+        return int(self._lib.tm_suggested_ncv(self._h, int(neig)))
+
+    def matvec_count(self) -> int:
+        return int(self._lib.tm_matvec_count(self._h))
+
+    def perform_op(self, x_in: np.ndarray, y_out: Optional[np.ndarray] = None) -> np.ndarray:
+        x = np.ascontiguousarray(x_in, dtype=np.float64)
+        if x.shape != (self.cols(),):
+            raise ValueError(f"x has shape {x.shape}, expected ({self.cols()},)")
+        y = y_out if y_out is not None else np.empty_like(x)
+        _check(self._lib.tm_perform_op(self._h, _ptr(x), _ptr(y)))
+        return y
+
+    def perform_op_dev(self, x_ptr: int, y_ptr: int, dtype: int = TM_F64, stream: int = 0):
+        """y = T x on device buffers (raw pointers, e.g. torch tensor.data_ptr())."""
+        _check(self._lib.tm_perform_op_dev(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), int(dtype),
+                                           ctypes.c_void_p(stream)))
+
+    def get_t_instance(self) -> "TMatOp":
+        h_ = ctypes.c_void_p()
+        _check(self._lib.tm_transpose(self._h, ctypes.byref(h_)))
+        return TMatOp(self.model, self.dim, self.axialdir, 0, 0, _handle=h_, _parent=self)
+
+    # --- reduced basis ------------------------------------------------
+    def orbit_table(self):
+        """(idxlist uint64, duplist uint16) of a reduced operator."""
+        n = ctypes.c_int64()
+        _check(self._lib.tm_orbit_table(self._h, None, None, 0, ctypes.byref(n)))
+        idx = np.empty(n.value, np.uint64)
+        dup = np.empty(n.value, np.uint16)
+        _check(self._lib.tm_orbit_table(self._h, _ptr(idx), _ptr(dup), n.value, ctypes.byref(n)))
+        return idx, dup
+
+    # --- eigensolver --------------------------------------------------
+    def eigs(self, nev: int, ncv: int = 0, tol: float = 1e-10, seed: int = 0, mode: int = TM_EIGS_F64,
+             vectors: bool = False, left: bool = False):
+        """Largest-magnitude eigenvalues (already divided by normfactor).
+
+        Returns (vals, vecs or None, vecl or None, info dict)."""
+        vr = np.zeros(nev)
+        vi = np.zeros(nev)
+        n = self.rows()
+        sym = self.is_symmetric()
+        vecs = None
+        if vectors:
+            vecs = np.zeros((nev, n) if sym else (nev, n, 2))
+        vecl = np.zeros(n) if (left and not sym) else None
+        info = tm_eigs_info()
+        _check(self._lib.tm_eigs(self._h, int(nev), int(ncv), float(tol), int(seed), int(mode), _ptr(vr), _ptr(vi),
+                                 _ptr(vecs) if vecs is not None else None,
+                                 _ptr(vecl) if vecl is not None else None, ctypes.byref(info)))
+        vals = vr if sym else vr + 1j * vi
+        if vecs is not None and not sym:
+            vecs = vecs[..., 0] + 1j * vecs[..., 1]
+        d = {k: getattr(info, k) for k, _ in tm_eigs_info._fields_}
+        return vals, vecs, vecl, d
+
+    # --- observables --------------------------------------------------
+    def moments(self, ql: np.ndarray, qr: Optional[np.ndarray] = None):
+        ql = np.ascontiguousarray(ql, dtype=np.float64)
+        qr = ql if qr is None else np.ascontiguousarray(qr, dtype=np.float64)
+        out = np.zeros(4)
+        st = ctypes.c_int()
+        _check(self._lib.tm_moments(self._h, _ptr(ql), _ptr(qr), _ptr(out), ctypes.byref(st)))
+        return out, st.value
+
+    def phys_extend(self, ql: np.ndarray, qr: Optional[np.ndarray] = None):
+        ql = np.ascontiguousarray(ql, dtype=np.float64)
+        qr = ql if qr is None else np.ascontiguousarray(qr, dtype=np.float64)
+        out = np.zeros(8)
+        nout = ctypes.c_int()
+        st = ctypes.c_int()
+        _check(self._lib.tm_phys_extend(self._h, _ptr(ql), _ptr(qr), _ptr(out), 8, ctypes.byref(nout),
+                                        ctypes.byref(st)))
+        return out[: nout.value].copy(), st.value
+
+    def grad(self, qr: np.ndarray, lambda_internal: float, ql: Optional[np.ndarray] = None) -> np.ndarray:
+        """d ln(lambda)/d(betaJ, kappa, kappa2, h) of the eigenvalue of qr (ql for general operators)."""
+        qr = np.ascontiguousarray(qr, dtype=np.float64)
+        qlp = None
+        if ql is not None:
+            ql = np.ascontiguousarray(ql, dtype=np.float64)
+            qlp = _ptr(ql)
+        g = np.zeros(4)
+        _check(self._lib.tm_grad(self._h, _ptr(qr), qlp, float(lambda_internal), _ptr(g)))
+        return g
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.tm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

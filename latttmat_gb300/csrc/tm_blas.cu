@@ -1,0 +1,321 @@
+// Krylov-solver vector kernels (FP64 Gram-Schmidt, norms, basis rotation) and
+// the small dense symmetric eigensolver, all on the device.
+#include <cmath>
+
+#include "tm_blas.cuh"
+
+namespace ltm {
+
+namespace {
+
+constexpr int BT = 256;        // threads per block
+constexpr int NVMAX = 16;      // vectors per fused pass
+
+int red_blocks(int64_t n) {
+  int64_t b = (n + BT * 4 - 1) / (BT * 4);
+  int64_t cap = (int64_t)num_sms() * 4;
+  return (int)std::max<int64_t>(1, std::min(b, cap));
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int NV, bool W32>
+__global__ void __launch_bounds__(BT) mdot_kernel(const double* __restrict__ V, int64_t ldv, int nv,
+                                                  const double* __restrict__ w, const float* __restrict__ w32,
+                                                  double scale, int64_t n, double* __restrict__ part) {
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    double wi = W32 ? scale * (double)w32[i] : w[i];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (k < nv) acc[k] = fma(V[k * ldv + i], wi, acc[k]);
+  }
+  __shared__ double sh[BT / 32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double v = warp_sum(acc[k]);
+    if (lane == 0) sh[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double t = 0.0;
+    for (int q = 0; q < BT / 32; ++q) t += sh[q][threadIdx.x];
+    part[(int64_t)blockIdx.x * NV + threadIdx.x] = t;
+  }
+}
+
+__global__ void mdot_final(const double* __restrict__ part, int nb, int nv, int stride, double* __restrict__ h) {
+  int k = blockIdx.x;
+  if (k >= nv) return;
+  double t = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) t += part[(int64_t)b * stride + k];
+  t = warp_sum(t);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sh[q];
+    h[k] = s;
+  }
+}
+
+template <int NV, bool W32>
+__global__ void __launch_bounds__(BT) maxpy_kernel(const double* __restrict__ V, int64_t ldv, int nv,
+                                                   const double* __restrict__ h, const float* __restrict__ w32,
+                                                   double scale, double* __restrict__ w, int64_t n) {
+  __shared__ double hs[NV];
+  if (threadIdx.x < NV) hs[threadIdx.x] = (threadIdx.x < nv) ? h[threadIdx.x] : 0.0;
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    double acc = W32 ? scale * (double)w32[i] : w[i];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (k < nv) acc = fma(-V[k * ldv + i], hs[k], acc);
+    w[i] = acc;
+  }
+}
+
+__global__ void nrm_kernel(const double* __restrict__ w, int64_t n, double* __restrict__ part) {
+  double acc = 0.0;
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) acc = fma(w[i], w[i], acc);
+  __shared__ double sh[BT / 32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < BT / 32; ++q) t += sh[q];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void normalize_kernel(const double* __restrict__ w, const double* __restrict__ nsq,
+                                 double* __restrict__ v, float* __restrict__ v32, int64_t n) {
+  double inv = 1.0 / sqrt(*nsq);
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    double x = w[i] * inv;
+    v[i] = x;
+    if (v32) v32[i] = (float)x;
+  }
+}
+
+// row-wise in-place V[:, :k] = V[:, :m] Y  (m <= 64)
+__global__ void __launch_bounds__(BT) rotate_kernel(double* __restrict__ V, int64_t ldv, int m,
+                                                    const double* __restrict__ Y, int k, int64_t n) {
+  __shared__ double Ys[64 * 64];
+  for (int t = threadIdx.x; t < m * k; t += BT) Ys[t] = Y[t];
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    double row[64];
+    for (int j = 0; j < m; ++j) row[j] = V[j * ldv + i];
+    for (int c = 0; c < k; ++c) {
+      double acc = 0.0;
+      for (int j = 0; j < m; ++j) acc = fma(row[j], Ys[c * m + j], acc);
+      V[c * ldv + i] = acc;
+    }
+  }
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) out[i] = (float)in[i];
+}
+
+__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                             double* __restrict__ out, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) out[i] = a * x[i] + b * y[i];
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void uniform_kernel(double* __restrict__ v, int64_t n, uint64_t seed) {
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    uint64_t r = splitmix64(seed * 0x100000001b3ull + (uint64_t)i);
+    v[i] = (double)(r >> 11) * (1.0 / 9007199254740992.0);
+  }
+}
+
+__global__ void nonfinite_kernel(const double* __restrict__ v, int64_t n, unsigned int* cnt) {
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  unsigned int c = 0;
+  for (; i < n; i += st) c += !isfinite(v[i]);
+  if (c) atomicAdd(cnt, c);
+}
+
+// One-warp cyclic Jacobi for a small symmetric matrix (m <= 48).  Rotation
+// parameters follow the classical formulation (Golub & Van Loan, Alg. 8.5.2).
+__global__ void symeig_kernel(const double* __restrict__ Ain, int m, int lda, double* __restrict__ w,
+                              double* __restrict__ Z) {
+  __shared__ double A[48 * 48];
+  __shared__ double Q[48 * 48];
+  const int lane = threadIdx.x;
+  for (int t = lane; t < m * m; t += 32) {
+    int r = t % m, c = t / m;
+    A[t] = 0.5 * (Ain[r + c * lda] + Ain[c + r * lda]);
+    Q[t] = (r == c) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int t = lane; t < m * m; t += 32) {
+      int r = t % m, c = t / m;
+      double v = A[t] * A[t];
+      tot += v;
+      if (r != c) off += v;
+    }
+    off = warp_sum(off);
+    tot = warp_sum(tot);
+    off = __shfl_sync(0xffffffffu, off, 0);
+    tot = __shfl_sync(0xffffffffu, tot, 0);
+    if (off <= 1e-30 * tot || off == 0.0) break;
+    for (int p = 0; p < m - 1; ++p) {
+      for (int q = p + 1; q < m; ++q) {
+        double apq = A[p + q * m];
+        if (apq == 0.0) continue;
+        double app = A[p + p * m], aqq = A[q + q * m];
+        double theta = (aqq - app) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        __syncwarp();
+        // A <- J^T A J ; columns p,q then rows p,q
+        for (int r = lane; r < m; r += 32) {
+          double arp = A[r + p * m], arq = A[r + q * m];
+          A[r + p * m] = c * arp - s * arq;
+          A[r + q * m] = s * arp + c * arq;
+        }
+        __syncwarp();
+        for (int r = lane; r < m; r += 32) {
+          double apr = A[p + r * m], aqr = A[q + r * m];
+          A[p + r * m] = c * apr - s * aqr;
+          A[q + r * m] = s * apr + c * aqr;
+        }
+        __syncwarp();
+        for (int r = lane; r < m; r += 32) {
+          double qrp = Q[r + p * m], qrq = Q[r + q * m];
+          Q[r + p * m] = c * qrp - s * qrq;
+          Q[r + q * m] = s * qrp + c * qrq;
+        }
+        __syncwarp();
+      }
+    }
+  }
+  for (int t = lane; t < m; t += 32) w[t] = A[t + t * m];
+  for (int t = lane; t < m * m; t += 32) Z[t] = Q[t];
+}
+
+}  // namespace
+
+static void mdot_impl(const double* V, int64_t ldv, int nv, const double* w, const float* w32, double scale,
+                      int64_t n, double* h, double* part, cudaStream_t s) {
+  for (int k0 = 0; k0 < nv; k0 += NVMAX) {
+    int kk = std::min(NVMAX, nv - k0);
+    int nb = red_blocks(n);
+    if (w32)
+      mdot_kernel<NVMAX, true><<<nb, BT, 0, s>>>(V + k0 * ldv, ldv, kk, nullptr, w32, scale, n, part);
+    else
+      mdot_kernel<NVMAX, false><<<nb, BT, 0, s>>>(V + k0 * ldv, ldv, kk, w, nullptr, 1.0, n, part);
+    TM_CKK("mdot");
+    mdot_final<<<kk, 256, 0, s>>>(part, nb, kk, NVMAX, h + k0);
+    TM_CKK("mdot_final");
+  }
+}
+
+void mdot(const double* V, int64_t ldv, int nv, const double* w, int64_t n, double* h, double* part,
+          cudaStream_t s) {
+  mdot_impl(V, ldv, nv, w, nullptr, 1.0, n, h, part, s);
+}
+void mdot32(const double* V, int64_t ldv, int nv, const float* w32, double scale, int64_t n, double* h,
+            double* part, cudaStream_t s) {
+  mdot_impl(V, ldv, nv, nullptr, w32, scale, n, h, part, s);
+}
+
+void maxpy(const double* V, int64_t ldv, int nv, const double* h, double* w, int64_t n, cudaStream_t s) {
+  for (int k0 = 0; k0 < nv; k0 += NVMAX) {
+    int kk = std::min(NVMAX, nv - k0);
+    maxpy_kernel<NVMAX, false><<<red_blocks(n), BT, 0, s>>>(V + k0 * ldv, ldv, kk, h + k0, nullptr, 1.0, w, n);
+    TM_CKK("maxpy");
+  }
+}
+
+void maxpy32(const double* V, int64_t ldv, int nv, const double* h, const float* w32, double scale, double* w,
+             int64_t n, cudaStream_t s) {
+  int kk = std::min(NVMAX, nv);
+  maxpy_kernel<NVMAX, true><<<red_blocks(n), BT, 0, s>>>(V, ldv, kk, h, w32, scale, w, n);
+  TM_CKK("maxpy32");
+  if (nv > NVMAX) maxpy(V + NVMAX * ldv, ldv, nv - NVMAX, h + NVMAX, w, n, s);
+}
+
+void nrm2sq(const double* w, int64_t n, double* out, double* part, cudaStream_t s) {
+  int nb = red_blocks(n);
+  nrm_kernel<<<nb, BT, 0, s>>>(w, n, part);
+  TM_CKK("nrm");
+  mdot_final<<<1, 256, 0, s>>>(part, nb, 1, 1, out);
+  TM_CKK("nrm_final");
+}
+
+void normalize(const double* w, const double* nsq, double* v, float* v32, int64_t n, cudaStream_t s) {
+  normalize_kernel<<<red_blocks(n), BT, 0, s>>>(w, nsq, v, v32, n);
+  TM_CKK("normalize");
+}
+
+void basis_rotate(double* V, int64_t ldv, int m, const double* Y, int k, int64_t n, cudaStream_t s) {
+  rotate_kernel<<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, n);
+  TM_CKK("rotate");
+}
+
+void to_f32(const double* in, float* out, int64_t n, cudaStream_t s) {
+  to_f32_kernel<<<red_blocks(n), BT, 0, s>>>(in, out, n);
+  TM_CKK("to_f32");
+}
+
+void axpby(double a, const double* x, double b, const double* y, double* out, int64_t n, cudaStream_t s) {
+  axpby_kernel<<<red_blocks(n), BT, 0, s>>>(a, x, b, y, out, n);
+  TM_CKK("axpby");
+}
+
+void fill_uniform(double* v, int64_t n, uint64_t seed, cudaStream_t s) {
+  uniform_kernel<<<red_blocks(n), BT, 0, s>>>(v, n, seed);
+  TM_CKK("uniform");
+}
+
+void count_nonfinite(const double* v, int64_t n, unsigned int* cnt, cudaStream_t s) {
+  nonfinite_kernel<<<red_blocks(n), BT, 0, s>>>(v, n, cnt);
+  TM_CKK("nonfinite");
+}
+
+void small_symeig(const double* A, int m, double* w, double* Z, cudaStream_t s, int lda) {
+  if (m > 48) fail(TM_ERR_LIMIT, "small eigenproblem larger than 48");
+  symeig_kernel<<<1, 32, 0, s>>>(A, m, lda, w, Z);
+  TM_CKK("symeig");
+}
+
+}  // namespace ltm

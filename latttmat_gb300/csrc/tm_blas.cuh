@@ -1,0 +1,40 @@
+// Device vector kernels for the Krylov solvers: fused multi-vector dot
+// products and updates over a column-major basis V (ld = n), FP64.
+#pragma once
+#include "tm_internal.h"
+
+namespace ltm {
+
+// h[k] = sum_i V[k][i] * w[i], k < nv  (two-stage reduction)
+void mdot(const double* V, int64_t ldv, int nv, const double* w, int64_t n, double* h_dev,
+          double* part, cudaStream_t s);
+// h[k] = sum_i V[k][i] * scale * (double)w32[i]  (FP32 right-hand side)
+void mdot32(const double* V, int64_t ldv, int nv, const float* w32, double scale, int64_t n,
+            double* h_dev, double* part, cudaStream_t s);
+// w[i] -= sum_k V[k][i] * h[k]; optionally also accumulates hsum[k] += h[k]
+void maxpy(const double* V, int64_t ldv, int nv, const double* h_dev, double* w, int64_t n,
+           cudaStream_t s);
+// w = scale * (double) w32, then w -= V h  (fused first CGS update)
+void maxpy32(const double* V, int64_t ldv, int nv, const double* h_dev, const float* w32, double scale,
+             double* w, int64_t n, cudaStream_t s);
+// out = ||w||^2 on device
+void nrm2sq(const double* w, int64_t n, double* out_dev, double* part, cudaStream_t s);
+// v = w / sqrt(*nsq_dev); also writes v32 = (float)v when v32 != nullptr
+void normalize(const double* w, const double* nsq_dev, double* v, float* v32, int64_t n, cudaStream_t s);
+// X[:, 0..k) = V[:, 0..m) * Y[0..m, 0..k)  in place, row-wise (Y on device, column-major m x k)
+void basis_rotate(double* V, int64_t ldv, int m, const double* Y_dev, int k, int64_t n, cudaStream_t s);
+// out = (float) in
+void to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
+// out = a*x + b*y
+void axpby(double a, const double* x, double b, const double* y, double* out, int64_t n, cudaStream_t s);
+// uniform(0,1) start vector from splitmix64(seed ^ index)
+void fill_uniform(double* v, int64_t n, uint64_t seed, cudaStream_t s);
+// count of non-finite entries (device counter)
+void count_nonfinite(const double* v, int64_t n, unsigned int* cnt_dev, cudaStream_t s);
+
+// small dense symmetric eigenproblem on device (one warp, cyclic Jacobi, m <= 48):
+// A (m x m column-major, symmetric) -> eigenvalues w[m], eigenvectors Z (m x m, column-major)
+// (lda = leading dimension of A)
+void small_symeig(const double* A_dev, int m, double* w_dev, double* Z_dev, cudaStream_t s, int lda);
+
+}  // namespace ltm

@@ -1,0 +1,153 @@
+// Symmetry groups of the reduced operators, as device functions.
+//
+// A reduced basis vector is the normalised sum over one orbit of spin states.
+// The reference enumerates orbits with a serial bitset scan:
+//   X-2D  genX2DDuplist  (TMat/tmatreduce.cpp:19-111): rotations x reflection (x flip)
+//   Z-2D  genZ2DDuplist  (TMat/tmatreduce.cpp:242-334): shift-by-2 x
+//         R(s)=bitreversal(rotate1(s)) (x flip)
+//   X-3D  genX3DDuplist  (TMat/tmat3d.cpp:17-98): row shifts x column shifts x
+//         two mirrors (x flip) (x 90-degree rotation)
+// Those scans keep the first unvisited state (the orbit minimum), so idxlist
+// is the ascending list of orbit minima and duplist the orbit sizes.  Here the
+// same tables come from a per-state test: s is a representative iff no group
+// image is smaller, and |orbit| = |group list| / #{list elements fixing s}.
+#pragma once
+#include "tm_bits.cuh"
+#include "tm_internal.h"
+
+namespace ltm {
+
+struct GroupDev {
+  int kind, L, size1, size2, periodic, flip, rotate;
+  uint64_t mask;
+};
+
+inline GroupDev to_dev(const GroupDesc& g) {
+  GroupDev d;
+  d.kind = g.kind;
+  d.L = g.L;
+  d.size1 = g.size1;
+  d.size2 = g.size2;
+  d.periodic = g.periodic;
+  d.flip = g.flip;
+  d.rotate = g.rotate;
+  d.mask = (g.L >= 64) ? ~0ull : ((1ull << g.L) - 1);
+  return d;
+}
+
+// Visit every element of the enumerated group list applied to s.  The
+// visitor returns false to stop early.  F: bool(uint64_t image)
+template <class F>
+TM_HD void for_each_image(const GroupDev& g, uint64_t s, F&& f) {
+  const uint64_t mask = g.mask;
+  if (g.kind == G_X2D) {
+    if (g.periodic) {
+      for (int k = 0; k < g.L; ++k) {
+        uint64_t a = rotr(s, g.L, k);
+        uint64_t b = brev(a, g.L);
+        if (!f(a)) return;
+        if (!f(b)) return;
+        if (g.flip) {
+          if (!f(~a & mask)) return;
+          if (!f(~b & mask)) return;
+        }
+      }
+    } else {
+      uint64_t b = brev(s, g.L);
+      if (!f(s)) return;
+      if (!f(b)) return;
+      if (g.flip) {
+        if (!f(~s & mask)) return;
+        if (!f(~b & mask)) return;
+      }
+    }
+  } else if (g.kind == G_Z2D) {
+    uint64_t r = brev(rotr(s, g.L, 1), g.L);
+    if (g.periodic) {
+      int ncyc = (g.L & 1) ? g.L : g.L / 2;
+      int d = 0;
+      for (int j = 0; j < ncyc; ++j) {
+        uint64_t a = rotr(s, g.L, d);
+        uint64_t b = rotr(r, g.L, d);
+        if (!f(a)) return;
+        if (!f(b)) return;
+        if (g.flip) {
+          if (!f(~a & mask)) return;
+          if (!f(~b & mask)) return;
+        }
+        d += 2;
+        if (d >= g.L) d -= g.L;
+      }
+    } else {
+      if (!f(s)) return;
+      if (!f(r)) return;
+      if (g.flip) {
+        if (!f(~s & mask)) return;
+        if (!f(~r & mask)) return;
+      }
+    }
+  } else if (g.kind == G_X3D) {
+    for (int rr = 0; rr <= g.rotate; ++rr) {
+      uint64_t s0 = rr ? rotate3d(s, g.size1) : s;
+      for (int c = 0; c <= g.flip; ++c) {
+        uint64_t s1 = c ? (~s0 & mask) : s0;
+        for (int a = 0; a < 2; ++a) {
+          uint64_t s2 = a ? reflect3d(s1, g.size1, g.size2, 0) : s1;
+          for (int b = 0; b < 2; ++b) {
+            uint64_t s3 = b ? reflect3d(s2, g.size1, g.size2, 1) : s2;
+            uint64_t t1 = s3;
+            for (int dx = 0; dx < g.size2; ++dx) {
+              uint64_t t2 = t1;
+              for (int dy = 0; dy < g.size1; ++dy) {
+                if (!f(t2)) return;
+                t2 = dshift3d(t2, g.size1, g.size2, 1);
+              }
+              t1 = rshift3d(t1, g.size1, g.size2, 1);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+TM_HD int group_order(const GroupDev& g) {
+  switch (g.kind) {
+    case G_X2D: return (g.periodic ? 2 * g.L : 2) * (g.flip ? 2 : 1);
+    case G_Z2D: return (g.periodic ? 2 * ((g.L & 1) ? g.L : g.L / 2) : 2) * (g.flip ? 2 : 1);
+    case G_X3D: return g.size1 * g.size2 * 4 * (g.flip ? 2 : 1) * (g.rotate ? 2 : 1);
+  }
+  return 1;
+}
+
+TM_HD bool is_rep(const GroupDev& g, uint64_t s) {
+  bool rep = true;
+  for_each_image(g, s, [&](uint64_t im) {
+    if (im < s) {
+      rep = false;
+      return false;
+    }
+    return true;
+  });
+  return rep;
+}
+
+TM_HD uint64_t canon(const GroupDev& g, uint64_t s) {
+  uint64_t m = s;
+  for_each_image(g, s, [&](uint64_t im) {
+    if (im < m) m = im;
+    return true;
+  });
+  return m;
+}
+
+TM_HD int orbit_size(const GroupDev& g, uint64_t s) {
+  int fix = 0;
+  for_each_image(g, s, [&](uint64_t im) {
+    fix += (im == s);
+    return true;
+  });
+  return group_order(g) / fix;
+}
+
+}  // namespace ltm

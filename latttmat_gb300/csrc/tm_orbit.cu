@@ -1,0 +1,407 @@
+// Orbit tables, state->representative rank maps and Boltzmann-weight vectors,
+// all built on the GPU.
+//
+//  * rep bitset: one bit per state, set iff the state is its orbit's minimum
+//    (warp ballot over 32 consecutive states);
+//  * exclusive prefix of per-word popcounts -> rank of any representative;
+//  * compaction -> idxlist (ascending, u32) and duplist (orbit sizes, u16),
+//    bit-exact with the reference's serial scans (see tm_group.cuh);
+//  * Tvec per operator, restating each reference genTvec.
+#include <cmath>
+#include <cstdio>
+
+#include "tm_group.cuh"
+#include "tm_internal.h"
+
+namespace ltm {
+
+// ------------------------------------------------------------------ scan
+namespace {
+constexpr int SCAN_T = 1024;
+constexpr int SCAN_E = 4;
+constexpr int SCAN_CHUNK = SCAN_T * SCAN_E;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[32];
+  __shared__ uint32_t block_total;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0;
+    uint32_t z = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
+    }
+    warp_sums[lane] = z - w;
+    if (lane == 31) block_total = z;
+  }
+  __syncthreads();
+  uint32_t res = warp_sums[wid] + x - v;
+  if (total) *total = block_total;
+  __syncthreads();
+  return res;
+}
+
+__global__ void scan_reduce_kernel(const uint32_t* in, uint32_t* part, int64_t n) {
+  int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK;
+  uint32_t s = 0;
+  for (int e = 0; e < SCAN_E; ++e) {
+    int64_t i = base + (int64_t)e * SCAN_T + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ uint32_t ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t t = ws[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+  }
+}
+
+__global__ void scan_down_kernel(const uint32_t* in, uint32_t* out, const uint32_t* part, int64_t n) {
+  int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK + (int64_t)threadIdx.x * SCAN_E;
+  uint32_t v[SCAN_E];
+  uint32_t loc = 0;
+  for (int e = 0; e < SCAN_E; ++e) {
+    int64_t i = base + e;
+    v[e] = (i < n) ? in[i] : 0;
+    loc += v[e];
+  }
+  uint32_t off = block_excl_scan(loc, nullptr) + (part ? part[blockIdx.x] : 0);
+  for (int e = 0; e < SCAN_E; ++e) {
+    int64_t i = base + e;
+    if (i < n) out[i] = off;
+    off += v[e];
+  }
+}
+}  // namespace
+
+int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t s) {
+  if (n <= 0) return 0;
+  int64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  if (nb == 1) {
+    scan_down_kernel<<<1, SCAN_T, 0, s>>>(in, out, nullptr, n);
+    TM_CKK("scan_down");
+    return 0;
+  }
+  DBuf part, partx;
+  part.alloc(nb * sizeof(uint32_t));
+  partx.alloc(nb * sizeof(uint32_t));
+  scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(in, part.as<uint32_t>(), n);
+  TM_CKK("scan_reduce");
+  exclusive_scan_u32(part.as<uint32_t>(), partx.as<uint32_t>(), nb, s);
+  scan_down_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(in, out, partx.as<uint32_t>(), n);
+  TM_CKK("scan_down");
+  TM_CK(cudaStreamSynchronize(s));  // temporaries are released on return
+  return 0;
+}
+
+uint32_t read_u32(const uint32_t* dptr, cudaStream_t s) {
+  uint32_t v = 0;
+  TM_CK(cudaMemcpyAsync(&v, dptr, sizeof(v), cudaMemcpyDeviceToHost, s));
+  TM_CK(cudaStreamSynchronize(s));
+  return v;
+}
+
+// ------------------------------------------------------------------ orbit table
+namespace {
+
+__global__ void rep_bits_kernel(GroupDev g, uint64_t nstate, uint32_t* bits, uint32_t* cnt,
+                                int64_t nwords) {
+  const int lane = threadIdx.x & 31;
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp; w < nwords; w += nwarps) {
+    uint64_t s = (uint64_t)w * 32 + lane;
+    bool rep = (s < nstate) && is_rep(g, s);
+    uint32_t word = __ballot_sync(0xffffffffu, rep);
+    if (lane == 0) {
+      bits[w] = word;
+      cnt[w] = __popc(word);
+    }
+  }
+}
+
+__global__ void compact_kernel(GroupDev g, const uint32_t* bits, const uint32_t* prefix,
+                               int64_t nwords, uint32_t* idx, uint16_t* dup) {
+  const int lane = threadIdx.x & 31;
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp; w < nwords; w += nwarps) {
+    uint32_t word = bits[w];
+    if (!word) continue;
+    if ((word >> lane) & 1u) {
+      uint64_t s = (uint64_t)w * 32 + lane;
+      uint32_t pos = prefix[w] + __popc(word & ((1u << lane) - 1u));
+      idx[pos] = (uint32_t)s;
+      dup[pos] = (uint16_t)orbit_size(g, s);
+    }
+  }
+}
+
+__global__ void state_map_kernel(GroupDev g, uint64_t nstate, const uint32_t* bits,
+                                 const uint32_t* prefix, uint32_t* smap) {
+  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = tid; s < (int64_t)nstate; s += nth) {
+    uint64_t c = canon(g, (uint64_t)s);
+    uint32_t w = (uint32_t)(c >> 5);
+    smap[s] = prefix[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+  }
+}
+
+}  // namespace
+
+int GroupDesc::order() const { return group_order(to_dev(*this)); }
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    TM_CK(cudaGetDevice(&dev));
+    TM_CK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+
+// Builds op.idx / op.dup, and keeps the rank structure (rep bitset + word
+// prefix) in ws_a / ws_b for the map builders that follow.
+void build_orbit_table(Op& op) {
+  GroupDev g = to_dev(op.grp);
+  const uint64_t nstate = 1ull << op.L;
+  const int64_t nwords = (int64_t)((nstate + 31) / 32);
+  op.ws_a.alloc(nwords * sizeof(uint32_t));  // bits
+  op.ws_b.alloc(nwords * sizeof(uint32_t));  // counts -> prefix
+  uint32_t* bits = op.ws_a.as<uint32_t>();
+  uint32_t* pre = op.ws_b.as<uint32_t>();
+  const int threads = 256;
+  int64_t want = (nwords * 32 + threads - 1) / threads;
+  int blocks = (int)std::min<int64_t>(want, (int64_t)num_sms() * 64);
+  rep_bits_kernel<<<blocks, threads, 0, op.stream>>>(g, nstate, bits, pre, nwords);
+  TM_CKK("rep_bits");
+  uint32_t last_cnt = 0, last_bits = 0;
+  TM_CK(cudaMemcpyAsync(&last_bits, bits + nwords - 1, 4, cudaMemcpyDeviceToHost, op.stream));
+  exclusive_scan_u32(pre, pre, nwords, op.stream);
+  uint32_t last_pre = read_u32(pre + nwords - 1, op.stream);
+  last_cnt = __builtin_popcount(last_bits);
+  const int64_t R = (int64_t)last_pre + last_cnt;
+  op.n = R;
+  op.idx.alloc(R * sizeof(uint32_t));
+  op.dup.alloc(R * sizeof(uint16_t));
+  compact_kernel<<<blocks, threads, 0, op.stream>>>(g, bits, pre, nwords, op.idx.as<uint32_t>(),
+                                                    op.dup.as<uint16_t>());
+  TM_CKK("compact");
+  TM_CK(cudaStreamSynchronize(op.stream));
+}
+
+void build_state_map(Op& op) {
+  GroupDev g = to_dev(op.grp);
+  const uint64_t nstate = 1ull << op.L;
+  op.smap.alloc(nstate * sizeof(uint32_t));
+  int blocks = (int)std::min<int64_t>((int64_t)(nstate + 255) / 256, (int64_t)num_sms() * 32);
+  state_map_kernel<<<blocks, 256, 0, op.stream>>>(g, nstate, op.ws_a.as<uint32_t>(),
+                                                  op.ws_b.as<uint32_t>(), op.smap.as<uint32_t>());
+  TM_CKK("state_map");
+  TM_CK(cudaStreamSynchronize(op.stream));
+}
+
+// ------------------------------------------------------------------ Tvec
+namespace {
+
+struct TvecParams {
+  int kind, L, size1, size2, boundary;
+  double betaJ, kappa, kappa2, h, nfexp, halfnf;
+};
+
+// XATMatVecProd2D::genTvec (TMat/tmat.hpp:208-310) evaluated at betaJ/2.
+__device__ double tv_xat(const TvecParams& p, uint64_t s) {
+  const int L = p.L;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, J2 = hb * p.kappa, hJ = -hb * p.h;
+  const uint64_t mask = (1ull << L) - 1;
+  int n1, n2, n0 = popc64(s);
+  int ns1 = L, ns2 = L;
+  uint64_t a, b;
+  switch (p.boundary) {
+    case 0:
+      n1 = popc64(s ^ rotr(s, L, 1));
+      n2 = popc64(s ^ rotr(s, L, 2));
+      break;
+    case 1:
+      n1 = popc64((s & (mask >> 1)) ^ (s >> 1));
+      n2 = popc64((s & (mask >> 2)) ^ (s >> 2));
+      ns1 = L - 1;
+      ns2 = L - 2;
+      break;
+    case 5:
+    case 9:
+      a = (s << 1) | (p.boundary == 9 ? 1ull : 0ull);
+      b = s >> 1;
+      n1 = popc64(s ^ a);
+      n2 = popc64((a & mask) ^ b);
+      ns1 = L + 1;
+      break;
+    default:  // 13, 17
+      a = (s << 1) | (p.boundary == 17 ? 1ull : 0ull);
+      b = (s << 2) | (p.boundary == 17 ? 3ull : 0ull);
+      n1 = popc64(s ^ a);
+      n2 = popc64(s ^ b);
+      ns1 = L + 1;
+      ns2 = L + 2;
+      break;
+  }
+  double bz1 = J1 * (2.0 * n1 - ns1);
+  double bz2 = J2 * (2.0 * n2 - ns2);
+  double bz0 = hJ * (2.0 * n0 - L);
+  return exp(bz1 + bz2 + bz0);
+}
+
+// XDTMatVecProd2D::genTvec (TMat/tmat.hpp:437-504) evaluated at betaJ/2.
+__device__ double tv_xdt(const TvecParams& p, uint64_t s) {
+  const int L = p.L;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, hJ = -hb * p.h;
+  const uint64_t nst = 1ull << L;
+  int n1, ns1 = L, n0 = popc64(s);
+  switch (p.boundary) {
+    case 0: n1 = popc64(s ^ rotr(s, L, 1)); break;
+    case 1: n1 = popc64((s & ((nst - 1) >> 1)) ^ (s >> 1)); ns1 = L - 1; break;
+    case 5: n1 = popc64((s << 1) ^ s); ns1 = L + 1; break;
+    default: n1 = popc64(((s << 1) | 1ull) ^ s); ns1 = L + 1; break;  // 9
+  }
+  double bz1 = J1 * (2.0 * n1 - ns1);
+  double bz0 = hJ * (2.0 * n0 - L);
+  return exp(bz1 + bz0);
+}
+
+// ZBTMatVecProd2D::genTvec (TMat/tmat.hpp:537-556) at betaJ/2, times the
+// half normfactor (TMat/tmat.cpp:512-517).
+__device__ double tv_zbt(const TvecParams& p, uint64_t s) {
+  const int L = p.L;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, J3 = p.kappa2 * hb, hJ = -hb * p.h;
+  int n1 = popc64(s ^ rotr(s, L, 1)), n2 = popc64(s ^ rotr(s, L, 2)), n0 = popc64(s);
+  double bz1 = J1 * (2.0 * n1 - L), bz2 = J3 * (2.0 * n2 - L), bz0 = hJ * (2.0 * n0 - L);
+  return exp(bz1 + bz2 + bz0) * p.halfnf;
+}
+
+// XAMMatVecProd2D::genTvec (TMat/tmatreduce.cpp:367-404), without the
+// 1/sqrt(dup) factor.
+__device__ double tv_xam(const TvecParams& p, uint64_t s) {
+  const int L = p.L;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, J2 = hb * p.kappa, hJ = -hb * p.h, Jn = hb * p.nfexp;
+  const uint64_t mask = (1ull << L) - 1;
+  int n1, n2;
+  if (!p.boundary) {
+    n1 = popc64(s ^ rotr(s, L, 1));
+    n2 = popc64(s ^ rotr(s, L, 2));
+  } else {
+    n1 = popc64((s & (mask >> 1)) ^ (s >> 1));
+    n2 = popc64((s & (mask >> 2)) ^ (s >> 2));
+  }
+  int n0 = popc64(s);
+  double bz = J1 * (2 * n1 - L) + J2 * (2 * n2 - L) + hJ * (2 * n0 - L) + Jn;
+  return exp(bz);
+}
+
+// XDMMatVecProd2D::genTvec (TMat/tmatreduce.cpp:1367-1400) without 1/sqrt(dup).
+__device__ double tv_xdm(const TvecParams& p, uint64_t s) {
+  const int L = p.L;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, hJ = -hb * p.h, Jn = hb * p.nfexp;
+  int n1 = popc64(s ^ rotr(s, L, 1)), n0 = popc64(s);
+  double bz = J1 * (2 * n1 - L) + hJ * (2 * n0 - L) + Jn;
+  return exp(bz);
+}
+
+// ZBMMatVecProd2D::genTvec (TMat/tmatreduce.cpp:1813-1855) without 1/sqrt(dup).
+__device__ double tv_zbm(const TvecParams& p, uint64_t s) {
+  const int L = p.L;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, J3 = hb * p.kappa2, hJ = -hb * p.h, Jn = hb * p.nfexp;
+  int n1 = popc64(s ^ rotr(s, L, 1)), n2 = popc64(s ^ rotr(s, L, 2)), n0 = popc64(s);
+  double bz1 = J1 * (2.0 * n1 - L), bz2 = J3 * (2.0 * n2 - L), bz0 = hJ * (2.0 * n0 - L);
+  return exp(bz1 + bz2 + bz0 + Jn);
+}
+
+// XAMMatVecProd3D::genTvec (TMat/tmat3d.cpp:179-201) without 1/sqrt(dup).
+__device__ double tv_xam3(const TvecParams& p, uint64_t s) {
+  const int L = p.L, s1 = p.size1, s2 = p.size2;
+  const double hb = 0.5 * p.betaJ;
+  const double J1 = -hb, J2 = hb * p.kappa, hJ = -hb * p.h, Jn = hb * p.nfexp;
+  int n1a = popc64(s ^ rshift3d(s, s1, s2, 1));
+  int n1b = popc64(s ^ dshift3d(s, s1, s2, 1));
+  int n2 = popc64(s ^ rshift3d(s, s1, s2, 2));
+  int n0 = popc64(s);
+  double bz = 2 * J1 * (n1a + n1b - L) + J2 * (2 * n2 - L) + hJ * (2 * n0 - L) + Jn;
+  return exp(bz);
+}
+
+__device__ double tv_eval(const TvecParams& p, uint64_t s) {
+  switch (p.kind) {
+    case K_XAT: return tv_xat(p, s);
+    case K_XDT: return tv_xdt(p, s);
+    case K_ZBT: return tv_zbt(p, s);
+    case K_XAM: return tv_xam(p, s);
+    case K_XDM: return tv_xdm(p, s);
+    case K_ZBM: return tv_zbm(p, s);
+    case K_XAM3: return tv_xam3(p, s);
+  }
+  return 0.0;
+}
+
+__global__ void tvec_full_kernel(TvecParams p, int64_t n, double* tv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) tv[i] = tv_eval(p, (uint64_t)i);
+}
+
+__global__ void tvec_red_kernel(TvecParams p, int64_t n, const uint32_t* idx, const uint16_t* dup,
+                                double* tv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) tv[i] = tv_eval(p, (uint64_t)idx[i]) / sqrt((double)dup[i]);
+}
+
+}  // namespace
+
+void build_tvec(Op& op) {
+  TvecParams p;
+  p.kind = op.kind;
+  p.L = op.L;
+  p.size1 = op.size1;
+  p.size2 = op.size2;
+  p.boundary = op.boundary;
+  p.betaJ = op.mp.betaJ;
+  p.kappa = op.mp.kappa;
+  p.kappa2 = op.mp.kappa2;
+  p.h = op.mp.h;
+  p.nfexp = op.nfexp;
+  p.halfnf = std::exp(0.5 * op.mp.betaJ * op.nfexp);
+  const bool reduced = (op.kind == K_XAM || op.kind == K_XDM || op.kind == K_ZBM || op.kind == K_XAM3);
+  const int64_t n = reduced ? op.n : (int64_t)op.nstate;
+  op.tvec.alloc(n * sizeof(double));
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 16);
+  if (blocks < 1) blocks = 1;
+  if (reduced)
+    tvec_red_kernel<<<blocks, 256, 0, op.stream>>>(p, n, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),
+                                                   op.tvec.as<double>());
+  else
+    tvec_full_kernel<<<blocks, 256, 0, op.stream>>>(p, n, op.tvec.as<double>());
+  TM_CKK("tvec");
+  TM_CK(cudaStreamSynchronize(op.stream));
+}
+
+}  // namespace ltm

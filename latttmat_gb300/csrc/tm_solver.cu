@@ -1,0 +1,377 @@
+// Largest-magnitude eigenpairs of a symmetric transfer matrix on the GPU.
+//
+// Replaces Spectra::SymEigsSolver as driven by pfunc_inner
+// (TMat/pfunc.hpp:79-114): nev wanted values, ncv = suggested_nev
+// (TMat/tmat.hpp:88), up to 3 attempts with ncv += 2 on non-convergence.
+//
+// Method: thick-restart Lanczos (Wu & Simon 2000), which is mathematically
+// equivalent to the implicitly restarted Lanczos with exact shifts that
+// ARPACK/Spectra use.  Gram-Schmidt with one full re-orthogonalisation (CGS2)
+// in FP64 on the device.  The small projected eigenproblem is solved by a
+// one-warp Jacobi kernel.  The host only reads Ritz values at restarts.
+//
+// Mixed precision (TM_EIGS_MIXED): matvecs run in FP32 until the Ritz
+// residuals reach the FP32 noise floor.  Then an FP64 Rayleigh-Ritz step on
+// the nev Ritz vectors (nev FP64 matvecs) gives eigenvalues whose error is
+// bounded by ||r||^2/gap (Kato-Temple).  FP64 Lanczos resumes only when that
+// bound misses the tolerance.
+#include <algorithm>
+#include <chrono>
+#include <memory>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "tm_blas.cuh"
+#include "tm_internal.h"
+
+namespace ltm {
+
+// matvec in the operator's internal order.  f32=true: x32 -> y32 with
+// T x = S * y32 (S returned).
+double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
+                      cudaStream_t s);
+
+namespace {
+
+__global__ void hcol_kernel(double* H, int ld, int j, const double* h1, const double* h2, const double* nsq,
+                            int write_beta) {
+  int i = threadIdx.x;
+  if (i <= j) {
+    double v = h1[i] + h2[i];
+    H[i + j * ld] = v;
+    H[j + i * ld] = v;
+  }
+  if (i == 0 && write_beta) {
+    double b = sqrt(*nsq);
+    H[(j + 1) + j * ld] = b;
+    H[j + (j + 1) * ld] = b;
+  }
+}
+
+__global__ void copy_kernel(const double* __restrict__ a, double* __restrict__ b, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) b[i] = a[i];
+}
+
+__global__ void resid_kernel(const double* __restrict__ W, const double* __restrict__ X, int64_t ld, int k,
+                             const double* __restrict__ theta, double* __restrict__ R, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st)
+    for (int c = 0; c < k; ++c) R[c * ld + i] = W[c * ld + i] - theta[c] * X[c * ld + i];
+}
+
+int blocks_for(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8));
+}
+
+struct Lanczos {
+  const Op& op;
+  cudaStream_t s;
+  int64_t n;
+  int m;
+  DBuf V, W, x32, y32, h1, h2, part, nsq, Hd, wd, Zd, Ysel;
+  int matvecs = 0, matvecs64 = 0, restarts = 0;
+
+  Lanczos(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), m(ncv) {
+    V.alloc((size_t)(m + 1) * n * sizeof(double));
+    W.alloc((size_t)n * sizeof(double));
+    h1.alloc(64 * 8);
+    h2.alloc(64 * 8);
+    part.alloc((size_t)num_sms() * 4 * 16 * 8 + 64);
+    nsq.alloc(8);
+    Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
+    wd.alloc(64 * 8);
+    Zd.alloc(64 * 64 * 8);
+    Ysel.alloc(64 * 64 * 8);
+  }
+  double* v(int j) const { return V.as<double>() + (int64_t)j * n; }
+
+  void ensure32() {
+    if (!x32.p) {
+      x32.alloc((size_t)n * 4);
+      y32.alloc((size_t)n * 4);
+    }
+  }
+
+  // one Lanczos step j: v(j) -> v(j+1), H column j
+  void step(int j, bool f32) {
+    double* w = W.as<double>();
+    if (f32) {
+      ensure32();
+      to_f32(v(j), x32.as<float>(), n, s);
+      double S = apply_internal(op, nullptr, nullptr, x32.as<float>(), y32.as<float>(), true, s);
+      mdot32(v(0), n, j + 1, y32.as<float>(), S, n, h1.as<double>(), part.as<double>(), s);
+      maxpy32(v(0), n, j + 1, h1.as<double>(), y32.as<float>(), S, w, n, s);
+    } else {
+      apply_internal(op, v(j), w, nullptr, nullptr, false, s);
+      ++matvecs64;
+      mdot(v(0), n, j + 1, w, n, h1.as<double>(), part.as<double>(), s);
+      maxpy(v(0), n, j + 1, h1.as<double>(), w, n, s);
+    }
+    ++matvecs;
+    mdot(v(0), n, j + 1, w, n, h2.as<double>(), part.as<double>(), s);
+    maxpy(v(0), n, j + 1, h2.as<double>(), w, n, s);
+    nrm2sq(w, n, nsq.as<double>(), part.as<double>(), s);
+    hcol_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m + 1, j, h1.as<double>(), h2.as<double>(), nsq.as<double>(),
+                                 1);
+    TM_CKK("hcol");
+    normalize(w, nsq.as<double>(), v(j + 1), nullptr, n, s);
+  }
+
+  struct CycleResult {
+    std::vector<double> theta;     // sorted by |theta| desc
+    std::vector<double> resid;     // |beta_m * y_{m-1,i}|
+    std::vector<int> order;        // column indices into Z
+    std::vector<double> Z;         // m x m
+    double beta;
+  };
+
+  CycleResult project() {
+    small_symeig(Hd.as<double>(), m, wd.as<double>(), Zd.as<double>(), s, m + 1);
+    CycleResult r;
+    std::vector<double> th(m), H((size_t)(m + 1) * (m + 1));
+    r.Z.resize((size_t)m * m);
+    TM_CK(cudaMemcpyAsync(th.data(), wd.p, m * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(r.Z.data(), Zd.p, (size_t)m * m * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(H.data(), Hd.p, H.size() * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+    r.beta = H[m + (size_t)(m - 1) * (m + 1)];
+    r.order.resize(m);
+    std::iota(r.order.begin(), r.order.end(), 0);
+    std::stable_sort(r.order.begin(), r.order.end(),
+                     [&](int a, int b) { return std::fabs(th[a]) > std::fabs(th[b]); });
+    for (int i = 0; i < m; ++i) {
+      int c = r.order[i];
+      r.theta.push_back(th[c]);
+      r.resid.push_back(std::fabs(r.beta * r.Z[(size_t)c * m + (m - 1)]));
+    }
+    return r;
+  }
+
+  // V[:, 0..k) <- V[:, 0..m) * Z[:, order[0..k)]
+  void rotate(const CycleResult& r, int k) {
+    std::vector<double> Y((size_t)m * k);
+    for (int c = 0; c < k; ++c)
+      for (int j = 0; j < m; ++j) Y[(size_t)c * m + j] = r.Z[(size_t)r.order[c] * m + j];
+    TM_CK(cudaMemcpyAsync(Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
+    basis_rotate(V.as<double>(), n, m, Ysel.as<double>(), k, n, s);
+  }
+
+  // restart with k kept Ritz vectors; v(k) <- v(m)
+  void restart(const CycleResult& r, int k) {
+    rotate(r, k);
+    copy_kernel<<<blocks_for(n), 256, 0, s>>>(v(m), v(k), n);
+    TM_CKK("copy");
+    std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0);
+    for (int i = 0; i < k; ++i) {
+      H[i + (size_t)i * (m + 1)] = r.theta[i];
+      double cpl = r.beta * r.Z[(size_t)r.order[i] * m + (m - 1)];
+      H[k + (size_t)i * (m + 1)] = cpl;
+      H[i + (size_t)k * (m + 1)] = cpl;
+    }
+    TM_CK(cudaMemcpyAsync(Hd.p, H.data(), H.size() * 8, cudaMemcpyHostToDevice, s));
+    ++restarts;
+  }
+
+  void start(const double* v0_dev, uint64_t seed) {
+    TM_CK(cudaMemsetAsync(Hd.p, 0, (size_t)(m + 1) * (m + 1) * 8, s));
+    if (v0_dev)
+      copy_kernel<<<blocks_for(n), 256, 0, s>>>(v0_dev, W.as<double>(), n);
+    else
+      fill_uniform(W.as<double>(), n, seed, s);
+    nrm2sq(W.as<double>(), n, nsq.as<double>(), part.as<double>(), s);
+    normalize(W.as<double>(), nsq.as<double>(), v(0), nullptr, n, s);
+  }
+
+  // run restart cycles; returns the last projection.  conv(r) decides.
+  template <class Conv>
+  CycleResult run(int nev, bool f32, int max_cycles, Conv conv, bool* ok) {
+    int k = 0;
+    CycleResult r;
+    *ok = false;
+    for (int cyc = 0; cyc < max_cycles; ++cyc) {
+      for (int j = k; j < m; ++j) step(j, f32);
+      r = project();
+      if (conv(r)) {
+        *ok = true;
+        return r;
+      }
+      int nconv = 0;
+      for (int i = 0; i < nev; ++i)
+        if (conv_one(r, i)) ++nconv;
+      k = std::min(m - 2, std::max(nev + 1, nev + std::min(nconv, (m - nev) / 2)));
+      k = std::max(k, std::min(m - 2, (m + nev) / 2));
+      restart(r, k);
+    }
+    return r;
+  }
+  double conv_tol = 1e-10;
+  bool conv_one(const CycleResult& r, int i) const {
+    return r.resid[i] <= conv_tol * std::max(std::fabs(r.theta[i]), 1e-300);
+  }
+};
+
+}  // namespace
+
+struct EigOut {
+  std::vector<double> vals;      // internal eigenvalues
+  std::vector<double> vecs;      // internal order, n x nev (host)
+  tm_eigs_info info;
+};
+
+// Symmetric solve.  vecs_host may be null.
+tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode, double* vals,
+                        double* vecs_host, tm_eigs_info* info_out) {
+  auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t s = op.stream;
+  const int64_t n = op.n;
+  if (nev < 1 || nev >= n) fail(TM_ERR_ARG, "nev must satisfy 1 <= nev < rows");
+  if (ncv <= 0) ncv = (nev > 4) ? 2 * nev + 1 : 2 * nev + 3;
+  if (ncv >= n) ncv = (int)n - 1;
+  if (ncv > 46) ncv = 46;
+  if (ncv <= nev) fail(TM_ERR_ARG, "ncv must exceed nev");
+  if (tol <= 0) tol = 1e-10;
+  tm_eigs_info info{};
+  std::vector<double> theta;
+  bool done = false;
+  int attempts = 0;
+  double max_resid = 0.0;
+  std::unique_ptr<Lanczos> Lz;
+  while (!done && attempts < 3) {
+    Lz.reset(new Lanczos(op, ncv, s));
+    Lanczos& lz = *Lz;
+    const bool mixed = (mode == TM_EIGS_MIXED);
+    lz.start(nullptr, seed);
+    bool ok = false;
+    Lanczos::CycleResult r;
+    if (mixed) {
+      // FP32 phase: residuals relative to the dominant Ritz value
+      const double tol32 = std::max(tol, 2e-6);
+      lz.conv_tol = tol32;
+      r = lz.run(nev, true, 200, [&](const Lanczos::CycleResult& rr) {
+        for (int i = 0; i < nev; ++i)
+          if (rr.resid[i] > tol32 * std::fabs(rr.theta[0])) return false;
+        return true;
+      }, &ok);
+      // Rayleigh-Ritz refinement in FP64 on the nev Ritz vectors
+      lz.rotate(r, nev);
+      const double theta_next = (nev < (int)r.theta.size()) ? r.theta[nev] : 0.0;
+      DBuf AX, G, Gw, Gz, th, R;
+      AX.alloc((size_t)nev * n * 8);
+      G.alloc((size_t)nev * nev * 8);
+      Gw.alloc(64 * 8);
+      Gz.alloc((size_t)64 * 64 * 8);
+      th.alloc(64 * 8);
+      R.alloc((size_t)nev * n * 8);
+      double* X = lz.v(0);
+      for (int i = 0; i < nev; ++i) {
+        apply_internal(op, X + (int64_t)i * n, AX.as<double>() + (int64_t)i * n, nullptr, nullptr, false, s);
+        ++lz.matvecs;
+        ++lz.matvecs64;
+      }
+      for (int i = 0; i < nev; ++i)
+        mdot(X, n, nev, AX.as<double>() + (int64_t)i * n, n, G.as<double>() + (int64_t)i * nev,
+             lz.part.as<double>(), s);
+      small_symeig(G.as<double>(), nev, Gw.as<double>(), Gz.as<double>(), s, nev);
+      std::vector<double> gw(nev), gz((size_t)nev * nev);
+      TM_CK(cudaMemcpyAsync(gw.data(), Gw.p, nev * 8, cudaMemcpyDeviceToHost, s));
+      TM_CK(cudaMemcpyAsync(gz.data(), Gz.p, (size_t)nev * nev * 8, cudaMemcpyDeviceToHost, s));
+      TM_CK(cudaStreamSynchronize(s));
+      std::vector<int> ord(nev);
+      std::iota(ord.begin(), ord.end(), 0);
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
+      std::vector<double> Y((size_t)nev * nev), thv(nev);
+      for (int c = 0; c < nev; ++c) {
+        thv[c] = gw[ord[c]];
+        for (int j = 0; j < nev; ++j) Y[(size_t)c * nev + j] = gz[(size_t)ord[c] * nev + j];
+      }
+      TM_CK(cudaMemcpyAsync(lz.Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
+      TM_CK(cudaMemcpyAsync(th.p, thv.data(), nev * 8, cudaMemcpyHostToDevice, s));
+      basis_rotate(X, n, nev, lz.Ysel.as<double>(), nev, n, s);
+      basis_rotate(AX.as<double>(), n, nev, lz.Ysel.as<double>(), nev, n, s);
+      resid_kernel<<<blocks_for(n), 256, 0, s>>>(AX.as<double>(), X, n, nev, th.as<double>(), R.as<double>(), n);
+      TM_CKK("resid");
+      std::vector<double> rn(nev);
+      for (int i = 0; i < nev; ++i) {
+        nrm2sq(R.as<double>() + (int64_t)i * n, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&rn[i], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+      }
+      TM_CK(cudaStreamSynchronize(s));
+      bool refined = true;
+      max_resid = 0.0;
+      for (int i = 0; i < nev; ++i) {
+        double res = std::sqrt(std::max(rn[i], 0.0));
+        double gap = std::fabs(thv[i] - theta_next);
+        for (int j = 0; j < nev; ++j)
+          if (j != i) gap = std::min(gap, std::fabs(thv[i] - thv[j]));
+        double bound = res * res / std::max(gap, 1e-300);
+        max_resid = std::max(max_resid, res / std::fabs(thv[i]));
+        if (!(bound <= tol * std::fabs(thv[i]))) refined = false;
+      }
+      if (refined) {
+        theta = thv;
+        done = true;
+      } else {
+        // FP64 continuation from the refined vectors
+        DBuf start;
+        start.alloc((size_t)n * 8);
+        TM_CK(cudaMemsetAsync(start.p, 0, (size_t)n * 8, s));
+        for (int i = 0; i < nev; ++i) axpby(1.0, start.as<double>(), 1.0, X + (int64_t)i * n, start.as<double>(), n, s);
+        int mv = lz.matvecs, mv64 = lz.matvecs64, rs = lz.restarts;
+        lz.matvecs = lz.matvecs64 = lz.restarts = 0;
+        lz.start(start.as<double>(), seed);
+        lz.matvecs += mv;
+        lz.matvecs64 += mv64;
+        lz.restarts += rs;
+        lz.conv_tol = tol;
+        r = lz.run(nev, false, 200, [&](const Lanczos::CycleResult& rr) {
+          for (int i = 0; i < nev; ++i)
+            if (!lz.conv_one(rr, i)) return false;
+          return true;
+        }, &ok);
+        lz.rotate(r, nev);
+        theta.assign(r.theta.begin(), r.theta.begin() + nev);
+        max_resid = 0;
+        for (int i = 0; i < nev; ++i) max_resid = std::max(max_resid, r.resid[i] / std::fabs(r.theta[i]));
+        done = ok;
+      }
+    } else {
+      lz.conv_tol = tol;
+      r = lz.run(nev, false, 300, [&](const Lanczos::CycleResult& rr) {
+        for (int i = 0; i < nev; ++i)
+          if (!lz.conv_one(rr, i)) return false;
+        return true;
+      }, &ok);
+      lz.rotate(r, nev);
+      theta.assign(r.theta.begin(), r.theta.begin() + nev);
+      max_resid = 0;
+      for (int i = 0; i < nev; ++i) max_resid = std::max(max_resid, r.resid[i] / std::fabs(r.theta[i]));
+      done = ok;
+    }
+    info.matvecs += lz.matvecs;
+    info.matvecs_f64 += lz.matvecs64;
+    info.restarts += lz.restarts;
+    info.ncv = ncv;
+    ++attempts;
+    if (!done) {
+      ncv += 2;
+      if (ncv >= n) ncv = (int)n - 1;
+    }
+  }
+  info.nconv = done ? nev : 0;
+  info.max_resid = max_resid;
+  for (int i = 0; i < nev && i < (int)theta.size(); ++i) vals[i] = theta[i];
+  if (vecs_host && Lz) {
+    TM_CK(cudaMemcpyAsync(vecs_host, Lz->v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+  }
+  const_cast<Op&>(op).matvecs += info.matvecs;
+  info.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (info_out) *info_out = info;
+  return done ? TM_OK : TM_ERR_NOCONV;
+}
+
+}  // namespace ltm

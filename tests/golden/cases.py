@@ -1,0 +1,86 @@
+"""Parity cases shared by the golden-fixture generator and the tests.
+
+Each case names one reference operator (model, dim, axialdir, extend_cond as
+TMat/pfunc.cpp constructs it) and a parameter point.  Inputs are seeded:
+x = default_rng(seed).uniform(-1, 1, n).  Fixtures hold the reference's own
+outputs on those inputs (generated by make_golden.py from the reference
+sources compiled here).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# (name, model, dim, axialdir, extend_cond, betaJ, kappa, kappa2, h, size, nev)
+CASES = [
+    # x-ANNNI full perpendicular TM (XATMatVecProd2D), incl. every boundary case
+    ("xat_L4", "A", 2, 1, 0, 0.5, 0.5, 0.0, 0.0, 4, 2),
+    ("xat_L8_h", "A", 2, 1, 0, 0.3, 0.7, 0.0, 0.1, 8, 2),
+    ("xat_L12_cfg1", "A", 2, 1, 0, 0.5, 0.5, 0.0, 0.0, 12, 2),
+    ("xat_L13", "A", 2, 1, 0, 0.45, 0.3, 0.0, 0.0, 13, 2),
+    ("xat_L14_h", "A", 2, 1, 0, 0.9, 0.2, 0.0, 0.05, 14, 2),
+    ("xat_open_L10", "A", 2, 9, 0, 0.4, 0.6, 0.0, 0.0, 10, 2),
+    ("xat_b5_L10", "A", 2, 17, 0, 0.4, 0.6, 0.0, 0.1, 10, 2),
+    ("xat_b9_L10", "A", 2, 18, 0, 0.4, 0.6, 0.0, 0.0, 10, 2),
+    ("xat_b13_L10", "A", 2, 19, 0, 0.35, 0.8, 0.0, 0.0, 10, 2),
+    ("xat_b17_L11", "A", 2, 20, 0, 0.35, 0.8, 0.0, 0.2, 11, 2),
+    # x-ANNNI reduced (XAMMatVecProd2D): flip on (ec 0, h 0) / off (ec 2 or h != 0)
+    ("xam_L8_flip", "A", 2, 5, 0, 0.5, 0.5, 0.0, 0.0, 8, 2),
+    ("xam_L8_noflip", "A", 2, 5, 2, 0.5, 0.5, 0.0, 0.0, 8, 2),
+    ("xam_L12_flip", "A", 2, 5, 0, 0.5, 0.5, 0.0, 0.0, 12, 2),
+    ("xam_L12_noflip", "A", 2, 5, 2, 0.5, 0.5, 0.0, 0.0, 12, 2),
+    ("xam_L13_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 13, 2),
+    ("xam_L14_h", "A", 2, 5, 0, 0.35, 0.55, 0.0, 0.05, 14, 2),
+    ("xam_L16_flip", "A", 2, 5, 0, 0.3, 0.6, 0.0, 0.0, 16, 4),
+    ("xam_L16_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 16, 4),
+    ("xam_L18_noflip", "A", 2, 5, 2, 0.7, 0.3, 0.0, 0.0, 18, 2),
+    ("xam_L20_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 20, 4),
+    ("xam_L24_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 24, 4),
+    ("xam_L24_h_cfg5", "A", 2, 5, 0, 0.35, 0.55, 0.0, 0.05, 24, 4),
+    ("xam_open_L12", "A", 2, 13, 2, 0.4, 0.6, 0.0, 0.0, 12, 2),
+    ("xam_open_L13_flip", "A", 2, 13, 0, 0.4, 0.6, 0.0, 0.0, 13, 2),
+    # DNNI full (XDTMatVecProd2D) and reduced (XDMMatVecProd2D)
+    ("xdt_L8", "D", 2, 1, 0, 0.4, 0.3, 0.0, 0.1, 8, 2),
+    ("xdt_L13_cfg3", "D", 2, 2, 0, 0.4, 0.3, 0.0, 0.1, 13, 2),
+    ("xdt_L10_k", "D", 2, 1, 0, 0.6, 0.7, 0.0, 0.0, 10, 2),
+    ("xdt_b5_L10", "D", 2, 17, 0, 0.4, 0.3, 0.0, 0.1, 10, 2),
+    ("xdt_b9_L10", "D", 2, 18, 0, 0.4, 0.3, 0.0, 0.0, 10, 2),
+    ("xdm_L10_flip", "D", 2, 5, 0, 0.4, 0.3, 0.0, 0.0, 10, 2),
+    ("xdm_L13_noflip", "D", 2, 5, 2, 0.4, 0.3, 0.0, 0.1, 13, 2),
+    ("xdm_L16_noflip", "D", 2, 6, 2, 0.5, 0.7, 0.0, 0.0, 16, 2),
+    # diagonal BNNNI+3NN full (ZBTMatVecProd2D) and reduced (ZBMMatVecProd2D)
+    ("zbt_L8", "B", 2, 3, 0, 0.5, 0.6, 0.2, 0.1, 8, 2),
+    ("zbt_L12", "B", 2, 3, 0, 0.4, 0.3, 0.0, 0.0, 12, 2),
+    ("zbm_L12_flip", "B", 2, 7, 0, 0.4, 0.3, 0.0, 0.0, 12, 2),
+    ("zbm_L12_noflip", "B", 2, 7, 2, 0.5, 0.6, 0.2, 0.0, 12, 2),
+    ("zbm_L16_noflip", "B", 2, 7, 2, 0.6, 0.8, 0.0, 0.0, 16, 2),
+    ("zbm_L14_h", "B", 2, 7, 0, 0.5, 0.45, 0.1, 0.05, 14, 2),
+    # 3D ANNNI reduced (XAMMatVecProd3D)
+    ("x3d_3x3", "A", 3, 1, 0, 0.3, 0.4, 0.0, 0.0, (3, 3), 2),
+    ("x3d_3x4_h", "A", 3, 1, 0, 0.25, 0.5, 0.0, 0.1, (3, 4), 2),
+    ("x3d_4x4_ising", "A", 3, 1, 0, 0.2, 0.0, 0.0, 0.0, (4, 4), 2),
+    ("x3d_5x5_cfg5", "A", 3, 1, 0, 0.2, 0.4, 0.0, 0.0, (5, 5), 2),
+]
+
+FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums only
+
+
+def case_dict(c):
+    name, model, dim, ax, ec, bj, k, k2, h, size, nev = c
+    return dict(name=name, model=model, dim=dim, axialdir=ax, extend_cond=ec, betaJ=bj, kappa=k, kappa2=k2,
+                h=h, size=size, nev=nev)
+
+
+def seeded_input(n: int, seed: int) -> np.ndarray:
+    return np.random.default_rng(seed).uniform(-1.0, 1.0, n)
+
+
+def checksum_weights(n: int) -> np.ndarray:
+    """Fixed weights for size-independent checksums of long outputs."""
+    return np.random.default_rng(12345).uniform(0.5, 1.5, n)
+
+
+def by_name(name):
+    for c in CASES:
+        if c[0] == name:
+            return case_dict(c)
+    raise KeyError(name)
