@@ -170,6 +170,19 @@ tm_status tm_phys_extend(const tm_op* op, const double* ql_host, const double* q
 tm_status tm_grad(const tm_op* op, const double* qr_host, const double* ql_host,
                   double lambda_internal, double grad4[4]);
 
+/* ---- diagnostics (no reference counterpart) ---------------------------- */
+
+/* Time the operator's matvec stages with CUDA events on the operator's
+ * stream, averaged over `iters` products in the internal vector order
+ * (dtype TM_F32 or TM_F64).  For the even/odd reduced x-ANNNI product the
+ * stages are {input scaling, pass 1, pass 2}; other operators report one
+ * stage {whole product}.  ms_out receives up to `cap` per-launch averages;
+ * *nstages the count. */
+tm_status tm_profile_matvec(const tm_op* op, tm_dtype dtype, int iters, double* ms_out, int cap, int* nstages);
+
+/* Number of CUDA kernels this library has launched since load (all ops). */
+int64_t tm_launch_count(void);
+
 /* ---- misc -------------------------------------------------------------- */
 
 const char* tm_last_error(void);

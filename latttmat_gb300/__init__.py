@@ -42,6 +42,7 @@ EXPORTED_SYMBOLS = (
     "tm_create", "tm_transpose", "tm_destroy", "tm_rows", "tm_cols", "tm_normfactor", "tm_layer_size",
     "tm_is_symmetric", "tm_suggested_ncv", "tm_matvec_count", "tm_perform_op", "tm_perform_op_dev",
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
+    "tm_profile_matvec", "tm_launch_count",
 )
 
 
@@ -96,14 +97,21 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.tm_phys_extend.argtypes = [P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                    ctypes.POINTER(ctypes.c_int)]
     lib.tm_grad.argtypes = [P, P, P, ctypes.c_double, P]
+    lib.tm_profile_matvec.argtypes = [P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.tm_launch_count.restype = ctypes.c_int64
     lib.tm_last_error.restype = ctypes.c_char_p
     lib.tm_version.restype = ctypes.c_char_p
     for f in ("tm_create", "tm_transpose", "tm_destroy", "tm_perform_op", "tm_perform_op_dev", "tm_orbit_table",
-              "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad"):
+              "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_profile_matvec"):
         getattr(lib, f).restype = ctypes.c_int
     if path is None:
         _lib = lib
     return lib
+
+
+def launch_count() -> int:
+    """Kernels launched by the library since load."""
+    return int(load_library().tm_launch_count())
 
 
 def _check(code: int):
@@ -248,6 +256,13 @@ class TMatOp:
         g = np.zeros(4)
         _check(self._lib.tm_grad(self._h, _ptr(qr), qlp, float(lambda_internal), _ptr(g)))
         return g
+
+    def profile_matvec(self, dtype: int = TM_F32, iters: int = 10):
+        """Per-stage average ms of the internal-order product (CUDA events)."""
+        out = np.zeros(8)
+        ns = ctypes.c_int()
+        _check(self._lib.tm_profile_matvec(self._h, int(dtype), int(iters), _ptr(out), 8, ctypes.byref(ns)))
+        return out[: ns.value].copy()
 
     def close(self):
         if getattr(self, "_h", None):

@@ -1,0 +1,633 @@
+// Largest-magnitude eigenpairs of a general (non-symmetric) transfer matrix.
+//
+// Replaces Spectra::GenEigsSolver as used by pfunc_inner and getlefteigvec
+// (TMat/pfunc.hpp:47-68, 84-98).  Method: Arnoldi with CGS2 in FP64 on the
+// device and thick restarts on an orthonormal basis of the kept Ritz vectors
+// (a Krylov-Schur style restart: A V_k = V_k H_k + f b^T with
+// span(W) H-invariant, so no implicit shifts are needed).  The small dense
+// eigenproblem runs on the device: Householder reduction to Hessenberg form
+// and Francis double-shift QR for the eigenvalues (Golub & Van Loan, Alg. 7.4.2,
+// 7.5.1-7.5.2), complex inverse iteration for the wanted eigenvectors.
+// Mixed mode: FP32 matvecs until the Ritz residuals hit the FP32 floor, then
+// FP64 restart cycles from the same basis until the tolerance is met.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "tm_blas.cuh"
+#include "tm_internal.h"
+
+namespace ltm {
+
+double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
+                      cudaStream_t s);
+
+namespace {
+
+constexpr int MMAX = 48;
+
+// --------------------------------------------------------------- small dense
+// Eigenvalues of a general m x m matrix (column-major, lda), one thread.
+__global__ void geneigval_kernel(const double* __restrict__ Ain, int m, int lda, double* __restrict__ wr,
+                                 double* __restrict__ wi, int* __restrict__ status) {
+  __shared__ double H[MMAX * MMAX];
+  if (threadIdx.x != 0) return;
+#define Hm(i, j) H[(i) + (j) * m]
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) Hm(i, j) = Ain[i + j * lda];
+  // Householder reduction to upper Hessenberg form
+  for (int k = 0; k + 2 < m; ++k) {
+    double nrm = 0.0;
+    for (int i = k + 1; i < m; ++i) nrm += Hm(i, k) * Hm(i, k);
+    nrm = sqrt(nrm);
+    if (nrm == 0.0) continue;
+    double x0 = Hm(k + 1, k);
+    double alpha = (x0 > 0) ? -nrm : nrm;
+    double v[MMAX];
+    for (int i = k + 1; i < m; ++i) v[i] = Hm(i, k);
+    v[k + 1] -= alpha;
+    double vn = 0.0;
+    for (int i = k + 1; i < m; ++i) vn += v[i] * v[i];
+    if (vn == 0.0) continue;
+    double sc = 2.0 / vn;
+    for (int j = k; j < m; ++j) {  // H = (I - sc v v^T) H
+      double d = 0.0;
+      for (int i = k + 1; i < m; ++i) d += v[i] * Hm(i, j);
+      d *= sc;
+      for (int i = k + 1; i < m; ++i) Hm(i, j) -= d * v[i];
+    }
+    for (int i = 0; i < m; ++i) {  // H = H (I - sc v v^T)
+      double d = 0.0;
+      for (int j = k + 1; j < m; ++j) d += Hm(i, j) * v[j];
+      d *= sc;
+      for (int j = k + 1; j < m; ++j) Hm(i, j) -= d * v[j];
+    }
+    for (int i = k + 2; i < m; ++i) Hm(i, k) = 0.0;
+  }
+  // Francis double-shift QR with deflation
+  const double eps = 2.220446049250313e-16;
+  double anorm = 0.0;
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i <= min(j + 1, m - 1); ++i) anorm += fabs(Hm(i, j));
+  int hi = m - 1;
+  int its = 0, total = 0;
+  *status = 0;
+  while (hi >= 0) {
+    // find the start lo of the unreduced block ending at hi
+    int lo = hi;
+    while (lo > 0) {
+      double s = fabs(Hm(lo - 1, lo - 1)) + fabs(Hm(lo, lo));
+      if (s == 0.0) s = anorm;
+      if (fabs(Hm(lo, lo - 1)) <= eps * s) {
+        Hm(lo, lo - 1) = 0.0;
+        break;
+      }
+      --lo;
+    }
+    if (lo == hi) {
+      wr[hi] = Hm(hi, hi);
+      wi[hi] = 0.0;
+      --hi;
+      its = 0;
+      continue;
+    }
+    if (lo == hi - 1) {
+      double a = Hm(hi - 1, hi - 1), b = Hm(hi - 1, hi), c = Hm(hi, hi - 1), d = Hm(hi, hi);
+      double p = 0.5 * (a - d), q = p * p + b * c;
+      double mid = 0.5 * (a + d);
+      if (q >= 0.0) {
+        double z = sqrt(q);
+        double e1 = mid + (p >= 0 ? z : -z);
+        double e2 = (e1 != 0.0) ? (a * d - b * c) / e1 : mid - (p >= 0 ? z : -z);
+        wr[hi - 1] = e1;
+        wr[hi] = e2;
+        wi[hi - 1] = wi[hi] = 0.0;
+      } else {
+        double z = sqrt(-q);
+        wr[hi - 1] = wr[hi] = mid;
+        wi[hi - 1] = z;
+        wi[hi] = -z;
+      }
+      hi -= 2;
+      its = 0;
+      continue;
+    }
+    if (++total > 60 * m) {
+      *status = 1;
+      for (int i = 0; i <= hi; ++i) {
+        wr[i] = Hm(i, i);
+        wi[i] = 0.0;
+      }
+      return;
+    }
+    ++its;
+    // shifts: eigenvalues of the trailing 2x2 (exceptional shift every 10 its)
+    double s, t;
+    if (its % 10 == 0) {
+      double e = fabs(Hm(hi, hi - 1)) + fabs(Hm(hi - 1, hi - 2));
+      s = 1.5 * e + Hm(hi, hi);
+      t = e * e;
+    } else {
+      s = Hm(hi - 1, hi - 1) + Hm(hi, hi);
+      t = Hm(hi - 1, hi - 1) * Hm(hi, hi) - Hm(hi - 1, hi) * Hm(hi, hi - 1);
+    }
+    double x = Hm(lo, lo) * Hm(lo, lo) + Hm(lo, lo + 1) * Hm(lo + 1, lo) - s * Hm(lo, lo) + t;
+    double y = Hm(lo + 1, lo) * (Hm(lo, lo) + Hm(lo + 1, lo + 1) - s);
+    double z = (lo + 2 <= hi) ? Hm(lo + 1, lo) * Hm(lo + 2, lo + 1) : 0.0;
+    for (int k = lo; k <= hi - 2; ++k) {
+      // 3-element Householder P with P [x y z]^T = beta e1
+      double nr = sqrt(x * x + y * y + z * z);
+      if (nr != 0.0) {
+        double alpha = (x > 0) ? -nr : nr;
+        double v0 = x - alpha, v1 = y, v2 = z;
+        double vn = v0 * v0 + v1 * v1 + v2 * v2;
+        if (vn != 0.0) {
+          double sc = 2.0 / vn;
+          int q = max(lo, k - 1);
+          for (int j = q; j <= hi; ++j) {
+            double d = sc * (v0 * Hm(k, j) + v1 * Hm(k + 1, j) + v2 * Hm(k + 2, j));
+            Hm(k, j) -= d * v0;
+            Hm(k + 1, j) -= d * v1;
+            Hm(k + 2, j) -= d * v2;
+          }
+          int r = min(k + 3, hi);
+          for (int i = lo; i <= r; ++i) {
+            double d = sc * (Hm(i, k) * v0 + Hm(i, k + 1) * v1 + Hm(i, k + 2) * v2);
+            Hm(i, k) -= d * v0;
+            Hm(i, k + 1) -= d * v1;
+            Hm(i, k + 2) -= d * v2;
+          }
+        }
+      }
+      x = Hm(k + 1, k);
+      y = Hm(k + 2, k);
+      if (k < hi - 2) z = Hm(k + 3, k);
+    }
+    // final 2-element reflector on rows/cols hi-1, hi
+    {
+      double nr = sqrt(x * x + y * y);
+      if (nr != 0.0) {
+        double alpha = (x > 0) ? -nr : nr;
+        double v0 = x - alpha, v1 = y;
+        double vn = v0 * v0 + v1 * v1;
+        double sc = 2.0 / vn;
+        int k = hi - 1;
+        for (int j = max(lo, k - 1); j <= hi; ++j) {
+          double d = sc * (v0 * Hm(k, j) + v1 * Hm(k + 1, j));
+          Hm(k, j) -= d * v0;
+          Hm(k + 1, j) -= d * v1;
+        }
+        for (int i = lo; i <= hi; ++i) {
+          double d = sc * (Hm(i, k) * v0 + Hm(i, k + 1) * v1);
+          Hm(i, k) -= d * v0;
+          Hm(i, k + 1) -= d * v1;
+        }
+      }
+    }
+  }
+#undef Hm
+}
+
+// Right eigenvectors for selected eigenvalues by complex inverse iteration on
+// (A - lambda I); one thread per eigenvalue.  Output unit-norm columns
+// (Yr, Yi: m x ksel column-major).
+__global__ void geneigvec_kernel(const double* __restrict__ A, int m, int lda, const double* __restrict__ lr,
+                                 const double* __restrict__ li, int ksel, double* __restrict__ scratch,
+                                 double* __restrict__ Yr, double* __restrict__ Yi) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ksel) return;
+  double* Br = scratch + (size_t)t * 2 * m * m;
+  double* Bi = Br + m * m;
+  double anorm = 0.0;
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) anorm = fmax(anorm, fabs(A[i + j * lda]));
+  const double tiny = 1e-14 * fmax(anorm, 1e-300);
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) {
+      Br[i + j * m] = A[i + j * lda] - (i == j ? lr[t] : 0.0);
+      Bi[i + j * m] = (i == j ? -li[t] : 0.0);
+    }
+  // complex LU with partial pivoting (in place), pivots in piv
+  int piv[MMAX];
+  for (int k = 0; k < m; ++k) {
+    int p = k;
+    double best = -1.0;
+    for (int i = k; i < m; ++i) {
+      double a = fabs(Br[i + k * m]) + fabs(Bi[i + k * m]);
+      if (a > best) {
+        best = a;
+        p = i;
+      }
+    }
+    piv[k] = p;
+    if (p != k)
+      for (int j = 0; j < m; ++j) {
+        double tr = Br[k + j * m], ti = Bi[k + j * m];
+        Br[k + j * m] = Br[p + j * m];
+        Bi[k + j * m] = Bi[p + j * m];
+        Br[p + j * m] = tr;
+        Bi[p + j * m] = ti;
+      }
+    double dr = Br[k + k * m], di = Bi[k + k * m];
+    if (fabs(dr) + fabs(di) < tiny) {
+      dr = tiny;
+      di = 0.0;
+      Br[k + k * m] = dr;
+      Bi[k + k * m] = di;
+    }
+    double den = dr * dr + di * di;
+    for (int i = k + 1; i < m; ++i) {
+      double ar = Br[i + k * m], ai = Bi[i + k * m];
+      double fr = (ar * dr + ai * di) / den, fi = (ai * dr - ar * di) / den;
+      Br[i + k * m] = fr;
+      Bi[i + k * m] = fi;
+      for (int j = k + 1; j < m; ++j) {
+        double br = Br[k + j * m], bi = Bi[k + j * m];
+        Br[i + j * m] -= fr * br - fi * bi;
+        Bi[i + j * m] -= fr * bi + fi * br;
+      }
+    }
+  }
+  double yr[MMAX], yi[MMAX];
+  for (int i = 0; i < m; ++i) {
+    yr[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * i);
+    yi[i] = 0.0;
+  }
+  for (int it = 0; it < 3; ++it) {
+    for (int k = 0; k < m; ++k) {  // apply row swaps
+      int p = piv[k];
+      if (p != k) {
+        double tr = yr[k], ti = yi[k];
+        yr[k] = yr[p];
+        yi[k] = yi[p];
+        yr[p] = tr;
+        yi[p] = ti;
+      }
+    }
+    for (int i = 0; i < m; ++i)  // forward (unit lower)
+      for (int j = 0; j < i; ++j) {
+        double lr_ = Br[i + j * m], li_ = Bi[i + j * m];
+        yr[i] -= lr_ * yr[j] - li_ * yi[j];
+        yi[i] -= lr_ * yi[j] + li_ * yr[j];
+      }
+    for (int i = m - 1; i >= 0; --i) {  // backward
+      double sr = yr[i], si = yi[i];
+      for (int j = i + 1; j < m; ++j) {
+        double ur = Br[i + j * m], ui = Bi[i + j * m];
+        sr -= ur * yr[j] - ui * yi[j];
+        si -= ur * yi[j] + ui * yr[j];
+      }
+      double dr = Br[i + i * m], di = Bi[i + i * m], den = dr * dr + di * di;
+      yr[i] = (sr * dr + si * di) / den;
+      yi[i] = (si * dr - sr * di) / den;
+    }
+    double nr = 0.0;
+    for (int i = 0; i < m; ++i) nr += yr[i] * yr[i] + yi[i] * yi[i];
+    nr = 1.0 / sqrt(nr);
+    for (int i = 0; i < m; ++i) {
+      yr[i] *= nr;
+      yi[i] *= nr;
+    }
+  }
+  // fix the phase: largest component real positive
+  int ib = 0;
+  double bm = -1;
+  for (int i = 0; i < m; ++i) {
+    double a = yr[i] * yr[i] + yi[i] * yi[i];
+    if (a > bm) {
+      bm = a;
+      ib = i;
+    }
+  }
+  double pr = yr[ib], pi_ = yi[ib], pn = sqrt(pr * pr + pi_ * pi_);
+  pr /= pn;
+  pi_ /= pn;
+  for (int i = 0; i < m; ++i) {
+    double a = yr[i] * pr + yi[i] * pi_, b = yi[i] * pr - yr[i] * pi_;
+    Yr[i + t * m] = a;
+    Yi[i + t * m] = b;
+  }
+}
+
+__global__ void hcolg_kernel(double* H, int ld, int j, const double* h1, const double* h2, const double* nsq) {
+  int i = threadIdx.x;
+  if (i <= j) H[i + j * ld] = h1[i] + h2[i];
+  if (i == 0) H[(j + 1) + j * ld] = sqrt(*nsq);
+}
+
+__global__ void copyv_kernel(const double* __restrict__ a, double* __restrict__ b, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) b[i] = a[i];
+}
+
+int nblk(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8)); }
+
+struct Ritz {
+  std::vector<std::complex<double>> theta;   // sorted by |theta| desc
+  std::vector<double> resid;
+  std::vector<std::vector<std::complex<double>>> y;  // eigenvectors of H (m)
+  double beta = 0;
+};
+
+struct Arnoldi {
+  const Op& op;
+  cudaStream_t s;
+  int64_t n;
+  int m;
+  DBuf V, W, x32, y32, h1, h2, part, nsq, Hd, wr, wi, lr, li, Yr, Yi, scr, Wd, st;
+  int matvecs = 0, matvecs64 = 0, restarts = 0;
+  std::vector<double> Hh;  // host copy (m+1)^2
+
+  Arnoldi(const Op& o, int ncv, cudaStream_t st_) : op(o), s(st_), n(o.n), m(ncv) {
+    V.alloc((size_t)(m + 1) * n * 8);
+    W.alloc((size_t)n * 8);
+    h1.alloc(64 * 8);
+    h2.alloc(64 * 8);
+    part.alloc((size_t)num_sms() * 4 * 16 * 8 + 64);
+    nsq.alloc(8);
+    Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
+    wr.alloc(64 * 8);
+    wi.alloc(64 * 8);
+    lr.alloc(64 * 8);
+    li.alloc(64 * 8);
+    Yr.alloc((size_t)64 * 64 * 8);
+    Yi.alloc((size_t)64 * 64 * 8);
+    scr.alloc((size_t)64 * 2 * 64 * 64 * 8);
+    Wd.alloc((size_t)64 * 64 * 8);
+    st.alloc(16);
+  }
+  double* v(int j) const { return V.as<double>() + (int64_t)j * n; }
+
+  void step(int j, bool f32) {
+    double* w = W.as<double>();
+    if (f32) {
+      if (!x32.p) {
+        x32.alloc((size_t)n * 4);
+        y32.alloc((size_t)n * 4);
+      }
+      to_f32(v(j), x32.as<float>(), n, s);
+      double S = apply_internal(op, nullptr, nullptr, x32.as<float>(), y32.as<float>(), true, s);
+      mdot32(v(0), n, j + 1, y32.as<float>(), S, n, h1.as<double>(), part.as<double>(), s);
+      maxpy32(v(0), n, j + 1, h1.as<double>(), y32.as<float>(), S, w, n, s);
+    } else {
+      apply_internal(op, v(j), w, nullptr, nullptr, false, s);
+      ++matvecs64;
+      mdot(v(0), n, j + 1, w, n, h1.as<double>(), part.as<double>(), s);
+      maxpy(v(0), n, j + 1, h1.as<double>(), w, n, s);
+    }
+    ++matvecs;
+    mdot(v(0), n, j + 1, w, n, h2.as<double>(), part.as<double>(), s);
+    maxpy(v(0), n, j + 1, h2.as<double>(), w, n, s);
+    nrm2sq(w, n, nsq.as<double>(), part.as<double>(), s);
+    hcolg_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m + 1, j, h1.as<double>(), h2.as<double>(), nsq.as<double>());
+    TM_CKK("hcolg");
+    normalize(w, nsq.as<double>(), v(j + 1), nullptr, n, s);
+  }
+
+  void start(const double* v0, uint64_t seed) {
+    TM_CK(cudaMemsetAsync(Hd.p, 0, (size_t)(m + 1) * (m + 1) * 8, s));
+    if (v0)
+      copyv_kernel<<<nblk(n), 256, 0, s>>>(v0, W.as<double>(), n);
+    else
+      fill_uniform(W.as<double>(), n, seed, s);
+    nrm2sq(W.as<double>(), n, nsq.as<double>(), part.as<double>(), s);
+    normalize(W.as<double>(), nsq.as<double>(), v(0), nullptr, n, s);
+  }
+
+  // eigen-decompose H_m on the device; eigenvectors for the first kvec by |theta|
+  Ritz project(int kvec) {
+    Ritz R;
+    Hh.assign((size_t)(m + 1) * (m + 1), 0.0);
+    TM_CK(cudaMemcpyAsync(Hh.data(), Hd.p, Hh.size() * 8, cudaMemcpyDeviceToHost, s));
+    geneigval_kernel<<<1, 32, 0, s>>>(Hd.as<double>(), m, m + 1, wr.as<double>(), wi.as<double>(), st.as<int>());
+    TM_CKK("geneigval");
+    std::vector<double> er(m), ei(m);
+    int status = 0;
+    TM_CK(cudaMemcpyAsync(er.data(), wr.p, m * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(ei.data(), wi.p, m * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(&status, st.p, 4, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+    if (status) fail(TM_ERR_NOCONV, "small Hessenberg QR did not converge");
+    std::vector<int> ord(m);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      double ma = std::hypot(er[a], ei[a]), mb = std::hypot(er[b], ei[b]);
+      if (ma != mb) return ma > mb;
+      return ei[a] > ei[b];
+    });
+    R.beta = Hh[m + (size_t)(m - 1) * (m + 1)];
+    kvec = std::min(kvec, m);
+    std::vector<double> sr(kvec), si(kvec);
+    for (int i = 0; i < kvec; ++i) {
+      sr[i] = er[ord[i]];
+      si[i] = ei[ord[i]];
+    }
+    TM_CK(cudaMemcpyAsync(lr.p, sr.data(), kvec * 8, cudaMemcpyHostToDevice, s));
+    TM_CK(cudaMemcpyAsync(li.p, si.data(), kvec * 8, cudaMemcpyHostToDevice, s));
+    geneigvec_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m, m + 1, lr.as<double>(), li.as<double>(), kvec,
+                                      scr.as<double>(), Yr.as<double>(), Yi.as<double>());
+    TM_CKK("geneigvec");
+    std::vector<double> yr((size_t)m * kvec), yi((size_t)m * kvec);
+    TM_CK(cudaMemcpyAsync(yr.data(), Yr.p, yr.size() * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(yi.data(), Yi.p, yi.size() * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < m; ++i) R.theta.push_back({er[ord[i]], ei[ord[i]]});
+    for (int c = 0; c < kvec; ++c) {
+      std::vector<std::complex<double>> y(m);
+      for (int i = 0; i < m; ++i) y[i] = {yr[(size_t)c * m + i], yi[(size_t)c * m + i]};
+      R.resid.push_back(std::fabs(R.beta) * std::abs(y[m - 1]));
+      R.y.push_back(y);
+    }
+    return R;
+  }
+
+  // real orthonormal basis W (m x k) of the span of the first kk Ritz vectors
+  // (a complex pair contributes Re and Im); returns k
+  int build_basis(const Ritz& R, int kk, std::vector<double>& Wm) {
+    std::vector<std::vector<double>> cols;
+    for (int c = 0; c < kk; ++c) {
+      bool cplx = std::fabs(R.theta[c].imag()) > 0.0;
+      std::vector<double> re(m), im(m);
+      for (int i = 0; i < m; ++i) {
+        re[i] = R.y[c][i].real();
+        im[i] = R.y[c][i].imag();
+      }
+      cols.push_back(re);
+      if (cplx) {
+        cols.push_back(im);
+        ++c;  // skip the conjugate partner
+      }
+    }
+    // modified Gram-Schmidt twice
+    std::vector<std::vector<double>> q;
+    for (auto& cvec : cols) {
+      std::vector<double> w = cvec;
+      for (int pass = 0; pass < 2; ++pass)
+        for (auto& b : q) {
+          double d = 0;
+          for (int i = 0; i < m; ++i) d += b[i] * w[i];
+          for (int i = 0; i < m; ++i) w[i] -= d * b[i];
+        }
+      double nr = 0;
+      for (int i = 0; i < m; ++i) nr += w[i] * w[i];
+      nr = std::sqrt(nr);
+      if (nr < 1e-10) continue;
+      for (int i = 0; i < m; ++i) w[i] /= nr;
+      q.push_back(w);
+    }
+    int k = (int)q.size();
+    Wm.assign((size_t)m * k, 0.0);
+    for (int c = 0; c < k; ++c)
+      for (int i = 0; i < m; ++i) Wm[(size_t)c * m + i] = q[c][i];
+    return k;
+  }
+
+  // restart: V_k = V_m W, H_k = W^T H_m W, coupling row b = beta * W[m-1,:], v_k = v_m
+  void restart(const Ritz& R, const std::vector<double>& Wm, int k) {
+    TM_CK(cudaMemcpyAsync(Wd.p, Wm.data(), Wm.size() * 8, cudaMemcpyHostToDevice, s));
+    basis_rotate(V.as<double>(), n, m, Wd.as<double>(), k, n, s);
+    copyv_kernel<<<nblk(n), 256, 0, s>>>(v(m), v(k), n);
+    TM_CKK("copyv");
+    const int ld = m + 1;
+    std::vector<double> HW((size_t)m * k, 0.0), Hn((size_t)ld * ld, 0.0);
+    for (int c = 0; c < k; ++c)
+      for (int i = 0; i < m; ++i) {
+        double acc = 0;
+        for (int j = 0; j < m; ++j) acc += Hh[i + (size_t)j * ld] * Wm[(size_t)c * m + j];
+        HW[(size_t)c * m + i] = acc;
+      }
+    for (int c = 0; c < k; ++c)
+      for (int r = 0; r < k; ++r) {
+        double acc = 0;
+        for (int i = 0; i < m; ++i) acc += Wm[(size_t)r * m + i] * HW[(size_t)c * m + i];
+        Hn[r + (size_t)c * ld] = acc;
+      }
+    for (int c = 0; c < k; ++c) Hn[k + (size_t)c * ld] = R.beta * Wm[(size_t)c * m + (m - 1)];
+    TM_CK(cudaMemcpyAsync(Hd.p, Hn.data(), Hn.size() * 8, cudaMemcpyHostToDevice, s));
+    ++restarts;
+  }
+
+  // returns converged flag; R holds the final projection
+  bool run(int nev, bool f32, double tol, bool tol_rel_dominant, int max_cycles, int k0, Ritz& R) {
+    int k = k0;
+    double best = 1e300;
+    int stall = 0;
+    for (int cyc = 0; cyc < max_cycles; ++cyc) {
+      for (int j = k; j < m; ++j) step(j, f32);
+      int kvec = std::min(m - 1, std::max(nev + 2, (m + nev) / 2 + 1));
+      R = project(kvec);
+      double ref = std::abs(R.theta[0]);
+      bool ok = true;
+      int nconv = 0;
+      double worst = 0.0;
+      for (int i = 0; i < nev; ++i) {
+        double lim = tol * (tol_rel_dominant ? ref : std::max(std::abs(R.theta[i]), 1e-300));
+        worst = std::max(worst, R.resid[i] / std::max(ref, 1e-300));
+        if (R.resid[i] <= lim)
+          ++nconv;
+        else
+          ok = false;
+      }
+      if (ok) return true;
+      if (f32) {  // stop the FP32 phase once its residuals stagnate at the FP32 floor
+        if (worst < 0.7 * best) {
+          best = worst;
+          stall = 0;
+        } else if (++stall >= 3 && worst < 1e-4) {
+          return false;
+        }
+      }
+      int kk = std::min(kvec, std::max(nev + 1, nev + std::min(nconv, (m - nev) / 2)));
+      kk = std::max(kk, std::min(kvec, (m + nev) / 2));
+      std::vector<double> Wm;
+      int knew = build_basis(R, kk, Wm);
+      if (knew >= m - 1) knew = m - 2;
+      restart(R, Wm, knew);
+      k = knew;
+    }
+    return false;
+  }
+
+  // final Ritz vectors x_c = V_m y_c for c < nev (complex): host arrays
+  void ritz_vectors(const Ritz& R, int nev, std::vector<double>& xr, std::vector<double>& xi) {
+    std::vector<double> Yc((size_t)m * 2 * nev);
+    for (int c = 0; c < nev; ++c)
+      for (int i = 0; i < m; ++i) {
+        Yc[(size_t)(2 * c) * m + i] = R.y[c][i].real();
+        Yc[(size_t)(2 * c + 1) * m + i] = R.y[c][i].imag();
+      }
+    // V has m+1 columns; rotate in place into columns 0..2nev-1 (needs 2nev <= m)
+    TM_CK(cudaMemcpyAsync(Wd.p, Yc.data(), Yc.size() * 8, cudaMemcpyHostToDevice, s));
+    basis_rotate(V.as<double>(), n, m, Wd.as<double>(), 2 * nev, n, s);
+    xr.resize((size_t)nev * n);
+    xi.resize((size_t)nev * n);
+    for (int c = 0; c < nev; ++c) {
+      TM_CK(cudaMemcpyAsync(xr.data() + (size_t)c * n, v(2 * c), (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+      TM_CK(cudaMemcpyAsync(xi.data() + (size_t)c * n, v(2 * c + 1), (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+    }
+    TM_CK(cudaStreamSynchronize(s));
+  }
+};
+
+}  // namespace
+
+// General solve: vals (complex, internal scale); vectors (complex, internal
+// order) when requested.
+tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode,
+                        std::vector<std::complex<double>>& vals, std::vector<double>* vr, std::vector<double>* vi,
+                        tm_eigs_info* info_out) {
+  auto t0 = std::chrono::steady_clock::now();
+  const int64_t n = op.n;
+  if (nev < 1 || nev >= n) fail(TM_ERR_ARG, "nev must satisfy 1 <= nev < rows");
+  if (ncv <= 0) ncv = (nev > 4) ? 2 * nev + 1 : 2 * nev + 3;
+  ncv = std::max(ncv, 2 * nev + 2);
+  if (ncv >= n) ncv = (int)n - 1;
+  if (ncv > MMAX - 2) ncv = MMAX - 2;
+  if (tol <= 0) tol = 1e-10;
+  tm_eigs_info info{};
+  bool done = false;
+  int attempts = 0;
+  std::unique_ptr<Arnoldi> Ar;
+  Ritz R;
+  while (!done && attempts < 3) {
+    Ar.reset(new Arnoldi(op, ncv, op.stream));
+    Arnoldi& a = *Ar;
+    a.start(nullptr, seed);
+    if (mode == TM_EIGS_MIXED) {
+      const double tol32 = std::max(tol, 3e-7);
+      a.run(nev, true, tol32, true, 200, 0, R);
+      // FP64 cycles from the FP32 basis: restart on the kept Ritz subspace
+      int kk = std::min(ncv - 2, std::max(nev + 1, (ncv + nev) / 2));
+      std::vector<double> Wm;
+      int knew = a.build_basis(R, std::min(kk, (int)R.y.size()), Wm);
+      if (knew >= ncv - 1) knew = ncv - 2;
+      a.restart(R, Wm, knew);
+      done = a.run(nev, false, tol, false, 200, knew, R);
+    } else {
+      done = a.run(nev, false, tol, false, 300, 0, R);
+    }
+    info.matvecs += a.matvecs;
+    info.matvecs_f64 += a.matvecs64;
+    info.restarts += a.restarts;
+    info.ncv = ncv;
+    ++attempts;
+    if (!done) ncv = std::min(ncv + 2, std::min((int)n - 1, MMAX - 2));
+  }
+  vals.assign(R.theta.begin(), R.theta.begin() + nev);
+  double mr = 0;
+  for (int i = 0; i < nev; ++i) mr = std::max(mr, R.resid[i] / std::max(std::abs(R.theta[i]), 1e-300));
+  info.max_resid = mr;
+  info.nconv = done ? nev : 0;
+  if (vr && vi) Ar->ritz_vectors(R, nev, *vr, *vi);
+  const_cast<Op&>(op).matvecs += info.matvecs;
+  info.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (info_out) *info_out = info;
+  return done ? TM_OK : TM_ERR_NOCONV;
+}
+
+}  // namespace ltm

@@ -134,6 +134,25 @@ __global__ void __launch_bounds__(BT) rotate_kernel(double* __restrict__ V, int6
   }
 }
 
+__global__ void __launch_bounds__(BT) combine_kernel(const double* __restrict__ V, int64_t ldv, int m,
+                                                     const double* __restrict__ Y, int k, double* __restrict__ out,
+                                                     int64_t ldo, int64_t n) {
+  __shared__ double Ys[64 * 64];
+  for (int t = threadIdx.x; t < m * k; t += BT) Ys[t] = Y[t];
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    double row[64];
+    for (int j = 0; j < m; ++j) row[j] = V[j * ldv + i];
+    for (int c = 0; c < k; ++c) {
+      double acc = 0.0;
+      for (int j = 0; j < m; ++j) acc = fma(row[j], Ys[c * m + j], acc);
+      out[c * ldo + i] = acc;
+    }
+  }
+}
+
 __global__ void to_f32_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * BT;
@@ -290,6 +309,13 @@ void normalize(const double* w, const double* nsq, double* v, float* v32, int64_
 void basis_rotate(double* V, int64_t ldv, int m, const double* Y, int k, int64_t n, cudaStream_t s) {
   rotate_kernel<<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, n);
   TM_CKK("rotate");
+}
+
+void basis_combine(const double* V, int64_t ldv, int m, const double* Y, int k, double* out, int64_t ldo, int64_t n,
+                   cudaStream_t s) {
+  if (m > 64 || m * k > 64 * 64) fail(TM_ERR_LIMIT, "basis_combine: block too large");
+  combine_kernel<<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  TM_CKK("combine");
 }
 
 void to_f32(const double* in, float* out, int64_t n, cudaStream_t s) {

@@ -23,6 +23,9 @@ void nrm2sq(const double* w, int64_t n, double* out_dev, double* part, cudaStrea
 void normalize(const double* w, const double* nsq_dev, double* v, float* v32, int64_t n, cudaStream_t s);
 // X[:, 0..k) = V[:, 0..m) * Y[0..m, 0..k)  in place, row-wise (Y on device, column-major m x k)
 void basis_rotate(double* V, int64_t ldv, int m, const double* Y_dev, int k, int64_t n, cudaStream_t s);
+// out[:, 0..k) = V[:, 0..m) * Y[0..m, 0..k)  (out-of-place; out columns spaced ldo)
+void basis_combine(const double* V, int64_t ldv, int m, const double* Y_dev, int k, double* out, int64_t ldo,
+                   int64_t n, cudaStream_t s);
 // out = (float) in
 void to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 // out = a*x + b*y

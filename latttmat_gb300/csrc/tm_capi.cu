@@ -1,8 +1,10 @@
 // C ABI of liblatttmat_gb300: operator construction (the dispatch of
 // TMat/pfunc.cpp:16-106), matvec entry points, orbit tables, observables and
 // the eigensolver front end.
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -25,6 +27,9 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
     throw Failure{e == cudaErrorMemoryAllocation ? TM_ERR_NOMEM : TM_ERR_CUDA, buf};
   }
 }
+
+static std::atomic<int64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void DBuf::alloc(size_t b) {
   release();
@@ -56,6 +61,9 @@ double matvec_aux(const Op& op, const T* x, T* y, bool scaled, cudaStream_t s);
 tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode, double* vals,
                         double* vecs_host, tm_eigs_info* info_out);
 void observables(const Op& op, const double* ql, const double* qr, double* sums /* 12 */);
+tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode,
+                        std::vector<std::complex<double>>& vals, std::vector<double>* vr, std::vector<double>* vi,
+                        tm_eigs_info* info_out);
 
 static bool is_reduced(int kind) { return kind == K_XAM || kind == K_XDM || kind == K_ZBM || kind == K_XAM3; }
 static bool bfly_core(int kind) { return kind == K_XAT || kind == K_XAM || kind == K_XAM3; }
@@ -74,7 +82,7 @@ double apply_internal(const Op& op, const double* x, double* y, const float* x32
   } else if (bfly_core(base.kind)) {
     S = f32 ? matvec_bfly<float>(base, x32, y32, true, s) : matvec_bfly<double>(base, x, y, false, s);
   } else {
-    S = f32 ? matvec_aux<float>(base, x32, y32, true, s) : matvec_aux<double>(base, x, y, false, s);
+    S = f32 ? matvec_aux<float>(op, x32, y32, true, s) : matvec_aux<double>(op, x, y, false, s);
   }
   const_cast<Op&>(op).matvecs++;
   return S;
@@ -91,13 +99,13 @@ void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStr
       } else if (bfly_core(base.kind)) {
         matvec_bfly<double>(base, (const double*)x, (double*)y, false, s);
       } else {
-        matvec_aux<double>(base, (const double*)x, (double*)y, false, s);
+        matvec_aux<double>(op, (const double*)x, (double*)y, false, s);
       }
     } else {
       if (bfly_core(base.kind))
         matvec_bfly<float>(base, (const float*)x, (float*)y, false, s);
       else
-        matvec_aux<float>(base, (const float*)x, (float*)y, false, s);
+        matvec_aux<float>(op, (const float*)x, (float*)y, false, s);
     }
   } else {
     const uint32_t* pi = base.pi.as<uint32_t>();
@@ -382,7 +390,7 @@ tm_status tm_perform_op_dev(const tm_op* op, const void* x, void* y, tm_dtype dt
   const Op& b = o.parent ? *o.parent : o;
   cudaStream_t s = stream ? (cudaStream_t)stream : b.stream;
   matvec_ref_order(o, x, y, dt, s);
-  TM_CKK("perform_op_dev");
+  TM_CK(cudaGetLastError());
   TM_API_END
 }
 
@@ -411,28 +419,69 @@ tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, 
   if (mode != TM_EIGS_F64 && mode != TM_EIGS_MIXED) fail(TM_ERR_ARG, "unknown mode");
   const Op& o = *op->impl;
   const Op& b = o.parent ? *o.parent : o;
-  if (!b.symmetric) fail(TM_ERR_UNSUPPORTED, "general (non-symmetric) eigensolver not available for this operator yet");
-  std::vector<double> th(nev);
-  std::vector<double> vint;
-  if (vecs) vint.resize((size_t)nev * b.n);
-  tm_status st = lanczos_solve(b, nev, ncv, tol, seed, mode, th.data(), vecs ? vint.data() : nullptr, info);
-  for (int i = 0; i < nev; ++i) {
-    vals_re[i] = th[i] / b.normfactor;
-    if (vals_im) vals_im[i] = 0.0;
-  }
-  if (vecs) {
-    if (b.has_pi) {
-      std::vector<uint32_t> pi((size_t)b.n);
-      TM_CK(cudaMemcpy(pi.data(), b.pi.p, (size_t)b.n * 4, cudaMemcpyDeviceToHost));
-      for (int c = 0; c < nev; ++c)
-        for (int64_t k = 0; k < b.n; ++k) vecs[(size_t)c * b.n + pi[k]] = vint[(size_t)c * b.n + k];
-    } else {
-      std::memcpy(vecs, vint.data(), vint.size() * 8);
+  tm_status st = TM_OK;
+  if (!b.symmetric) {
+    // general operator (TMat/pfunc.hpp:84-98 GenEigsSolver path)
+    std::vector<std::complex<double>> cv;
+    std::vector<double> xr, xi;
+    st = arnoldi_solve(o, nev, ncv, tol, seed, mode, cv, vecs ? &xr : nullptr, vecs ? &xi : nullptr, info);
+    for (int i = 0; i < nev; ++i) {
+      vals_re[i] = cv[i].real() / b.normfactor;
+      if (vals_im) vals_im[i] = cv[i].imag() / b.normfactor;
     }
-  }
-  if (vecl) {
-    // symmetric operators have no separate left vector (TMat/pfunc.hpp:33-44)
-    fail(TM_ERR_NOTRANSPOSE, "symmetric operators have no separate left eigenvector");
+    if (vecs) {
+      for (int c = 0; c < nev; ++c)
+        for (int64_t k = 0; k < b.n; ++k) {
+          vecs[2 * ((size_t)c * b.n + k)] = xr[(size_t)c * b.n + k];
+          vecs[2 * ((size_t)c * b.n + k) + 1] = xi[(size_t)c * b.n + k];
+        }
+    }
+    if (vecl) {
+      // left eigenvector: leading eigenvector of the transpose, nev=1, ncv=7
+      // (TMat/pfunc.hpp:51-54), real part written out (TMat/pfunc.hpp:159-164)
+      Op tv;
+      tv.kind = b.kind;
+      tv.L = b.L;
+      tv.n = b.n;
+      tv.symmetric = 0;
+      tv.is_view = true;
+      tv.transposed = !o.transposed;
+      tv.parent = &b;
+      tv.stream = b.stream;
+      std::vector<std::complex<double>> lv;
+      std::vector<double> lr, li;
+      tm_eigs_info linfo{};
+      tm_status lst = arnoldi_solve(tv, 1, 7, tol, seed + 1, mode, lv, &lr, &li, &linfo);
+      if (info) {
+        info->matvecs += linfo.matvecs;
+        info->matvecs_f64 += linfo.matvecs_f64;
+      }
+      for (int64_t k = 0; k < b.n; ++k) vecl[k] = lr[k];
+      if (lst != TM_OK) fail(lst, "left eigenvector solve did not converge");
+    }
+  } else {
+    std::vector<double> th(nev);
+    std::vector<double> vint;
+    if (vecs) vint.resize((size_t)nev * b.n);
+    st = lanczos_solve(b, nev, ncv, tol, seed, mode, th.data(), vecs ? vint.data() : nullptr, info);
+    for (int i = 0; i < nev; ++i) {
+      vals_re[i] = th[i] / b.normfactor;
+      if (vals_im) vals_im[i] = 0.0;
+    }
+    if (vecs) {
+      if (b.has_pi) {
+        std::vector<uint32_t> pi((size_t)b.n);
+        TM_CK(cudaMemcpy(pi.data(), b.pi.p, (size_t)b.n * 4, cudaMemcpyDeviceToHost));
+        for (int c = 0; c < nev; ++c)
+          for (int64_t k = 0; k < b.n; ++k) vecs[(size_t)c * b.n + pi[k]] = vint[(size_t)c * b.n + k];
+      } else {
+        std::memcpy(vecs, vint.data(), vint.size() * 8);
+      }
+    }
+    if (vecl) {
+      // symmetric operators have no separate left vector (TMat/pfunc.hpp:33-44)
+      fail(TM_ERR_NOTRANSPOSE, "symmetric operators have no separate left eigenvector");
+    }
   }
   if (st != TM_OK) fail(st, "eigensolver did not converge");
   TM_API_END
@@ -483,6 +532,69 @@ tm_status tm_phys_extend(const tm_op* op, const double* ql, const double* qr, do
   for (int i = 0; i < cnt && i < cap; ++i) out[i] = r[i];
   if (nout) *nout = cnt;
   if (ref_status) *ref_status = st;
+  TM_API_END
+}
+
+int64_t tm_launch_count(void) { return g_launches.load(); }
+
+tm_status tm_profile_matvec(const tm_op* op, tm_dtype dt, int iters, double* ms_out, int cap, int* nstages) {
+  TM_API_BEGIN
+  if (!op || !ms_out || iters < 1) fail(TM_ERR_ARG, "bad argument");
+  const Op& o = *op->impl;
+  const Op& b = o.parent ? *o.parent : o;
+  cudaStream_t s = b.stream;
+  DBuf x, y, x32, y32;
+  x.alloc((size_t)b.n * 8);
+  y.alloc((size_t)b.n * 8);
+  TM_CK(cudaMemsetAsync(x.p, 0, (size_t)b.n * 8, s));
+  const bool f32 = (dt == TM_F32);
+  if (f32) {
+    x32.alloc((size_t)b.n * 4);
+    y32.alloc((size_t)b.n * 4);
+    TM_CK(cudaMemsetAsync(x32.p, 0, (size_t)b.n * 4, s));
+  }
+  auto run = [&]() {
+    apply_internal(o, x.as<double>(), y.as<double>(), x32.as<float>(), y32.as<float>(), f32, s);
+  };
+  run();  // warm-up
+  TM_CK(cudaStreamSynchronize(s));
+  int ns = 1;
+  std::vector<double> acc(3, 0.0);
+  EOPlan& P = const_cast<EOPlan&>(b.eo);
+  if (b.eo.active) {
+    ns = 3;
+    for (int k = 0; k < 4; ++k) TM_CK(cudaEventCreate(&P.prof_ev[k]));
+    P.prof_on = true;
+    for (int it = 0; it < iters; ++it) {
+      run();
+      TM_CK(cudaStreamSynchronize(s));
+      for (int k = 0; k < 3; ++k) {
+        float ms = 0.f;
+        TM_CK(cudaEventElapsedTime(&ms, P.prof_ev[k], P.prof_ev[k + 1]));
+        acc[k] += ms;
+      }
+    }
+    P.prof_on = false;
+    for (int k = 0; k < 4; ++k) {
+      cudaEventDestroy(P.prof_ev[k]);
+      P.prof_ev[k] = nullptr;
+    }
+  } else {
+    cudaEvent_t e0, e1;
+    TM_CK(cudaEventCreate(&e0));
+    TM_CK(cudaEventCreate(&e1));
+    TM_CK(cudaEventRecord(e0, s));
+    for (int it = 0; it < iters; ++it) run();
+    TM_CK(cudaEventRecord(e1, s));
+    TM_CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    TM_CK(cudaEventElapsedTime(&ms, e0, e1));
+    acc[0] = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  for (int k = 0; k < ns && k < cap; ++k) ms_out[k] = acc[k] / iters;
+  if (nstages) *nstages = ns;
   TM_API_END
 }
 

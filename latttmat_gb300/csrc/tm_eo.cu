@@ -574,17 +574,21 @@ void eo_dispatch(const Op& op, const EOArgs& A, const T* x, T* y, bool scaled32,
   const int64_t R = op.n;
   T* u = static_cast<T*>(op.ws_c.p);
   T* w1 = (sizeof(T) == 8) ? P.w1_64.as<T>() : P.w1_32.as<T>();
+  if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[0], s));
   eo_scale_in<T><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R);
   TM_CKK("eo_scale_in");
+  if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[1], s));
   launch_pass1<T, KB>(A, P.n_orep, u, P.map1.as<uint32_t>(), w1, s);
-  const uint32_t* off = (A.c == P.c64 && sizeof(T) == 8) ? P.out_off.as<uint32_t>()
-                        : (A.c == P.c32)                 ? P.out_off32.as<uint32_t>()
-                                                         : P.out_off.as<uint32_t>();
+  TM_CKK("eo_pass1");
+  if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[2], s));
+  const uint32_t* off = (sizeof(T) == 8) ? P.out_off.as<uint32_t>() : P.out_off32.as<uint32_t>();
   const double S = std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);
   if (scaled32)
     launch_pass2<T, KB, false>(A, P.n_erep, w1, P, off, op.sout64.as<double>(), op.sout32.as<float>(), 1.0, y, s);
   else
     launch_pass2<T, KB, true>(A, P.n_erep, w1, P, off, op.sout64.as<double>(), op.sout32.as<float>(), S, y, s);
+  TM_CKK("eo_pass2");
+  if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[3], s));
 }
 
 }  // namespace

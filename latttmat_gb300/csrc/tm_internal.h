@@ -21,7 +21,9 @@ struct Failure {
 [[noreturn]] void fail(tm_status code, const std::string& msg);
 void check_cuda(cudaError_t e, const char* what, const char* file, int line);
 #define TM_CK(call) ::ltm::check_cuda((call), #call, __FILE__, __LINE__)
-#define TM_CKK(what) ::ltm::check_cuda(cudaGetLastError(), what, __FILE__, __LINE__)
+// after every kernel launch: error check + launch counter
+void note_launch();
+#define TM_CKK(what) (::ltm::note_launch(), ::ltm::check_cuda(cudaGetLastError(), what, __FILE__, __LINE__))
 
 // ---------------------------------------------------------------- memory
 // Owning device buffer (freed in the destructor).
@@ -78,6 +80,8 @@ struct EOPlan {
   DBuf out_o;         // u16 [R]: o of each designated output (pi order)
   DBuf out_off32;     // offsets for the FP32 cluster split
   DBuf w1_32, w1_64;  // pass-1 intermediates
+  cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // stage timing (diagnostics)
+  bool prof_on = false;
 };
 
 struct Op {

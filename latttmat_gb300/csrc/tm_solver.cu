@@ -192,12 +192,24 @@ struct Lanczos {
     int k = 0;
     CycleResult r;
     *ok = false;
+    double best = 1e300;
+    int stall = 0;
     for (int cyc = 0; cyc < max_cycles; ++cyc) {
       for (int j = k; j < m; ++j) step(j, f32);
       r = project();
       if (conv(r)) {
         *ok = true;
         return r;
+      }
+      if (stagnation_stop) {
+        double worst = 0.0;
+        for (int i = 0; i < nev; ++i) worst = std::max(worst, r.resid[i] / std::fabs(r.theta[0]));
+        if (worst < 0.7 * best) {
+          best = worst;
+          stall = 0;
+        } else if (++stall >= 3 && worst < 1e-4) {
+          return r;  // FP32 floor reached
+        }
       }
       int nconv = 0;
       for (int i = 0; i < nev; ++i)
@@ -209,6 +221,7 @@ struct Lanczos {
     return r;
   }
   double conv_tol = 1e-10;
+  bool stagnation_stop = false;
   bool conv_one(const CycleResult& r, int i) const {
     return r.resid[i] <= conv_tol * std::max(std::fabs(r.theta[i]), 1e-300);
   }
@@ -248,69 +261,98 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
     bool ok = false;
     Lanczos::CycleResult r;
     if (mixed) {
-      // FP32 phase: residuals relative to the dominant Ritz value
-      const double tol32 = std::max(tol, 2e-6);
+      // FP32 phase: Ritz residuals down to the FP32 floor (relative to the
+      // dominant Ritz value), stopping early if they stagnate
+      const double tol32 = std::max(tol, 2e-7);
       lz.conv_tol = tol32;
+      lz.stagnation_stop = true;
       r = lz.run(nev, true, 200, [&](const Lanczos::CycleResult& rr) {
         for (int i = 0; i < nev; ++i)
           if (rr.resid[i] > tol32 * std::fabs(rr.theta[0])) return false;
         return true;
       }, &ok);
-      // Rayleigh-Ritz refinement in FP64 on the nev Ritz vectors
+      lz.stagnation_stop = false;
       lz.rotate(r, nev);
-      const double theta_next = (nev < (int)r.theta.size()) ? r.theta[nev] : 0.0;
-      DBuf AX, G, Gw, Gz, th, R;
-      AX.alloc((size_t)nev * n * 8);
-      G.alloc((size_t)nev * nev * 8);
+      double theta_next = (nev < (int)r.theta.size()) ? std::fabs(r.theta[nev]) : 0.0;
+      // FP64 refinement: Rayleigh-Ritz on B = [Ritz vectors], growing B by the
+      // orthonormalised residual block (a block-Davidson step) while the
+      // Kato-Temple bound ||r||^2/gap misses tol.  B lives in V's columns.
+      const int cap = ncv + 1;
+      DBuf AB, XB, AXB, RB, G, Gw, Gz, th;
+      AB.alloc((size_t)cap * n * 8);
+      XB.alloc((size_t)nev * n * 8);
+      AXB.alloc((size_t)nev * n * 8);
+      RB.alloc((size_t)nev * n * 8);
+      G.alloc((size_t)cap * cap * 8);
       Gw.alloc(64 * 8);
       Gz.alloc((size_t)64 * 64 * 8);
       th.alloc(64 * 8);
-      R.alloc((size_t)nev * n * 8);
-      double* X = lz.v(0);
-      for (int i = 0; i < nev; ++i) {
-        apply_internal(op, X + (int64_t)i * n, AX.as<double>() + (int64_t)i * n, nullptr, nullptr, false, s);
-        ++lz.matvecs;
-        ++lz.matvecs64;
+      double* B = lz.v(0);
+      int nb = nev, nnew = nev;
+      bool refined = false;
+      std::vector<double> thv(nev);
+      for (int round = 0; round < 4; ++round) {
+        for (int i = nb - nnew; i < nb; ++i) {
+          apply_internal(op, B + (int64_t)i * n, AB.as<double>() + (int64_t)i * n, nullptr, nullptr, false, s);
+          ++lz.matvecs;
+          ++lz.matvecs64;
+        }
+        for (int i = 0; i < nb; ++i)
+          mdot(B, n, nb, AB.as<double>() + (int64_t)i * n, n, G.as<double>() + (int64_t)i * nb, lz.part.as<double>(), s);
+        small_symeig(G.as<double>(), nb, Gw.as<double>(), Gz.as<double>(), s, nb);
+        std::vector<double> gw(nb), gz((size_t)nb * nb);
+        TM_CK(cudaMemcpyAsync(gw.data(), Gw.p, nb * 8, cudaMemcpyDeviceToHost, s));
+        TM_CK(cudaMemcpyAsync(gz.data(), Gz.p, (size_t)nb * nb * 8, cudaMemcpyDeviceToHost, s));
+        TM_CK(cudaStreamSynchronize(s));
+        std::vector<int> ord(nb);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
+        std::vector<double> Y((size_t)nb * nev);
+        for (int c = 0; c < nev; ++c) {
+          thv[c] = gw[ord[c]];
+          for (int j = 0; j < nb; ++j) Y[(size_t)c * nb + j] = gz[(size_t)ord[c] * nb + j];
+        }
+        if (nb > nev) theta_next = std::min(theta_next > 0 ? theta_next : 1e300, std::fabs(gw[ord[nev]]));
+        TM_CK(cudaMemcpyAsync(lz.Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
+        TM_CK(cudaMemcpyAsync(th.p, thv.data(), nev * 8, cudaMemcpyHostToDevice, s));
+        basis_combine(B, n, nb, lz.Ysel.as<double>(), nev, XB.as<double>(), n, n, s);
+        basis_combine(AB.as<double>(), n, nb, lz.Ysel.as<double>(), nev, AXB.as<double>(), n, n, s);
+        resid_kernel<<<blocks_for(n), 256, 0, s>>>(AXB.as<double>(), XB.as<double>(), n, nev, th.as<double>(),
+                                                     RB.as<double>(), n);
+        TM_CKK("resid");
+        std::vector<double> rn(nev);
+        for (int i = 0; i < nev; ++i) {
+          nrm2sq(RB.as<double>() + (int64_t)i * n, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+          TM_CK(cudaMemcpyAsync(&rn[i], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        }
+        TM_CK(cudaStreamSynchronize(s));
+        refined = true;
+        max_resid = 0.0;
+        for (int i = 0; i < nev; ++i) {
+          double res = std::sqrt(std::max(rn[i], 0.0));
+          double gap = std::fabs(std::fabs(thv[i]) - theta_next);
+          for (int j = 0; j < nev; ++j)
+            if (j != i) gap = std::min(gap, std::fabs(thv[i] - thv[j]));
+          double bound = res * res / std::max(gap, 1e-300);
+          max_resid = std::max(max_resid, res / std::fabs(thv[i]));
+          if (!(bound <= tol * std::fabs(thv[i]))) refined = false;
+        }
+        if (refined || nb + nev > cap) break;
+        // append the residual block, orthonormalised against B (CGS2)
+        for (int i = 0; i < nev; ++i) {
+          double* rv = RB.as<double>() + (int64_t)i * n;
+          for (int pass = 0; pass < 2; ++pass) {
+            mdot(B, n, nb, rv, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+            maxpy(B, n, nb, lz.h1.as<double>(), rv, n, s);
+          }
+          nrm2sq(rv, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+          normalize(rv, lz.nsq.as<double>(), B + (int64_t)nb * n, nullptr, n, s);
+          ++nb;
+        }
+        nnew = nev;
       }
-      for (int i = 0; i < nev; ++i)
-        mdot(X, n, nev, AX.as<double>() + (int64_t)i * n, n, G.as<double>() + (int64_t)i * nev,
-             lz.part.as<double>(), s);
-      small_symeig(G.as<double>(), nev, Gw.as<double>(), Gz.as<double>(), s, nev);
-      std::vector<double> gw(nev), gz((size_t)nev * nev);
-      TM_CK(cudaMemcpyAsync(gw.data(), Gw.p, nev * 8, cudaMemcpyDeviceToHost, s));
-      TM_CK(cudaMemcpyAsync(gz.data(), Gz.p, (size_t)nev * nev * 8, cudaMemcpyDeviceToHost, s));
-      TM_CK(cudaStreamSynchronize(s));
-      std::vector<int> ord(nev);
-      std::iota(ord.begin(), ord.end(), 0);
-      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
-      std::vector<double> Y((size_t)nev * nev), thv(nev);
-      for (int c = 0; c < nev; ++c) {
-        thv[c] = gw[ord[c]];
-        for (int j = 0; j < nev; ++j) Y[(size_t)c * nev + j] = gz[(size_t)ord[c] * nev + j];
-      }
-      TM_CK(cudaMemcpyAsync(lz.Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
-      TM_CK(cudaMemcpyAsync(th.p, thv.data(), nev * 8, cudaMemcpyHostToDevice, s));
-      basis_rotate(X, n, nev, lz.Ysel.as<double>(), nev, n, s);
-      basis_rotate(AX.as<double>(), n, nev, lz.Ysel.as<double>(), nev, n, s);
-      resid_kernel<<<blocks_for(n), 256, 0, s>>>(AX.as<double>(), X, n, nev, th.as<double>(), R.as<double>(), n);
-      TM_CKK("resid");
-      std::vector<double> rn(nev);
-      for (int i = 0; i < nev; ++i) {
-        nrm2sq(R.as<double>() + (int64_t)i * n, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&rn[i], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-      }
-      TM_CK(cudaStreamSynchronize(s));
-      bool refined = true;
-      max_resid = 0.0;
-      for (int i = 0; i < nev; ++i) {
-        double res = std::sqrt(std::max(rn[i], 0.0));
-        double gap = std::fabs(thv[i] - theta_next);
-        for (int j = 0; j < nev; ++j)
-          if (j != i) gap = std::min(gap, std::fabs(thv[i] - thv[j]));
-        double bound = res * res / std::max(gap, 1e-300);
-        max_resid = std::max(max_resid, res / std::fabs(thv[i]));
-        if (!(bound <= tol * std::fabs(thv[i]))) refined = false;
-      }
+      // final Ritz vectors into V's leading columns
+      TM_CK(cudaMemcpyAsync(lz.v(0), XB.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
       if (refined) {
         theta = thv;
         done = true;
@@ -319,7 +361,8 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         DBuf start;
         start.alloc((size_t)n * 8);
         TM_CK(cudaMemsetAsync(start.p, 0, (size_t)n * 8, s));
-        for (int i = 0; i < nev; ++i) axpby(1.0, start.as<double>(), 1.0, X + (int64_t)i * n, start.as<double>(), n, s);
+        for (int i = 0; i < nev; ++i)
+          axpby(1.0, start.as<double>(), 1.0, lz.v(i), start.as<double>(), n, s);
         int mv = lz.matvecs, mv64 = lz.matvecs64, rs = lz.restarts;
         lz.matvecs = lz.matvecs64 = lz.restarts = 0;
         lz.start(start.as<double>(), seed);
