@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "tm_blas.cuh"
+#include "tm_hqr.cuh"
 #include "tm_internal.h"
 
 namespace ltm {
@@ -31,169 +32,19 @@ namespace {
 constexpr int MMAX = 48;
 
 // --------------------------------------------------------------- small dense
-// Eigenvalues of a general m x m matrix (column-major, lda), one thread.
+// Eigenvalues of a general m x m matrix (column-major, lda), one thread
+// (tm_hqr.cuh: Hessenberg reduction + Francis double-shift QR).
 __global__ void geneigval_kernel(const double* __restrict__ Ain, int m, int lda, double* __restrict__ wr,
                                  double* __restrict__ wi, int* __restrict__ status) {
   __shared__ double H[MMAX * MMAX];
   if (threadIdx.x != 0) return;
-#define Hm(i, j) H[(i) + (j) * m]
   for (int j = 0; j < m; ++j)
-    for (int i = 0; i < m; ++i) Hm(i, j) = Ain[i + j * lda];
-  // Householder reduction to upper Hessenberg form
-  for (int k = 0; k + 2 < m; ++k) {
-    double nrm = 0.0;
-    for (int i = k + 1; i < m; ++i) nrm += Hm(i, k) * Hm(i, k);
-    nrm = sqrt(nrm);
-    if (nrm == 0.0) continue;
-    double x0 = Hm(k + 1, k);
-    double alpha = (x0 > 0) ? -nrm : nrm;
-    double v[MMAX];
-    for (int i = k + 1; i < m; ++i) v[i] = Hm(i, k);
-    v[k + 1] -= alpha;
-    double vn = 0.0;
-    for (int i = k + 1; i < m; ++i) vn += v[i] * v[i];
-    if (vn == 0.0) continue;
-    double sc = 2.0 / vn;
-    for (int j = k; j < m; ++j) {  // H = (I - sc v v^T) H
-      double d = 0.0;
-      for (int i = k + 1; i < m; ++i) d += v[i] * Hm(i, j);
-      d *= sc;
-      for (int i = k + 1; i < m; ++i) Hm(i, j) -= d * v[i];
-    }
-    for (int i = 0; i < m; ++i) {  // H = H (I - sc v v^T)
-      double d = 0.0;
-      for (int j = k + 1; j < m; ++j) d += Hm(i, j) * v[j];
-      d *= sc;
-      for (int j = k + 1; j < m; ++j) Hm(i, j) -= d * v[j];
-    }
-    for (int i = k + 2; i < m; ++i) Hm(i, k) = 0.0;
-  }
-  // Francis double-shift QR with deflation
-  const double eps = 2.220446049250313e-16;
-  double anorm = 0.0;
-  for (int j = 0; j < m; ++j)
-    for (int i = 0; i <= min(j + 1, m - 1); ++i) anorm += fabs(Hm(i, j));
-  int hi = m - 1;
-  int its = 0, total = 0;
-  *status = 0;
-  while (hi >= 0) {
-    // find the start lo of the unreduced block ending at hi
-    int lo = hi;
-    while (lo > 0) {
-      double s = fabs(Hm(lo - 1, lo - 1)) + fabs(Hm(lo, lo));
-      if (s == 0.0) s = anorm;
-      if (fabs(Hm(lo, lo - 1)) <= eps * s) {
-        Hm(lo, lo - 1) = 0.0;
-        break;
-      }
-      --lo;
-    }
-    if (lo == hi) {
-      wr[hi] = Hm(hi, hi);
-      wi[hi] = 0.0;
-      --hi;
-      its = 0;
-      continue;
-    }
-    if (lo == hi - 1) {
-      double a = Hm(hi - 1, hi - 1), b = Hm(hi - 1, hi), c = Hm(hi, hi - 1), d = Hm(hi, hi);
-      double p = 0.5 * (a - d), q = p * p + b * c;
-      double mid = 0.5 * (a + d);
-      if (q >= 0.0) {
-        double z = sqrt(q);
-        double e1 = mid + (p >= 0 ? z : -z);
-        double e2 = (e1 != 0.0) ? (a * d - b * c) / e1 : mid - (p >= 0 ? z : -z);
-        wr[hi - 1] = e1;
-        wr[hi] = e2;
-        wi[hi - 1] = wi[hi] = 0.0;
-      } else {
-        double z = sqrt(-q);
-        wr[hi - 1] = wr[hi] = mid;
-        wi[hi - 1] = z;
-        wi[hi] = -z;
-      }
-      hi -= 2;
-      its = 0;
-      continue;
-    }
-    if (++total > 60 * m) {
-      *status = 1;
-      for (int i = 0; i <= hi; ++i) {
-        wr[i] = Hm(i, i);
-        wi[i] = 0.0;
-      }
-      return;
-    }
-    ++its;
-    // shifts: eigenvalues of the trailing 2x2 (exceptional shift every 10 its)
-    double s, t;
-    if (its % 10 == 0) {
-      double e = fabs(Hm(hi, hi - 1)) + fabs(Hm(hi - 1, hi - 2));
-      s = 1.5 * e + Hm(hi, hi);
-      t = e * e;
-    } else {
-      s = Hm(hi - 1, hi - 1) + Hm(hi, hi);
-      t = Hm(hi - 1, hi - 1) * Hm(hi, hi) - Hm(hi - 1, hi) * Hm(hi, hi - 1);
-    }
-    double x = Hm(lo, lo) * Hm(lo, lo) + Hm(lo, lo + 1) * Hm(lo + 1, lo) - s * Hm(lo, lo) + t;
-    double y = Hm(lo + 1, lo) * (Hm(lo, lo) + Hm(lo + 1, lo + 1) - s);
-    double z = (lo + 2 <= hi) ? Hm(lo + 1, lo) * Hm(lo + 2, lo + 1) : 0.0;
-    for (int k = lo; k <= hi - 2; ++k) {
-      // 3-element Householder P with P [x y z]^T = beta e1
-      double nr = sqrt(x * x + y * y + z * z);
-      if (nr != 0.0) {
-        double alpha = (x > 0) ? -nr : nr;
-        double v0 = x - alpha, v1 = y, v2 = z;
-        double vn = v0 * v0 + v1 * v1 + v2 * v2;
-        if (vn != 0.0) {
-          double sc = 2.0 / vn;
-          int q = max(lo, k - 1);
-          for (int j = q; j <= hi; ++j) {
-            double d = sc * (v0 * Hm(k, j) + v1 * Hm(k + 1, j) + v2 * Hm(k + 2, j));
-            Hm(k, j) -= d * v0;
-            Hm(k + 1, j) -= d * v1;
-            Hm(k + 2, j) -= d * v2;
-          }
-          int r = min(k + 3, hi);
-          for (int i = lo; i <= r; ++i) {
-            double d = sc * (Hm(i, k) * v0 + Hm(i, k + 1) * v1 + Hm(i, k + 2) * v2);
-            Hm(i, k) -= d * v0;
-            Hm(i, k + 1) -= d * v1;
-            Hm(i, k + 2) -= d * v2;
-          }
-        }
-      }
-      x = Hm(k + 1, k);
-      y = Hm(k + 2, k);
-      if (k < hi - 2) z = Hm(k + 3, k);
-    }
-    // final 2-element reflector on rows/cols hi-1, hi
-    {
-      double nr = sqrt(x * x + y * y);
-      if (nr != 0.0) {
-        double alpha = (x > 0) ? -nr : nr;
-        double v0 = x - alpha, v1 = y;
-        double vn = v0 * v0 + v1 * v1;
-        double sc = 2.0 / vn;
-        int k = hi - 1;
-        for (int j = max(lo, k - 1); j <= hi; ++j) {
-          double d = sc * (v0 * Hm(k, j) + v1 * Hm(k + 1, j));
-          Hm(k, j) -= d * v0;
-          Hm(k + 1, j) -= d * v1;
-        }
-        for (int i = lo; i <= hi; ++i) {
-          double d = sc * (Hm(i, k) * v0 + Hm(i, k + 1) * v1);
-          Hm(i, k) -= d * v0;
-          Hm(i, k + 1) -= d * v1;
-        }
-      }
-    }
-  }
-#undef Hm
+    for (int i = 0; i < m; ++i) H[i + j * m] = Ain[i + j * lda];
+  *status = geneig_values(H, m, wr, wi);
 }
 
-// Right eigenvectors for selected eigenvalues by complex inverse iteration on
-// (A - lambda I); one thread per eigenvalue.  Output unit-norm columns
+// Right eigenvectors for selected eigenvalues by complex inverse iteration
+// (tm_hqr.cuh); one thread per eigenvalue.  Output unit-norm columns
 // (Yr, Yi: m x ksel column-major).
 __global__ void geneigvec_kernel(const double* __restrict__ A, int m, int lda, const double* __restrict__ lr,
                                  const double* __restrict__ li, int ksel, double* __restrict__ scratch,
@@ -202,115 +53,7 @@ __global__ void geneigvec_kernel(const double* __restrict__ A, int m, int lda, c
   if (t >= ksel) return;
   double* Br = scratch + (size_t)t * 2 * m * m;
   double* Bi = Br + m * m;
-  double anorm = 0.0;
-  for (int j = 0; j < m; ++j)
-    for (int i = 0; i < m; ++i) anorm = fmax(anorm, fabs(A[i + j * lda]));
-  const double tiny = 1e-14 * fmax(anorm, 1e-300);
-  for (int j = 0; j < m; ++j)
-    for (int i = 0; i < m; ++i) {
-      Br[i + j * m] = A[i + j * lda] - (i == j ? lr[t] : 0.0);
-      Bi[i + j * m] = (i == j ? -li[t] : 0.0);
-    }
-  // complex LU with partial pivoting (in place), pivots in piv
-  int piv[MMAX];
-  for (int k = 0; k < m; ++k) {
-    int p = k;
-    double best = -1.0;
-    for (int i = k; i < m; ++i) {
-      double a = fabs(Br[i + k * m]) + fabs(Bi[i + k * m]);
-      if (a > best) {
-        best = a;
-        p = i;
-      }
-    }
-    piv[k] = p;
-    if (p != k)
-      for (int j = 0; j < m; ++j) {
-        double tr = Br[k + j * m], ti = Bi[k + j * m];
-        Br[k + j * m] = Br[p + j * m];
-        Bi[k + j * m] = Bi[p + j * m];
-        Br[p + j * m] = tr;
-        Bi[p + j * m] = ti;
-      }
-    double dr = Br[k + k * m], di = Bi[k + k * m];
-    if (fabs(dr) + fabs(di) < tiny) {
-      dr = tiny;
-      di = 0.0;
-      Br[k + k * m] = dr;
-      Bi[k + k * m] = di;
-    }
-    double den = dr * dr + di * di;
-    for (int i = k + 1; i < m; ++i) {
-      double ar = Br[i + k * m], ai = Bi[i + k * m];
-      double fr = (ar * dr + ai * di) / den, fi = (ai * dr - ar * di) / den;
-      Br[i + k * m] = fr;
-      Bi[i + k * m] = fi;
-      for (int j = k + 1; j < m; ++j) {
-        double br = Br[k + j * m], bi = Bi[k + j * m];
-        Br[i + j * m] -= fr * br - fi * bi;
-        Bi[i + j * m] -= fr * bi + fi * br;
-      }
-    }
-  }
-  double yr[MMAX], yi[MMAX];
-  for (int i = 0; i < m; ++i) {
-    yr[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * i);
-    yi[i] = 0.0;
-  }
-  for (int it = 0; it < 3; ++it) {
-    for (int k = 0; k < m; ++k) {  // apply row swaps
-      int p = piv[k];
-      if (p != k) {
-        double tr = yr[k], ti = yi[k];
-        yr[k] = yr[p];
-        yi[k] = yi[p];
-        yr[p] = tr;
-        yi[p] = ti;
-      }
-    }
-    for (int i = 0; i < m; ++i)  // forward (unit lower)
-      for (int j = 0; j < i; ++j) {
-        double lr_ = Br[i + j * m], li_ = Bi[i + j * m];
-        yr[i] -= lr_ * yr[j] - li_ * yi[j];
-        yi[i] -= lr_ * yi[j] + li_ * yr[j];
-      }
-    for (int i = m - 1; i >= 0; --i) {  // backward
-      double sr = yr[i], si = yi[i];
-      for (int j = i + 1; j < m; ++j) {
-        double ur = Br[i + j * m], ui = Bi[i + j * m];
-        sr -= ur * yr[j] - ui * yi[j];
-        si -= ur * yi[j] + ui * yr[j];
-      }
-      double dr = Br[i + i * m], di = Bi[i + i * m], den = dr * dr + di * di;
-      yr[i] = (sr * dr + si * di) / den;
-      yi[i] = (si * dr - sr * di) / den;
-    }
-    double nr = 0.0;
-    for (int i = 0; i < m; ++i) nr += yr[i] * yr[i] + yi[i] * yi[i];
-    nr = 1.0 / sqrt(nr);
-    for (int i = 0; i < m; ++i) {
-      yr[i] *= nr;
-      yi[i] *= nr;
-    }
-  }
-  // fix the phase: largest component real positive
-  int ib = 0;
-  double bm = -1;
-  for (int i = 0; i < m; ++i) {
-    double a = yr[i] * yr[i] + yi[i] * yi[i];
-    if (a > bm) {
-      bm = a;
-      ib = i;
-    }
-  }
-  double pr = yr[ib], pi_ = yi[ib], pn = sqrt(pr * pr + pi_ * pi_);
-  pr /= pn;
-  pi_ /= pn;
-  for (int i = 0; i < m; ++i) {
-    double a = yr[i] * pr + yi[i] * pi_, b = yi[i] * pr - yr[i] * pi_;
-    Yr[i + t * m] = a;
-    Yi[i + t * m] = b;
-  }
+  geneig_vector(A, m, lda, lr[t], li[t], Br, Bi, Yr + (size_t)t * m, Yi + (size_t)t * m);
 }
 
 __global__ void hcolg_kernel(double* H, int ld, int j, const double* h1, const double* h2, const double* nsq) {
@@ -601,13 +344,22 @@ tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
     if (mode == TM_EIGS_MIXED) {
       const double tol32 = std::max(tol, 3e-7);
       a.run(nev, true, tol32, true, 200, 0, R);
-      // FP64 cycles from the FP32 basis: restart on the kept Ritz subspace
-      int kk = std::min(ncv - 2, std::max(nev + 1, (ncv + nev) / 2));
-      std::vector<double> Wm;
-      int knew = a.build_basis(R, std::min(kk, (int)R.y.size()), Wm);
-      if (knew >= ncv - 1) knew = ncv - 2;
-      a.restart(R, Wm, knew);
-      done = a.run(nev, false, tol, false, 200, knew, R);
+      // FP64 Arnoldi restarted from the sum of the wanted FP32 Ritz vectors'
+      // real parts (the projected matrix of the FP32 phase is only FP32
+      // accurate, so it is rebuilt with FP64 products)
+      std::vector<double> Yc((size_t)ncv * nev);
+      for (int c = 0; c < nev; ++c)
+        for (int i = 0; i < ncv; ++i) Yc[(size_t)c * ncv + i] = R.y[c][i].real();
+      std::vector<double> comb(ncv, 0.0);
+      for (int c = 0; c < nev; ++c)
+        for (int i = 0; i < ncv; ++i) comb[i] += Yc[(size_t)c * ncv + i];
+      TM_CK(cudaMemcpyAsync(a.Wd.p, comb.data(), ncv * 8, cudaMemcpyHostToDevice, op.stream));
+      basis_rotate(a.V.as<double>(), n, ncv, a.Wd.as<double>(), 1, n, op.stream);
+      DBuf start;
+      start.alloc((size_t)n * 8);
+      TM_CK(cudaMemcpyAsync(start.p, a.v(0), (size_t)n * 8, cudaMemcpyDeviceToDevice, op.stream));
+      a.start(start.as<double>(), seed);
+      done = a.run(nev, false, tol, false, 200, 0, R);
     } else {
       done = a.run(nev, false, tol, false, 300, 0, R);
     }

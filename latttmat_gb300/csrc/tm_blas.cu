@@ -251,7 +251,233 @@ __global__ void symeig_kernel(const double* __restrict__ Ain, int m, int lda, do
   for (int t = lane; t < m * m; t += 32) Z[t] = Q[t];
 }
 
+// ---------------------------------------------------------------- FP32 basis
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(float (&acc)[NV], int nv, double* __restrict__ part) {
+  __shared__ double sh[BT / 32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double v = warp_sum((double)acc[k]);
+    if (lane == 0) sh[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double t = 0.0;
+    for (int q = 0; q < BT / 32; ++q) t += sh[q][threadIdx.x];
+    part[(int64_t)blockIdx.x * NV + threadIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(BT) mdot_f32_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                      const float* __restrict__ w, int64_t n,
+                                                      double* __restrict__ part) {
+  float acc[NV32];
+#pragma unroll
+  for (int k = 0; k < NV32; ++k) acc[k] = 0.f;
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    const float wi = w[i];
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) acc[k] = fmaf(V[k * ldv + i], wi, acc[k]);
+  }
+  block_reduce_store<NV32>(acc, nv, part);
+}
+
+__global__ void __launch_bounds__(BT) axpy_dot_f32_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                          const double* __restrict__ h,
+                                                          const float* __restrict__ win, float* __restrict__ wout,
+                                                          int64_t n, double* __restrict__ part) {
+  __shared__ float hs[NV32];
+  if (threadIdx.x < NV32) hs[threadIdx.x] = (threadIdx.x < nv) ? (float)h[threadIdx.x] : 0.f;
+  __syncthreads();
+  float acc[NV32];
+#pragma unroll
+  for (int k = 0; k < NV32; ++k) acc[k] = 0.f;
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float v[NV32];
+    float w = win[i];
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) {
+        v[k] = V[k * ldv + i];
+        w = fmaf(-v[k], hs[k], w);
+      }
+    wout[i] = w;
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) acc[k] = fmaf(v[k], w, acc[k]);
+  }
+  block_reduce_store<NV32>(acc, nv, part);
+}
+
+__global__ void __launch_bounds__(BT) axpy_nrm_f32_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                          const double* __restrict__ h, float* __restrict__ w,
+                                                          int64_t n, double* __restrict__ part) {
+  __shared__ float hs[NV32];
+  if (threadIdx.x < NV32) hs[threadIdx.x] = (threadIdx.x < nv) ? (float)h[threadIdx.x] : 0.f;
+  __syncthreads();
+  float acc[1] = {0.f};
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float x = w[i];
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) x = fmaf(-V[k * ldv + i], hs[k], x);
+    w[i] = x;
+    acc[0] = fmaf(x, x, acc[0]);
+  }
+  block_reduce_store<1>(acc, 1, part);
+}
+
+__global__ void normalize_f32_kernel(const float* __restrict__ w, const double* __restrict__ nsq,
+                                     float* __restrict__ v, int64_t n) {
+  const float inv = (float)(1.0 / sqrt(*nsq));
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) v[i] = w[i] * inv;
+}
+
+template <int MM>
+__global__ void __launch_bounds__(BT) rotate_f32_kernel(float* __restrict__ V, int64_t ldv, int m,
+                                                        const double* __restrict__ Y, int k, int64_t n) {
+  __shared__ float Ys[MM * MM];
+  for (int t = threadIdx.x; t < m * k; t += BT) Ys[t] = (float)Y[t];
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float row[MM];
+#pragma unroll
+    for (int j = 0; j < MM; ++j) row[j] = (j < m) ? V[j * ldv + i] : 0.f;
+#pragma unroll
+    for (int c = 0; c < MM; ++c) {
+      if (c < k) {
+        float acc = 0.f;
+#pragma unroll
+        for (int j = 0; j < MM; ++j)
+          if (j < m) acc = fmaf(row[j], Ys[c * m + j], acc);
+        V[c * ldv + i] = acc;
+      }
+    }
+  }
+}
+
+template <int MM>
+__global__ void __launch_bounds__(BT) combine_f32_f64_kernel(const float* __restrict__ V, int64_t ldv, int m,
+                                                             const double* __restrict__ Y, int k,
+                                                             double* __restrict__ out, int64_t ldo, int64_t n) {
+  __shared__ double Ys[MM * MM];
+  for (int t = threadIdx.x; t < m * k; t += BT) Ys[t] = Y[t];
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float row[MM];
+#pragma unroll
+    for (int j = 0; j < MM; ++j) row[j] = (j < m) ? V[j * ldv + i] : 0.f;
+    for (int c = 0; c < k; ++c) {
+      double acc = 0.0;
+#pragma unroll
+      for (int j = 0; j < MM; ++j)
+        if (j < m) acc = fma((double)row[j], Ys[c * m + j], acc);
+      out[c * ldo + i] = acc;
+    }
+  }
+}
+
+__global__ void uniform_f32_kernel(float* __restrict__ v, int64_t n, uint64_t seed) {
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    uint64_t r = splitmix64(seed * 0x100000001b3ull + (uint64_t)i);
+    v[i] = (float)((double)(r >> 11) * (1.0 / 9007199254740992.0));
+  }
+}
+
+__global__ void nrm_f32_kernel(const float* __restrict__ w, int64_t n, double* __restrict__ part) {
+  float acc[1] = {0.f};
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) acc[0] = fmaf(w[i], w[i], acc[0]);
+  block_reduce_store<1>(acc, 1, part);
+}
+
 }  // namespace
+
+void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
+              cudaStream_t s) {
+  if (nv > NV32) fail(TM_ERR_LIMIT, "mdot_f32: too many vectors");
+  int nb = red_blocks(n);
+  mdot_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, w, n, part);
+  TM_CKK("mdot_f32");
+  mdot_final<<<nv, 256, 0, s>>>(part, nb, nv, NV32, h);
+  TM_CKK("mdot_final");
+}
+
+void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const float* win, float* wout, int64_t n,
+                  double* h2, double* part, cudaStream_t s) {
+  if (nv > NV32) fail(TM_ERR_LIMIT, "axpy_dot_f32: too many vectors");
+  int nb = red_blocks(n);
+  axpy_dot_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+  TM_CKK("axpy_dot_f32");
+  mdot_final<<<nv, 256, 0, s>>>(part, nb, nv, NV32, h2);
+  TM_CKK("mdot_final");
+}
+
+void axpy_nrm_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, double* nsq,
+                  double* part, cudaStream_t s) {
+  if (nv > NV32) fail(TM_ERR_LIMIT, "axpy_nrm_f32: too many vectors");
+  int nb = red_blocks(n);
+  axpy_nrm_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, w, n, part);
+  TM_CKK("axpy_nrm_f32");
+  mdot_final<<<1, 256, 0, s>>>(part, nb, 1, 1, nsq);
+  TM_CKK("mdot_final");
+}
+
+void normalize_f32(const float* w, const double* nsq, float* v, int64_t n, cudaStream_t s) {
+  normalize_f32_kernel<<<red_blocks(n), BT, 0, s>>>(w, nsq, v, n);
+  TM_CKK("normalize_f32");
+}
+
+void rotate_f32(float* V, int64_t ldv, int m, const double* Y, int k, int64_t n, cudaStream_t s) {
+  if (m <= 16)
+    rotate_f32_kernel<16><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, n);
+  else if (m <= 32)
+    rotate_f32_kernel<32><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, n);
+  else
+    fail(TM_ERR_LIMIT, "rotate_f32: basis too large");
+  TM_CKK("rotate_f32");
+}
+
+void combine_f32_f64(const float* V, int64_t ldv, int m, const double* Y, int k, double* out, int64_t ldo, int64_t n,
+                     cudaStream_t s) {
+  if (m <= 16)
+    combine_f32_f64_kernel<16><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  else if (m <= 32)
+    combine_f32_f64_kernel<32><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  else
+    fail(TM_ERR_LIMIT, "combine_f32_f64: basis too large");
+  TM_CKK("combine_f32_f64");
+}
+
+void fill_uniform_f32(float* v, int64_t n, uint64_t seed, cudaStream_t s) {
+  uniform_f32_kernel<<<red_blocks(n), BT, 0, s>>>(v, n, seed);
+  TM_CKK("uniform_f32");
+}
+
+void nrm2sq_f32(const float* w, int64_t n, double* out, double* part, cudaStream_t s) {
+  int nb = red_blocks(n);
+  nrm_f32_kernel<<<nb, BT, 0, s>>>(w, n, part);
+  TM_CKK("nrm_f32");
+  mdot_final<<<1, 256, 0, s>>>(part, nb, 1, 1, out);
+  TM_CKK("mdot_final");
+}
 
 static void mdot_impl(const double* V, int64_t ldv, int nv, const double* w, const float* w32, double scale,
                       int64_t n, double* h, double* part, cudaStream_t s) {

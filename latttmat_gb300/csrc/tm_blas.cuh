@@ -35,6 +35,30 @@ void fill_uniform(double* v, int64_t n, uint64_t seed, cudaStream_t s);
 // count of non-finite entries (device counter)
 void count_nonfinite(const double* v, int64_t n, unsigned int* cnt_dev, cudaStream_t s);
 
+// ---- FP32-basis Krylov kernels (nv <= 16): FP32 data, per-thread FP32
+// partial sums, FP64 block/global reductions.
+constexpr int NV32 = 16;
+// h[k] = sum_i V[k][i] w[i]
+void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
+              cudaStream_t s);
+// wout = win - V h ; h2[k] = sum_i V[k][i] wout[i]   (one pass)
+void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const float* win, float* wout, int64_t n,
+                  double* h2, double* part, cudaStream_t s);
+// w -= V h (in place) ; nsq = ||w||^2   (one pass)
+void axpy_nrm_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, double* nsq,
+                  double* part, cudaStream_t s);
+// v = w / sqrt(*nsq)
+void normalize_f32(const float* w, const double* nsq, float* v, int64_t n, cudaStream_t s);
+// V[:, 0..k) = V[:, 0..m) Y in place (FP32 storage), m <= 32
+void rotate_f32(float* V, int64_t ldv, int m, const double* Y, int k, int64_t n, cudaStream_t s);
+// out64[:, 0..k) = V32[:, 0..m) Y  (FP64 accumulation), m <= 32
+void combine_f32_f64(const float* V, int64_t ldv, int m, const double* Y, int k, double* out, int64_t ldo, int64_t n,
+                     cudaStream_t s);
+// uniform(0,1) FP32 start vector
+void fill_uniform_f32(float* v, int64_t n, uint64_t seed, cudaStream_t s);
+// ||w||^2 of an FP32 vector (FP64 result on device)
+void nrm2sq_f32(const float* w, int64_t n, double* out, double* part, cudaStream_t s);
+
 // small dense symmetric eigenproblem on device (one warp, cyclic Jacobi, m <= 48):
 // A (m x m column-major, symmetric) -> eigenvalues w[m], eigenvectors Z (m x m, column-major)
 // (lda = leading dimension of A)

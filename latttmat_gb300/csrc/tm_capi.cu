@@ -61,6 +61,7 @@ double matvec_aux(const Op& op, const T* x, T* y, bool scaled, cudaStream_t s);
 tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode, double* vals,
                         double* vecs_host, tm_eigs_info* info_out);
 void observables(const Op& op, const double* ql, const double* qr, double* sums /* 12 */);
+void adjoint_grad(const Op& op, const double* qr_h, const double* ql_h, double lam, double grad[4]);
 tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode,
                         std::vector<std::complex<double>>& vals, std::vector<double>* vr, std::vector<double>* vi,
                         tm_eigs_info* info_out);
@@ -600,7 +601,11 @@ tm_status tm_profile_matvec(const tm_op* op, tm_dtype dt, int iters, double* ms_
 
 tm_status tm_grad(const tm_op* op, const double* qr, const double* ql, double lambda_internal, double grad4[4]) {
   TM_API_BEGIN
-  fail(TM_ERR_UNSUPPORTED, "adjoint not available yet");
+  if (!op || !qr || !grad4) fail(TM_ERR_ARG, "null argument");
+  if (!(lambda_internal != 0.0) || !std::isfinite(lambda_internal)) fail(TM_ERR_ARG, "eigenvalue must be finite, nonzero");
+  const Op& b = op->impl->parent ? *op->impl->parent : *op->impl;
+  if (!b.symmetric && !ql) fail(TM_ERR_ARG, "general operators need the left eigenvector");
+  adjoint_grad(b, qr, b.symmetric ? nullptr : ql, lambda_internal, grad4);
   TM_API_END
 }
 

@@ -94,6 +94,7 @@ namespace {
 struct EOArgs {
   int m, c, n, p;       // tile bits, cluster bits, local bits, thread bits
   int ng;               // H elements
+  int64_t n_orep;       // pass-1 tiles (row length of the transposed w1)
   float a32, b32;       // normalised butterfly coefficients
   double a64, b64;
 };
@@ -200,12 +201,15 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const T* __restric
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A);
-  T* wrow = w1 + (tile << A.m) + ((int64_t)rank << n);
+  // w1 is stored transposed, w1[e][tile]: pass 2 then reads, for one e-tile,
+  // only the rows of that tile's H-orbit of e (each row read by one tile).
+  T* wcol = w1 + tile + (((int64_t)rank << n) * A.n_orep);
   if (A.c == 0) {
-    for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) wrow[j] = sm[spad(j)];
+    for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) wcol[(int64_t)j * A.n_orep] = sm[spad(j)];
   } else {
     cl.sync();
-    for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) wrow[j] = cluster_combine<T>(cl, sm, rank, j, A);
+    for (int j = threadIdx.x; j < (1 << n); j += blockDim.x)
+      wcol[(int64_t)j * A.n_orep] = cluster_combine<T>(cl, sm, rank, j, A);
     cl.sync();
   }
 }
@@ -239,7 +243,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
         int j = threadIdx.x + (i << p);
         uint32_t o = ((uint32_t)rank << n) | (uint32_t)j;
         uint32_t code = __ldg(t2 + o);
-        v[i] = w1[((int64_t)(code >> 8) << A.m) + he[code & 255u]];
+        v[i] = w1[(int64_t)he[code & 255u] * A.n_orep + (code >> 8)];
       }
     }
     reg_bfly<T, KB>(v, kb, ca<T>(A), cb<T>(A));
@@ -559,6 +563,7 @@ EOArgs make_args(const Op& op, int c) {
   A.p = A.n - kb;
   if (A.p > 10) A.p = 10;
   A.ng = op.eo.ng;
+  A.n_orep = op.eo.n_orep;
   const double K = op.mp.betaJ;
   double ea = std::exp(K), eb = std::exp(-K);
   A.a64 = ea / (ea + eb);

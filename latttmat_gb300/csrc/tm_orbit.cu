@@ -205,6 +205,30 @@ void build_orbit_table(Op& op) {
   TM_CK(cudaStreamSynchronize(op.stream));
 }
 
+// state -> rank map for operators built without one (the even/odd plan frees
+// its rank structure): rebuild the representative bitset and prefix in
+// temporaries, then map every state.
+void ensure_state_map(Op& op) {
+  if (op.smap.p) return;
+  if (op.L > 30) fail(TM_ERR_LIMIT, "full-space state map limited to L <= 30");
+  GroupDev g = to_dev(op.grp);
+  const uint64_t nstate = 1ull << op.L;
+  const int64_t nwords = (int64_t)((nstate + 31) / 32);
+  DBuf bits, pre;
+  bits.alloc(nwords * 4);
+  pre.alloc(nwords * 4);
+  int blocks = (int)std::min<int64_t>((nwords * 32 + 255) / 256, (int64_t)num_sms() * 64);
+  rep_bits_kernel<<<blocks, 256, 0, op.stream>>>(g, nstate, bits.as<uint32_t>(), pre.as<uint32_t>(), nwords);
+  TM_CKK("rep_bits");
+  exclusive_scan_u32(pre.as<uint32_t>(), pre.as<uint32_t>(), nwords, op.stream);
+  op.smap.alloc(nstate * sizeof(uint32_t));
+  int mb = (int)std::min<int64_t>((int64_t)(nstate + 255) / 256, (int64_t)num_sms() * 32);
+  state_map_kernel<<<mb, 256, 0, op.stream>>>(g, nstate, bits.as<uint32_t>(), pre.as<uint32_t>(),
+                                              op.smap.as<uint32_t>());
+  TM_CKK("state_map");
+  TM_CK(cudaStreamSynchronize(op.stream));
+}
+
 void build_state_map(Op& op) {
   GroupDev g = to_dev(op.grp);
   const uint64_t nstate = 1ull << op.L;

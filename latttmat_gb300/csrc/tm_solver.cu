@@ -227,6 +227,152 @@ struct Lanczos {
   }
 };
 
+__global__ void hcol32_kernel(double* H, int ld, int j, const double* h1, const double* h2, const double* nsq,
+                              double S) {
+  int i = threadIdx.x;
+  if (i <= j) {
+    double v = S * (h1[i] + h2[i]);
+    H[i + j * ld] = v;
+    H[j + i * ld] = v;
+  }
+  if (i == 0) {
+    double b = S * sqrt(*nsq);
+    H[(j + 1) + j * ld] = b;
+    H[j + (j + 1) * ld] = b;
+  }
+}
+
+// FP32-basis thick-restart Lanczos for the FP32 phase of mixed precision
+// (ncv <= 16).  The matvec returns y = T v / S; CGS2 runs on y with FP32
+// data and FP64 reductions, and S is folded into H, so no large factor ever
+// enters FP32 storage.  Sweeps over the basis per step: dots, fused
+// update+dots, fused update+norm (3 instead of 4).
+struct Lanczos32 {
+  const Op& op;
+  cudaStream_t s;
+  int64_t n;
+  int m;
+  DBuf V, W, Y, h1, h2, part, nsq, Hd, wd, Zd, Ysel;
+  int matvecs = 0, restarts = 0;
+  bool stagnation_stop = true;
+
+  Lanczos32(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), m(ncv) {
+    V.alloc((size_t)(m + 1) * n * 4);
+    W.alloc((size_t)n * 4);
+    Y.alloc((size_t)n * 4);
+    h1.alloc(64 * 8);
+    h2.alloc(64 * 8);
+    part.alloc((size_t)num_sms() * 4 * 16 * 8 + 64);
+    nsq.alloc(8);
+    Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
+    wd.alloc(64 * 8);
+    Zd.alloc(64 * 64 * 8);
+    Ysel.alloc(64 * 64 * 8);
+  }
+  float* v(int j) const { return V.as<float>() + (int64_t)j * n; }
+
+  void start(uint64_t seed) {
+    TM_CK(cudaMemsetAsync(Hd.p, 0, (size_t)(m + 1) * (m + 1) * 8, s));
+    fill_uniform_f32(W.as<float>(), n, seed, s);
+    nrm2sq_f32(W.as<float>(), n, nsq.as<double>(), part.as<double>(), s);
+    normalize_f32(W.as<float>(), nsq.as<double>(), v(0), n, s);
+  }
+
+  void step(int j) {
+    double S = apply_internal(op, nullptr, nullptr, v(j), Y.as<float>(), true, s);
+    ++matvecs;
+    mdot_f32(v(0), n, j + 1, Y.as<float>(), n, h1.as<double>(), part.as<double>(), s);
+    axpy_dot_f32(v(0), n, j + 1, h1.as<double>(), Y.as<float>(), W.as<float>(), n, h2.as<double>(),
+                 part.as<double>(), s);
+    axpy_nrm_f32(v(0), n, j + 1, h2.as<double>(), W.as<float>(), n, nsq.as<double>(), part.as<double>(), s);
+    hcol32_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m + 1, j, h1.as<double>(), h2.as<double>(), nsq.as<double>(), S);
+    TM_CKK("hcol32");
+    normalize_f32(W.as<float>(), nsq.as<double>(), v(j + 1), n, s);
+  }
+
+  Lanczos::CycleResult project() {
+    small_symeig(Hd.as<double>(), m, wd.as<double>(), Zd.as<double>(), s, m + 1);
+    Lanczos::CycleResult r;
+    std::vector<double> th(m), H((size_t)(m + 1) * (m + 1));
+    r.Z.resize((size_t)m * m);
+    TM_CK(cudaMemcpyAsync(th.data(), wd.p, m * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(r.Z.data(), Zd.p, (size_t)m * m * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaMemcpyAsync(H.data(), Hd.p, H.size() * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+    r.beta = H[m + (size_t)(m - 1) * (m + 1)];
+    r.order.resize(m);
+    std::iota(r.order.begin(), r.order.end(), 0);
+    std::stable_sort(r.order.begin(), r.order.end(),
+                     [&](int a, int b) { return std::fabs(th[a]) > std::fabs(th[b]); });
+    for (int i = 0; i < m; ++i) {
+      int c = r.order[i];
+      r.theta.push_back(th[c]);
+      r.resid.push_back(std::fabs(r.beta * r.Z[(size_t)c * m + (m - 1)]));
+    }
+    return r;
+  }
+
+  std::vector<double> ysel(const Lanczos::CycleResult& r, int k) const {
+    std::vector<double> Y((size_t)m * k);
+    for (int c = 0; c < k; ++c)
+      for (int j = 0; j < m; ++j) Y[(size_t)c * m + j] = r.Z[(size_t)r.order[c] * m + j];
+    return Y;
+  }
+
+  void restart(const Lanczos::CycleResult& r, int k) {
+    std::vector<double> Yh = ysel(r, k);
+    TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
+    rotate_f32(V.as<float>(), n, m, Ysel.as<double>(), k, n, s);
+    TM_CK(cudaMemcpyAsync(v(k), v(m), (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0);
+    for (int i = 0; i < k; ++i) {
+      H[i + (size_t)i * (m + 1)] = r.theta[i];
+      double cpl = r.beta * r.Z[(size_t)r.order[i] * m + (m - 1)];
+      H[k + (size_t)i * (m + 1)] = cpl;
+      H[i + (size_t)k * (m + 1)] = cpl;
+    }
+    TM_CK(cudaMemcpyAsync(Hd.p, H.data(), H.size() * 8, cudaMemcpyHostToDevice, s));
+    ++restarts;
+  }
+
+  // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k
+  void ritz_f64(const Lanczos::CycleResult& r, int k, double* out) {
+    std::vector<double> Yh = ysel(r, k);
+    TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
+    combine_f32_f64(V.as<float>(), n, m, Ysel.as<double>(), k, out, n, n, s);
+  }
+
+  template <class Conv>
+  Lanczos::CycleResult run(int nev, int max_cycles, Conv conv) {
+    int k = 0;
+    Lanczos::CycleResult r;
+    double best = 1e300;
+    int stall = 0;
+    for (int cyc = 0; cyc < max_cycles; ++cyc) {
+      for (int j = k; j < m; ++j) step(j);
+      r = project();
+      if (conv(r)) return r;
+      double worst = 0.0;
+      for (int i = 0; i < nev; ++i) worst = std::max(worst, r.resid[i] / std::fabs(r.theta[0]));
+      if (stagnation_stop) {
+        if (worst < 0.7 * best) {
+          best = worst;
+          stall = 0;
+        } else if (++stall >= 3 && worst < 1e-4) {
+          return r;
+        }
+      }
+      int nconv = 0;
+      for (int i = 0; i < nev; ++i)
+        if (r.resid[i] <= 2e-7 * std::fabs(r.theta[0])) ++nconv;
+      k = std::min(m - 2, std::max(nev + 1, nev + std::min(nconv, (m - nev) / 2)));
+      k = std::max(k, std::min(m - 2, (m + nev) / 2));
+      restart(r, k);
+    }
+    return r;
+  }
+};
+
 }  // namespace
 
 struct EigOut {
@@ -264,31 +410,46 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       // FP32 phase: Ritz residuals down to the FP32 floor (relative to the
       // dominant Ritz value), stopping early if they stagnate
       const double tol32 = std::max(tol, 2e-7);
-      lz.conv_tol = tol32;
-      lz.stagnation_stop = true;
-      r = lz.run(nev, true, 200, [&](const Lanczos::CycleResult& rr) {
+      const int nb0 = std::min(ncv - 1, nev);
+      auto conv32 = [&](const Lanczos::CycleResult& rr) {
         for (int i = 0; i < nev; ++i)
           if (rr.resid[i] > tol32 * std::fabs(rr.theta[0])) return false;
         return true;
-      }, &ok);
-      lz.stagnation_stop = false;
-      lz.rotate(r, nev);
-      double theta_next = (nev < (int)r.theta.size()) ? std::fabs(r.theta[nev]) : 0.0;
-      // FP64 refinement: Rayleigh-Ritz on B = [Ritz vectors], growing B by the
-      // orthonormalised residual block (a block-Davidson step) while the
-      // Kato-Temple bound ||r||^2/gap misses tol.  B lives in V's columns.
+      };
+      if (ncv <= NV32) {
+        // FP32 Krylov basis (half the bytes of the FP64 basis per sweep)
+        Lanczos32 l32(op, ncv, s);
+        l32.start(seed);
+        r = l32.run(nev, 200, conv32);
+        l32.ritz_f64(r, nb0, lz.v(0));
+        lz.matvecs += l32.matvecs;
+        lz.restarts += l32.restarts;
+      } else {
+        lz.conv_tol = tol32;
+        lz.stagnation_stop = true;
+        r = lz.run(nev, true, 200, conv32, &ok);
+        lz.stagnation_stop = false;
+        lz.rotate(r, nb0);
+      }
+      // FP64 refinement (block Davidson).  Rayleigh-Ritz on B = the nev FP32
+      // Ritz vectors with FP64 matvecs, FP64 residuals r_j of every Ritz pair;
+      // B grows by the orthonormalised residual block of the wanted pairs.  A
+      // wanted value is accepted, after at least one growth step, when its
+      // residual is well inside the gap to every other Ritz value of B
+      // (r_i <= gap_i / 100) and the Kato-Temple bound r_i^2 / gap_i meets
+      // tol.  B lives in V's columns.
       const int cap = ncv + 1;
       DBuf AB, XB, AXB, RB, G, Gw, Gz, th;
       AB.alloc((size_t)cap * n * 8);
-      XB.alloc((size_t)nev * n * 8);
-      AXB.alloc((size_t)nev * n * 8);
-      RB.alloc((size_t)nev * n * 8);
+      XB.alloc((size_t)cap * n * 8);
+      AXB.alloc((size_t)cap * n * 8);
+      RB.alloc((size_t)cap * n * 8);
       G.alloc((size_t)cap * cap * 8);
       Gw.alloc(64 * 8);
       Gz.alloc((size_t)64 * 64 * 8);
       th.alloc(64 * 8);
       double* B = lz.v(0);
-      int nb = nev, nnew = nev;
+      int nb = nb0, nnew = nb0;
       bool refined = false;
       std::vector<double> thv(nev);
       for (int round = 0; round < 4; ++round) {
@@ -307,38 +468,42 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         std::vector<int> ord(nb);
         std::iota(ord.begin(), ord.end(), 0);
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
-        std::vector<double> Y((size_t)nb * nev);
-        for (int c = 0; c < nev; ++c) {
-          thv[c] = gw[ord[c]];
+        std::vector<double> Y((size_t)nb * nb), tha(nb);
+        for (int c = 0; c < nb; ++c) {
+          tha[c] = gw[ord[c]];
           for (int j = 0; j < nb; ++j) Y[(size_t)c * nb + j] = gz[(size_t)ord[c] * nb + j];
         }
-        if (nb > nev) theta_next = std::min(theta_next > 0 ? theta_next : 1e300, std::fabs(gw[ord[nev]]));
+        for (int c = 0; c < nev; ++c) thv[c] = tha[c];
         TM_CK(cudaMemcpyAsync(lz.Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
-        TM_CK(cudaMemcpyAsync(th.p, thv.data(), nev * 8, cudaMemcpyHostToDevice, s));
-        basis_combine(B, n, nb, lz.Ysel.as<double>(), nev, XB.as<double>(), n, n, s);
-        basis_combine(AB.as<double>(), n, nb, lz.Ysel.as<double>(), nev, AXB.as<double>(), n, n, s);
-        resid_kernel<<<blocks_for(n), 256, 0, s>>>(AXB.as<double>(), XB.as<double>(), n, nev, th.as<double>(),
+        TM_CK(cudaMemcpyAsync(th.p, tha.data(), nb * 8, cudaMemcpyHostToDevice, s));
+        basis_combine(B, n, nb, lz.Ysel.as<double>(), nb, XB.as<double>(), n, n, s);
+        basis_combine(AB.as<double>(), n, nb, lz.Ysel.as<double>(), nb, AXB.as<double>(), n, n, s);
+        resid_kernel<<<blocks_for(n), 256, 0, s>>>(AXB.as<double>(), XB.as<double>(), n, nb, th.as<double>(),
                                                      RB.as<double>(), n);
         TM_CKK("resid");
-        std::vector<double> rn(nev);
-        for (int i = 0; i < nev; ++i) {
+        std::vector<double> rn(nb);
+        for (int i = 0; i < nb; ++i) {
           nrm2sq(RB.as<double>() + (int64_t)i * n, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
           TM_CK(cudaMemcpyAsync(&rn[i], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
         }
         TM_CK(cudaStreamSynchronize(s));
+        for (auto& x : rn) x = std::sqrt(std::max(x, 0.0));
         refined = true;
         max_resid = 0.0;
         for (int i = 0; i < nev; ++i) {
-          double res = std::sqrt(std::max(rn[i], 0.0));
-          double gap = std::fabs(std::fabs(thv[i]) - theta_next);
-          for (int j = 0; j < nev; ++j)
-            if (j != i) gap = std::min(gap, std::fabs(thv[i] - thv[j]));
-          double bound = res * res / std::max(gap, 1e-300);
-          max_resid = std::max(max_resid, res / std::fabs(thv[i]));
-          if (!(bound <= tol * std::fabs(thv[i]))) refined = false;
+          double gap = 1e300;
+          for (int j = 0; j < nb; ++j)
+            if (j != i) gap = std::min(gap, std::fabs(tha[i] - tha[j]));
+          const double res = rn[i];
+          max_resid = std::max(max_resid, res / std::fabs(tha[i]));
+          if (!(gap > 0.0 && res <= 0.01 * gap && res * res / gap <= tol * std::fabs(tha[i]))) refined = false;
         }
+        // at least one residual-block step before accepting: the residual of
+        // a Ritz vector points along any eigenvector the FP32 subspace missed
+        // next to it, so a missed neighbour shows up as a nearby Ritz value
+        if (round == 0) refined = false;
         if (refined || nb + nev > cap) break;
-        // append the residual block, orthonormalised against B (CGS2)
+        // append the wanted residual block, orthonormalised against B (CGS2)
         for (int i = 0; i < nev; ++i) {
           double* rv = RB.as<double>() + (int64_t)i * n;
           for (int pass = 0; pass < 2; ++pass) {

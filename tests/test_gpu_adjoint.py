@@ -1,0 +1,77 @@
+"""GPU: adjoint d ln(lambda)/d(betaJ, kappa, kappa2, h) against central finite
+differences (step 1e-5) of the GPU FP64 eigenvalues, and against the reference
+magnetisation moment: d ln(lambda0)/dh = -betaJ * L * <M>/L
+(TMat/tmatphys.cpp:13-38 with the field term of genTvec, TMat/tmat.hpp:213).
+Tolerances: 2e-6 relative to max(|grad|, 1) for the FD check (the FD error of
+1e-12-accurate eigenvalues at step 1e-5 is about 1e-7)."""
+import numpy as np
+import pytest
+
+import latttmat_gb300 as lt
+
+pytestmark = pytest.mark.gpu
+
+STEP = 1e-5
+# (model, dim, axialdir, extend_cond, betaJ, kappa, h, size, nev)
+POINTS = [
+    ("A", 2, 1, 0, 0.5, 0.3, 0.1, 10, 2),
+    ("A", 2, 5, 2, 0.4, 0.6, 0.0, 14, 2),
+    ("A", 2, 5, 0, 0.35, 0.55, 0.05, 16, 2),
+    ("A", 3, 1, 0, 0.25, 0.4, 0.0, (3, 4), 2),
+    ("A", 3, 1, 0, 0.3, 0.2, 0.05, (3, 3), 2),
+]
+
+
+def lam(model, dim, ax, ec, bj, k, h, size, nev, which=0):
+    op = lt.TMatOp(model, dim, ax, bj, k, h, size, 0.0, ec)
+    vals, vecs, _, _ = op.eigs(nev, tol=1e-13, mode=lt.TM_EIGS_F64, vectors=True)
+    return op, vals, vecs
+
+
+@pytest.mark.parametrize("pt", POINTS)
+def test_grad_vs_finite_differences(pt):
+    model, dim, ax, ec, bj, k, h, size, nev = pt
+    op, vals, vecs = lam(model, dim, ax, ec, bj, k, h, size, nev)
+    g = op.grad(vecs[0], vals[0] * op.getnormfactor())
+    params = [bj, k, 0.0, h]
+    for t in (0, 1, 3):
+        if t == 3 and h == 0.0 and ec == 0 and ax in (5, 13):
+            continue  # the flip-reduced sector is only defined at h = 0
+        if dim == 3 and t == 3 and h == 0.0:
+            continue
+        if t == 1 and k == 0.5:
+            continue
+        pp, pm = list(params), list(params)
+        pp[t] += STEP
+        pm[t] -= STEP
+        _, vp, _ = lam(model, dim, ax, ec, pp[0], pp[1], pp[3], size, nev)
+        _, vm, _ = lam(model, dim, ax, ec, pm[0], pm[1], pm[3], size, nev)
+        fd = (np.log(vp[0]) - np.log(vm[0])) / (2 * STEP)
+        assert abs(g[t] - fd) < 2e-6 * max(1.0, abs(fd)), (t, g[t], fd)
+
+
+@pytest.mark.parametrize("pt", [p for p in POINTS if p[0] == "A"])
+def test_field_derivative_equals_magnetisation(pt):
+    model, dim, ax, ec, bj, k, h, size, nev = pt
+    op, vals, vecs = lam(model, dim, ax, ec, bj, k, h, size, nev)
+    g = op.grad(vecs[0], vals[0] * op.getnormfactor())
+    q = vecs[0] / np.linalg.norm(vecs[0])
+    m, _ = op.moments(q)
+    L = op.getLayerSize()
+    assert g[3] == pytest.approx(-bj * L * m[0], rel=1e-9, abs=1e-10)
+
+
+def test_grad_xi_from_lambda1():
+    """d xi from lambda1's eigenpair: xi = 1/ln(lambda0/|lambda1|)."""
+    args = ("A", 2, 5, 2, 0.4, 0.6, 0.0, 14, 3)
+    op, vals, vecs = lam(*args)
+    nf = op.getnormfactor()
+    g0 = op.grad(vecs[0], vals[0] * nf)
+    g1 = op.grad(vecs[1], vals[1] * nf)
+    xi = 1.0 / np.log(vals[0] / abs(vals[1]))
+    dxi = -xi * xi * (g0[0] - g1[0])
+    _, vp, _ = lam("A", 2, 5, 2, 0.4 + STEP, 0.6, 0.0, 14, 3)
+    _, vm, _ = lam("A", 2, 5, 2, 0.4 - STEP, 0.6, 0.0, 14, 3)
+    xp = 1.0 / np.log(vp[0] / abs(vp[1]))
+    xm = 1.0 / np.log(vm[0] / abs(vm[1]))
+    assert dxi == pytest.approx((xp - xm) / (2 * STEP), rel=1e-5)

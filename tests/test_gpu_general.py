@@ -1,0 +1,52 @@
+"""GPU: general (non-symmetric) operators -- diagonal BNNNI full (ZBT) and
+reduced (ZBM) -- transpose products, complex-capable eigenvalues and the left
+eigenvector from the transpose solve, against the reference's own outputs."""
+import numpy as np
+import pytest
+
+import latttmat_gb300 as lt
+from gpu_util import case_names, fixture, make_op, rel_err, seeded_input
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_eigs_match(vals, ref, rtol):
+    """Match as multisets: the order inside a complex-conjugate pair (equal
+    modulus) is a convention, not part of the result."""
+    for z in ref:
+        err = np.min(np.abs(vals - z)) / abs(z)
+        assert err < rtol, (z, vals)
+    for z in vals:
+        assert np.min(np.abs(ref - z)) / abs(z) < rtol, (z, ref)
+
+
+@pytest.mark.parametrize("name", case_names(["zbt", "zbm"]))
+def test_transpose_product(name):
+    f = fixture(name)
+    op = make_op(name)
+    t = op.get_t_instance()
+    x = seeded_input(op.rows(), 1)
+    yt = t.perform_op(x)
+    assert rel_err(yt, f["yt"]) < 1e-12
+    # <y, T x> == <T^T y, x>
+    z = seeded_input(op.rows(), 2)
+    assert np.dot(z, op.perform_op(x)) == pytest.approx(np.dot(t.perform_op(z), x), rel=1e-11)
+
+
+@pytest.mark.parametrize("mode", [lt.TM_EIGS_F64, lt.TM_EIGS_MIXED])
+@pytest.mark.parametrize("name", case_names(["zbt", "zbm"]))
+def test_general_eigenvalues_and_left_vector(name, mode):
+    f = fixture(name)
+    op = make_op(name)
+    nev = len(f["evals_re"])
+    vals, vecs, vecl, info = op.eigs(nev, tol=1e-12, mode=mode, vectors=True, left=True)
+    ref = f["evals_re"] + 1j * f["evals_im"]
+    assert_eigs_match(vals, ref, 1e-10)
+    q = np.real(vecs[0])
+    q = q / np.linalg.norm(q) * np.sign(q.sum())
+    assert rel_err(q, f["q0"]) < 1e-6
+    ql = vecl / np.linalg.norm(vecl) * np.sign(vecl.sum())
+    assert rel_err(ql, f["ql"]) < 1e-6
+    m, st = op.moments(ql, q)
+    np.testing.assert_allclose(m, f["moments"], rtol=1e-6, atol=1e-9)
+    assert st == int(f["moments_status"])
