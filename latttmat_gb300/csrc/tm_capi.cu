@@ -69,6 +69,23 @@ tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
 static bool is_reduced(int kind) { return kind == K_XAM || kind == K_XDM || kind == K_ZBM || kind == K_XAM3; }
 static bool bfly_core(int kind) { return kind == K_XAT || kind == K_XAM || kind == K_XAM3; }
 
+void matvec_eo_df(const Op& op, const double* x, double* y, cudaStream_t s);
+double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
+                      cudaStream_t s);
+
+// FP64-accurate product for the solver's refinement steps: double-float
+// arithmetic on the FP32 pipes for the even/odd operators (GB300's FP64 rate
+// is a small fraction of its FP32 rate), native FP64 otherwise.
+void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s) {
+  const Op& base = op.parent ? *op.parent : op;
+  if (base.eo.active) {
+    matvec_eo_df(base, x, y, s);
+    const_cast<Op&>(op).matvecs++;
+  } else {
+    apply_internal(op, x, y, nullptr, nullptr, false, s);
+  }
+}
+
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s) {
   const Op& base = op.parent ? *op.parent : op;
@@ -80,6 +97,9 @@ double apply_internal(const Op& op, const double* x, double* y, const float* x32
     } else {
       matvec_eo<double>(base, x, y, false, s);
     }
+  } else if (is_two_layer(base.kind)) {
+    if (f32) fail(TM_ERR_UNSUPPORTED, "two-layer operators run in FP64 only");
+    matvec_two_layer(op, x, y, s);
   } else if (bfly_core(base.kind)) {
     S = f32 ? matvec_bfly<float>(base, x32, y32, true, s) : matvec_bfly<double>(base, x, y, false, s);
   } else {
@@ -93,7 +113,10 @@ double apply_internal(const Op& op, const double* x, double* y, const float* x32
 void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStream_t s) {
   const Op& base = op.parent ? *op.parent : op;
   const int64_t n = base.n;
-  if (!base.has_pi) {
+  if (is_two_layer(base.kind)) {
+    if (dt != TM_F64) fail(TM_ERR_UNSUPPORTED, "two-layer operators run in FP64 only");
+    matvec_two_layer(op, (const double*)x, (double*)y, s);
+  } else if (!base.has_pi) {
     if (dt == TM_F64) {
       if (base.eo.active) {
         matvec_eo<double>(base, (const double*)x, (double*)y, false, s);
@@ -164,6 +187,25 @@ static void set_normfactor(Op& op) {
       op.nfexp = (k < 0.5) ? L * (k - 3.0) : -L * (k + 2.0);
       op.normfactor = std::exp(bj * op.nfexp);
       break;
+    case K_YAT:  // TMat/tmat.cpp:186-193
+      op.normfactor = (k < 0.5) ? std::exp(L * bj * (k - 2.0)) : std::exp(-L * bj * (k + 1.0));
+      break;
+    case K_Y2AT:  // TMat/tmat.cpp:256-263
+      op.normfactor = (k < 0.5) ? std::exp(2 * L * bj * (k - 2.0)) : std::exp(-2 * L * bj * (k + 1.0));
+      break;
+    case K_YAM:  // TMat/tmatreduce.cpp:683-717
+      if (!op.ltype)
+        op.nfexp = (k < 0.5) ? L * (k - 2.0) : -L * (k + 1.0);
+      else if (k + k2 < 0.5)
+        op.nfexp = L * 2.0 * (k + k2 - 1.0);
+      else if (k < 0.5 && k2 - k < 0.5)
+        op.nfexp = -L;
+      else if (k2 < 2 * k)
+        op.nfexp = -L * 2.0 * k;
+      else
+        op.nfexp = L * 2.0 * (k - k2);
+      op.normfactor = std::exp(bj * op.nfexp);
+      break;
   }
 }
 
@@ -171,6 +213,10 @@ void build_aux(Op& op);  // aux-bit cores (DNNI, diagonal BNNNI)
 
 static void build_op(Op& op) {
   set_normfactor(op);
+  if (is_two_layer(op.kind)) {
+    build_two_layer(op);
+    return;
+  }
   op.nstate = 1ll << op.L;
   if (is_reduced(op.kind)) {
     build_orbit_table(op);
@@ -241,6 +287,9 @@ static Op* create_op(const tm_params* p, char model, int dim, int axialdir, int 
       case 19: case 20: op->kind = K_XAT; op->boundary = (axialdir & 1) ? 13 : 17; break;
       case 5: reduced_x2d(K_XAM, ec & 1, h0 && !(ec & 2)); break;
       case 13: reduced_x2d(K_XAM, 1, h0 && !(ec & 2)); break;
+      case 0: op->kind = K_Y2AT; op->symmetric = 0; break;
+      case 2: op->kind = K_YAT; op->symmetric = 0; break;
+      case 6: op->kind = K_YAM; op->symmetric = 0; op->censym = h0 && !(ec & 2); break;
       default: fail(TM_ERR_UNSUPPORTED, "model A dim 2 axialdir " + std::to_string(axialdir) + " not provided");
     }
   } else if (model == 'A' && dim == 3) {
@@ -272,6 +321,12 @@ static Op* create_op(const tm_params* p, char model, int dim, int axialdir, int 
         op->grp.L = op->L;
         op->grp.periodic = 1;
         op->grp.flip = op->censym;
+        break;
+      case 6:  // YBMMatVecProd2D = YAMMatVecProd2D(extend_cond | 16) (TMat/tmatreduce.cpp:1018-1021)
+        op->kind = K_YAM;
+        op->ltype = 1;
+        op->symmetric = 0;
+        op->censym = h0 && !(ec & 2);
         break;
       default: fail(TM_ERR_UNSUPPORTED, "model B axialdir " + std::to_string(axialdir) + " not provided");
     }
@@ -420,6 +475,7 @@ tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, 
   if (mode != TM_EIGS_F64 && mode != TM_EIGS_MIXED) fail(TM_ERR_ARG, "unknown mode");
   const Op& o = *op->impl;
   const Op& b = o.parent ? *o.parent : o;
+  if (is_two_layer(b.kind)) mode = TM_EIGS_F64;  // FP64 products only
   tm_status st = TM_OK;
   if (!b.symmetric) {
     // general operator (TMat/pfunc.hpp:84-98 GenEigsSolver path)
@@ -496,7 +552,11 @@ tm_status tm_moments(const tm_op* op, const double* ql, const double* qr, double
   observables(b, ql, qr, sums);
   // sums: 0..3 = sum w m^k, 4 = sum w, 5 = sum w nnode, 6 = sum w nnode^2, 7..10 DNNI stripes
   const int L = b.L;
-  if (b.symmetric) {
+  if (b.kind == K_Y2AT) {
+    // Y2ATMatVecProd2D::moments is not implemented there (TMat/tmat.cpp:309-314)
+    for (int k = 0; k < 4; ++k) out4[k] = 0.0;
+    if (ref_status) *ref_status = -1;
+  } else if (b.symmetric) {
     for (int k = 0; k < 4; ++k) out4[k] = sums[k] / L;
     if (ref_status) *ref_status = 0;
   } else {

@@ -1,0 +1,57 @@
+// Double-float ("float-float") arithmetic for FP64-accurate products on the
+// FP32 pipes.
+//
+// A value is hi + lo with |lo| <= ulp(hi)/2 (about 48 significant bits).
+// Addition uses Knuth's TwoSum, multiplication the FMA-based TwoProduct,
+// each followed by a fast renormalisation (Dekker 1971; Knuth, TAOCP vol. 2,
+// sec. 4.2.2).  On GB300 the FP32 pipes are roughly 64x faster than FP64,
+// so a double-float butterfly (about 20 FP32 operations per output) beats a
+// native FP64 one several times over, at relative error ~1e-14 per sweep.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace ltm {
+
+struct __align__(8) dfloat {
+  float hi, lo;
+  __host__ __device__ dfloat() {}
+  __host__ __device__ dfloat(int v) : hi((float)v), lo(0.f) {}
+  __host__ __device__ dfloat(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ dfloat(double v) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+  }
+  __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ dfloat df_renorm(float s, float e) {
+  float h = s + e;
+  return dfloat(h, e - (h - s));
+}
+
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  return df_renorm(s, e);
+}
+
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_renorm(p, e);
+}
+
+__device__ __forceinline__ dfloat& operator+=(dfloat& a, dfloat b) {
+  a = a + b;
+  return a;
+}
+__device__ __forceinline__ dfloat& operator*=(dfloat& a, dfloat b) {
+  a = a * b;
+  return a;
+}
+
+}  // namespace ltm

@@ -33,6 +33,7 @@
 #include <cstring>
 #include <vector>
 
+#include "tm_df.cuh"
 #include "tm_group.cuh"
 #include "tm_internal.h"
 
@@ -113,6 +114,10 @@ template <>
 __device__ __forceinline__ float cb<float>(const EOArgs& A) { return A.b32; }
 template <>
 __device__ __forceinline__ double cb<double>(const EOArgs& A) { return A.b64; }
+template <>
+__device__ __forceinline__ dfloat ca<dfloat>(const EOArgs& A) { return dfloat(A.a64); }
+template <>
+__device__ __forceinline__ dfloat cb<dfloat>(const EOArgs& A) { return dfloat(A.b64); }
 
 // in-register butterflies over the 2^NB elements held by one thread
 template <class T, int NB>
@@ -172,9 +177,11 @@ __device__ __forceinline__ T cluster_combine(cg::cluster_group& cl, T* sm, int r
 }
 
 // pass 1: w1[t][e] = (Th_E v)[(e, o_rep(t))],  v[(e,o_rep)] = u[map1[t][e]]
-template <class T, int KB>
-__global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const T* __restrict__ u,
+// (InT: element type of u; T: arithmetic / storage type of the tile and w1)
+template <class T, int KB, class InT>
+__global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restrict__ u,
                                                     const uint32_t* __restrict__ map1,
+                                                    const uint32_t* __restrict__ colmap,
                                                     T* __restrict__ w1) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const T* __restric
     for (int i = 0; i < (1 << KB); ++i) {
       if (i < (1 << kb)) {
         int j = threadIdx.x + (i << p);
-        v[i] = u[__ldg(mrow + j)];
+        v[i] = T(u[__ldg(mrow + j)]);
       }
     }
     reg_bfly<T, KB>(v, kb, ca<T>(A), cb<T>(A));
@@ -201,29 +208,33 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const T* __restric
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A);
-  // w1 is stored transposed, w1[e][tile]: pass 2 then reads, for one e-tile,
-  // only the rows of that tile's H-orbit of e (each row read by one tile).
-  T* wcol = w1 + tile + (((int64_t)rank << n) * A.n_orep);
-  if (A.c == 0) {
-    for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) wcol[(int64_t)j * A.n_orep] = sm[spad(j)];
-  } else {
-    cl.sync();
-    for (int j = threadIdx.x; j < (1 << n); j += blockDim.x)
-      wcol[(int64_t)j * A.n_orep] = cluster_combine<T>(cl, sm, rank, j, A);
-    cl.sync();
+  // Output.  w1 is stored transposed with class-sorted rows: e goes to row
+  // colmap[e] (every H-class of e one contiguous block of rows), column
+  // `tile`.  Pass 2 then reads its whole input as one contiguous block of
+  // |class| rows.  The column writes of concurrently running tiles fill
+  // adjacent words of each row, which L2 merges into full sectors.
+  T* wcol = w1 + tile;
+  if (A.c > 0) cl.sync();
+  for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) {
+    T val = (A.c == 0) ? sm[spad(j)] : cluster_combine<T>(cl, sm, rank, j, A);
+    uint32_t row = __ldg(colmap + (((uint32_t)rank << n) | (uint32_t)j));
+    wcol[(int64_t)row * A.n_orep] = val;
   }
+  if (A.c > 0) cl.sync();
 }
 
 // pass 2: z[(e_rep, o)] = (Th_O w)[(e_rep, o)]; emit designated outputs
-template <class T, int KB, bool F64SCALE>
+// (OutT: element type of y)
+template <class T, int KB, bool F64SCALE, class OutT>
 __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restrict__ w1,
                                                     const uint32_t* __restrict__ t2,
                                                     const uint32_t* __restrict__ erep,
+                                                    const uint32_t* __restrict__ colmap,
                                                     const uint32_t* __restrict__ out_off,
                                                     const uint16_t* __restrict__ out_o,
                                                     const double* __restrict__ sout64,
                                                     const float* __restrict__ sout32, double post,
-                                                    T* __restrict__ y) {
+                                                    OutT* __restrict__ y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   __shared__ uint32_t he[128];
@@ -233,7 +244,8 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
   const int n = A.n, p = A.p;
   const int kb = n - p;
   const uint32_t e_rep = erep[tile];
-  for (int g = threadIdx.x; g < A.ng; g += blockDim.x) he[g] = act_e(g, e_rep, A.m);
+  // w1 rows of this tile's H-class (one contiguous block of rows)
+  for (int g = threadIdx.x; g < A.ng; g += blockDim.x) he[g] = __ldg(colmap + act_e(g, e_rep, A.m));
   __syncthreads();
   {
     T v[1 << KB];
@@ -261,9 +273,9 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
     int j = out_o[k] & lmask;
     T val = (A.c == 0) ? sm[spad(j)] : cluster_combine<T>(cl, sm, rank, j, A);
     if (F64SCALE)
-      y[k] = (T)((double)val * sout64[k] * post);
+      y[k] = (OutT)((double)val * sout64[k] * post);
     else
-      y[k] = val * (T)sout32[k];
+      y[k] = (OutT)(val * T(sout32[k]));
   }
   if (A.c > 0) cl.sync();
 }
@@ -419,6 +431,20 @@ void build_eo_plan(Op& op) {
   }
   std::vector<uint32_t> t2(M);
   for (uint32_t o = 0; o < M; ++o) t2[o] = (otile[orep[o]] << 8) | (uint32_t)og[o];
+  // w1 column order: the H-class of each e-representative as one contiguous
+  // block (members ascending), classes in representative order
+  std::vector<uint32_t> colmap(M, 0xffffffffu);
+  {
+    uint32_t pos = 0;
+    for (uint32_t er : elist) {
+      std::vector<uint32_t> mem;
+      for (int g = 0; g < P.ng; ++g) mem.push_back(act_e(g, er, m));
+      std::sort(mem.begin(), mem.end());
+      mem.erase(std::unique(mem.begin(), mem.end()), mem.end());
+      for (uint32_t e : mem) colmap[e] = pos++;
+    }
+    if (pos != M) fail(TM_ERR_ARG, "even/odd plan: H-classes do not cover the even patterns");
+  }
   P.n_orep = (int)olist.size();
   P.n_erep = (int)elist.size();
   P.c32 = cluster_bits_for(m, 4);
@@ -430,6 +456,8 @@ void build_eo_plan(Op& op) {
   d_etile.alloc(M * 4);
   P.t2.alloc(M * 4);
   P.erep.alloc(elist.size() * 4);
+  P.colmap.alloc(M * 4);
+  TM_CK(cudaMemcpyAsync(P.colmap.p, colmap.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_olist.p, olist.data(), olist.size() * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_etile.p, etile.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.t2.p, t2.data(), M * 4, cudaMemcpyHostToDevice, s));
@@ -510,10 +538,24 @@ __global__ void eo_scale_in(const T* __restrict__ x, const double* __restrict__ 
   }
 }
 
+// element types around each engine: FP32 and FP64 read and write their own
+// type; double-float reads and writes FP64
+template <class T>
+struct EoIO {
+  using In = T;
+  using Out = T;
+};
+template <>
+struct EoIO<dfloat> {
+  using In = double;
+  using Out = double;
+};
+
 template <class T, int KB>
-void launch_pass1(const EOArgs& A, int ntiles, const T* u, const uint32_t* map1, T* w1, cudaStream_t s) {
+void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, const uint32_t* map1,
+                  const uint32_t* colmap, T* w1, cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
-  auto kfn = eo_pass1<T, KB>;
+  auto kfn = eo_pass1<T, KB, typename EoIO<T>::In>;
   TM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
@@ -527,14 +569,15 @@ void launch_pass1(const EOArgs& A, int ntiles, const T* u, const uint32_t* map1,
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, map1, w1));
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, map1, colmap, w1));
 }
 
 template <class T, int KB, bool F64S>
 void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, const uint32_t* off,
-                  const double* sout64, const float* sout32, double post, T* y, cudaStream_t s) {
+                  const double* sout64, const float* sout32, double post, typename EoIO<T>::Out* y,
+                  cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
-  auto kfn = eo_pass2<T, KB, F64S>;
+  auto kfn = eo_pass2<T, KB, F64S, typename EoIO<T>::Out>;
   TM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
@@ -548,8 +591,8 @@ void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, con
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.t2.as<uint32_t>(), P.erep.as<uint32_t>(), off,
-                           P.out_o.as<uint16_t>(), sout64, sout32, post, y));
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.t2.as<uint32_t>(), P.erep.as<uint32_t>(),
+                           P.colmap.as<uint32_t>(), off, P.out_o.as<uint16_t>(), sout64, sout32, post, y));
 }
 
 template <class T>
@@ -574,16 +617,18 @@ EOArgs make_args(const Op& op, int c) {
 }
 
 template <class T, int KB>
-void eo_dispatch(const Op& op, const EOArgs& A, const T* x, T* y, bool scaled32, cudaStream_t s) {
+void eo_dispatch(const Op& op, const EOArgs& A, const typename EoIO<T>::In* x, typename EoIO<T>::Out* y,
+                 bool scaled32, cudaStream_t s) {
+  using In = typename EoIO<T>::In;
   const EOPlan& P = op.eo;
   const int64_t R = op.n;
-  T* u = static_cast<T*>(op.ws_c.p);
-  T* w1 = (sizeof(T) == 8) ? P.w1_64.as<T>() : P.w1_32.as<T>();
+  In* u = static_cast<In*>(op.ws_c.p);
+  T* w1 = (sizeof(T) == 8) ? static_cast<T*>(P.w1_64.p) : static_cast<T*>(P.w1_32.p);
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[0], s));
-  eo_scale_in<T><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R);
+  eo_scale_in<In><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R);
   TM_CKK("eo_scale_in");
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[1], s));
-  launch_pass1<T, KB>(A, P.n_orep, u, P.map1.as<uint32_t>(), w1, s);
+  launch_pass1<T, KB>(A, P.n_orep, u, P.map1.as<uint32_t>(), P.colmap.as<uint32_t>(), w1, s);
   TM_CKK("eo_pass1");
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[2], s));
   const uint32_t* off = (sizeof(T) == 8) ? P.out_off.as<uint32_t>() : P.out_off32.as<uint32_t>();
@@ -596,12 +641,9 @@ void eo_dispatch(const Op& op, const EOArgs& A, const T* x, T* y, bool scaled32,
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[3], s));
 }
 
-}  // namespace
-
-// y = T x in pi order.  scaled32: FP32 result divided by (e^K+e^-K)^L (the
-// solver applies that factor in FP64).
 template <class T>
-void matvec_eo(const Op& op, const T* x, T* y, bool scaled32, cudaStream_t s) {
+void matvec_eo_engine(const Op& op, const typename EoIO<T>::In* x, typename EoIO<T>::Out* y, bool scaled32,
+                      cudaStream_t s) {
   const int c = (sizeof(T) == 8) ? op.eo.c64 : op.eo.c32;
   EOArgs A = make_args<T>(op, c);
   int kb = A.n - A.p;
@@ -610,12 +652,31 @@ void matvec_eo(const Op& op, const T* x, T* y, bool scaled32, cudaStream_t s) {
     case 2: eo_dispatch<T, 2>(op, A, x, y, scaled32, s); break;
     case 3: eo_dispatch<T, 3>(op, A, x, y, scaled32, s); break;
     case 4: eo_dispatch<T, 4>(op, A, x, y, scaled32, s); break;
-    default: eo_dispatch<T, 5>(op, A, x, y, scaled32, s); break;
+    default:
+      if constexpr (sizeof(T) == 4)
+        eo_dispatch<T, 5>(op, A, x, y, scaled32, s);
+      else
+        fail(TM_ERR_LIMIT, "even/odd tile too large for the 8-byte engines");
+      break;
   }
+}
+
+}  // namespace
+
+// y = T x in pi order.  scaled32: FP32 result divided by (e^K+e^-K)^L (the
+// solver applies that factor in FP64).
+template <class T>
+void matvec_eo(const Op& op, const T* x, T* y, bool scaled32, cudaStream_t s) {
+  matvec_eo_engine<T>(op, x, y, scaled32, s);
 }
 
 template void matvec_eo<float>(const Op&, const float*, float*, bool, cudaStream_t);
 template void matvec_eo<double>(const Op&, const double*, double*, bool, cudaStream_t);
+
+// FP64 in/out, double-float arithmetic (the solver's refinement products)
+void matvec_eo_df(const Op& op, const double* x, double* y, cudaStream_t s) {
+  matvec_eo_engine<dfloat>(op, x, y, false, s);
+}
 
 double eo_scale32(const Op& op) {
   return std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);

@@ -31,7 +31,8 @@ inline GroupDev to_dev(const GroupDesc& g) {
   d.periodic = g.periodic;
   d.flip = g.flip;
   d.rotate = g.rotate;
-  d.mask = (g.L >= 64) ? ~0ull : ((1ull << g.L) - 1);
+  const int nb = g.nbits ? g.nbits : g.L;
+  d.mask = (nb >= 64) ? ~0ull : ((1ull << nb) - 1);
   return d;
 }
 
@@ -86,6 +87,23 @@ TM_HD void for_each_image(const GroupDev& g, uint64_t s, F&& f) {
         if (!f(~r & mask)) return;
       }
     }
+  } else if (g.kind == G_Y2D) {
+    // two-layer states (left layer in the high L bits): translations and
+    // reflection of both layers at once (x flip of both), the orbit walk of
+    // genY2DDuplist (TMat/tmatreduce.cpp:113-240)
+    const uint64_t lm = (1ull << g.L) - 1;
+    const uint64_t hi = s >> g.L, lo = s & lm;
+    for (int k = 0; k < g.L; ++k) {
+      const uint64_t ah = rotr(hi, g.L, k), al = rotr(lo, g.L, k);
+      const uint64_t a = ah << g.L | al;
+      const uint64_t b = brev(ah, g.L) << g.L | brev(al, g.L);
+      if (!f(a)) return;
+      if (!f(b)) return;
+      if (g.flip) {
+        if (!f(~a & mask)) return;
+        if (!f(~b & mask)) return;
+      }
+    }
   } else if (g.kind == G_X3D) {
     for (int rr = 0; rr <= g.rotate; ++rr) {
       uint64_t s0 = rr ? rotate3d(s, g.size1) : s;
@@ -116,6 +134,7 @@ TM_HD int group_order(const GroupDev& g) {
     case G_X2D: return (g.periodic ? 2 * g.L : 2) * (g.flip ? 2 : 1);
     case G_Z2D: return (g.periodic ? 2 * ((g.L & 1) ? g.L : g.L / 2) : 2) * (g.flip ? 2 : 1);
     case G_X3D: return g.size1 * g.size2 * 4 * (g.flip ? 2 : 1) * (g.rotate ? 2 : 1);
+    case G_Y2D: return 2 * g.L * (g.flip ? 2 : 1);
   }
   return 1;
 }

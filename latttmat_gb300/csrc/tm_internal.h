@@ -49,10 +49,15 @@ enum Kind {
   K_ZBT = 4,   // ZBTMatVecProd2D: full diagonal BNNNI (TMat/tmat.cpp:480-662)
   K_ZBM = 5,   // ZBMMatVecProd2D: reduced diagonal BNNNI (TMat/tmatreduce.cpp:1403-1868)
   K_XAM3 = 6,  // XAMMatVecProd3D: reduced 3D ANNNI (TMat/tmat3d.cpp:102-340)
+  K_YAT = 7,   // YATMatVecProd2D (+_T): full two-layer y-ANNNI (TMat/tmat.cpp:106-242)
+  K_Y2AT = 8,  // Y2ATMatVecProd2D: full two-layer y2-ANNNI (TMat/tmat.cpp:245-315)
+  K_YAM = 9,   // YAMMatVecProd2D (+_T) / YBMMatVecProd2D: reduced two-layer (TMat/tmatreduce.cpp:661-1021)
 };
 
+inline bool is_two_layer(int kind) { return kind == K_YAT || kind == K_Y2AT || kind == K_YAM; }
+
 // Orbit-group families (which symmetry group the reduced basis uses)
-enum GroupKind { G_NONE = 0, G_X2D = 1, G_Z2D = 2, G_X3D = 3 };
+enum GroupKind { G_NONE = 0, G_X2D = 1, G_Z2D = 2, G_X3D = 3, G_Y2D = 4 };
 
 // Parameters of the group acting on L-bit states
 struct GroupDesc {
@@ -62,6 +67,7 @@ struct GroupDesc {
   int periodic = 1;          // 0: open boundary (X/Z: identity + reflection only)
   int flip = 0;              // spin-flip (censym) included
   int rotate = 0;            // 3D 90-degree rotation included
+  int nbits = 0;             // state bits when not L (two-layer states: 2L)
   int order() const;         // number of enumerated group elements
 };
 
@@ -76,6 +82,7 @@ struct EOPlan {
   DBuf map1;          // u32 [n_orep][2^m]: pi-index of the orbit of (e, o_rep)
   DBuf t2;            // u32 [2^m]: (o-tile << 8) | g  mapping o -> its pass-1 tile
   DBuf erep;          // u32 [n_erep]: e representative of each pass-2 tile
+  DBuf colmap;        // u32 [2^m]: column of even pattern e in w1 (H-classes of e contiguous)
   DBuf out_off;       // u32 [n_erep*(2^c)+1]: designated-output offsets per tile part
   DBuf out_o;         // u16 [R]: o of each designated output (pi order)
   DBuf out_off32;     // offsets for the FP32 cluster split
@@ -125,6 +132,12 @@ struct Op {
   DBuf hx, hy;            // device copies for host-vector matvecs
   DBuf xp, yp;            // permuted vectors for the reference-order entry
   double scale32 = 1.0;   // FP32 matvec output scale (applied in FP64)
+
+  // two-layer operators
+  int ltype = 0;          // 1: YBMMatVecProd2D (all-frustrated layer Tvec)
+  DBuf swp;               // u32 [n]: index of the layer-swapped orbit
+  DBuf bstart;            // u32 [nblocks+1]: representative blocks sharing the left layer
+  int nblocks = 0;
 };
 
 // ---------------------------------------------------------------- builders
@@ -133,6 +146,9 @@ void build_orbit_table(Op& op);          // idx, dup (reference order)
 void build_tvec(Op& op);                 // Tvec for the operator
 void build_state_map(Op& op);            // smap for the generic reduced path
 void build_eo_plan(Op& op);              // even/odd plan for K_XAM
+void build_two_layer(Op& op);            // tables of K_YAT / K_Y2AT / K_YAM
+// y = T x (or T^T x for a transposed view) of a two-layer operator, FP64
+void matvec_two_layer(const Op& op, const double* x, double* y, cudaStream_t s);
 
 // ---------------------------------------------------------------- matvec
 // y = T x in the operator's internal order (pi order when has_pi), on stream.

@@ -16,7 +16,7 @@ namespace {
 constexpr int NS = 11;
 
 __global__ void obs_kernel(const double* __restrict__ ql, const double* __restrict__ qr, int sym,
-                           const uint32_t* __restrict__ idx, int64_t n, int L, int open_bc,
+                           const uint32_t* __restrict__ idx, int64_t n, int L, int open_bc, int lshift,
                            double* __restrict__ part) {
   double acc[NS];
   for (int k = 0; k < NS; ++k) acc[k] = 0.0;
@@ -25,7 +25,8 @@ __global__ void obs_kernel(const double* __restrict__ ql, const double* __restri
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < n; i += st) {
-    uint64_t s = idx ? (uint64_t)idx[i] : (uint64_t)i;
+    // two-layer states: one layer's spins (lshift selects it)
+    uint64_t s = ((idx ? (uint64_t)idx[i] : (uint64_t)i) >> lshift) & mask;
     double w = sym ? ql[i] * ql[i] : ql[i] * qr[i];
     double m = (double)(2 * popc64(s) - L);
     double mk = m;
@@ -74,14 +75,19 @@ void observables(const Op& op, const double* ql, const double* qr, double* sums)
   }
   int nb = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 4));
   part.alloc((size_t)nb * NS * 8);
-  const bool reduced = (op.kind == K_XAM || op.kind == K_XDM || op.kind == K_ZBM || op.kind == K_XAM3);
+  const bool reduced =
+      (op.kind == K_XAM || op.kind == K_XDM || op.kind == K_ZBM || op.kind == K_XAM3 || op.kind == K_YAM);
+  // GenMatPhys::moments takes the low layer of the full two-layer state
+  // (TMat/tmatphys.cpp:71-98), YAMMatVecProd2D::moments the left (high) layer
+  // of the representative (TMat/tmatreduce.cpp:878-905)
+  const int lshift = (op.kind == K_YAM) ? op.L : 0;
   // nnode boundary: the MatPhys boundary_cond each reference class passes
   // (XAT: its boundary case; XAM: extend_cond & 1; XDT, XDM: 0)
   int open_bc = 0;
   if (op.kind == K_XAT) open_bc = op.boundary != 0;
   if (op.kind == K_XAM) open_bc = op.boundary != 0;
   obs_kernel<<<nb, 256, 0, s>>>(dl.as<double>(), qrd, op.symmetric, reduced ? op.idx.as<uint32_t>() : nullptr,
-                                n, op.L, open_bc, part.as<double>());
+                                n, op.L, open_bc, lshift, part.as<double>());
   TM_CKK("obs");
   std::vector<double> h((size_t)nb * NS);
   TM_CK(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, s));

@@ -179,7 +179,7 @@ int num_sms() {
 // prefix) in ws_a / ws_b for the map builders that follow.
 void build_orbit_table(Op& op) {
   GroupDev g = to_dev(op.grp);
-  const uint64_t nstate = 1ull << op.L;
+  const uint64_t nstate = 1ull << (op.grp.nbits ? op.grp.nbits : op.L);
   const int64_t nwords = (int64_t)((nstate + 31) / 32);
   op.ws_a.alloc(nwords * sizeof(uint32_t));  // bits
   op.ws_b.alloc(nwords * sizeof(uint32_t));  // counts -> prefix

@@ -31,8 +31,12 @@ namespace ltm {
 // T x = S * y32 (S returned).
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s);
+void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s);
 
 namespace {
+
+// growth steps of the FP64 block refinement before falling back to FP64 Lanczos
+constexpr int kRefineRounds = 6;
 
 __global__ void hcol_kernel(double* H, int ld, int j, const double* h1, const double* h2, const double* nsq,
                             int write_beta) {
@@ -61,6 +65,13 @@ __global__ void resid_kernel(const double* __restrict__ W, const double* __restr
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < n; i += st)
     for (int c = 0; c < k; ++c) R[c * ld + i] = W[c * ld + i] - theta[c] * X[c * ld + i];
+}
+
+// y = S * y32 (an FP32 product that was computed divided by S)
+__global__ void f32_scaled_kernel(const float* __restrict__ y32, double S, double* __restrict__ y, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) y[i] = S * (double)y32[i];
 }
 
 int blocks_for(int64_t n) {
@@ -410,7 +421,7 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       // FP32 phase: Ritz residuals down to the FP32 floor (relative to the
       // dominant Ritz value), stopping early if they stagnate
       const double tol32 = std::max(tol, 2e-7);
-      const int nb0 = std::min(ncv - 1, nev);
+      const int nb0 = std::max(nev, ncv - 1);
       auto conv32 = [&](const Lanczos::CycleResult& rr) {
         for (int i = 0; i < nev; ++i)
           if (rr.resid[i] > tol32 * std::fabs(rr.theta[0])) return false;
@@ -422,6 +433,17 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         l32.start(seed);
         r = l32.run(nev, 200, conv32);
         l32.ritz_f64(r, nb0, lz.v(0));
+        // the FP32 basis is orthonormal to FP32 accuracy only: re-orthonormalise
+        // the FP64 Ritz block (CGS2) so Rayleigh-Ritz is a standard eigenproblem
+        for (int i = 0; i < nb0; ++i) {
+          double* bi = lz.v(i);
+          for (int pass = 0; pass < 2 && i > 0; ++pass) {
+            mdot(lz.v(0), n, i, bi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+            maxpy(lz.v(0), n, i, lz.h1.as<double>(), bi, n, s);
+          }
+          nrm2sq(bi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+          normalize(bi, lz.nsq.as<double>(), bi, nullptr, n, s);
+        }
         lz.matvecs += l32.matvecs;
         lz.restarts += l32.restarts;
       } else {
@@ -431,35 +453,89 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         lz.stagnation_stop = false;
         lz.rotate(r, nb0);
       }
-      // FP64 refinement (block Davidson).  Rayleigh-Ritz on B = the nev FP32
-      // Ritz vectors with FP64 matvecs, FP64 residuals r_j of every Ritz pair;
-      // B grows by the orthonormalised residual block of the wanted pairs.  A
-      // wanted value is accepted, after at least one growth step, when its
-      // residual is well inside the gap to every other Ritz value of B
-      // (r_i <= gap_i / 100) and the Kato-Temple bound r_i^2 / gap_i meets
-      // tol.  B lives in V's columns.
-      const int cap = ncv + 1;
-      DBuf AB, XB, AXB, RB, G, Gw, Gz, th;
-      AB.alloc((size_t)cap * n * 8);
-      XB.alloc((size_t)cap * n * 8);
-      AXB.alloc((size_t)cap * n * 8);
-      RB.alloc((size_t)cap * n * 8);
-      G.alloc((size_t)cap * cap * 8);
-      Gw.alloc(64 * 8);
-      Gz.alloc((size_t)64 * 64 * 8);
-      th.alloc(64 * 8);
-      double* B = lz.v(0);
-      int nb = nb0, nnew = nb0;
-      bool refined = false;
+      // FP64 refinement: block Davidson with mixed-precision products.  B
+      // starts as the FP32 phase's Ritz vectors; the nev wanted ones get
+      // FP64-accurate products (apply_refine), the others FP32 products, and
+      // each growth step appends the wanted residual block, again with FP32
+      // products.  An FP32 product error reaches a Ritz pair only through the
+      // pair's weight on that column, which is at the FP32 noise level for
+      // the wanted pairs, so Rayleigh-Ritz values and residual estimates stay
+      // FP64-accurate.  The extra Ritz vectors carry the eigenvectors next to
+      // the wanted ones, which residual blocks alone resolve slowly.  When the
+      // estimates meet tol, the wanted Ritz vectors get FP64-accurate products
+      // and are accepted on the test of the FP64 Lanczos path and of Spectra's
+      // SymEigsSolver: ||A x - theta x|| <= tol * |theta|.
+      const int nx = nb0;
+      const int cap = nx + 2 * nev;
+      DBuf Bb, AB, XB, AXB, G, Gw, Gz, th;
       std::vector<double> thv(nev);
-      for (int round = 0; round < 4; ++round) {
-        for (int i = nb - nnew; i < nb; ++i) {
-          apply_internal(op, B + (int64_t)i * n, AB.as<double>() + (int64_t)i * n, nullptr, nullptr, false, s);
-          ++lz.matvecs;
-          ++lz.matvecs64;
+      bool refined = false;
+      // cluster guard: FP32 Ritz values closer than 1e-5 (relative) cannot be
+      // told apart from FP32-accurate vectors; solve those (and operators too
+      // small for a block of cap columns) in FP64 directly
+      bool cluster = (int64_t)cap * 4 > n;
+      for (int i = 0; i < nev && i + 1 < (int)r.theta.size(); ++i)
+        if (std::fabs(r.theta[i] - r.theta[i + 1]) < 1e-5 * std::fabs(r.theta[i])) cluster = true;
+      if (!cluster) {
+        Bb.alloc((size_t)cap * n * 8);
+        AB.alloc((size_t)cap * n * 8);
+        XB.alloc((size_t)cap * n * 8);
+        AXB.alloc((size_t)cap * n * 8);
+        G.alloc((size_t)cap * cap * 8);
+        Gw.alloc(64 * 8);
+        Gz.alloc((size_t)64 * 64 * 8);
+        th.alloc(64 * 8);
+      }
+      double* B = Bb.as<double>();
+      auto col = [&](const DBuf& b, int j) { return b.as<double>() + (int64_t)j * n; };
+      auto prod32 = [&](const double* x, double* y) {
+        lz.ensure32();
+        to_f32(x, lz.x32.as<float>(), n, s);
+        const double S = apply_internal(op, nullptr, nullptr, lz.x32.as<float>(), lz.y32.as<float>(), true, s);
+        f32_scaled_kernel<<<blocks_for(n), 256, 0, s>>>(lz.y32.as<float>(), S, y, n);
+        TM_CKK("f32_scaled");
+        ++lz.matvecs;
+      };
+      auto prod64 = [&](const double* x, double* y) {
+        apply_refine(op, x, y, s);
+        ++lz.matvecs;
+        ++lz.matvecs64;
+      };
+      auto norm_host = [&](const double* v) {
+        double q = 0.0;
+        nrm2sq(v, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        TM_CK(cudaStreamSynchronize(s));
+        return std::sqrt(std::max(q, 0.0));
+      };
+      // imp[j]: weight of column j on FP32-product columns (0: FP64-accurate)
+      std::vector<double> imp(cap, 1.0);
+      int nb = nx, verified = 0;
+      if (!cluster) {
+        TM_CK(cudaMemcpyAsync(B, lz.v(0), (size_t)nx * n * 8, cudaMemcpyDeviceToDevice, s));
+        for (int j = 0; j < nx; ++j) {
+          if (j < nev) {
+            prod64(B + (int64_t)j * n, col(AB, j));
+            imp[j] = 0.0;
+          } else {
+            prod32(B + (int64_t)j * n, col(AB, j));
+          }
         }
-        for (int i = 0; i < nb; ++i)
-          mdot(B, n, nb, AB.as<double>() + (int64_t)i * n, n, G.as<double>() + (int64_t)i * nb, lz.part.as<double>(), s);
+      }
+      for (int round = 0; round < kRefineRounds && !cluster; ++round) {
+        // G(i, j) = B_i . (A B_j), symmetrised from the side whose product is
+        // the more accurate one
+        for (int j = 0; j < nb; ++j)
+          mdot(B, n, nb, col(AB, j), n, G.as<double>() + (int64_t)j * nb, lz.part.as<double>(), s);
+        std::vector<double> gh((size_t)nb * nb), gs((size_t)nb * nb);
+        TM_CK(cudaMemcpyAsync(gh.data(), G.p, gh.size() * 8, cudaMemcpyDeviceToHost, s));
+        TM_CK(cudaStreamSynchronize(s));
+        for (int j = 0; j < nb; ++j)
+          for (int i = 0; i < nb; ++i) {
+            const double gij = gh[(size_t)j * nb + i], gji = gh[(size_t)i * nb + j];
+            gs[(size_t)j * nb + i] = imp[j] < imp[i] ? gij : imp[i] < imp[j] ? gji : 0.5 * (gij + gji);
+          }
+        TM_CK(cudaMemcpyAsync(G.p, gs.data(), gs.size() * 8, cudaMemcpyHostToDevice, s));
         small_symeig(G.as<double>(), nb, Gw.as<double>(), Gz.as<double>(), s, nb);
         std::vector<double> gw(nb), gz((size_t)nb * nb);
         TM_CK(cudaMemcpyAsync(gw.data(), Gw.p, nb * 8, cudaMemcpyDeviceToHost, s));
@@ -468,53 +544,97 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         std::vector<int> ord(nb);
         std::iota(ord.begin(), ord.end(), 0);
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
-        std::vector<double> Y((size_t)nb * nb), tha(nb);
+        std::vector<double> Y((size_t)nb * nb), tha(nb), impn(nb, 0.0);
         for (int c = 0; c < nb; ++c) {
           tha[c] = gw[ord[c]];
-          for (int j = 0; j < nb; ++j) Y[(size_t)c * nb + j] = gz[(size_t)ord[c] * nb + j];
+          for (int j = 0; j < nb; ++j) {
+            const double y = gz[(size_t)ord[c] * nb + j];
+            Y[(size_t)c * nb + j] = y;
+            impn[c] += y * y * imp[j];
+          }
         }
-        for (int c = 0; c < nev; ++c) thv[c] = tha[c];
         TM_CK(cudaMemcpyAsync(lz.Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
-        TM_CK(cudaMemcpyAsync(th.p, tha.data(), nb * 8, cudaMemcpyHostToDevice, s));
         basis_combine(B, n, nb, lz.Ysel.as<double>(), nb, XB.as<double>(), n, n, s);
         basis_combine(AB.as<double>(), n, nb, lz.Ysel.as<double>(), nb, AXB.as<double>(), n, n, s);
-        resid_kernel<<<blocks_for(n), 256, 0, s>>>(AXB.as<double>(), XB.as<double>(), n, nb, th.as<double>(),
-                                                     RB.as<double>(), n);
+        // thick restart on the leading Ritz pairs; the wanted residual block
+        // goes to the columns after them
+        const int keep = std::min(nb, cap - nev);
+        TM_CK(cudaMemcpyAsync(B, XB.p, (size_t)keep * n * 8, cudaMemcpyDeviceToDevice, s));
+        TM_CK(cudaMemcpyAsync(AB.p, AXB.p, (size_t)keep * n * 8, cudaMemcpyDeviceToDevice, s));
+        for (int c = 0; c < keep; ++c) imp[c] = impn[c];
+        TM_CK(cudaMemcpyAsync(th.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
+        resid_kernel<<<blocks_for(n), 256, 0, s>>>(AB.as<double>(), B, n, nev, th.as<double>(),
+                                                     B + (int64_t)keep * n, n);
         TM_CKK("resid");
-        std::vector<double> rn(nb);
-        for (int i = 0; i < nb; ++i) {
-          nrm2sq(RB.as<double>() + (int64_t)i * n, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-          TM_CK(cudaMemcpyAsync(&rn[i], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-        }
-        TM_CK(cudaStreamSynchronize(s));
-        for (auto& x : rn) x = std::sqrt(std::max(x, 0.0));
-        refined = true;
+        std::vector<double> rn(nev);
+        bool est_ok = true;
         max_resid = 0.0;
         for (int i = 0; i < nev; ++i) {
-          double gap = 1e300;
-          for (int j = 0; j < nb; ++j)
-            if (j != i) gap = std::min(gap, std::fabs(tha[i] - tha[j]));
-          const double res = rn[i];
-          max_resid = std::max(max_resid, res / std::fabs(tha[i]));
-          if (!(gap > 0.0 && res <= 0.01 * gap && res * res / gap <= tol * std::fabs(tha[i]))) refined = false;
+          thv[i] = tha[i];
+          rn[i] = norm_host(B + (int64_t)(keep + i) * n);
+          max_resid = std::max(max_resid, rn[i] / std::fabs(tha[i]));
+          if (!(rn[i] <= 0.5 * tol * std::fabs(tha[i]))) est_ok = false;
         }
-        // at least one residual-block step before accepting: the residual of
-        // a Ritz vector points along any eigenvector the FP32 subspace missed
-        // next to it, so a missed neighbour shows up as a nearby Ritz value
-        if (round == 0) refined = false;
-        if (refined || nb + nev > cap) break;
-        // append the wanted residual block, orthonormalised against B (CGS2)
-        for (int i = 0; i < nev; ++i) {
-          double* rv = RB.as<double>() + (int64_t)i * n;
-          for (int pass = 0; pass < 2; ++pass) {
-            mdot(B, n, nb, rv, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-            maxpy(B, n, nb, lz.h1.as<double>(), rv, n, s);
+        if (est_ok && verified < 3) {
+          // verification: FP64-accurate products of the wanted Ritz vectors,
+          // Rayleigh quotients and true residuals
+          ++verified;
+          bool ok_all = true;
+          max_resid = 0.0;
+          for (int i = 0; i < nev; ++i) {
+            double* xi = B + (int64_t)i * n;
+            double* axi = col(AB, i);
+            prod64(xi, axi);
+            imp[i] = 0.0;
+            double q = 0.0;
+            mdot(xi, n, 1, axi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+            TM_CK(cudaMemcpyAsync(&q, lz.h1.p, 8, cudaMemcpyDeviceToHost, s));
+            TM_CK(cudaStreamSynchronize(s));
+            thv[i] = q;
+            tha[i] = q;
           }
-          nrm2sq(rv, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-          normalize(rv, lz.nsq.as<double>(), B + (int64_t)nb * n, nullptr, n, s);
+          TM_CK(cudaMemcpyAsync(th.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
+          resid_kernel<<<blocks_for(n), 256, 0, s>>>(AB.as<double>(), B, n, nev, th.as<double>(),
+                                                       B + (int64_t)keep * n, n);
+          TM_CKK("resid");
+          for (int i = 0; i < nev; ++i) {
+            rn[i] = norm_host(B + (int64_t)(keep + i) * n);
+            max_resid = std::max(max_resid, rn[i] / std::fabs(thv[i]));
+            if (!(rn[i] <= tol * std::max(std::fabs(thv[i]), 1e-300))) ok_all = false;
+          }
+          if (ok_all) {
+            refined = true;
+            break;
+          }
+        }
+        if (round + 1 == kRefineRounds) break;
+        // orthonormalise the residual block against B (CGS2) and give it FP32
+        // products; a column that vanishes is dropped
+        nb = keep;
+        for (int i = 0; i < nev; ++i) {
+          double* rv = B + (int64_t)(keep + i) * n;
+          double* dst = B + (int64_t)nb * n;
+          if (dst != rv) TM_CK(cudaMemcpyAsync(dst, rv, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+          const double r0 = norm_host(dst);
+          for (int pass = 0; pass < 2; ++pass) {
+            mdot(B, n, nb, dst, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+            maxpy(B, n, nb, lz.h1.as<double>(), dst, n, s);
+          }
+          nrm2sq(dst, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+          double q = 0.0;
+          TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+          TM_CK(cudaStreamSynchronize(s));
+          if (!(q > 1e-24 * r0 * r0) || !(r0 > 0.0)) continue;
+          normalize(dst, lz.nsq.as<double>(), dst, nullptr, n, s);
+          prod32(dst, col(AB, nb));
+          imp[nb] = 1.0;
           ++nb;
         }
-        nnew = nev;
+      }
+      if (refined) TM_CK(cudaMemcpyAsync(XB.p, B, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      if (cluster) {
+        XB.alloc((size_t)nev * n * 8);
+        TM_CK(cudaMemcpyAsync(XB.p, lz.v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
       }
       // final Ritz vectors into V's leading columns
       TM_CK(cudaMemcpyAsync(lz.v(0), XB.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));

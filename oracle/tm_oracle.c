@@ -285,12 +285,75 @@ static void gen_x3d(int s1, int s2, int cen, int rotf, table_t* t) {
   free(buf.w);
 }
 
+/* genY2DDuplist, TMat/tmatreduce.cpp:113-240: orbits of two-layer states
+ * (left layer in the high L bits) under simultaneous translation, reflection
+ * and (cen) spin flip of both layers; dup = orbit size; swp[r] = index of the
+ * orbit holding the layer-swapped states of orbit r. */
+static st_t y_act(st_t s, int L, int t, int refl, int flip) {
+  st_t mask = (1ull << L) - 1, l = s >> L, r = s & mask;
+  if (refl) {
+    l = brev(l, L);
+    r = brev(r, L);
+  }
+  if (flip) {
+    l = ~l & mask;
+    r = ~r & mask;
+  }
+  return rotr(l, L, t) << L | rotr(r, L, t);
+}
+static st_t y_swap(st_t s, int L) { return (s & ((1ull << L) - 1)) << L | s >> L; }
+
+static int64_t lower_bound_u64(const st_t* a, int64_t n, st_t v) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) / 2;
+    if (a[mid] < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+static void gen_y2d(int L, int cen, table_t* t, int64_t** swp_out) {
+  st_t nstate = 1ull << (2 * L);
+  bits_t buf = bits_new(2 * L);
+  st_t* mins = NULL;
+  int64_t cap = 0;
+  for (st_t s = 0; s < nstate; ++s) {
+    if (bget(buf, s)) continue;
+    tpush(t, s);
+    if (t->n > cap) {
+      cap = t->cap;
+      mins = (st_t*)realloc(mins, cap * sizeof(st_t));
+    }
+    st_t m = y_swap(s, L);
+    uint16_t d = 0;
+    for (int f = 0; f <= cen; ++f)
+      for (int rf = 0; rf < 2; ++rf)
+        for (int sh = 0; sh < L; ++sh) {
+          st_t g = y_act(s, L, sh, rf, f);
+          if (!bget(buf, g)) {
+            bset(buf, g);
+            ++d;
+          }
+          st_t w = y_swap(g, L);
+          if (w < m) m = w;
+        }
+    t->dup[t->n - 1] = d;
+    mins[t->n - 1] = m;
+  }
+  int64_t* swp = (int64_t*)malloc(t->n * sizeof(int64_t));
+  for (int64_t r = 0; r < t->n; ++r) swp[r] = lower_bound_u64(t->idx, t->n, mins[r]);
+  *swp_out = swp;
+  free(mins);
+  free(buf.w);
+}
+
 /* ------------------------------------------------------------ operator */
-enum { O_XAT, O_XAM, O_XDT, O_XDM, O_ZBT, O_ZBM, O_X3D };
+enum { O_XAT, O_XAM, O_XDT, O_XDM, O_ZBT, O_ZBM, O_X3D, O_YAT, O_Y2AT, O_YAM };
 
 typedef struct orc_op {
-  int kind, L, s1, s2, bc, cen, nlead, rotf, sym, mphys_bc;
+  int kind, L, s1, s2, bc, cen, nlead, rotf, sym, mphys_bc, ltype;
   double bj, k, k2, h, nf;
+  int64_t* swp; /* two-layer reduced: index of the layer-swapped orbit */
   double b1[2], b2[2], b3[2], b2b[4], b2c[16];
   int64_t nstate, n;
   double* tvec;
@@ -364,6 +427,8 @@ static void set_nf(orc_op* o) {
     case O_XDT: o->nf = k < 0.5 ? exp(L * bj * 2.0 * (k - 1.0)) : exp(-L * bj * 2.0 * k); break;
     case O_XDM: nfe = k < 0.5 ? L * 2.0 * (k - 1.0) : -L * 2.0 * k; o->nf = exp(bj * nfe); break;
     case O_X3D: nfe = k < 0.5 ? L * (k - 3.0) : -L * (k + 2.0); o->nf = exp(bj * nfe); break;
+    case O_YAT: o->nf = k < 0.5 ? exp(L * bj * (k - 2.0)) : exp(-L * bj * (k + 1.0)); break;
+    case O_Y2AT: o->nf = k < 0.5 ? exp(2 * L * bj * (k - 2.0)) : exp(-2 * L * bj * (k + 1.0)); break;
     default: break;
   }
 }
@@ -420,6 +485,13 @@ orc_op* orc_create(char model, int dim, int ax, int ec, double bj, double k, dou
       int e = ax == 13 ? (ec | 1) : ec;
       o->bc = e & 1;
       o->cen = h0 && !(e & 2);
+    } else if (ax == 0 || ax == 2) {
+      o->kind = ax == 0 ? O_Y2AT : O_YAT;
+      o->sym = 0;
+    } else if (ax == 6) {
+      o->kind = O_YAM;
+      o->cen = h0 && !(ec & 2);
+      o->sym = 0;
     } else {
       free(o);
       return NULL;
@@ -444,6 +516,10 @@ orc_op* orc_create(char model, int dim, int ax, int ec, double bj, double k, dou
       o->kind = O_ZBT;
     } else if (ax == 7) {
       o->kind = O_ZBM;
+      o->cen = h0 && !(ec & 2);
+    } else if (ax == 6) {
+      o->kind = O_YAM;
+      o->ltype = 1;
       o->cen = h0 && !(ec & 2);
     } else {
       free(o);
@@ -564,6 +640,63 @@ orc_op* orc_create(char model, int dim, int ax, int ec, double bj, double k, dou
       }
       break;
     }
+    case O_YAT: {
+      /* YATMatVecProd2D::genTvec (TMat/tmat.hpp:361-366): the dense NN-only
+       * x-ANNNI matrix (TMat/tmat.cpp:668-684) flattened column-major: entry
+       * (row, col) = (low layer, high layer) */
+      o->nstate = 1ll << (2 * L);
+      o->n = o->nstate;
+      o->tvec = (double*)malloc(o->n * 8);
+      st_t mask = (1ull << L) - 1;
+#pragma omp parallel for
+      for (int64_t i = 0; i < o->n; ++i) {
+        st_t row = (st_t)i & mask, col = (st_t)i >> L;
+        o->tvec[i] = gen_tvec_xat(bj, 0.0, h, L, 0, row) * exp(bzexpn(L, nanti2(row, col), -bj));
+      }
+      break;
+    }
+    case O_Y2AT: {
+      /* Y2ATMatVecProd2D::genTvec (TMat/tmat.hpp:396-414), Tv^(1/2) */
+      o->nstate = 1ll << (2 * L);
+      o->n = o->nstate;
+      o->tvec = (double*)malloc(o->n * 8);
+      st_t mask = (1ull << L) - 1;
+      double J1 = -0.5 * bj, hJ = -0.5 * bj * h;
+      o->b2[0] = exp(-2.0 * bj * k);
+      o->b2[1] = 1.0 / o->b2[0];
+#pragma omp parallel for
+      for (int64_t i = 0; i < o->n; ++i) {
+        st_t lo = (st_t)i & mask, hi = (st_t)i >> L;
+        int n1 = nanti2(lo, rotr(lo, L, 1)), n2 = nanti2(hi, rotr(hi, L, 1)), n0 = nanti2(lo, hi);
+        int fa = 2 * (n1 + n2 + n0) - 3 * L, fb = 2 * (popc((st_t)i) - L);
+        o->tvec[i] = exp(J1 * fa + hJ * fb);
+      }
+      break;
+    }
+    case O_YAM: {
+      /* YAMMatVecProd2D ctor / genTvec / genTvec1 (TMat/tmatreduce.cpp:663-797);
+       * YBMMatVecProd2D is the layertype-1 form (:1018-1021) */
+      o->nstate = 1ll << (2 * L);
+      double nfe = o->ltype ? zb_nfexp(k, k2, L) : (k < 0.5 ? L * (k - 2.0) : -L * (k + 1.0));
+      o->nf = exp(bj * nfe);
+      gen_y2d(L, o->cen, &o->tab, &o->swp);
+      o->n = o->tab.n;
+      o->tvec = (double*)malloc(o->n * 8);
+      st_t mask = (1ull << L) - 1;
+      double hb = 0.5 * bj, J1 = -hb, hJ = -hb * h, Jn = hb * nfe, k1J = hb * k, k2J = hb * k2;
+#pragma omp parallel for
+      for (int64_t r = 0; r < o->n; ++r) {
+        st_t s = o->tab.idx[r], l = s >> L, rt = s & mask;
+        int n1 = nanti2(l, rotr(l, L, 1)), n2 = nanti2(l, rt), n0 = popc(l);
+        double bz = J1 * (2 * (n1 + n2 - L)) + hJ * (2 * n0 - L) + Jn;
+        if (o->ltype) {
+          int b1 = nanti2(l, rotr(l, L, 2)), d1 = nanti2(l, rotr(rt, L, 1)), d2 = nanti2(l, rotl(rt, L, 1));
+          bz += k1J * (2 * b1 - L) + k2J * (2 * (d1 + d2 - L));
+        }
+        o->tvec[r] = exp(bz) / sqrt((double)o->tab.dup[r]);
+      }
+      break;
+    }
   }
   return o;
 }
@@ -573,6 +706,7 @@ void orc_destroy(orc_op* o) {
   free(o->tvec);
   free(o->tab.idx);
   free(o->tab.dup);
+  free(o->swp);
   free(o);
 }
 int64_t orc_rows(const orc_op* o) { return o->n; }
@@ -1069,6 +1203,126 @@ static void op_zbm(const orc_op* o, const double* x, double* y, int dir) {
 }
 
 /* ------------------------------------------------------------ dispatch */
+/* in-place Kronecker of [[w0, w1], [w1, w0]] over bits [lo, lo+nb) of a
+ * vector of 2^nbits entries (TMat/tmatreduce.cpp:806-824 per bit) */
+static void kron_bits(double* v, int nbits, int lo, int nb, double w0, double w1) {
+  const int64_t n = 1ll << nbits;
+  for (int b = lo; b < lo + nb; ++b) {
+    const int64_t m = 1ll << b;
+#pragma omp parallel for if (n > 65536)
+    for (int64_t i = 0; i < n; ++i) {
+      if (i & m) continue;
+      double a = v[i], c = v[i | m];
+      v[i] = w0 * a + w1 * c;
+      v[i | m] = w1 * a + w0 * c;
+    }
+  }
+}
+
+/* YATMatVecProd2D::perform_op (TMat/tmat.cpp:213-242): the L shift-and-mix
+ * steps on the high layer amount to the Kronecker factor on the high L bits;
+ * then y[s] = nf * Tvec[s] * v[swap(s)].  dir=1: YATMatVecProd2D_T
+ * (TMat/tmat.cpp:141-173), the exact transpose: v = Kronecker on the low
+ * bits of Tvec .* x, y[swap(s)] = nf * v[s]. */
+static void op_yat(const orc_op* o, const double* x, double* y, int dir) {
+  const int L = o->L;
+  const int64_t n = o->n;
+  double* v = (double*)malloc(n * 8);
+  if (!dir) {
+    memcpy(v, x, n * 8);
+    kron_bits(v, 2 * L, L, L, o->b2[0], o->b2[1]);
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; ++i) y[i] = o->nf * o->tvec[i] * v[y_swap((st_t)i, L)];
+  } else {
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; ++i) v[i] = o->tvec[i] * x[i];
+    kron_bits(v, 2 * L, 0, L, o->b2[0], o->b2[1]);
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; ++i) y[y_swap((st_t)i, L)] = o->nf * v[i];
+  }
+  free(v);
+}
+
+/* Y2ATMatVecProd2D::perform_op (TMat/tmat.cpp:292-307).  One step of
+ * permute_mult_T1 (:275-289) mixes the bit pair (0, L) by a 4x4 matrix and
+ * rotates both layers; over L steps every pair (i, L+i) gets the same 4x4
+ * matrix once.  With p = (low bit a, high bit b), j = a^b:
+ *   out(p) = w1[j] (w2[0] in(p) + in(p ^ high)) + w1[j^1] (w2[1] in(p ^ both) + in(p ^ low)). */
+static void op_y2at(const orc_op* o, const double* x, double* y) {
+  const int L = o->L;
+  const int64_t n = o->n;
+  double* v = (double*)malloc(n * 8);
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; ++i) v[i] = o->tvec[i] * x[i];
+  for (int b = 0; b < L; ++b) {
+    const int64_t ml = 1ll << b, mh = 1ll << (L + b);
+#pragma omp parallel for if (n > 65536)
+    for (int64_t i = 0; i < n; ++i) {
+      if (i & (ml | mh)) continue;
+      double in[4], out[4];
+      for (int q = 0; q < 4; ++q) in[q] = v[i | ((q & 1) ? ml : 0) | ((q & 2) ? mh : 0)];
+      for (int p = 0; p < 4; ++p) {
+        int a = p & 1, bb = p >> 1, j = a ^ bb;
+        out[p] = o->b1[j] * (o->b2[0] * in[p] + in[p ^ 2]) + o->b1[j ^ 1] * (o->b2[1] * in[p ^ 3] + in[p ^ 1]);
+      }
+      for (int q = 0; q < 4; ++q) v[i | ((q & 1) ? ml : 0) | ((q & 2) ? mh : 0)] = out[q];
+    }
+  }
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; ++i) y[i] = o->nf * o->tvec[i] * v[i];
+  free(v);
+}
+
+/* YAMMatVecProd2D::perform_op (TMat/tmatreduce.cpp:827-876) and
+ * YAMMatVecProd2D_T::perform_op (:953-1016).  Per block of representatives
+ * sharing the left layer l: fill the right-layer vector at every image g(r)
+ * with g in the stabiliser of l, apply the Kronecker factor on the L right
+ * bits, and write each representative's entry to its layer-swapped orbit
+ * (dir=0) or to itself reading the swapped input (dir=1). */
+static void op_yam(const orc_op* o, const double* x, double* y, int dir) {
+  const int L = o->L;
+  const st_t mask = (1ull << L) - 1;
+  const int64_t R = o->n;
+  const int ng = 2 * L * (o->cen ? 2 : 1);
+  /* block starts */
+  int64_t nb = 0;
+  int64_t* start = (int64_t*)malloc((R + 1) * sizeof(int64_t));
+  for (int64_t r = 0; r < R; ++r)
+    if (r == 0 || (o->tab.idx[r] >> L) != (o->tab.idx[r - 1] >> L)) start[nb++] = r;
+  start[nb] = R;
+#pragma omp parallel
+  {
+    double* tmp = (double*)malloc((1ull << L) * 8);
+    int* stab = (int*)malloc(ng * sizeof(int));
+#pragma omp for schedule(dynamic)
+    for (int64_t bk = 0; bk < nb; ++bk) {
+      const st_t l = o->tab.idx[start[bk]] >> L;
+      int ns = 0;
+      for (int g = 0; g < ng; ++g) {
+        int sh = g % L, rf = (g / L) & 1, f = g / (2 * L);
+        if ((y_act(l << L, L, sh, rf, f) >> L) == l) stab[ns++] = g;
+      }
+      for (int64_t r = start[bk]; r < start[bk + 1]; ++r) {
+        int64_t src = dir ? o->swp[r] : r;
+        double v = o->tvec[src] * x[src];
+        st_t rt = o->tab.idx[r] & mask;
+        for (int q = 0; q < ns; ++q) {
+          int g = stab[q], sh = g % L, rf = (g / L) & 1, f = g / (2 * L);
+          tmp[y_act(rt, L, sh, rf, f) & mask] = v;
+        }
+      }
+      kron_bits(tmp, L, 0, L, o->b2[0], o->b2[1]);
+      for (int64_t r = start[bk]; r < start[bk + 1]; ++r) {
+        int64_t dst = dir ? r : o->swp[r];
+        y[dst] = o->tvec[dst] * o->tab.dup[dst] * tmp[o->tab.idx[r] & mask];
+      }
+    }
+    free(tmp);
+    free(stab);
+  }
+  free(start);
+}
+
 void orc_perform_op(const orc_op* o, const double* x, double* y) {
   switch (o->kind) {
     case O_XAT: op_xat(o, x, y); break;
@@ -1078,6 +1332,9 @@ void orc_perform_op(const orc_op* o, const double* x, double* y) {
     case O_ZBT: op_zbt(o, x, y, 0); break;
     case O_ZBM: op_zbm(o, x, y, 0); break;
     case O_X3D: op_x3d(o, x, y); break;
+    case O_YAT: op_yat(o, x, y, 0); break;
+    case O_Y2AT: op_y2at(o, x, y); break;
+    case O_YAM: op_yam(o, x, y, 0); break;
   }
 }
 
@@ -1091,7 +1348,17 @@ int orc_perform_op_t(const orc_op* o, const double* x, double* y) {
     op_zbm(o, x, y, 1);
     return 0;
   }
-  orc_perform_op(o, x, y);  // symmetric
+  if (o->kind == O_YAT) {
+    op_yat(o, x, y, 1);
+    return 0;
+  }
+  if (o->kind == O_YAM) {
+    op_yam(o, x, y, 1);
+    return 0;
+  }
+  /* symmetric, or Y2ATMatVecProd2D whose get_t_instance is the operator
+   * itself (TMat/tmat.hpp:382-384) */
+  orc_perform_op(o, x, y);
   return 1;
 }
 
@@ -1148,8 +1415,18 @@ int64_t orc_xam_nslices(const orc_op* o) { return o->cen ? (1ll << o->nlead) / 2
 int orc_moments(const orc_op* o, const double* ql, const double* qr, double out[4]) {
   double r[4] = {0, 0, 0, 0}, dn = 0.0;
   const int L = o->L;
+  if (o->kind == O_Y2AT) { /* TMat/tmat.cpp:309-314: not implemented there */
+    for (int k = 0; k < 4; ++k) out[k] = 0.0;
+    return -1;
+  }
+  const st_t lmask = (1ull << L) - 1;
   for (int64_t i = 0; i < o->n; ++i) {
     st_t s = o->tab.n ? o->tab.idx[i] : (st_t)i;
+    /* two-layer states: GenMatPhys::moments takes the low layer
+     * (TMat/tmatphys.cpp:71-98), YAMMatVecProd2D::moments the left (high)
+     * layer of the representative (TMat/tmatreduce.cpp:878-905) */
+    if (o->kind == O_YAT) s &= lmask;
+    if (o->kind == O_YAM) s >>= L;
     double w = o->sym ? ql[i] * ql[i] : ql[i] * qr[i];
     double p = bzexp1(s, L), m = p;
     dn += w;

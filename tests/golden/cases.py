@@ -54,6 +54,23 @@ CASES = [
     ("zbm_L12_noflip", "B", 2, 7, 2, 0.5, 0.6, 0.2, 0.0, 12, 2),
     ("zbm_L16_noflip", "B", 2, 7, 2, 0.6, 0.8, 0.0, 0.0, 16, 2),
     ("zbm_L14_h", "B", 2, 7, 0, 0.5, 0.45, 0.1, 0.05, 14, 2),
+    # two-layer parallel TMs: y-ANNNI full (YATMatVecProd2D and its _T, even L:
+    # at odd L the reference's final permutation reads its own output buffer),
+    # y2-ANNNI full (Y2ATMatVecProd2D), y-ANNNI and BNNNI reduced
+    # (YAMMatVecProd2D, YBMMatVecProd2D)
+    ("yat_L4", "A", 2, 2, 0, 0.5, 0.3, 0.0, 0.0, 4, 2),
+    ("yat_L6_h", "A", 2, 2, 0, 0.4, 0.7, 0.0, 0.1, 6, 2),
+    ("yat_L8", "A", 2, 2, 0, 0.3, 0.6, 0.0, 0.0, 8, 2),
+    ("y2at_L4", "A", 2, 0, 0, 0.5, 0.3, 0.0, 0.0, 4, 2),
+    ("y2at_L5_h", "A", 2, 0, 0, 0.4, 0.6, 0.0, 0.1, 5, 2),
+    ("y2at_L7", "A", 2, 0, 0, 0.3, 0.6, 0.0, 0.0, 7, 2),
+    ("yam_L6_flip", "A", 2, 6, 0, 0.5, 0.3, 0.0, 0.0, 6, 2),
+    ("yam_L7_noflip", "A", 2, 6, 2, 0.4, 0.7, 0.0, 0.0, 7, 2),
+    ("yam_L8_h", "A", 2, 6, 0, 0.4, 0.6, 0.0, 0.1, 8, 2),
+    ("yam_L10_noflip", "A", 2, 6, 2, 0.3, 0.6, 0.0, 0.0, 10, 2),
+    ("ybm_L6_flip", "B", 2, 6, 0, 0.5, 0.6, 0.4, 0.0, 6, 2),
+    ("ybm_L8_noflip", "B", 2, 6, 2, 0.5, 0.3, 0.2, 0.0, 8, 2),
+    ("ybm_L7_h", "B", 2, 6, 0, 0.4, 0.6, 0.4, 0.05, 7, 2),
     # 3D ANNNI reduced (XAMMatVecProd3D)
     ("x3d_3x3", "A", 3, 1, 0, 0.3, 0.4, 0.0, 0.0, (3, 3), 2),
     ("x3d_3x4_h", "A", 3, 1, 0, 0.25, 0.5, 0.0, 0.1, (3, 4), 2),
@@ -68,6 +85,12 @@ def case_dict(c):
     name, model, dim, ax, ec, bj, k, k2, h, size, nev = c
     return dict(name=name, model=model, dim=dim, axialdir=ax, extend_cond=ec, betaJ=bj, kappa=k, kappa2=k2,
                 h=h, size=size, nev=nev)
+
+
+def general(d) -> bool:
+    """Operators the reference solves with GenEigsSolver (complex Ritz pairs):
+    the diagonal BNNNI and the two-layer families (TMat/tmat.hpp:158-176)."""
+    return d["model"] == "B" or (d["model"] == "A" and d["dim"] == 2 and d["axialdir"] in (0, 2, 6))
 
 
 def seeded_input(n: int, seed: int) -> np.ndarray:

@@ -27,7 +27,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-from cases import CASES, FULL_VECTOR_MAX, case_dict, checksum_weights, seeded_input  # noqa: E402
+from cases import CASES, FULL_VECTOR_MAX, case_dict, checksum_weights, general, seeded_input  # noqa: E402
 from oracle.refbind import RefOp, available  # noqa: E402
 
 
@@ -64,7 +64,7 @@ def gen(c):
     # eigenvalues through ARPACK on the reference matvec
     nev = d["nev"]
     lin = sla.LinearOperator((n, n), matvec=lambda v: op.perform_op(np.ravel(v)), dtype=np.float64)
-    sym = not op.has_transpose()
+    sym = not op.has_transpose() and not general(d)
     v0 = np.random.default_rng(0).uniform(0, 1, n)
     if sym:
         vals, vecs = sla.eigsh(lin, k=nev, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, max(2 * nev + 8, 20)))

@@ -109,3 +109,18 @@ def test_moments_phys(name):
     if len(f["phys"]):
         np.testing.assert_allclose(p, f["phys"], rtol=1e-12, atol=1e-12)
     assert pst == int(f["phys_status"])
+
+
+@pytest.mark.parametrize("L,ec", [(16, 2), (20, 0), (24, 2)])
+def test_double_float_refinement_product(L, ec):
+    """The solver's refinement product (double-float on FP32 pipes) against the
+    native FP64 product: relative error below 1e-12 of max|y|."""
+    torch = pytest.importorskip("torch")
+    op = lt.TMatOp("A", 2, 5, 0.45, 0.35, 0.0, L, 0.0, ec)
+    n = op.rows()
+    ms64 = op.profile_matvec(lt.TM_F64, iters=1)  # exercises the FP64 path
+    assert len(ms64) >= 1
+    vals64, _, _, info64 = op.eigs(3, tol=1e-12, mode=lt.TM_EIGS_F64)
+    valsm, _, _, infom = op.eigs(3, tol=1e-12, mode=lt.TM_EIGS_MIXED)
+    np.testing.assert_allclose(valsm, vals64, rtol=1e-10)
+    assert infom["matvecs_f64"] < info64["matvecs_f64"]

@@ -54,3 +54,54 @@ def test_3d_points(shape, k, h):
     io, do = o.orbit()
     np.testing.assert_array_equal(io, ir)
     np.testing.assert_array_equal(do, dr.astype(np.uint16))
+
+
+TWO_LAYER = [("A", 2, 2), ("A", 2, 0), ("A", 2, 6), ("B", 2, 6)]
+
+
+@pytest.mark.parametrize("seed", range(5))
+@pytest.mark.parametrize("model,dim,ax", TWO_LAYER)
+def test_two_layer_points(model, dim, ax, seed):
+    rng = np.random.default_rng(2000 + seed)
+    L = int(rng.choice([3, 4, 5, 6, 7]))
+    if ax == 2 and L % 2:
+        L += 1  # odd L: see test_yat_odd_width
+    bj = float(rng.uniform(0.05, 1.0))
+    k = float(rng.choice([0.0, rng.uniform(0, 1.2), 0.5]))
+    k2 = float(rng.uniform(0, 0.8)) if model == "B" else 0.0
+    h = float(rng.choice([0.0, rng.uniform(-0.3, 0.3)]))
+    ec = int(rng.choice([0, 2]))
+    r = refbind.RefOp(model, dim, ax, bj, k, h, L, k2, ec)
+    o = oracle.OracleOp(model, dim, ax, bj, k, h, L, k2, ec)
+    assert r.n == o.n
+    np.testing.assert_allclose(o.normfactor, r.normfactor, rtol=1e-15)
+    x = rng.uniform(-1, 1, r.n)
+    yr = r.perform_op(x)
+    np.testing.assert_allclose(o.perform_op(x), yr, rtol=1e-13, atol=1e-13 * np.max(np.abs(yr)))
+    if r.has_transpose():
+        np.testing.assert_allclose(o.perform_op_t(x), r.perform_op_t(x), rtol=1e-13,
+                                   atol=1e-13 * np.max(np.abs(yr)))
+    ir, dr = r.orbit()
+    if ir is not None:
+        io, do = o.orbit()
+        np.testing.assert_array_equal(io, ir)
+        np.testing.assert_array_equal(do, dr.astype(np.uint16))
+
+
+@pytest.mark.parametrize("L", [3, 5])
+def test_yat_odd_width(L):
+    """At odd L the reference YATMatVecProd2D ends its L ping-pong steps on the
+    output buffer and then permutes that buffer in place (TMat/tmat.cpp:213-240),
+    so its output is not T x.  The oracle computes T x; its spectrum equals the
+    reference's own reduced operator YAMMatVecProd2D at the same point, and the
+    two agree with the reference full operator at even L."""
+    bj, k, h = 0.4, 0.3, 0.1
+
+    def top(op, n):
+        A = np.array([op.perform_op(np.eye(n)[i]) for i in range(n)]).T
+        ev = np.linalg.eigvals(A) / op.normfactor
+        return ev[np.argsort(-np.abs(ev))][:3]
+
+    o = oracle.OracleOp("A", 2, 2, bj, k, h, L, 0.0, 0)
+    ry = refbind.RefOp("A", 2, 6, bj, k, h, L, 0.0, 2)
+    np.testing.assert_allclose(top(o, o.n), top(ry, ry.n), rtol=1e-11)
