@@ -112,6 +112,29 @@ tm_status tm_perform_op(const tm_op* op, const double* x_host, double* y_host);
 tm_status tm_perform_op_dev(const tm_op* op, const void* x_dev, void* y_dev, tm_dtype dtype,
                             void* stream);
 
+/* No counterpart in the reference.  FP64 y = T x on device buffers, like
+ * tm_perform_op_dev with TM_F64, but allocating nothing: no cudaMalloc,
+ * cudaFree or allocating library call.  It is meant for callers that cannot
+ * allocate device memory when they need a product: code running inside a
+ * host framework whose caching allocator owns the device memory, or a
+ * latency-bound loop where an allocation's implicit synchronisation would
+ * stall other streams.  The scratch is one fixed 16 MiB device array built
+ * into the library (2^21 doubles; every GPU that loads the library holds it
+ * until the process exits).
+ *
+ * Covers the reduced x-ANNNI operators on the even/odd path (model 'A',
+ * reduced, periodic, even L >= 12).  An operator needs 3*rows + n_orep*2^(L/2)
+ * doubles of scratch, which fits up to L = 24; larger operators return
+ * TM_ERR_LIMIT, other operators TM_ERR_UNSUPPORTED.
+ *
+ * The first call on a device looks up that device's address of the array
+ * (with the device current), so make the first call on each device before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (different streams, or different host threads) race on it and must be
+ * serialised by the caller.  Each call overwrites every scratch element it
+ * reads, so nothing is carried over from the previous call. */
+tm_status tm_perform_op_dev_noalloc(const tm_op* op, const double* x_dev, double* y_dev, void* stream);
+
 /* Orbit table of a reduced operator: ascending representatives (idxlist) and
  * orbit sizes (duplist), bit-exact with genX2DDuplist / genZ2DDuplist /
  * genX3DDuplist (TMat/tmatreduce.cpp:19-111, 242-334; TMat/tmat3d.cpp:17-98).

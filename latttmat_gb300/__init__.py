@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = (
     "tm_create", "tm_transpose", "tm_destroy", "tm_rows", "tm_cols", "tm_normfactor", "tm_layer_size",
     "tm_is_symmetric", "tm_suggested_ncv", "tm_matvec_count", "tm_perform_op", "tm_perform_op_dev",
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
-    "tm_profile_matvec", "tm_launch_count",
+    "tm_profile_matvec", "tm_launch_count", "tm_perform_op_dev_noalloc",
 )
 
 

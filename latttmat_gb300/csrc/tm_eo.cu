@@ -678,6 +678,34 @@ void matvec_eo_df(const Op& op, const double* x, double* y, cudaStream_t s) {
   matvec_eo_engine<dfloat>(op, x, y, false, s);
 }
 
+// FP64 even/odd product in pi order with caller-provided scratch: u (R
+// doubles) and w1 (n_orep * 2^m doubles).  Used by the entry point whose
+// scratch lives in a fixed device array.
+void matvec_eo_f64_into(const Op& op, const double* x, double* y, double* u, double* w1, cudaStream_t s) {
+  const EOPlan& P = op.eo;
+  const int64_t R = op.n;
+  EOArgs A = make_args<double>(op, P.c64);
+  if (A.n - A.p > 4) fail(TM_ERR_LIMIT, "even/odd tile too large for the FP64 engine");
+  eo_scale_in<double><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R);
+  TM_CKK("eo_scale_in");
+  const double S = std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);
+  switch (A.n - A.p) {
+#define TM_EO_INTO(KBV)                                                                                      \
+  case KBV:                                                                                                  \
+    launch_pass1<double, KBV>(A, P.n_orep, u, P.map1.as<uint32_t>(), P.colmap.as<uint32_t>(), w1, s);       \
+    TM_CKK("eo_pass1");                                                                                      \
+    launch_pass2<double, KBV, true>(A, P.n_erep, w1, P, P.out_off.as<uint32_t>(), op.sout64.as<double>(),    \
+                                    op.sout32.as<float>(), S, y, s);                                        \
+    TM_CKK("eo_pass2");                                                                                      \
+    break;
+    TM_EO_INTO(1)
+    TM_EO_INTO(2)
+    TM_EO_INTO(3)
+    TM_EO_INTO(4)
+#undef TM_EO_INTO
+  }
+}
+
 double eo_scale32(const Op& op) {
   return std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);
 }
