@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-L", type=int, default=28)
+    ap.add_argument("--batch", type=int, default=256,
+                    help="instances of the diagonal BNNNI parameter sweep timed beside the headline (0: skip)")
     return ap.parse_args()
 
 
@@ -288,6 +290,12 @@ def gpu_arm(args, world, rank, local):
         except Exception:
             traffic = None
     del op
+    batch = None
+    if args.batch > 0 and rank == 0:
+        try:
+            batch = batch_sweep(args.batch)
+        except Exception as exc:  # reported beside the headline, never required
+            batch = {"failed": f"{exc}"}
 
     out = None
     if rank == 0:
@@ -323,8 +331,46 @@ def gpu_arm(args, world, rank, local):
                          "alg_bytes": {"pass1": b1, "pass2": b2}},
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "batch_sweep": batch,
         }
         print(json.dumps(out), flush=True)
+
+
+def batch_points(count, seed_L=0, seed_k=1):
+    """The parameter sweep: B/7 (reduced diagonal BNNNI), L uniform in
+    {16,...,24} (seed 0), betaJ on a uniform grid in [0.2, 1.0], kappa1
+    uniform in [0, 1] (seed 1), kappa2 = h = 0."""
+    import numpy as np
+
+    Ls = np.random.default_rng(seed_L).choice([16, 18, 20, 22, 24], count)
+    bj = np.linspace(0.2, 1.0, count)
+    k1 = np.random.default_rng(seed_k).uniform(0.0, 1.0, count)
+    return [(float(bj[i]), float(k1[i]), 0.0, 0.0, int(Ls[i])) for i in range(count)]
+
+
+def batch_sweep(count):
+    """Seconds for the sweep solved concurrently (tm_eigs_batch, mixed
+    precision) and one instance at a time in FP64, both to 1e-10, k=2."""
+    import latttmat_gb300 as lt
+
+    pts = batch_points(count)
+    lt.eigs_batch("B", 2, 7, pts[:4], nev=2, tol=1e-10, mode=lt.TM_EIGS_MIXED, extend_cond=2)  # warm-up
+    t0 = time.perf_counter()
+    vals, info, st = lt.eigs_batch("B", 2, 7, pts, nev=2, tol=1e-10, mode=lt.TM_EIGS_MIXED, extend_cond=2)
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for (bj, k, k2, h, L) in pts:
+        op = lt.TMatOp("B", 2, 7, bj, k, h, L, k2, 2)
+        op.eigs(2, tol=1e-10, mode=lt.TM_EIGS_F64)
+        op.close()
+    t_plain = time.perf_counter() - t0
+    return {"workload": f"{count} x B/7 reduced diagonal BNNNI, L in {{16..24}} (seed 0), betaJ in [0.2,1.0], "
+                        "kappa1 ~ U[0,1] (seed 1), neigs=2, tol 1e-10",
+            "batched_mixed_s": t_batch, "points_per_s": count / t_batch,
+            "plain_f64_sequential_s": t_plain, "speedup": t_plain / t_batch,
+            "failed": int(sum(1 for c in st if c != 0)),
+            "note": "batched: tm_eigs_batch, 16 host threads, one CUDA stream per instance; plain: one "
+                    "FP64 solve after another through the same library"}
 
 
 def eo_plan_sizes(L):

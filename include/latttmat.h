@@ -43,7 +43,9 @@ enum {
   TM_ERR_LIMIT = 8        /* size outside an entry point's stated maximum */
 };
 
-typedef enum { TM_F64 = 0, TM_F32 = 1 } tm_dtype;
+/* TM_F64_DF: FP64 values computed in double-float (FP32 pair) arithmetic,
+ * the solver's refinement product; accepted by tm_profile_matvec. */
+typedef enum { TM_F64 = 0, TM_F32 = 1, TM_F64_DF = 2 } tm_dtype;
 
 /* Model parameters; mirrors MParameter (TMat/commondef.hpp:18-24).  For dim=3
  * `size` is packed as (size1 << 16) | size2, as TMat/read_input.cpp:41 does. */
@@ -70,6 +72,13 @@ typedef struct {
   int ncv;            /* subspace size used */
   double max_resid;   /* max relative residual ||T v - lambda v|| / |lambda| of the returned pairs (FP64) */
   double seconds;     /* wall time inside tm_eigs */
+  /* mixed mode only: the FP64-accurate refinement of the FP32 phase */
+  int refine_rounds;    /* Rayleigh-Ritz rounds */
+  int refine_checks;    /* verifications with FP64-accurate products */
+  int refine_outcome;   /* 0 not run, 1 accepted on the certified estimate, 2 accepted after a
+                           verification, 3 not accepted (FP64 Lanczos continued) */
+  double refine_est;    /* last estimated max relative residual */
+  double refine_true;   /* last verified max relative residual (0 if none) */
 } tm_eigs_info;
 
 /* ---- operator lifetime ------------------------------------------------- */
@@ -166,6 +175,19 @@ tm_status tm_orbit_table(const tm_op* op, uint64_t* idx_host, uint16_t* dup_host
 tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, int mode,
                   double* vals_re, double* vals_im, double* vecs, double* vecl, tm_eigs_info* info);
 
+/* Parameter sweep: solve `count` independent operators (params[i], and the
+ * same model/dim/axialdir/extend_cond for all) concurrently, each built,
+ * solved with tm_eigs (ncv = tm_suggested_ncv, seed 0) and released on its
+ * own CUDA stream by a pool of `nthreads` host threads (0 = 16).  Replaces
+ * running the reference tmat once per parameter point (TMat/main.cpp,
+ * TMat/pfunc.cpp:16-106).  vals_re/vals_im: host, count*nev; infos: host
+ * count or NULL; status: host count or NULL, per-instance codes.  Returns
+ * TM_OK if every instance succeeded, else the first failing code (message
+ * names the instance). */
+tm_status tm_eigs_batch(const tm_params* params, int count, char model, int dim, int axialdir,
+                        int extend_cond, int nev, double tol, int mode, int nthreads, double* vals_re,
+                        double* vals_im, tm_eigs_info* infos, tm_status* status);
+
 /* ---- observables ------------------------------------------------------- */
 
 /* Magnetisation moments <M^k>/L, k=1..4 (TMat/tmatphys.cpp:13-38, 71-98,
@@ -197,7 +219,7 @@ tm_status tm_grad(const tm_op* op, const double* qr_host, const double* ql_host,
 
 /* Time the operator's matvec stages with CUDA events on the operator's
  * stream, averaged over `iters` products in the internal vector order
- * (dtype TM_F32 or TM_F64).  For the even/odd reduced x-ANNNI product the
+ * (dtype TM_F32, TM_F64 or TM_F64_DF).  For the even/odd reduced x-ANNNI product the
  * stages are {input scaling, pass 1, pass 2}; other operators report one
  * stage {whole product}.  ms_out receives up to `cap` per-launch averages;
  * *nstages the count. */

@@ -34,6 +34,7 @@ TM_ERR_LIMIT = 8
 
 TM_F64 = 0
 TM_F32 = 1
+TM_F64_DF = 2
 TM_EIGS_F64 = 0
 TM_EIGS_MIXED = 1
 
@@ -42,7 +43,7 @@ EXPORTED_SYMBOLS = (
     "tm_create", "tm_transpose", "tm_destroy", "tm_rows", "tm_cols", "tm_normfactor", "tm_layer_size",
     "tm_is_symmetric", "tm_suggested_ncv", "tm_matvec_count", "tm_perform_op", "tm_perform_op_dev",
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
-    "tm_profile_matvec", "tm_launch_count", "tm_perform_op_dev_noalloc",
+    "tm_profile_matvec", "tm_launch_count", "tm_perform_op_dev_noalloc", "tm_eigs_batch",
 )
 
 
@@ -60,7 +61,9 @@ class tm_params(ctypes.Structure):
 class tm_eigs_info(ctypes.Structure):
     _fields_ = [("nconv", ctypes.c_int), ("matvecs", ctypes.c_int), ("matvecs_f64", ctypes.c_int),
                 ("restarts", ctypes.c_int), ("ncv", ctypes.c_int), ("max_resid", ctypes.c_double),
-                ("seconds", ctypes.c_double)]
+                ("seconds", ctypes.c_double), ("refine_rounds", ctypes.c_int), ("refine_checks", ctypes.c_int),
+                ("refine_outcome", ctypes.c_int), ("refine_est", ctypes.c_double),
+                ("refine_true", ctypes.c_double)]
 
 
 _lib = None
@@ -98,6 +101,9 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
                                    ctypes.POINTER(ctypes.c_int)]
     lib.tm_grad.argtypes = [P, P, P, ctypes.c_double, P]
     lib.tm_profile_matvec.argtypes = [P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.tm_eigs_batch.argtypes = [P, ctypes.c_int, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, P, P, P, P]
+    lib.tm_eigs_batch.restype = ctypes.c_int
     lib.tm_launch_count.restype = ctypes.c_int64
     lib.tm_last_error.restype = ctypes.c_char_p
     lib.tm_version.restype = ctypes.c_char_p
@@ -107,6 +113,32 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     if path is None:
         _lib = lib
     return lib
+
+
+def eigs_batch(model: str, dim: int, axialdir: int, points, nev: int = 2, tol: float = 1e-10,
+               mode: int = TM_EIGS_MIXED, extend_cond: int = 0, nthreads: int = 0):
+    """Solve many parameter points concurrently (tm_eigs_batch).
+
+    points: sequence of (betaJ, kappa, kappa2, h, size) tuples.  Returns
+    (vals complex [count, nev] already divided by normfactor, info dicts,
+    per-instance status codes)."""
+    lib = load_library()
+    count = len(points)
+    arr = (tm_params * max(count, 1))()
+    for i, (bj, k, k2, h, size) in enumerate(points):
+        arr[i] = tm_params(float(bj), float(k), float(k2), float(h), int(size))
+    vr = np.zeros(count * nev)
+    vi = np.zeros(count * nev)
+    infos = (tm_eigs_info * max(count, 1))()
+    st = np.zeros(max(count, 1), dtype=np.int32)
+    code = lib.tm_eigs_batch(ctypes.byref(arr), count, model.encode()[:1], int(dim), int(axialdir),
+                             int(extend_cond), int(nev), float(tol), int(mode), int(nthreads), _ptr(vr), _ptr(vi),
+                             ctypes.byref(infos), _ptr(st))
+    if code != TM_OK and not np.any(st[:count] == TM_OK):
+        _check(code)
+    vals = (vr + 1j * vi).reshape(count, nev)
+    info = [{k: getattr(infos[i], k) for k, _ in tm_eigs_info._fields_} for i in range(count)]
+    return vals, info, st[:count].copy()
 
 
 def launch_count() -> int:

@@ -142,20 +142,18 @@ struct Arnoldi {
     normalize(W.as<double>(), nsq.as<double>(), v(0), nullptr, n, s);
   }
 
-  // eigen-decompose H_m on the device; eigenvectors for the first kvec by |theta|
+  // eigen-decompose H_m (host; the routines of tm_hqr.cuh take microseconds
+  // at these sizes); eigenvectors for the first kvec by |theta|
   Ritz project(int kvec) {
     Ritz R;
     Hh.assign((size_t)(m + 1) * (m + 1), 0.0);
     TM_CK(cudaMemcpyAsync(Hh.data(), Hd.p, Hh.size() * 8, cudaMemcpyDeviceToHost, s));
-    geneigval_kernel<<<1, 32, 0, s>>>(Hd.as<double>(), m, m + 1, wr.as<double>(), wi.as<double>(), st.as<int>());
-    TM_CKK("geneigval");
-    std::vector<double> er(m), ei(m);
-    int status = 0;
-    TM_CK(cudaMemcpyAsync(er.data(), wr.p, m * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaMemcpyAsync(ei.data(), wi.p, m * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaMemcpyAsync(&status, st.p, 4, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaStreamSynchronize(s));
-    if (status) fail(TM_ERR_NOCONV, "small Hessenberg QR did not converge");
+    std::vector<double> Hm((size_t)m * m);
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) Hm[i + (size_t)j * m] = Hh[i + (size_t)j * (m + 1)];
+    std::vector<double> er(m), ei(m);
+    if (geneig_values(Hm.data(), m, er.data(), ei.data())) fail(TM_ERR_NOCONV, "small Hessenberg QR did not converge");
     std::vector<int> ord(m);
     std::iota(ord.begin(), ord.end(), 0);
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
@@ -165,20 +163,10 @@ struct Arnoldi {
     });
     R.beta = Hh[m + (size_t)(m - 1) * (m + 1)];
     kvec = std::min(kvec, m);
-    std::vector<double> sr(kvec), si(kvec);
-    for (int i = 0; i < kvec; ++i) {
-      sr[i] = er[ord[i]];
-      si[i] = ei[ord[i]];
-    }
-    TM_CK(cudaMemcpyAsync(lr.p, sr.data(), kvec * 8, cudaMemcpyHostToDevice, s));
-    TM_CK(cudaMemcpyAsync(li.p, si.data(), kvec * 8, cudaMemcpyHostToDevice, s));
-    geneigvec_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m, m + 1, lr.as<double>(), li.as<double>(), kvec,
-                                      scr.as<double>(), Yr.as<double>(), Yi.as<double>());
-    TM_CKK("geneigvec");
-    std::vector<double> yr((size_t)m * kvec), yi((size_t)m * kvec);
-    TM_CK(cudaMemcpyAsync(yr.data(), Yr.p, yr.size() * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaMemcpyAsync(yi.data(), Yi.p, yi.size() * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaStreamSynchronize(s));
+    std::vector<double> yr((size_t)m * kvec), yi((size_t)m * kvec), Br((size_t)m * m), Bi((size_t)m * m);
+    for (int c = 0; c < kvec; ++c)
+      geneig_vector(Hh.data(), m, m + 1, er[ord[c]], ei[ord[c]], Br.data(), Bi.data(), yr.data() + (size_t)c * m,
+                    yi.data() + (size_t)c * m);
     for (int i = 0; i < m; ++i) R.theta.push_back({er[ord[i]], ei[ord[i]]});
     for (int c = 0; c < kvec; ++c) {
       std::vector<std::complex<double>> y(m);

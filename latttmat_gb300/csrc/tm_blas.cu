@@ -335,6 +335,24 @@ __global__ void __launch_bounds__(BT) axpy_nrm_f32_kernel(const float* __restric
   block_reduce_store<1>(acc, 1, part);
 }
 
+// w -= V h with FP32 data and FP32 arithmetic (h rounded to FP32)
+__global__ void __launch_bounds__(BT) maxpy_f32_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                       const double* __restrict__ h, float* __restrict__ w,
+                                                       int64_t n) {
+  __shared__ float hs[NV32];
+  if (threadIdx.x < NV32) hs[threadIdx.x] = (threadIdx.x < nv) ? (float)h[threadIdx.x] : 0.f;
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float acc = w[i];
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) acc = fmaf(-V[k * ldv + i], hs[k], acc);
+    w[i] = acc;
+  }
+}
+
 __global__ void normalize_f32_kernel(const float* __restrict__ w, const double* __restrict__ nsq,
                                      float* __restrict__ v, int64_t n) {
   const float inv = (float)(1.0 / sqrt(*nsq));
@@ -391,6 +409,29 @@ __global__ void __launch_bounds__(BT) combine_f32_f64_kernel(const float* __rest
   }
 }
 
+template <int MM>
+__global__ void __launch_bounds__(BT) combine_f32_f32_kernel(const float* __restrict__ V, int64_t ldv, int m,
+                                                             const double* __restrict__ Y, int k,
+                                                             float* __restrict__ out, int64_t ldo, int64_t n) {
+  __shared__ float Ys[MM * MM];
+  for (int t = threadIdx.x; t < m * k; t += BT) Ys[t] = (float)Y[t];
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float row[MM];
+#pragma unroll
+    for (int j = 0; j < MM; ++j) row[j] = (j < m) ? V[j * ldv + i] : 0.f;
+    for (int c = 0; c < k; ++c) {
+      float acc = 0.f;
+#pragma unroll
+      for (int j = 0; j < MM; ++j)
+        if (j < m) acc = fmaf(row[j], Ys[c * m + j], acc);
+      out[c * ldo + i] = acc;
+    }
+  }
+}
+
 __global__ void uniform_f32_kernel(float* __restrict__ v, int64_t n, uint64_t seed) {
   int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * BT;
@@ -412,12 +453,22 @@ __global__ void nrm_f32_kernel(const float* __restrict__ w, int64_t n, double* _
 
 void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
               cudaStream_t s) {
-  if (nv > NV32) fail(TM_ERR_LIMIT, "mdot_f32: too many vectors");
-  int nb = red_blocks(n);
-  mdot_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, w, n, part);
-  TM_CKK("mdot_f32");
-  mdot_final<<<nv, 256, 0, s>>>(part, nb, nv, NV32, h);
-  TM_CKK("mdot_final");
+  for (int k0 = 0; k0 < nv; k0 += NV32) {
+    const int kk = std::min(NV32, nv - k0);
+    int nb = red_blocks(n);
+    mdot_f32_kernel<<<nb, BT, 0, s>>>(V + k0 * ldv, ldv, kk, w, n, part);
+    TM_CKK("mdot_f32");
+    mdot_final<<<kk, 256, 0, s>>>(part, nb, kk, NV32, h + k0);
+    TM_CKK("mdot_final");
+  }
+}
+
+void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, cudaStream_t s) {
+  for (int k0 = 0; k0 < nv; k0 += NV32) {
+    const int kk = std::min(NV32, nv - k0);
+    maxpy_f32_kernel<<<red_blocks(n), BT, 0, s>>>(V + k0 * ldv, ldv, kk, h + k0, w, n);
+    TM_CKK("maxpy_f32");
+  }
 }
 
 void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const float* win, float* wout, int64_t n,
@@ -464,6 +515,17 @@ void combine_f32_f64(const float* V, int64_t ldv, int m, const double* Y, int k,
   else
     fail(TM_ERR_LIMIT, "combine_f32_f64: basis too large");
   TM_CKK("combine_f32_f64");
+}
+
+void combine_f32(const float* V, int64_t ldv, int m, const double* Y, int k, float* out, int64_t ldo, int64_t n,
+                 cudaStream_t s) {
+  if (m <= 16)
+    combine_f32_f32_kernel<16><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  else if (m <= 32)
+    combine_f32_f32_kernel<32><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  else
+    fail(TM_ERR_LIMIT, "combine_f32: basis too large");
+  TM_CKK("combine_f32");
 }
 
 void fill_uniform_f32(float* v, int64_t n, uint64_t seed, cudaStream_t s) {

@@ -41,6 +41,8 @@ constexpr int NV32 = 16;
 // h[k] = sum_i V[k][i] w[i]
 void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
               cudaStream_t s);
+// w -= V h (FP32 data and arithmetic), any nv (chunks of NV32)
+void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, cudaStream_t s);
 // wout = win - V h ; h2[k] = sum_i V[k][i] wout[i]   (one pass)
 void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const float* win, float* wout, int64_t n,
                   double* h2, double* part, cudaStream_t s);
@@ -54,6 +56,9 @@ void rotate_f32(float* V, int64_t ldv, int m, const double* Y, int k, int64_t n,
 // out64[:, 0..k) = V32[:, 0..m) Y  (FP64 accumulation), m <= 32
 void combine_f32_f64(const float* V, int64_t ldv, int m, const double* Y, int k, double* out, int64_t ldo, int64_t n,
                      cudaStream_t s);
+// out[:, c] = V Y[:, c] with FP32 data and arithmetic (m <= 32)
+void combine_f32(const float* V, int64_t ldv, int m, const double* Y, int k, float* out, int64_t ldo, int64_t n,
+                 cudaStream_t s);
 // uniform(0,1) FP32 start vector
 void fill_uniform_f32(float* v, int64_t n, uint64_t seed, cudaStream_t s);
 // ||w||^2 of an FP32 vector (FP64 result on device)

@@ -31,10 +31,21 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
 static std::atomic<int64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static thread_local cudaStream_t g_alloc_stream = nullptr;
+AllocStream::AllocStream(cudaStream_t s) : prev(g_alloc_stream) { g_alloc_stream = s; }
+AllocStream::~AllocStream() { g_alloc_stream = prev; }
+
 void DBuf::alloc(size_t b) {
   release();
   if (b == 0) b = 16;
-  cudaError_t e = cudaMalloc(&p, b);
+  cudaError_t e;
+  if (g_alloc_stream) {
+    e = cudaMallocAsync(&p, b, g_alloc_stream);
+    st = g_alloc_stream;
+  } else {
+    e = cudaMalloc(&p, b);
+    st = nullptr;
+  }
   if (e != cudaSuccess) {
     p = nullptr;
     (void)cudaGetLastError();
@@ -45,8 +56,14 @@ void DBuf::alloc(size_t b) {
   bytes = b;
 }
 void DBuf::release() {
-  if (p) cudaFree(p);
+  if (p) {
+    if (st)
+      cudaFreeAsync(p, st);
+    else
+      cudaFree(p);
+  }
   p = nullptr;
+  st = nullptr;
   bytes = 0;
 }
 
@@ -66,7 +83,9 @@ tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
                         std::vector<std::complex<double>>& vals, std::vector<double>* vr, std::vector<double>* vi,
                         tm_eigs_info* info_out);
 
-static bool is_reduced(int kind) { return kind == K_XAM || kind == K_XDM || kind == K_ZBM || kind == K_XAM3; }
+static bool is_reduced(int kind) {
+  return kind == K_XAM || kind == K_XDM || kind == K_ZBM || kind == K_XAM3 || kind == K_YAM;
+}
 static bool bfly_core(int kind) { return kind == K_XAT || kind == K_XAM || kind == K_XAM3; }
 
 void matvec_eo_df(const Op& op, const double* x, double* y, cudaStream_t s);
@@ -333,6 +352,7 @@ static Op* create_op(const tm_params* p, char model, int dim, int axialdir, int 
   }
   if (dim == 2 && op->kind == K_XAM3) fail(TM_ERR_ARG, "internal dispatch error");
   TM_CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  AllocStream guard(op->stream);
   build_op(*op);
   return op.release();
 }
@@ -403,12 +423,14 @@ tm_status tm_destroy(tm_op* op) {
   TM_API_BEGIN
   if (!op) return TM_OK;
   Op* o = op->impl;
-  if (o && !o->is_view && o->stream) {
-    cudaStreamSynchronize(o->stream);
-    cudaStreamDestroy(o->stream);
-  }
+  // buffers are freed in order on the operator's stream, then the stream goes
+  cudaStream_t st = (o && !o->is_view) ? o->stream : nullptr;
   delete o;
   delete op;
+  if (st) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
   TM_API_END
 }
 
@@ -475,6 +497,7 @@ tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, 
   if (mode != TM_EIGS_F64 && mode != TM_EIGS_MIXED) fail(TM_ERR_ARG, "unknown mode");
   const Op& o = *op->impl;
   const Op& b = o.parent ? *o.parent : o;
+  AllocStream guard(b.stream);
   if (is_two_layer(b.kind)) mode = TM_EIGS_F64;  // FP64 products only
   tm_status st = TM_OK;
   if (!b.symmetric) {
@@ -548,6 +571,7 @@ tm_status tm_moments(const tm_op* op, const double* ql, const double* qr, double
   TM_API_BEGIN
   if (!op || !ql || !qr || !out4) fail(TM_ERR_ARG, "null argument");
   const Op& b = op->impl->parent ? *op->impl->parent : *op->impl;
+  AllocStream guard(b.stream);
   double sums[12];
   observables(b, ql, qr, sums);
   // sums: 0..3 = sum w m^k, 4 = sum w, 5 = sum w nnode, 6 = sum w nnode^2, 7..10 DNNI stripes
@@ -571,6 +595,7 @@ tm_status tm_phys_extend(const tm_op* op, const double* ql, const double* qr, do
   TM_API_BEGIN
   if (!op || !ql || !qr) fail(TM_ERR_ARG, "null argument");
   const Op& b = op->impl->parent ? *op->impl->parent : *op->impl;
+  AllocStream guard(b.stream);
   double sums[12];
   int cnt = 0, st = 0;
   std::vector<double> r;
@@ -604,6 +629,7 @@ tm_status tm_profile_matvec(const tm_op* op, tm_dtype dt, int iters, double* ms_
   const Op& o = *op->impl;
   const Op& b = o.parent ? *o.parent : o;
   cudaStream_t s = b.stream;
+  AllocStream guard(s);
   DBuf x, y, x32, y32;
   x.alloc((size_t)b.n * 8);
   y.alloc((size_t)b.n * 8);
@@ -614,8 +640,13 @@ tm_status tm_profile_matvec(const tm_op* op, tm_dtype dt, int iters, double* ms_
     y32.alloc((size_t)b.n * 4);
     TM_CK(cudaMemsetAsync(x32.p, 0, (size_t)b.n * 4, s));
   }
+  if (dt != TM_F64 && dt != TM_F32 && dt != TM_F64_DF) fail(TM_ERR_ARG, "unknown dtype");
+  const bool df = (dt == TM_F64_DF);
   auto run = [&]() {
-    apply_internal(o, x.as<double>(), y.as<double>(), x32.as<float>(), y32.as<float>(), f32, s);
+    if (df)
+      apply_refine(o, x.as<double>(), y.as<double>(), s);
+    else
+      apply_internal(o, x.as<double>(), y.as<double>(), x32.as<float>(), y32.as<float>(), f32, s);
   };
   run();  // warm-up
   TM_CK(cudaStreamSynchronize(s));
@@ -664,6 +695,7 @@ tm_status tm_grad(const tm_op* op, const double* qr, const double* ql, double la
   if (!op || !qr || !grad4) fail(TM_ERR_ARG, "null argument");
   if (!(lambda_internal != 0.0) || !std::isfinite(lambda_internal)) fail(TM_ERR_ARG, "eigenvalue must be finite, nonzero");
   const Op& b = op->impl->parent ? *op->impl->parent : *op->impl;
+  AllocStream guard(b.stream);
   if (!b.symmetric && !ql) fail(TM_ERR_ARG, "general operators need the left eigenvector");
   adjoint_grad(b, qr, b.symmetric ? nullptr : ql, lambda_internal, grad4);
   TM_API_END

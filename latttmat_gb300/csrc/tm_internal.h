@@ -27,9 +27,15 @@ void note_launch();
 
 // ---------------------------------------------------------------- memory
 // Owning device buffer (freed in the destructor).
+// Device buffer.  Allocation is stream-ordered (cudaMallocAsync on the
+// stream an AllocStream guard set for the calling thread) when a guard is
+// active, so that freeing does not synchronise the device while other
+// operators' solves run concurrently; the buffer is then freed on the same
+// stream.  Without a guard it is a plain cudaMalloc.
 struct DBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t st = nullptr;
   DBuf() {}
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
@@ -38,6 +44,15 @@ struct DBuf {
   void release();
   template <class T>
   T* as() const { return static_cast<T*>(p); }
+};
+
+// Sets the allocation stream of DBuf::alloc for the calling thread while in
+// scope (every use of such a buffer must be ordered after its allocation on
+// that stream, and its last use before the free that ends the scope).
+struct AllocStream {
+  cudaStream_t prev;
+  explicit AllocStream(cudaStream_t s);
+  ~AllocStream();
 };
 
 // ---------------------------------------------------------------- kinds

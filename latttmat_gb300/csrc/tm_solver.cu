@@ -10,13 +10,15 @@
 // in FP64 on the device.  The small projected eigenproblem is solved by a
 // one-warp Jacobi kernel.  The host only reads Ritz values at restarts.
 //
-// Mixed precision (TM_EIGS_MIXED): matvecs run in FP32 until the Ritz
-// residuals reach the FP32 noise floor.  Then an FP64 Rayleigh-Ritz step on
-// the nev Ritz vectors (nev FP64 matvecs) gives eigenvalues whose error is
-// bounded by ||r||^2/gap (Kato-Temple).  FP64 Lanczos resumes only when that
-// bound misses the tolerance.
+// Mixed precision (TM_EIGS_MIXED): Lanczos with an FP32 basis and FP32
+// matvecs until the Ritz residuals reach the FP32 noise floor, then the
+// refinement of refine_mixed: FP64-accurate products only for the nev wanted
+// Ritz vectors, everything else in FP32, and acceptance on true FP64
+// residuals (the same test as the FP64 path).  FP64 Lanczos resumes from the
+// refined vectors only when the refinement does not get there.
 #include <algorithm>
 #include <chrono>
+#include <functional>
 #include <memory>
 #include <cmath>
 #include <numeric>
@@ -76,6 +78,105 @@ __global__ void f32_scaled_kernel(const float* __restrict__ y32, double S, doubl
 
 int blocks_for(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8));
+}
+
+// Eigen-decomposition of a small symmetric matrix (m <= 64) on the host:
+// cyclic Jacobi (Golub & Van Loan, Alg. 8.5.2).  A: column-major with leading
+// dimension lda (symmetrised on entry); w[k] eigenvalues, Z[k*m + j] the
+// components of eigenvector k.  Microseconds for the projected matrices here,
+// where a one-warp device kernel costs about a millisecond per call.
+void sym_eig_host(const double* Ain, int m, int lda, double* w, double* Z) {
+  std::vector<double> A((size_t)m * m);
+  for (int c = 0; c < m; ++c)
+    for (int r = 0; r < m; ++r) A[r + (size_t)c * m] = 0.5 * (Ain[r + (size_t)c * lda] + Ain[c + (size_t)r * lda]);
+  for (int c = 0; c < m; ++c)
+    for (int r = 0; r < m; ++r) Z[r + (size_t)c * m] = (r == c) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int c = 0; c < m; ++c)
+      for (int r = 0; r < m; ++r) {
+        const double v = A[r + (size_t)c * m] * A[r + (size_t)c * m];
+        tot += v;
+        if (r != c) off += v;
+      }
+    if (off <= 1e-30 * tot || off == 0.0) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = A[p + (size_t)q * m];
+        if (apq == 0.0) continue;
+        const double app = A[p + (size_t)p * m], aqq = A[q + (size_t)q * m];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int r = 0; r < m; ++r) {
+          const double arp = A[r + (size_t)p * m], arq = A[r + (size_t)q * m];
+          A[r + (size_t)p * m] = c * arp - sn * arq;
+          A[r + (size_t)q * m] = sn * arp + c * arq;
+        }
+        for (int r = 0; r < m; ++r) {
+          const double apr = A[p + (size_t)r * m], aqr = A[q + (size_t)r * m];
+          A[p + (size_t)r * m] = c * apr - sn * aqr;
+          A[q + (size_t)r * m] = sn * apr + c * aqr;
+        }
+        for (int r = 0; r < m; ++r) {
+          const double zrp = Z[r + (size_t)p * m], zrq = Z[r + (size_t)q * m];
+          Z[r + (size_t)p * m] = c * zrp - sn * zrq;
+          Z[r + (size_t)q * m] = sn * zrp + c * zrq;
+        }
+      }
+  }
+  for (int k = 0; k < m; ++k) w[k] = A[k + (size_t)k * m];
+}
+
+// G y = theta M y for symmetric G and symmetric positive definite M (m <=
+// 64), by Cholesky M = L L^T and the standard problem L^-1 G L^-T.  Column-
+// major inputs with leading dimension m.  Z[k*m + j]: eigenvector k,
+// M-orthonormal.  Returns false when M is not numerically positive definite.
+bool gen_sym_eig_host(const double* G, const double* M, int m, double* w, double* Z) {
+  std::vector<double> L((size_t)m * m, 0.0);
+  for (int j = 0; j < m; ++j) {
+    double d = M[j + (size_t)j * m];
+    for (int k = 0; k < j; ++k) d -= L[j + (size_t)k * m] * L[j + (size_t)k * m];
+    if (!(d > 0.0)) return false;
+    const double ljj = std::sqrt(d);
+    L[j + (size_t)j * m] = ljj;
+    for (int i = j + 1; i < m; ++i) {
+      double v = 0.5 * (M[i + (size_t)j * m] + M[j + (size_t)i * m]);
+      for (int k = 0; k < j; ++k) v -= L[i + (size_t)k * m] * L[j + (size_t)k * m];
+      L[i + (size_t)j * m] = v / ljj;
+    }
+  }
+  // T = L^-1 G (column by column), then A = L^-1 T^T
+  std::vector<double> T((size_t)m * m), A((size_t)m * m);
+  auto fsolve = [&](const double* b, double* x) {  // L x = b
+    for (int i = 0; i < m; ++i) {
+      double v = b[i];
+      for (int k = 0; k < i; ++k) v -= L[i + (size_t)k * m] * x[k];
+      x[i] = v / L[i + (size_t)i * m];
+    }
+  };
+  std::vector<double> col(m), tr(m);
+  for (int j = 0; j < m; ++j) {
+    for (int i = 0; i < m; ++i) col[i] = 0.5 * (G[i + (size_t)j * m] + G[j + (size_t)i * m]);
+    fsolve(col.data(), &T[(size_t)j * m]);
+  }
+  for (int j = 0; j < m; ++j) {
+    for (int i = 0; i < m; ++i) tr[i] = T[j + (size_t)i * m];  // row j of T
+    fsolve(tr.data(), &A[(size_t)j * m]);
+  }
+  std::vector<double> Zs((size_t)m * m);
+  sym_eig_host(A.data(), m, m, w, Zs.data());
+  // y = L^-T z
+  for (int k = 0; k < m; ++k) {
+    const double* z = &Zs[(size_t)k * m];
+    double* y = &Z[(size_t)k * m];
+    for (int i = m - 1; i >= 0; --i) {
+      double v = z[i];
+      for (int r = i + 1; r < m; ++r) v -= L[r + (size_t)i * m] * y[r];
+      y[i] = v / L[i + (size_t)i * m];
+    }
+  }
+  return true;
 }
 
 struct Lanczos {
@@ -141,14 +242,12 @@ struct Lanczos {
   };
 
   CycleResult project() {
-    small_symeig(Hd.as<double>(), m, wd.as<double>(), Zd.as<double>(), s, m + 1);
     CycleResult r;
     std::vector<double> th(m), H((size_t)(m + 1) * (m + 1));
     r.Z.resize((size_t)m * m);
-    TM_CK(cudaMemcpyAsync(th.data(), wd.p, m * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaMemcpyAsync(r.Z.data(), Zd.p, (size_t)m * m * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaMemcpyAsync(H.data(), Hd.p, H.size() * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaStreamSynchronize(s));
+    sym_eig_host(H.data(), m, m + 1, th.data(), r.Z.data());
     r.beta = H[m + (size_t)(m - 1) * (m + 1)];
     r.order.resize(m);
     std::iota(r.order.begin(), r.order.end(), 0);
@@ -302,14 +401,12 @@ struct Lanczos32 {
   }
 
   Lanczos::CycleResult project() {
-    small_symeig(Hd.as<double>(), m, wd.as<double>(), Zd.as<double>(), s, m + 1);
     Lanczos::CycleResult r;
     std::vector<double> th(m), H((size_t)(m + 1) * (m + 1));
     r.Z.resize((size_t)m * m);
-    TM_CK(cudaMemcpyAsync(th.data(), wd.p, m * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaMemcpyAsync(r.Z.data(), Zd.p, (size_t)m * m * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaMemcpyAsync(H.data(), Hd.p, H.size() * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaStreamSynchronize(s));
+    sym_eig_host(H.data(), m, m + 1, th.data(), r.Z.data());
     r.beta = H[m + (size_t)(m - 1) * (m + 1)];
     r.order.resize(m);
     std::iota(r.order.begin(), r.order.end(), 0);
@@ -347,6 +444,15 @@ struct Lanczos32 {
   }
 
   // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k
+  // Ritz vectors first .. first+k-1 as FP32 columns
+  void ritz_f32(const Lanczos::CycleResult& r, int first, int k, float* out) {
+    std::vector<double> Yh((size_t)m * k);
+    for (int c = 0; c < k; ++c)
+      for (int j = 0; j < m; ++j) Yh[(size_t)c * m + j] = r.Z[(size_t)r.order[first + c] * m + j];
+    TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
+    combine_f32(V.as<float>(), n, m, Ysel.as<double>(), k, out, n, n, s);
+  }
+
   void ritz_f64(const Lanczos::CycleResult& r, int k, double* out) {
     std::vector<double> Yh = ysel(r, k);
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
@@ -393,6 +499,380 @@ struct EigOut {
 };
 
 // Symmetric solve.  vecs_host may be null.
+constexpr int kMaxRefineNev = 8;
+
+// Ritz pairs of the refinement subspace [X0 | B32] (X0: nx FP64 columns with
+// FP64-accurate products AX0; B32: FP32 columns nx..nb-1 with FP32 products
+// AB32 = A b / S).  For each wanted pair c < nv with coefficients Y(:, c):
+//   x = X0 y_x + B32 y_b,  ax = AX0 y_x + S AB32 y_b,  r = ax - theta_c x,
+// the B32 part in FP32 arithmetic (its weights are at the FP32 noise level).
+// Writes r as FP32 into R32 (column c), optionally x into Xo (FP64), and the
+// block partial sums of ||r||^2 into part[block * NVW + c].
+template <int NVW>
+__global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restrict__ X0,
+                                                         const double* __restrict__ AX0, int nx,
+                                                         const float* __restrict__ B32,
+                                                         const float* __restrict__ AB32, int nb,
+                                                         const double* __restrict__ Y, int nv,
+                                                         const double* __restrict__ theta, double S,
+                                                         float* __restrict__ R32, double* __restrict__ Xo,
+                                                         int64_t n, double* __restrict__ part) {
+  __shared__ double Yd[48 * NVW];
+  __shared__ float Yf[48 * NVW];
+  __shared__ double th[NVW];
+  for (int t = threadIdx.x; t < nb * nv; t += blockDim.x) {
+    Yd[t] = Y[t];
+    Yf[t] = (float)Y[t];
+  }
+  if (threadIdx.x < nv) th[threadIdx.x] = theta[threadIdx.x];
+  __syncthreads();
+  double acc[NVW];
+#pragma unroll
+  for (int c = 0; c < NVW; ++c) acc[c] = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double x[NVW], ax[NVW];
+    float xs[NVW], axs[NVW];
+#pragma unroll
+    for (int c = 0; c < NVW; ++c) {
+      x[c] = ax[c] = 0.0;
+      xs[c] = axs[c] = 0.f;
+    }
+    for (int j = 0; j < nx; ++j) {
+      const double xv = X0[(int64_t)j * n + i], av = AX0[(int64_t)j * n + i];
+#pragma unroll
+      for (int c = 0; c < NVW; ++c)
+        if (c < nv) {
+          x[c] = fma(xv, Yd[c * nb + j], x[c]);
+          ax[c] = fma(av, Yd[c * nb + j], ax[c]);
+        }
+    }
+    for (int j = nx; j < nb; ++j) {
+      const float bv = B32[(int64_t)j * n + i], abv = AB32[(int64_t)j * n + i];
+#pragma unroll
+      for (int c = 0; c < NVW; ++c)
+        if (c < nv) {
+          xs[c] = fmaf(bv, Yf[c * nb + j], xs[c]);
+          axs[c] = fmaf(abv, Yf[c * nb + j], axs[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NVW; ++c)
+      if (c < nv) {
+        const double xx = x[c] + (double)xs[c];
+        const double r = fma(S, (double)axs[c], ax[c]) - th[c] * xx;
+        R32[(int64_t)c * n + i] = (float)r;
+        if (Xo) Xo[(int64_t)c * n + i] = xx;
+        acc[c] = fma(r, r, acc[c]);
+      }
+  }
+  __shared__ double sh[8][NVW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NVW; ++c) {
+    double v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[wid][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NVW) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q][threadIdx.x];
+    part[(int64_t)blockIdx.x * NVW + threadIdx.x] = t;
+  }
+}
+
+// out = (float)(in * scale)
+__global__ void f64_to_f32_scaled_kernel(const double* __restrict__ in, double scale, float* __restrict__ out,
+                                         int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)(in[i] * scale);
+}
+
+// FP64-accurate refinement of the FP32 phase's Ritz pairs.
+//
+// On GB300 FP64 arithmetic runs at a small fraction of the FP32 rate, so the
+// refinement keeps FP64 where the result needs it and nowhere else.  The
+// subspace is [X0 | C]: X0 = the nev wanted Ritz vectors (FP64, with
+// FP64-accurate products), C = the other FP32 Ritz vectors and, each round,
+// the wanted residual block (FP32 storage, FP32 products, FP32 Gram-Schmidt).
+// C's weight in a wanted Ritz vector is at the FP32 noise level (~1e-7), so
+// FP32 errors in C, in A C and in the C-rows of the projected matrix reach
+// the wanted pairs only at ~1e-14 relative.  The projected matrix takes each
+// entry from the side whose product is the more accurate one (A X0 for the
+// X0 rows).  The extra Ritz vectors carry the eigenvectors next to the wanted
+// ones, which residual blocks alone resolve slowly.  When the estimated
+// residuals meet tol, the Ritz vectors get FP64-accurate products and are
+// accepted on the test of the FP64 path and of Spectra's SymEigsSolver,
+// ||A x - theta x|| <= tol |theta|, with theta the Rayleigh quotient; else the
+// verified vectors become the new X0 and the rounds go on.
+//
+// In: lz.v(0..nev-1) the wanted Ritz vectors (FP64, orthonormal); the other
+// nx - nev Ritz vectors from fill_extras (FP32 columns) or, without it, from
+// lz.v(nev..nx-1).
+// Out: lz.v(0..nev-1) the best Ritz vectors; thv, max_resid; true when accepted.
+bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::vector<double>& thv,
+                  double& max_resid, const std::function<void(float*)>& fill_extras, tm_eigs_info& info) {
+  cudaStream_t s = lz.s;
+  const int64_t n = lz.n;
+  const int cap = std::min(48, nx + 5 * nev);
+  const int gblocks = blocks_for(n);
+  DBuf AX0, B32, AB32, R32, Xo, AXo, Yd, thd, part;
+  AX0.alloc((size_t)nev * n * 8);
+  B32.alloc((size_t)cap * n * 4);
+  AB32.alloc((size_t)cap * n * 4);
+  R32.alloc((size_t)nev * n * 4);
+  Xo.alloc((size_t)nev * n * 8);
+  AXo.alloc((size_t)nev * n * 8);
+  Yd.alloc((size_t)48 * kMaxRefineNev * 8);
+  thd.alloc(kMaxRefineNev * 8);
+  part.alloc((size_t)gblocks * kMaxRefineNev * 8);
+  auto f32col = [&](const DBuf& b, int j) { return b.as<float>() + (int64_t)j * n; };
+  auto host_sync = [&]() { TM_CK(cudaStreamSynchronize(s)); };
+  double S = 0.0;
+  auto prod32 = [&](const float* x, float* y) {
+    const double Sj = apply_internal(op, nullptr, nullptr, x, y, true, s);
+    ++lz.matvecs;
+    if (S == 0.0) S = Sj;
+    if (Sj != S) fail(TM_ERR_CUDA, "inconsistent FP32 product scale");
+  };
+  auto prod64 = [&](const double* x, double* y) {
+    apply_refine(op, x, y, s);
+    ++lz.matvecs;
+    ++lz.matvecs64;
+  };
+  auto dots32 = [&](const DBuf& V, int nv, const float* w) {
+    std::vector<double> h(nv);
+    mdot_f32(V.as<float>(), n, nv, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+    TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nv * 8, cudaMemcpyDeviceToHost, s));
+    host_sync();
+    return h;
+  };
+  // projected matrix G = B^T A B and Gram matrix M = B^T B of B = [X0 | C].
+  // The X0 rows take FP64 dots against the exact FP32 values of C (A X0 and
+  // X0 in FP64): C is orthogonal to X0 only to FP32 accuracy (~1e-7), the
+  // size of the couplings that carry the correction, so those entries and
+  // the Gram block must be exact.  The C-C block is FP32 (second order).
+  std::vector<double> G((size_t)cap * cap, 0.0), M((size_t)cap * cap, 0.0);
+  auto g = [&](int i, int j) -> double& { return G[(size_t)j * cap + i]; };
+  auto mm = [&](int i, int j) -> double& { return M[(size_t)j * cap + i]; };
+  auto dots64 = [&](const double* V, int nv, const float* w) {
+    std::vector<double> h(nv);
+    mdot32(V, n, nv, w, 1.0, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+    TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nv * 8, cudaMemcpyDeviceToHost, s));
+    host_sync();
+    return h;
+  };
+  auto x0_rows = [&](int j) {  // X0 rows of column j >= nev
+    std::vector<double> ga = dots64(AX0.as<double>(), nev, f32col(B32, j));
+    std::vector<double> mb = dots64(lz.v(0), nev, f32col(B32, j));
+    for (int i = 0; i < nev; ++i) {
+      g(i, j) = g(j, i) = ga[i];
+      mm(i, j) = mm(j, i) = mb[i];
+    }
+  };
+  auto add_gcol = [&](int j) {  // column j >= nev against columns 0..j
+    std::vector<double> gl = dots32(B32, j + 1, f32col(AB32, j));  // b_i . A b_j / S
+    std::vector<double> gr = dots32(AB32, j + 1, f32col(B32, j));  // (A b_i / S) . b_j
+    std::vector<double> mc = dots32(B32, j + 1, f32col(B32, j));
+    for (int i = nev; i <= j; ++i) {
+      g(i, j) = g(j, i) = S * 0.5 * (gl[i] + gr[i]);
+      mm(i, j) = mm(j, i) = mc[i];
+    }
+    x0_rows(j);
+  };
+  // X0 block (FP64 products and dots) and its rows against every C column
+  auto set_x0 = [&](int nb) {
+    for (int j = 0; j < nev; ++j) {
+      std::vector<double> h(nev), q(nev);
+      mdot(lz.v(0), n, nev, AX0.as<double>() + (int64_t)j * n, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+      TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nev * 8, cudaMemcpyDeviceToHost, s));
+      mdot(lz.v(0), n, nev, lz.v(j), n, lz.h2.as<double>(), lz.part.as<double>(), s);
+      TM_CK(cudaMemcpyAsync(q.data(), lz.h2.p, nev * 8, cudaMemcpyDeviceToHost, s));
+      host_sync();
+      for (int i = 0; i < nev; ++i) {
+        g(i, j) = h[i];
+        mm(i, j) = q[i];
+      }
+    }
+    for (int j = 0; j < nev; ++j)
+      for (int i = 0; i < j; ++i) {
+        g(i, j) = g(j, i) = 0.5 * (g(i, j) + g(j, i));
+        mm(i, j) = mm(j, i) = 0.5 * (mm(i, j) + mm(j, i));
+      }
+    for (int j = 0; j < nev; ++j) {  // FP32 copy of X0 for the FP32 Gram-Schmidt of C
+      f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
+      TM_CKK("to_f32");
+    }
+    for (int j = nev; j < nb; ++j) x0_rows(j);
+  };
+  // start: the extra Ritz vectors to FP32 with FP32 products, the wanted ones
+  // with FP64-accurate products
+  for (int j = 0; j < nev; ++j) {
+    f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
+    TM_CKK("to_f32");
+  }
+  if (fill_extras) {
+    if (nx > nev) fill_extras(f32col(B32, nev));
+  } else {
+    for (int j = nev; j < nx; ++j) {
+      f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
+      TM_CKK("to_f32");
+    }
+  }
+  for (int j = nev; j < nx; ++j) prod32(f32col(B32, j), f32col(AB32, j));
+  if (S == 0.0) prod32(f32col(B32, 0), f32col(AB32, 0));  // only its scale is used; set_x0 overwrites it
+  for (int i = 0; i < nev; ++i) prod64(lz.v(i), AX0.as<double>() + (int64_t)i * n);
+  int nb = nx;
+  set_x0(nev);
+  for (int j = nev; j < nb; ++j) add_gcol(j);
+  int verified = 0;
+  bool have_x = false;
+  // after a failed verification: grow before verifying again, and accept
+  // only verified pairs from then on
+  bool force_grow = false, trust_bound = true;
+  for (int round = 0; round < 3 * kRefineRounds; ++round) {
+    // Rayleigh-Ritz on [X0 | C]
+    std::vector<double> Gc((size_t)nb * nb), Mc((size_t)nb * nb);
+    for (int j = 0; j < nb; ++j)
+      for (int i = 0; i < nb; ++i) {
+        Gc[(size_t)j * nb + i] = g(i, j);
+        Mc[(size_t)j * nb + i] = mm(i, j);
+      }
+    std::vector<double> gw(nb), gz((size_t)nb * nb);
+    if (!gen_sym_eig_host(Gc.data(), Mc.data(), nb, gw.data(), gz.data())) break;
+    std::vector<int> ord(nb);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
+    std::vector<double> Y((size_t)nb * nev), tha(nev);
+    for (int c = 0; c < nev; ++c) {
+      tha[c] = gw[ord[c]];
+      for (int j = 0; j < nb; ++j) Y[(size_t)c * nb + j] = gz[(size_t)ord[c] * nb + j];
+    }
+    TM_CK(cudaMemcpyAsync(Yd.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
+    TM_CK(cudaMemcpyAsync(thd.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
+    // wanted Ritz vectors (FP64) and residuals (FP32 copy, norms in FP64)
+    ritz_resid_kernel<kMaxRefineNev><<<gblocks, 256, 0, s>>>(
+        lz.v(0), AX0.as<double>(), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(), nev,
+        thd.as<double>(), S, R32.as<float>(), Xo.as<double>(), n, part.as<double>());
+    TM_CKK("ritz_resid");
+    std::vector<double> ph((size_t)gblocks * kMaxRefineNev), rn(nev, 0.0);
+    TM_CK(cudaMemcpyAsync(ph.data(), part.p, ph.size() * 8, cudaMemcpyDeviceToHost, s));
+    host_sync();
+    have_x = true;
+    for (int b = 0; b < gblocks; ++b)
+      for (int c = 0; c < nev; ++c) rn[c] += ph[(size_t)b * kMaxRefineNev + c];
+    // The estimate differs from the true residual of x only through the
+    // FP32 products in the C block: |r - r_est| <= eps32 ||A|| ||y_c||, with
+    // eps32 = (2L + 8) 2^-24 per FP32 product (one rounding per butterfly
+    // level and scaling step; A is entrywise non-negative, so ||A|x||| <=
+    // ||A|| ||x||) taken 4x, and ||A|| <= 1.01 |theta_0|.  The FP64-accurate
+    // products of X0 are the ones a verification would use too.
+    const double eps32 = 4.0 * (2.0 * op.L + 8.0) * std::ldexp(1.0, -24);
+    bool est_ok = true, certified = true;
+    max_resid = 0.0;
+    ++info.refine_rounds;
+    for (int c = 0; c < nev; ++c) {
+      rn[c] = std::sqrt(std::max(rn[c], 0.0));
+      thv[c] = tha[c];
+      max_resid = std::max(max_resid, rn[c] / std::fabs(tha[c]));
+      double yc2 = 0.0;
+      for (int j = nev; j < nb; ++j) yc2 += Y[(size_t)c * nb + j] * Y[(size_t)c * nb + j];
+      const double bound = eps32 * 1.01 * std::fabs(tha[0]) * std::sqrt(yc2);
+      if (!(rn[c] <= 0.5 * tol * std::fabs(tha[c]))) est_ok = false;
+      if (!(rn[c] + bound <= tol * std::fabs(tha[c]))) certified = false;
+    }
+    info.refine_est = max_resid;
+    if (est_ok && certified && trust_bound) {
+      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      info.refine_outcome = 1;
+      return true;
+    }
+    if (est_ok && !force_grow && verified < 3) {
+      // verification with FP64-accurate products of the Ritz vectors
+      ++verified;
+      bool ok_all = true;
+      max_resid = 0.0;
+      for (int c = 0; c < nev; ++c) {
+        double* xc = Xo.as<double>() + (int64_t)c * n;
+        double* axc = AXo.as<double>() + (int64_t)c * n;
+        prod64(xc, axc);
+        double q[2];
+        mdot(xc, n, 1, axc, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+        nrm2sq(xc, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q[0], lz.h1.p, 8, cudaMemcpyDeviceToHost, s));
+        TM_CK(cudaMemcpyAsync(&q[1], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        host_sync();
+        const double th = q[0] / q[1];
+        axpby(1.0, axc, -th, xc, lz.W.as<double>(), n, s);
+        nrm2sq(lz.W.as<double>(), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        double rr = 0.0;
+        TM_CK(cudaMemcpyAsync(&rr, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        host_sync();
+        const double res = std::sqrt(std::max(rr, 0.0) / q[1]);
+        thv[c] = th;
+        max_resid = std::max(max_resid, res / std::fabs(th));
+        if (!(res <= tol * std::max(std::fabs(th), 1e-300))) ok_all = false;
+      }
+      ++info.refine_checks;
+      info.refine_true = max_resid;
+      // the verified vectors become X0 either way
+      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(AX0.p, AXo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      if (ok_all) {
+        info.refine_outcome = 2;
+        return true;
+      }
+      // re-orthonormalise X0 (its products follow linearly) and rebuild its rows
+      for (int i = 0; i < nev; ++i) {
+        double* xi = lz.v(i);
+        double* ai = AX0.as<double>() + (int64_t)i * n;
+        for (int pass = 0; pass < 2 && i > 0; ++pass) {
+          mdot(lz.v(0), n, i, xi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+          maxpy(lz.v(0), n, i, lz.h1.as<double>(), xi, n, s);
+          maxpy(AX0.as<double>(), n, i, lz.h1.as<double>(), ai, n, s);
+        }
+        double q = 0.0;
+        nrm2sq(xi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        host_sync();
+        const double inv = 1.0 / std::sqrt(q);
+        axpby(inv, xi, 0.0, xi, xi, n, s);
+        axpby(inv, ai, 0.0, ai, ai, n, s);
+      }
+      set_x0(nb);
+      force_grow = true;
+      trust_bound = false;
+      continue;
+    }
+    force_grow = false;
+    if (verified >= 3 || round + 1 >= 3 * kRefineRounds || nb + nev > cap) break;
+    // grow: the wanted residual block, FP32 Gram-Schmidt (two passes) against
+    // the subspace, FP32 products; a column that vanishes is dropped
+    for (int c = 0; c < nev; ++c) {
+      float* w = f32col(B32, nb);
+      TM_CK(cudaMemcpyAsync(w, R32.as<float>() + (int64_t)c * n, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+      double q0 = 0.0, q = 0.0;
+      nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+      TM_CK(cudaMemcpyAsync(&q0, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+      for (int pass = 0; pass < 2; ++pass) {
+        mdot_f32(B32.as<float>(), n, nb, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+        maxpy_f32(B32.as<float>(), n, nb, lz.h1.as<double>(), w, n, s);
+      }
+      nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+      TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+      host_sync();
+      if (!(q0 > 0.0) || !(q > 1e-10 * q0)) continue;
+      normalize_f32(w, lz.nsq.as<double>(), w, n, s);
+      prod32(w, f32col(AB32, nb));
+      add_gcol(nb);
+      ++nb;
+    }
+  }
+  if (have_x) TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+  info.refine_outcome = 3;
+  return false;
+}
+
 tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t seed, int mode, double* vals,
                         double* vecs_host, tm_eigs_info* info_out) {
   auto t0 = std::chrono::steady_clock::now();
@@ -427,15 +907,17 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
           if (rr.resid[i] > tol32 * std::fabs(rr.theta[0])) return false;
         return true;
       };
+      std::unique_ptr<Lanczos32> l32;
+      std::function<void(float*)> extras;
       if (ncv <= NV32) {
         // FP32 Krylov basis (half the bytes of the FP64 basis per sweep)
-        Lanczos32 l32(op, ncv, s);
-        l32.start(seed);
-        r = l32.run(nev, 200, conv32);
-        l32.ritz_f64(r, nb0, lz.v(0));
-        // the FP32 basis is orthonormal to FP32 accuracy only: re-orthonormalise
-        // the FP64 Ritz block (CGS2) so Rayleigh-Ritz is a standard eigenproblem
-        for (int i = 0; i < nb0; ++i) {
+        l32.reset(new Lanczos32(op, ncv, s));
+        l32->start(seed);
+        r = l32->run(nev, 200, conv32);
+        // wanted Ritz vectors in FP64, re-orthonormalised (CGS2): the FP32
+        // basis is orthonormal to FP32 accuracy only
+        l32->ritz_f64(r, nev, lz.v(0));
+        for (int i = 0; i < nev; ++i) {
           double* bi = lz.v(i);
           for (int pass = 0; pass < 2 && i > 0; ++pass) {
             mdot(lz.v(0), n, i, bi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
@@ -444,8 +926,11 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
           nrm2sq(bi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
           normalize(bi, lz.nsq.as<double>(), bi, nullptr, n, s);
         }
-        lz.matvecs += l32.matvecs;
-        lz.restarts += l32.restarts;
+        // the other Ritz vectors stay FP32
+        Lanczos32* lp = l32.get();
+        extras = [lp, &r, nev, nb0](float* out) { lp->ritz_f32(r, nev, nb0 - nev, out); };
+        lz.matvecs += l32->matvecs;
+        lz.restarts += l32->restarts;
       } else {
         lz.conv_tol = tol32;
         lz.stagnation_stop = true;
@@ -453,191 +938,15 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         lz.stagnation_stop = false;
         lz.rotate(r, nb0);
       }
-      // FP64 refinement: block Davidson with mixed-precision products.  B
-      // starts as the FP32 phase's Ritz vectors; the nev wanted ones get
-      // FP64-accurate products (apply_refine), the others FP32 products, and
-      // each growth step appends the wanted residual block, again with FP32
-      // products.  An FP32 product error reaches a Ritz pair only through the
-      // pair's weight on that column, which is at the FP32 noise level for
-      // the wanted pairs, so Rayleigh-Ritz values and residual estimates stay
-      // FP64-accurate.  The extra Ritz vectors carry the eigenvectors next to
-      // the wanted ones, which residual blocks alone resolve slowly.  When the
-      // estimates meet tol, the wanted Ritz vectors get FP64-accurate products
-      // and are accepted on the test of the FP64 Lanczos path and of Spectra's
-      // SymEigsSolver: ||A x - theta x|| <= tol * |theta|.
-      const int nx = nb0;
-      const int cap = nx + 2 * nev;
-      DBuf Bb, AB, XB, AXB, G, Gw, Gz, th;
+      // FP64-accurate refinement (refine_mixed); leaves the best Ritz
+      // vectors in V's leading columns either way
       std::vector<double> thv(nev);
-      bool refined = false;
-      // cluster guard: FP32 Ritz values closer than 1e-5 (relative) cannot be
-      // told apart from FP32-accurate vectors; solve those (and operators too
-      // small for a block of cap columns) in FP64 directly
-      bool cluster = (int64_t)cap * 4 > n;
+      bool cluster = false;
       for (int i = 0; i < nev && i + 1 < (int)r.theta.size(); ++i)
         if (std::fabs(r.theta[i] - r.theta[i + 1]) < 1e-5 * std::fabs(r.theta[i])) cluster = true;
-      if (!cluster) {
-        Bb.alloc((size_t)cap * n * 8);
-        AB.alloc((size_t)cap * n * 8);
-        XB.alloc((size_t)cap * n * 8);
-        AXB.alloc((size_t)cap * n * 8);
-        G.alloc((size_t)cap * cap * 8);
-        Gw.alloc(64 * 8);
-        Gz.alloc((size_t)64 * 64 * 8);
-        th.alloc(64 * 8);
-      }
-      double* B = Bb.as<double>();
-      auto col = [&](const DBuf& b, int j) { return b.as<double>() + (int64_t)j * n; };
-      auto prod32 = [&](const double* x, double* y) {
-        lz.ensure32();
-        to_f32(x, lz.x32.as<float>(), n, s);
-        const double S = apply_internal(op, nullptr, nullptr, lz.x32.as<float>(), lz.y32.as<float>(), true, s);
-        f32_scaled_kernel<<<blocks_for(n), 256, 0, s>>>(lz.y32.as<float>(), S, y, n);
-        TM_CKK("f32_scaled");
-        ++lz.matvecs;
-      };
-      auto prod64 = [&](const double* x, double* y) {
-        apply_refine(op, x, y, s);
-        ++lz.matvecs;
-        ++lz.matvecs64;
-      };
-      auto norm_host = [&](const double* v) {
-        double q = 0.0;
-        nrm2sq(v, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-        TM_CK(cudaStreamSynchronize(s));
-        return std::sqrt(std::max(q, 0.0));
-      };
-      // imp[j]: weight of column j on FP32-product columns (0: FP64-accurate)
-      std::vector<double> imp(cap, 1.0);
-      int nb = nx, verified = 0;
-      if (!cluster) {
-        TM_CK(cudaMemcpyAsync(B, lz.v(0), (size_t)nx * n * 8, cudaMemcpyDeviceToDevice, s));
-        for (int j = 0; j < nx; ++j) {
-          if (j < nev) {
-            prod64(B + (int64_t)j * n, col(AB, j));
-            imp[j] = 0.0;
-          } else {
-            prod32(B + (int64_t)j * n, col(AB, j));
-          }
-        }
-      }
-      for (int round = 0; round < kRefineRounds && !cluster; ++round) {
-        // G(i, j) = B_i . (A B_j), symmetrised from the side whose product is
-        // the more accurate one
-        for (int j = 0; j < nb; ++j)
-          mdot(B, n, nb, col(AB, j), n, G.as<double>() + (int64_t)j * nb, lz.part.as<double>(), s);
-        std::vector<double> gh((size_t)nb * nb), gs((size_t)nb * nb);
-        TM_CK(cudaMemcpyAsync(gh.data(), G.p, gh.size() * 8, cudaMemcpyDeviceToHost, s));
-        TM_CK(cudaStreamSynchronize(s));
-        for (int j = 0; j < nb; ++j)
-          for (int i = 0; i < nb; ++i) {
-            const double gij = gh[(size_t)j * nb + i], gji = gh[(size_t)i * nb + j];
-            gs[(size_t)j * nb + i] = imp[j] < imp[i] ? gij : imp[i] < imp[j] ? gji : 0.5 * (gij + gji);
-          }
-        TM_CK(cudaMemcpyAsync(G.p, gs.data(), gs.size() * 8, cudaMemcpyHostToDevice, s));
-        small_symeig(G.as<double>(), nb, Gw.as<double>(), Gz.as<double>(), s, nb);
-        std::vector<double> gw(nb), gz((size_t)nb * nb);
-        TM_CK(cudaMemcpyAsync(gw.data(), Gw.p, nb * 8, cudaMemcpyDeviceToHost, s));
-        TM_CK(cudaMemcpyAsync(gz.data(), Gz.p, (size_t)nb * nb * 8, cudaMemcpyDeviceToHost, s));
-        TM_CK(cudaStreamSynchronize(s));
-        std::vector<int> ord(nb);
-        std::iota(ord.begin(), ord.end(), 0);
-        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
-        std::vector<double> Y((size_t)nb * nb), tha(nb), impn(nb, 0.0);
-        for (int c = 0; c < nb; ++c) {
-          tha[c] = gw[ord[c]];
-          for (int j = 0; j < nb; ++j) {
-            const double y = gz[(size_t)ord[c] * nb + j];
-            Y[(size_t)c * nb + j] = y;
-            impn[c] += y * y * imp[j];
-          }
-        }
-        TM_CK(cudaMemcpyAsync(lz.Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
-        basis_combine(B, n, nb, lz.Ysel.as<double>(), nb, XB.as<double>(), n, n, s);
-        basis_combine(AB.as<double>(), n, nb, lz.Ysel.as<double>(), nb, AXB.as<double>(), n, n, s);
-        // thick restart on the leading Ritz pairs; the wanted residual block
-        // goes to the columns after them
-        const int keep = std::min(nb, cap - nev);
-        TM_CK(cudaMemcpyAsync(B, XB.p, (size_t)keep * n * 8, cudaMemcpyDeviceToDevice, s));
-        TM_CK(cudaMemcpyAsync(AB.p, AXB.p, (size_t)keep * n * 8, cudaMemcpyDeviceToDevice, s));
-        for (int c = 0; c < keep; ++c) imp[c] = impn[c];
-        TM_CK(cudaMemcpyAsync(th.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
-        resid_kernel<<<blocks_for(n), 256, 0, s>>>(AB.as<double>(), B, n, nev, th.as<double>(),
-                                                     B + (int64_t)keep * n, n);
-        TM_CKK("resid");
-        std::vector<double> rn(nev);
-        bool est_ok = true;
-        max_resid = 0.0;
-        for (int i = 0; i < nev; ++i) {
-          thv[i] = tha[i];
-          rn[i] = norm_host(B + (int64_t)(keep + i) * n);
-          max_resid = std::max(max_resid, rn[i] / std::fabs(tha[i]));
-          if (!(rn[i] <= 0.5 * tol * std::fabs(tha[i]))) est_ok = false;
-        }
-        if (est_ok && verified < 3) {
-          // verification: FP64-accurate products of the wanted Ritz vectors,
-          // Rayleigh quotients and true residuals
-          ++verified;
-          bool ok_all = true;
-          max_resid = 0.0;
-          for (int i = 0; i < nev; ++i) {
-            double* xi = B + (int64_t)i * n;
-            double* axi = col(AB, i);
-            prod64(xi, axi);
-            imp[i] = 0.0;
-            double q = 0.0;
-            mdot(xi, n, 1, axi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-            TM_CK(cudaMemcpyAsync(&q, lz.h1.p, 8, cudaMemcpyDeviceToHost, s));
-            TM_CK(cudaStreamSynchronize(s));
-            thv[i] = q;
-            tha[i] = q;
-          }
-          TM_CK(cudaMemcpyAsync(th.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
-          resid_kernel<<<blocks_for(n), 256, 0, s>>>(AB.as<double>(), B, n, nev, th.as<double>(),
-                                                       B + (int64_t)keep * n, n);
-          TM_CKK("resid");
-          for (int i = 0; i < nev; ++i) {
-            rn[i] = norm_host(B + (int64_t)(keep + i) * n);
-            max_resid = std::max(max_resid, rn[i] / std::fabs(thv[i]));
-            if (!(rn[i] <= tol * std::max(std::fabs(thv[i]), 1e-300))) ok_all = false;
-          }
-          if (ok_all) {
-            refined = true;
-            break;
-          }
-        }
-        if (round + 1 == kRefineRounds) break;
-        // orthonormalise the residual block against B (CGS2) and give it FP32
-        // products; a column that vanishes is dropped
-        nb = keep;
-        for (int i = 0; i < nev; ++i) {
-          double* rv = B + (int64_t)(keep + i) * n;
-          double* dst = B + (int64_t)nb * n;
-          if (dst != rv) TM_CK(cudaMemcpyAsync(dst, rv, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
-          const double r0 = norm_host(dst);
-          for (int pass = 0; pass < 2; ++pass) {
-            mdot(B, n, nb, dst, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-            maxpy(B, n, nb, lz.h1.as<double>(), dst, n, s);
-          }
-          nrm2sq(dst, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-          double q = 0.0;
-          TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-          TM_CK(cudaStreamSynchronize(s));
-          if (!(q > 1e-24 * r0 * r0) || !(r0 > 0.0)) continue;
-          normalize(dst, lz.nsq.as<double>(), dst, nullptr, n, s);
-          prod32(dst, col(AB, nb));
-          imp[nb] = 1.0;
-          ++nb;
-        }
-      }
-      if (refined) TM_CK(cudaMemcpyAsync(XB.p, B, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
-      if (cluster) {
-        XB.alloc((size_t)nev * n * 8);
-        TM_CK(cudaMemcpyAsync(XB.p, lz.v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
-      }
-      // final Ritz vectors into V's leading columns
-      TM_CK(cudaMemcpyAsync(lz.v(0), XB.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      const bool refined = !cluster && nev <= kMaxRefineNev && (int64_t)(nb0 + 6 * nev) * 4 <= n &&
+                           refine_mixed(op, lz, nev, nb0, tol, thv, max_resid, extras, info);
+      if (!refined && info.refine_outcome == 0) info.refine_outcome = 3;
       if (refined) {
         theta = thv;
         done = true;

@@ -1,5 +1,6 @@
 """GPU: general (non-symmetric) operators -- diagonal BNNNI full (ZBT) and
-reduced (ZBM) -- transpose products, complex-capable eigenvalues and the left
+reduced (ZBM), the two-layer y-ANNNI / y2-ANNNI / BNNNI operators (YAT, Y2AT,
+YAM, YBM) -- transpose products, complex-capable eigenvalues and the left
 eigenvector from the transpose solve, against the reference's own outputs."""
 import numpy as np
 import pytest
@@ -20,7 +21,7 @@ def assert_eigs_match(vals, ref, rtol):
         assert err < rtol, (z, vals)
 
 
-@pytest.mark.parametrize("name", case_names(["zbt", "zbm"]))
+@pytest.mark.parametrize("name", case_names(["zbt", "zbm", "yat", "yam", "ybm"]))
 def test_transpose_product(name):
     f = fixture(name)
     op = make_op(name)
@@ -34,7 +35,7 @@ def test_transpose_product(name):
 
 
 @pytest.mark.parametrize("mode", [lt.TM_EIGS_F64, lt.TM_EIGS_MIXED])
-@pytest.mark.parametrize("name", case_names(["zbt", "zbm"]))
+@pytest.mark.parametrize("name", case_names(["zbt", "zbm", "yat", "y2at", "yam", "ybm"]))
 def test_general_eigenvalues_and_left_vector(name, mode):
     f = fixture(name)
     op = make_op(name)
@@ -50,3 +51,11 @@ def test_general_eigenvalues_and_left_vector(name, mode):
     m, st = op.moments(ql, q)
     np.testing.assert_allclose(m, f["moments"], rtol=1e-6, atol=1e-9)
     assert st == int(f["moments_status"])
+
+
+def test_y2at_transpose_is_the_operator():
+    """Y2ATMatVecProd2D's get_t_instance returns the operator itself
+    (TMat/tmat.hpp:382-384); the transposed view here does the same."""
+    op = make_op("y2at_L5_h")
+    x = seeded_input(op.rows(), 4)
+    assert rel_err(op.get_t_instance().perform_op(x), op.perform_op(x)) == 0.0

@@ -12,7 +12,7 @@ from gpu_util import case_names, checksum_weights, fixture, make_op, rel_err, se
 
 pytestmark = pytest.mark.gpu
 
-IMPLEMENTED = ["xat", "xam", "x3d", "xdt", "xdm", "zbt", "zbm"]
+IMPLEMENTED = ["xat", "xam", "x3d", "xdt", "xdm", "zbt", "zbm", "yat", "y2at", "yam", "ybm"]
 SYM = ["xat", "xam", "x3d", "xdt", "xdm"]
 
 
@@ -41,7 +41,7 @@ def test_matvec_fp64(name):
     np.testing.assert_allclose(chk, f["y_chk"], rtol=1e-12)
 
 
-@pytest.mark.parametrize("name", case_names(["xam", "x3d", "xdm", "zbm"]))
+@pytest.mark.parametrize("name", case_names(["xam", "x3d", "xdm", "zbm", "yam", "ybm"]))
 def test_orbit_table_bit_exact(name):
     f = fixture(name)
     op = _skip_if_unavailable(lambda: make_op(name))
@@ -75,6 +75,39 @@ def test_matvec_fp32_device(name):
     op.perform_op_dev(xd64.data_ptr(), yd64.data_ptr(), lt.TM_F64, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert rel_err(yd64.cpu().numpy(), ref) < 1e-12
+
+
+@pytest.mark.parametrize("name", case_names(["yat", "y2at", "yam", "ybm"]))
+def test_two_layer_fp64_only(name):
+    """The two-layer operators run in FP64 only: an FP32 device product is
+    refused with TM_ERR_UNSUPPORTED, the FP64 one matches the reference."""
+    torch = pytest.importorskip("torch")
+    f = fixture(name)
+    op = make_op(name)
+    x = seeded_input(op.rows(), 1)
+    x32 = torch.tensor(x, dtype=torch.float32, device="cuda")
+    y32 = torch.empty_like(x32)
+    with pytest.raises(lt.TMError) as e:
+        op.perform_op_dev(x32.data_ptr(), y32.data_ptr(), lt.TM_F32)
+    assert e.value.code == lt.TM_ERR_UNSUPPORTED
+    x64 = torch.tensor(x, dtype=torch.float64, device="cuda")
+    y64 = torch.empty_like(x64)
+    op.perform_op_dev(x64.data_ptr(), y64.data_ptr(), lt.TM_F64)
+    torch.cuda.synchronize()
+    assert rel_err(y64.cpu().numpy(), f["y"]) < 1e-12
+
+
+@pytest.mark.parametrize("L", [5, 7])
+def test_yat_odd_width_against_oracle(L):
+    """Odd widths: the reference's YATMatVecProd2D output is not T x there (its
+    final permutation reads its own output buffer); the oracle computes T x,
+    and its spectrum matches the reference's reduced YAMMatVecProd2D."""
+    oracle = pytest.importorskip("oracle.oracle")
+    op = lt.TMatOp("A", 2, 2, 0.4, 0.3, 0.1, L)
+    ref = oracle.OracleOp("A", 2, 2, 0.4, 0.3, 0.1, L)
+    x = seeded_input(op.rows(), 3)
+    assert rel_err(op.perform_op(x), ref.perform_op(x)) < 1e-12
+    assert rel_err(op.get_t_instance().perform_op(x), ref.perform_op_t(x)) < 1e-12
 
 
 @pytest.mark.parametrize("mode", [lt.TM_EIGS_F64, lt.TM_EIGS_MIXED])
