@@ -8,17 +8,25 @@
 // sites per step with two carried bits; its transpose swaps the roles of the
 // coupling factors (optdirection = 1).
 //
-// GPU form: every sweep step is one output-centric kernel over all
-// (lastbit pass, aux, state) elements at once.  The reference runs its
-// lastbit passes (2 for DNNI, 4 for BNNNI) one after another; here they are
-// independent slices of one launch.  Each output element is computed directly
-// from its 2 or 4 inputs (no scatter).  Steps are scaled by the inverse of
-// their largest row sum, so FP32 intermediates stay in range; the product of
-// the scales is applied in FP64 at the fold.  Reduced operators (XDM, ZBM)
-// expand through the state->rank map, run the same core, and contract at the
-// orbit representatives.
+// The reference rotates the state by one (two) sites after every step, so the
+// sites a step touches are always the low ones.  Undoing the rotation (a
+// fixed frame: after L/KS steps the rotation is the identity) shows that step
+// t is a local gate: it rewrites the aux bits and the KS sites at positions
+// KS*t .. KS*t+KS-1 from the same 2^(NA+KS) values, with weights that depend on
+// the next KS sites (or, at the last step, on the lastbit pass).  Here a pass
+// gathers tiles of 2^12 (FP64) or 2^13 (FP32) elements whose index bits are the
+// aux bits, a few contiguous low sites (coalescing) and the sites of several
+// consecutive steps, applies those steps in shared memory and writes the tile
+// back in place: ceil(steps / steps-per-pass) sweeps over HBM instead of one
+// per step.  The first pass builds its tiles from x (the reference's sparse
+// initial vector), the last pass folds aux bits and lastbit passes into y.
+// Arithmetic per element is the reference's, in its order.  FP32 steps are
+// scaled by the inverse of their largest row sum; the product of the scales
+// is applied in FP64.  Reduced operators (XDM, ZBM) gather x through the
+// state->rank map and contract the full-space result at the representatives.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "tm_internal.h"
 
@@ -41,154 +49,212 @@ int grid_for(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)num_sms() * 32));
 }
 
-// ------------------------------------------------------------------ DNNI
-// element e of a 2*2*N buffer: e = (lb << (L+1)) | (aux << L) | r
-template <class T>
-__global__ void xdt_init(const T* __restrict__ x, const double* __restrict__ pre, int L, int bc,
-                         AuxCoefT<T> c, int npass, T* __restrict__ P) {
-  const int64_t N = 1ll << L;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < N * npass; i += st) {
-    const int lb = (int)(i >> L);
-    const uint64_t rp = (uint64_t)(i & (N - 1));
-    T* Q = P + (int64_t)lb * 2 * N;
-    T v = pre ? (T)((double)x[rp] * pre[rp]) : x[rp];
-    if (bc == 0) {
-      // TMat/tmat.cpp:392-405: aux bit = copy of the top bit
-      const uint64_t rpb = ((rp & (uint64_t)(N >> 1)) << 1) | rp;
-      Q[rpb] = ((int)(rp & 1) == lb) ? v : (T)0;
-      Q[rpb ^ (uint64_t)N] = 0;
-    } else if (bc == 5) {
-      // TMat/tmat.cpp:440-449
-      Q[rp] = v * c.b2[rp & 1] * c.b2[rp >> (L - 1)];
-      Q[rp | (uint64_t)N] = 0;
-    } else {
-      // bc 9, TMat/tmat.cpp:452-457
-      Q[rp | (uint64_t)N] = v * c.b2[(rp & 1) ^ 1] * c.b2[rp >> (L - 1)];
-      Q[rp] = 0;
+__device__ __forceinline__ int spad(int e) { return e + (e >> 5); }
+
+// byte offset of the fold accumulators in chain_kernel's shared memory
+__host__ __device__ __forceinline__ size_t chain_acc_offset(int tile, size_t elem) {
+  return (((size_t)(tile + tile / 32 + 1) * elem) + 15) & ~(size_t)15;
+}
+
+// Geometry of one pass.  Element index in HBM: ((lb << L | r) << NA) | aux.
+// Tile index e: bits [0, NA) aux, then tile state bits k -> state position
+// spos[k]; the outer index (blockIdx) deposits into opos[] (state bits) and,
+// when the lastbit pass is outer, into lb.
+struct ChainPass {
+  int nst;         // tile state bits
+  int spos[16];
+  int no;          // outer state bits
+  int opos[32];
+  int t0, T;       // steps [t0, t0 + T)
+  int jbit0;       // tile state bit of step t0's lowest site
+  int first, last; // build from x / fold into y
+  int nlb;         // lastbit passes (DNNI 2 or 1, BNNNI 4)
+};
+
+__device__ __forceinline__ uint64_t dep(uint64_t v, const int* pos, int nb) {
+  uint64_t g = 0;
+  for (int k = 0; k < nb; ++k) g |= ((v >> k) & 1ull) << pos[k];
+  return g;
+}
+
+// Initial (lastbit pass lb) value of element (aux, r): TMat/tmat.cpp:392-457
+// (DNNI: aux = copy of the top site, site 0 = lb; boundary cases 5 and 9) and
+// :604-612 (BNNNI: aux = copy of the two top sites, sites 0-1 = lb).
+template <class T, int ZB>
+__device__ __forceinline__ T chain_init(const T* __restrict__ x, const double* __restrict__ pre,
+                                        const uint32_t* __restrict__ smap, int L, int bc, uint64_t r, int aux, int lb,
+                                        const AuxCoefT<T>& c) {
+  auto u = [&]() -> T {
+    if (smap) {
+      const uint32_t q = smap[r];
+      return (T)((double)x[q] * pre[q]);
     }
+    return pre ? (T)((double)x[r] * pre[r]) : x[r];
+  };
+  if (ZB) {
+    if ((int)(r >> (L - 2)) == aux && (int)(r & 3) == lb) return u();
+    return (T)0;
   }
+  if (bc == 0) {
+    if ((int)(r >> (L - 1)) == aux && (int)(r & 1) == lb) return u();
+    return (T)0;
+  }
+  if (bc == 5) return aux == 0 ? u() * c.b2[r & 1] * c.b2[r >> (L - 1)] : (T)0;
+  return aux == 1 ? u() * c.b2[(r & 1) ^ 1] * c.b2[r >> (L - 1)] : (T)0;  // bc 9
 }
 
-// one sweep step (permute_mult_T1 / _last, TMat/tmat.cpp:344-376), output-centric
-template <class T>
-__global__ void xdt_step(const T* __restrict__ X, T* __restrict__ Y, int L, AuxCoefT<T> c, int last,
-                         int bc, int npass) {
-  const int64_t N = 1ll << L;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < 2 * N * npass; i += st) {
-    const int lb = (int)(i >> (L + 1));
-    const uint64_t loc = (uint64_t)(i & (2 * N - 1));
-    const uint64_t a = loc >> L, r = loc & (uint64_t)(N - 1);
-    const uint64_t rp = rotl(r, L, 1);
-    const uint64_t s = rp & 1;
-    const uint64_t rq = (rp & ~1ull) | a;
-    const uint64_t nb = last ? (bc == 0 ? (uint64_t)lb : 0ull) : ((rq >> 1) & 1);
-    const T* Xp = X + (int64_t)lb * 2 * N;
-    T v = c.b1[s ^ a] * c.b2[nb ^ s] * (c.b2[s] * Xp[rq] + c.b2[s ^ 1] * Xp[rq | (uint64_t)N]);
-    Y[i] = v * c.g;
-  }
-}
-
-template <class T>
-__global__ void xdt_fold(const T* __restrict__ P, const double* __restrict__ post, double postc, int L, int npass,
-                         T* __restrict__ y) {
-  const int64_t N = 1ll << L;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < N; i += st) {
-    double acc = 0.0;
-    for (int lb = 0; lb < npass; ++lb) acc += (double)P[(int64_t)lb * 2 * N + i] + (double)P[(int64_t)lb * 2 * N + N + i];
-    if (post) acc *= post[i];
-    y[i] = (T)(acc * postc);
-  }
-}
-
-// ------------------------------------------------------------------ diagonal BNNNI
-// element e of a 4*4*N buffer: e = (lb << (L+2)) | (aux << L) | r
-template <class T>
-__global__ void zbt_init(const T* __restrict__ x, const double* __restrict__ pre, int L, T* __restrict__ P) {
-  const int64_t N = 1ll << L;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < N * 4; i += st) {
-    const int lb = (int)(i >> L);
-    const uint64_t rp = (uint64_t)(i & (N - 1));
-    T* Q = P + (int64_t)lb * 4 * N;
-    // TMat/tmat.cpp:607-619: aux bits = copy of the top two bits
-    const uint64_t nc = (uint64_t)((N >> 1) | (N >> 2));
-    const uint64_t rpb = ((rp & nc) << 2) | rp;
-    T v = pre ? (T)((double)x[rp] * pre[rp]) : x[rp];
-    Q[rpb] = ((int)(rp & 3) == lb) ? v : (T)0;
-    Q[rpb ^ (uint64_t)N] = 0;
-    Q[rpb ^ (uint64_t)(2 * N)] = 0;
-    Q[rpb ^ (nc << 2)] = 0;
-  }
-}
-
-// permute_mult_T1 / _last of ZBTMatVecProd2D (TMat/tmat.cpp:521-588), output-centric
-template <class T>
-__global__ void zbt_step(const T* __restrict__ X, T* __restrict__ Y, int L, AuxCoefT<T> c, int last, int dir) {
-  const int64_t N = 1ll << L;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < 16 * N; i += st) {
-    const uint64_t lb = (uint64_t)(i >> (L + 2));
-    const uint64_t loc = (uint64_t)(i & (4 * N - 1));
-    const uint64_t aux = loc >> L, r = loc & (uint64_t)(N - 1);
-    const uint64_t rp = rotl(r, L, 2);
-    const uint64_t rq = (rp & ~3ull) | aux;
-    const uint64_t sl = (rp >> 1) & 1, sr = rp & 1, pl = aux >> 1, pr = aux & 1;
-    const uint64_t fl = last ? (lb >> 1) : ((rp >> 3) & 1), fr = last ? (lb & 1) : ((rp >> 2) & 1);
-    T v;
-    if (!dir)
-      v = c.b1[sr ^ pl] * c.b2[sr ^ fr] * c.b2[sl ^ fl] * c.b3[sr ^ pr] * c.b3[sl ^ pl];
-    else
-      v = c.b1[sl ^ fr] * c.b1[sl ^ pr] * c.b2[sr ^ fr] * c.b2[sl ^ fl] * c.b3[sr ^ pr] * c.b3[sl ^ pl];
-    const T* Xp = X + (int64_t)lb * 4 * N;
-    T d = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const uint64_t al = (uint64_t)q >> 1, ar = (uint64_t)q & 1;
-      const T xv = Xp[((uint64_t)q << L) | rq];
+// One pass of steps over tiles in shared memory.
+//   ZB = 0: DNNI, NA = 1 aux bit, one site per step (permute_mult_T1 /
+//           _last, TMat/tmat.cpp:344-376); L steps.
+//   ZB = 1: diagonal BNNNI, NA = 2, two sites per step (TMat/tmat.cpp:521-588,
+//           dir = optdirection); L/2 steps.
+// P: the nlb*2^L*2^NA buffer (in place).  first: tiles built from x; last:
+// y[r] = postc * post[r] * sum_{lb, aux} (one CTA loops the lastbit passes).
+template <class T, int ZB>
+__global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const T* __restrict__ x,
+                                                    const double* __restrict__ pre, const uint32_t* __restrict__ smap,
+                                                    T* __restrict__ y, const double* __restrict__ post, double postc,
+                                                    int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {
+  constexpr int NA = ZB ? 2 : 1, KS = ZB ? 2 : 1, GB = NA + KS;  // group bits
+  extern __shared__ unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int tile = 1 << (NA + cp.nst);
+  const int nsteps = ZB ? L / 2 : L;
+  // FP64 fold accumulators after the padded tile, at a 16-byte boundary
+  // (the FP32 tile's padded size is not a multiple of 8 bytes)
+  double* acc = reinterpret_cast<double*>(smraw + chain_acc_offset(tile, sizeof(T)));
+  // Step coefficients, functions of the control bits only, multiplied out
+  // once per launch.  BNNNI: out(aux, s) = vt[f][aux][s] * sum_q wt[s][q]
+  // in(q, aux) with f = (fl, fr) (the reference's v and d factors, the step
+  // normalisation folded into vt).  DNNI: out(a, s) = sum_q cf[nb][a][s][q]
+  // in(q, a).
+  __shared__ T vt[64];
+  __shared__ T wt[16];
+  if (ZB) {
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) {
+      const int f = k >> 4, aux = (k >> 2) & 3, sv = k & 3;
+      const int fl = f >> 1, fr = f & 1, pl = aux >> 1, pr = aux & 1, sl = sv >> 1, sr = sv & 1;
+      T v;
       if (!dir)
-        d += xv * c.b1[sr ^ al] * c.b2[sr ^ ar] * c.b2[sl ^ al];
+        v = c.b1[sr ^ pl] * c.b2[sr ^ fr] * c.b2[sl ^ fl] * c.b3[sr ^ pr] * c.b3[sl ^ pl];
       else
-        d += xv * c.b2[sr ^ ar] * c.b2[sl ^ al];
+        v = c.b1[sl ^ fr] * c.b1[sl ^ pr] * c.b2[sr ^ fr] * c.b2[sl ^ fl] * c.b3[sr ^ pr] * c.b3[sl ^ pl];
+      vt[k] = v * c.g;
     }
-    Y[i] = v * d * c.g;
+    for (int k = threadIdx.x; k < 16; k += blockDim.x) {
+      const int sv = k >> 2, q = k & 3, sl = sv >> 1, sr = sv & 1, al = q >> 1, ar = q & 1;
+      wt[k] = !dir ? c.b1[sr ^ al] * c.b2[sr ^ ar] * c.b2[sl ^ al] : c.b2[sr ^ ar] * c.b2[sl ^ al];
+    }
+  } else {
+    for (int k = threadIdx.x; k < 16; k += blockDim.x) {
+      const int nb = k >> 3, a = (k >> 2) & 1, sv = (k >> 1) & 1, q = k & 1;
+      wt[k] = c.b1[sv ^ a] * c.b2[nb ^ sv] * c.b2[sv ^ q] * c.g;
+    }
+  }
+  // outer index: state bits, then (unless last) the lastbit pass
+  const uint64_t ob = blockIdx.x & ((1ull << cp.no) - 1);
+  const int lb_outer = (int)(blockIdx.x >> cp.no);
+  const uint64_t rbase = dep(ob, cp.opos, cp.no);
+  const int nloop = cp.last ? cp.nlb : 1;
+  if (cp.last)
+    for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) acc[e] = 0.0;
+  for (int li = 0; li < nloop; ++li) {
+    const int lb = cp.last ? li : lb_outer;
+    // load / build the tile
+    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+      const int aux = e & ((1 << NA) - 1);
+      const uint64_t r = rbase | dep((uint64_t)(e >> NA), cp.spos, cp.nst);
+      T v;
+      if (cp.first)
+        v = chain_init<T, ZB>(x, pre, smap, L, bc, r, aux, lb, c);
+      else
+        v = P[(((uint64_t)lb << L | r) << NA) | (uint64_t)aux];
+      sm[spad(e)] = v;
+    }
+    __syncthreads();
+    for (int j = 0; j < cp.T; ++j) {
+      const int t = cp.t0 + j;
+      const int sb = NA + cp.jbit0 + KS * j;  // tile bit of the step's lowest site
+      const bool lastst = (t == nsteps - 1);
+      const int groups = tile >> GB;
+      for (int gi = threadIdx.x; gi < groups; gi += blockDim.x) {
+        // tile index of the group base: insert zeros at [0, NA) and [sb, sb+KS)
+        int rest = gi;
+        const int lo = rest & ((1 << (sb - NA)) - 1);
+        const int hi = rest >> (sb - NA);
+        const int ebase = (hi << (sb + KS)) | (lo << NA);
+        const uint64_t r = rbase | dep((uint64_t)(ebase >> NA), cp.spos, cp.nst);
+        if (!ZB) {
+          // DNNI: out(a, s) = b1[s^a] b2[nb^s] (b2[s] in(0, a) + b2[s^1] in(1, a)),
+          // in(q, s') = value with aux q and site t = s'
+          const int nb = lastst ? (bc == 0 ? lb : 0) : (int)((r >> (t + 1)) & 1);
+          const T* cfn = wt + nb * 8;
+          T in[2][2];
+#pragma unroll
+          for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int sp = 0; sp < 2; ++sp) in[q][sp] = sm[spad(ebase | q | (sp << sb))];
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int sv = 0; sv < 2; ++sv)
+              sm[spad(ebase | a | (sv << sb))] = cfn[a * 4 + sv * 2] * in[0][a] + cfn[a * 4 + sv * 2 + 1] * in[1][a];
+        } else {
+          // BNNNI: out((pl,pr), (sl,sr)) = v * sum_q w(q) in(q, (pl,pr))
+          const int fl = lastst ? (lb >> 1) : (int)((r >> (2 * t + 3)) & 1);
+          const int fr = lastst ? (lb & 1) : (int)((r >> (2 * t + 2)) & 1);
+          const T* vf = vt + ((fl << 1) | fr) * 16;
+          T in[4][4], out[4][4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int sp = 0; sp < 4; ++sp) in[q][sp] = sm[spad(ebase | q | (sp << sb))];
+#pragma unroll
+          for (int sv = 0; sv < 4; ++sv) {
+            const T w0 = wt[sv * 4], w1 = wt[sv * 4 + 1], w2 = wt[sv * 4 + 2], w3 = wt[sv * 4 + 3];
+#pragma unroll
+            for (int aux = 0; aux < 4; ++aux) {
+              T d = in[0][aux] * w0;
+              d += in[1][aux] * w1;
+              d += in[2][aux] * w2;
+              d += in[3][aux] * w3;
+              out[aux][sv] = vf[aux * 4 + sv] * d;
+            }
+          }
+#pragma unroll
+          for (int aux = 0; aux < 4; ++aux)
+#pragma unroll
+            for (int sv = 0; sv < 4; ++sv) sm[spad(ebase | aux | (sv << sb))] = out[aux][sv];
+        }
+      }
+      __syncthreads();
+    }
+    if (cp.last) {
+      for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) {
+        double a = acc[e];
+#pragma unroll
+        for (int aux = 0; aux < (1 << NA); ++aux) a += (double)sm[spad((e << NA) | aux)];
+        acc[e] = a;
+      }
+    } else {
+      for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        const uint64_t r = rbase | dep((uint64_t)(e >> NA), cp.spos, cp.nst);
+        P[(((uint64_t)lb << L | r) << NA) | (uint64_t)(e & ((1 << NA) - 1))] = sm[spad(e)];
+      }
+    }
+    __syncthreads();
+  }
+  if (cp.last) {
+    for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) {
+      const uint64_t r = rbase | dep((uint64_t)e, cp.spos, cp.nst);
+      double v = acc[e];
+      if (post) v *= post[r];
+      y[r] = (T)(v * postc);
+    }
   }
 }
 
-template <class T>
-__global__ void zbt_fold(const T* __restrict__ P, const double* __restrict__ post, double postc, int L,
-                         T* __restrict__ y) {
-  const int64_t N = 1ll << L;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < N; i += st) {
-    double acc = 0.0;
-    for (int lb = 0; lb < 4; ++lb)
-      for (int a = 0; a < 4; ++a) acc += (double)P[(int64_t)lb * 4 * N + (int64_t)a * N + i];
-    if (post) acc *= post[i];
-    y[i] = (T)(acc * postc);
-  }
-}
-
-// ------------------------------------------------------------------ reduced expand / contract
-template <class T>
-__global__ void red_expand(const T* __restrict__ x, const double* __restrict__ tv, const uint32_t* __restrict__ smap,
-                           int64_t N, T* __restrict__ v) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < N; i += st) {
-    uint32_t r = smap[i];
-    v[i] = (T)((double)x[r] * tv[r]);
-  }
-}
-
+// ------------------------------------------------------------------ reduced contract
 template <class T>
 __global__ void red_contract(const T* __restrict__ z, const uint32_t* __restrict__ idx, const uint16_t* __restrict__ dup,
                              const double* __restrict__ tv, double post, T* __restrict__ y, int64_t n) {
@@ -245,13 +311,11 @@ void build_aux(Op& op) {
   const int L = op.L;
   const int64_t N = 1ll << L;
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
-  if (op.kind == K_ZBT || op.kind == K_ZBM) {
-    if (L % 2) fail(TM_ERR_ARG, "diagonal BNNNI operators need an even width");
-  }
-  const int64_t per = zb ? 16 * N : 4 * N;  // elements per sweep buffer
+  if (zb && L % 2) fail(TM_ERR_ARG, "diagonal BNNNI operators need an even width");
+  // one in-place pass buffer of nlb * 2^NA * 2^L elements (FP64 size)
+  const int64_t per = zb ? 16 * N : 4 * N;
   op.ws_a.alloc((size_t)per * 8);
-  op.ws_b.alloc((size_t)per * 8);
-  if (op.kind == K_XDM || op.kind == K_ZBM) op.xp.alloc((size_t)N * 8);  // expanded / contracted full vector
+  if (op.kind == K_XDM || op.kind == K_ZBM) op.xp.alloc((size_t)N * 8);  // full-space result before contraction
 }
 
 // y = T x (or T^T x for transposed views); scaled: FP32 result divided by the
@@ -259,7 +323,6 @@ void build_aux(Op& op) {
 template <class T>
 double matvec_aux_dir(const Op& op, const T* x, T* y, bool scaled, int dir, cudaStream_t s) {
   const int L = op.L;
-  const int64_t N = 1ll << L;
   const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
   AuxCoef c64 = coef_of(op);
@@ -272,44 +335,57 @@ double matvec_aux_dir(const Op& op, const T* x, T* y, bool scaled, int dir, cuda
     c.b3[k] = (T)c64.b3[k];
   }
   c.g = norm ? (T)(1.0 / gb) : (T)1;
+  const int NA = zb ? 2 : 1, KS = zb ? 2 : 1;
   const int nsteps = zb ? L / 2 : L;
   const double gscale = norm ? std::pow(gb, (double)nsteps) : 1.0;
-  T* A = op.ws_a.as<T>();
-  T* B = op.ws_b.as<T>();
-  const T* xin = x;
-  const double* pre = op.tvec.as<double>();
-  if (reduced) {
-    T* v = op.xp.as<T>();
-    red_expand<T><<<grid_for(N), 256, 0, s>>>(x, op.tvec.as<double>(), op.smap.as<uint32_t>(), N, v);
-    TM_CKK("red_expand");
-    xin = v;
-    pre = nullptr;
-  }
   const double sf = scaled ? 1.0 : gscale;
+  const int bc = zb ? 0 : op.boundary;
+  const int nlb = zb ? 4 : (bc == 0 ? 2 : 1);
+  const int tile_bits = (sizeof(T) == 8) ? 12 : 13;  // 32 KB tiles
+  T* P = op.ws_a.as<T>();
+  const uint32_t* smap = reduced ? op.smap.as<uint32_t>() : nullptr;
   T* fold_out = reduced ? op.xp.as<T>() : y;
-  if (!zb) {
-    const int bc = op.boundary;
-    const int npass = (bc == 0) ? 2 : 1;
-    xdt_init<T><<<grid_for(N * npass), 256, 0, s>>>(xin, pre, L, bc, c, npass, A);
-    TM_CKK("xdt_init");
-    for (int st = 0; st < L; ++st) {
-      xdt_step<T><<<grid_for(2 * N * npass), 256, 0, s>>>(A, B, L, c, st == L - 1, bc, npass);
-      TM_CKK("xdt_step");
-      std::swap(A, B);
+  const double postc = zb ? sf : (reduced ? sf : op.normfactor * sf);
+  const double* post = reduced ? nullptr : op.tvec.as<double>();
+  int t0 = 0;
+  while (t0 < nsteps) {
+    // tile state bits: contiguous low sites for coalescing (none when the
+    // steps start at site 0), then the sites of as many steps as fit
+    const int cb = (t0 == 0) ? 0 : std::min(KS * t0, (zb ? 2 : 3));
+    const int room = tile_bits - NA - cb;
+    const int T_ = std::max(1, std::min(nsteps - t0, room / KS));
+    ChainPass cp{};
+    std::vector<int> sp;
+    for (int k = 0; k < cb; ++k) sp.push_back(k);
+    for (int k = 0; k < KS * T_; ++k) sp.push_back(KS * t0 + k);
+    cp.nst = (int)sp.size();
+    for (int k = 0; k < cp.nst; ++k) cp.spos[k] = sp[k];
+    uint64_t used = 0;
+    for (int k : sp) used |= 1ull << k;
+    cp.no = 0;
+    for (int b = 0; b < L; ++b)
+      if (!((used >> b) & 1ull)) cp.opos[cp.no++] = b;
+    cp.t0 = t0;
+    cp.T = T_;
+    cp.jbit0 = cb;
+    cp.first = (t0 == 0);
+    cp.last = (t0 + T_ >= nsteps);
+    cp.nlb = nlb;
+    const int64_t nblocks = (int64_t)(cp.last ? 1 : nlb) << cp.no;
+    const int tile = 1 << (NA + cp.nst);
+    const size_t shm = chain_acc_offset(tile, sizeof(T)) + (cp.last ? (size_t)(tile >> NA) * 8 : 0);
+    const int threads = 256;
+    if (zb) {
+      raise_smem_limit((const void*)chain_kernel<T, 1>, shm);
+      chain_kernel<T, 1><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
+                                                                postc, L, bc, dir, c, cp);
+    } else {
+      raise_smem_limit((const void*)chain_kernel<T, 0>, shm);
+      chain_kernel<T, 0><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
+                                                                postc, L, bc, dir, c, cp);
     }
-    const double postc = reduced ? sf : op.normfactor * sf;
-    xdt_fold<T><<<grid_for(N), 256, 0, s>>>(A, reduced ? nullptr : op.tvec.as<double>(), postc, L, npass, fold_out);
-    TM_CKK("xdt_fold");
-  } else {
-    zbt_init<T><<<grid_for(4 * N), 256, 0, s>>>(xin, pre, L, A);
-    TM_CKK("zbt_init");
-    for (int st = 0; st < L / 2; ++st) {
-      zbt_step<T><<<grid_for(16 * N), 256, 0, s>>>(A, B, L, c, st == L / 2 - 1, dir);
-      TM_CKK("zbt_step");
-      std::swap(A, B);
-    }
-    zbt_fold<T><<<grid_for(N), 256, 0, s>>>(A, reduced ? nullptr : op.tvec.as<double>(), sf, L, fold_out);
-    TM_CKK("zbt_fold");
+    TM_CKK("aux_chain");
+    t0 += T_;
   }
   if (reduced) {
     red_contract<T><<<grid_for(op.n), 256, 0, s>>>(fold_out, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),

@@ -8,7 +8,9 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "tm_blas.cuh"
@@ -31,16 +33,55 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
 static std::atomic<int64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+void raise_smem_limit(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> cur;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& c = cur[kernel];
+  if (bytes <= c) return;
+  TM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  c = bytes;
+}
+
 static thread_local cudaStream_t g_alloc_stream = nullptr;
 AllocStream::AllocStream(cudaStream_t s) : prev(g_alloc_stream) { g_alloc_stream = s; }
 AllocStream::~AllocStream() { g_alloc_stream = prev; }
+
+// The device's default memory pool backs the stream-ordered buffers.  It
+// keeps freed memory for reuse (release threshold raised once per device), so
+// repeated solves do not map and unmap tens of GB each time; an allocation
+// that fails trims the pool and retries once.
+static void pool_setup(int dev) {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev < 0 || dev >= 64 || done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
+}
 
 void DBuf::alloc(size_t b) {
   release();
   if (b == 0) b = 16;
   cudaError_t e;
   if (g_alloc_stream) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    pool_setup(dev);
     e = cudaMallocAsync(&p, b, g_alloc_stream);
+    if (e == cudaErrorMemoryAllocation) {
+      (void)cudaGetLastError();
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        cudaStreamSynchronize(g_alloc_stream);
+        cudaMemPoolTrimTo(pool, 0);
+      }
+      e = cudaMallocAsync(&p, b, g_alloc_stream);
+    }
     st = g_alloc_stream;
   } else {
     e = cudaMalloc(&p, b);

@@ -556,7 +556,7 @@ void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, co
                   const uint32_t* colmap, T* w1, cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
   auto kfn = eo_pass1<T, KB, typename EoIO<T>::In>;
-  TM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+  raise_smem_limit((const void*)kfn, shm);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
   cfg.blockDim = dim3(1u << A.p);
@@ -578,7 +578,7 @@ void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, con
                   cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
   auto kfn = eo_pass2<T, KB, F64S, typename EoIO<T>::Out>;
-  TM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+  raise_smem_limit((const void*)kfn, shm);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
   cfg.blockDim = dim3(1u << A.p);

@@ -175,6 +175,11 @@ void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStr
 void full_apply(const Op& op, const void* xin, void* out, tm_dtype dt, cudaStream_t s, int transpose);
 
 // ---------------------------------------------------------------- helpers
+// Raise a kernel's dynamic shared-memory limit to at least `bytes`.  The
+// limit is per-kernel process state: it only ever grows here, so concurrent
+// host threads launching the same kernel with different tile sizes never see
+// a limit below what their launch needs.
+void raise_smem_limit(const void* kernel, size_t bytes);
 int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t s);  // returns 0
 uint32_t read_u32(const uint32_t* dptr, cudaStream_t s);
 int num_sms();

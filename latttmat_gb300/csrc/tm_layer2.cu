@@ -402,7 +402,7 @@ void matvec_two_layer(const Op& op, const double* x, double* y, cudaStream_t s) 
   } else if (b.kind == K_YAM) {
     const double w0 = std::exp(-bj * k), w1 = 1.0 / w0;
     const size_t shm = (size_t)((1 << L) + (1 << L) / 32 + 1) * sizeof(double);
-    TM_CK(cudaFuncSetAttribute(yam_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    raise_smem_limit((const void*)yam_block_kernel, shm);
     const int ng = 2 * L * (b.censym ? 2 : 1);
     yam_block_kernel<<<(unsigned)b.nblocks, 512, shm, s>>>(x, y, b.idx.as<uint32_t>(), b.dup.as<uint16_t>(),
                                                            b.tvec.as<double>(), b.swp.as<uint32_t>(),

@@ -187,8 +187,13 @@ struct Lanczos {
   DBuf V, W, x32, y32, h1, h2, part, nsq, Hd, wd, Zd, Ysel;
   int matvecs = 0, matvecs64 = 0, restarts = 0;
 
-  Lanczos(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), m(ncv) {
-    V.alloc((size_t)(m + 1) * n * sizeof(double));
+  int vcols = 0;  // columns of V allocated (m + 1 once full)
+
+  // cols0 > 0: allocate only that many basis columns (the mixed path needs
+  // the FP64 basis for the wanted vectors only); ensure_full() grows V.
+  Lanczos(const Op& o, int ncv, cudaStream_t st, int cols0 = 0) : op(o), s(st), n(o.n), m(ncv) {
+    vcols = (cols0 > 0) ? std::min(cols0, m + 1) : m + 1;
+    V.alloc((size_t)vcols * n * sizeof(double));
     W.alloc((size_t)n * sizeof(double));
     h1.alloc(64 * 8);
     h2.alloc(64 * 8);
@@ -200,6 +205,17 @@ struct Lanczos {
     Ysel.alloc(64 * 64 * 8);
   }
   double* v(int j) const { return V.as<double>() + (int64_t)j * n; }
+
+  void ensure_full() {
+    if (vcols >= m + 1) return;
+    DBuf nv;
+    nv.alloc((size_t)(m + 1) * n * sizeof(double));
+    TM_CK(cudaMemcpyAsync(nv.p, V.p, (size_t)vcols * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    std::swap(V.p, nv.p);
+    std::swap(V.bytes, nv.bytes);
+    std::swap(V.st, nv.st);
+    vcols = m + 1;
+  }
 
   void ensure32() {
     if (!x32.p) {
@@ -891,7 +907,8 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
   double max_resid = 0.0;
   std::unique_ptr<Lanczos> Lz;
   while (!done && attempts < 3) {
-    Lz.reset(new Lanczos(op, ncv, s));
+    const bool mixed_nv32 = (mode == TM_EIGS_MIXED) && ncv <= NV32;
+    Lz.reset(new Lanczos(op, ncv, s, mixed_nv32 ? nev + 1 : 0));
     Lanczos& lz = *Lz;
     const bool mixed = (mode == TM_EIGS_MIXED);
     lz.start(nullptr, seed);
@@ -959,6 +976,7 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
           axpby(1.0, start.as<double>(), 1.0, lz.v(i), start.as<double>(), n, s);
         int mv = lz.matvecs, mv64 = lz.matvecs64, rs = lz.restarts;
         lz.matvecs = lz.matvecs64 = lz.restarts = 0;
+        lz.ensure_full();
         lz.start(start.as<double>(), seed);
         lz.matvecs += mv;
         lz.matvecs64 += mv64;
