@@ -208,12 +208,12 @@ def gpu_arm(args, world, rank, local):
 
     split = {"create": [], "eigs": []}
 
-    def solve(vectors=False):
+    def solve(vectors=False, vecs_out=None):
         t0 = time.perf_counter()
         op = lt.TMatOp("A", 2, 5, BETAJ, KAPPA, H, L, 0.0, 2)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        vals, vecs, _, info = op.eigs(NEV, tol=1e-10, mode=mode, vectors=vectors)
+        vals, vecs, _, info = op.eigs(NEV, tol=1e-10, mode=mode, vectors=vectors, vecs_out=vecs_out)
         t2 = time.perf_counter()
         split["create"].append(t1 - t0)
         split["eigs"].append(t2 - t1)
@@ -250,16 +250,19 @@ def gpu_arm(args, world, rank, local):
     t_create = statistics.mean(split["create"])
     t_eigs = statistics.mean(split["eigs"])
 
-    # end-to-end through the C ABI with host outputs (eigenvalues + eigenvectors to host)
+    # end-to-end through the C ABI with host outputs (eigenvalues + eigenvectors
+    # to a pinned host buffer)
     te = []
     d2h = 0
+    pinned = torch.empty((NEV, n), dtype=torch.float64, pin_memory=True).numpy()
     for _ in range(max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        op, vals_e, vecs, info_e, n = solve(vectors=True)
+        op, vals_e, vecs, info_e, n = solve(vectors=True, vecs_out=pinned)
         te.append(time.perf_counter() - t0)
         d2h = vecs.nbytes + vals_e.nbytes
-        del op, vecs
+        del op
+    del pinned
     e2e = max_over_ranks(statistics.mean(te), world)
 
     # roofline of the dominant kernel: per-stage launch times on the operator's stream

@@ -237,7 +237,7 @@ class TMatOp:
 
     # --- eigensolver --------------------------------------------------
     def eigs(self, nev: int, ncv: int = 0, tol: float = 1e-10, seed: int = 0, mode: int = TM_EIGS_F64,
-             vectors: bool = False, left: bool = False):
+             vectors: bool = False, left: bool = False, vecs_out: Optional[np.ndarray] = None):
         """Largest-magnitude eigenvalues (already divided by normfactor).
 
         Returns (vals, vecs or None, vecl or None, info dict)."""
@@ -247,7 +247,13 @@ class TMatOp:
         sym = self.is_symmetric()
         vecs = None
         if vectors:
-            vecs = np.zeros((nev, n) if sym else (nev, n, 2))
+            shape = (nev, n) if sym else (nev, n, 2)
+            if vecs_out is not None:  # caller-provided (e.g. pinned) host buffer
+                if vecs_out.shape != shape or vecs_out.dtype != np.float64 or not vecs_out.flags.c_contiguous:
+                    raise ValueError(f"vecs_out must be a C-contiguous float64 array of shape {shape}")
+                vecs = vecs_out
+            else:
+                vecs = np.zeros(shape)
         vecl = np.zeros(n) if (left and not sym) else None
         info = tm_eigs_info()
         _check(self._lib.tm_eigs(self._h, int(nev), int(ncv), float(tol), int(seed), int(mode), _ptr(vr), _ptr(vi),

@@ -24,6 +24,7 @@
 
 namespace ltm {
 
+void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s);
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s);
 
@@ -91,7 +92,7 @@ struct Arnoldi {
     W.alloc((size_t)n * 8);
     h1.alloc(64 * 8);
     h2.alloc(64 * 8);
-    part.alloc((size_t)num_sms() * 4 * 16 * 8 + 64);
+    part.alloc(red_part_bytes(16));
     nsq.alloc(8);
     Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
     wr.alloc(64 * 8);
@@ -106,6 +107,10 @@ struct Arnoldi {
   }
   double* v(int j) const { return V.as<double>() + (int64_t)j * n; }
 
+  // mixed mode: the FP64 phase uses the FP64-accurate refinement products
+  // (double-float where the operator has them)
+  bool refine_products = false;
+
   void step(int j, bool f32) {
     double* w = W.as<double>();
     if (f32) {
@@ -118,7 +123,10 @@ struct Arnoldi {
       mdot32(v(0), n, j + 1, y32.as<float>(), S, n, h1.as<double>(), part.as<double>(), s);
       maxpy32(v(0), n, j + 1, h1.as<double>(), y32.as<float>(), S, w, n, s);
     } else {
-      apply_internal(op, v(j), w, nullptr, nullptr, false, s);
+      if (refine_products)
+        apply_refine(op, v(j), w, s);
+      else
+        apply_internal(op, v(j), w, nullptr, nullptr, false, s);
       ++matvecs64;
       mdot(v(0), n, j + 1, w, n, h1.as<double>(), part.as<double>(), s);
       maxpy(v(0), n, j + 1, h1.as<double>(), w, n, s);
@@ -347,6 +355,7 @@ tm_status arnoldi_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       start.alloc((size_t)n * 8);
       TM_CK(cudaMemcpyAsync(start.p, a.v(0), (size_t)n * 8, cudaMemcpyDeviceToDevice, op.stream));
       a.start(start.as<double>(), seed);
+      a.refine_products = true;
       done = a.run(nev, false, tol, false, 200, 0, R);
     } else {
       done = a.run(nev, false, tol, false, 300, 0, R);

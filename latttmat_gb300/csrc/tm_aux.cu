@@ -26,8 +26,10 @@
 // state->rank map and contract the full-space result at the representatives.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
+#include "tm_df.cuh"
 #include "tm_internal.h"
 
 namespace ltm {
@@ -71,6 +73,12 @@ struct ChainPass {
   int nlb;         // lastbit passes (DNNI 2 or 1, BNNNI 4)
 };
 
+// tile state index -> state bits: the tile's state bits are the contiguous
+// runs [0, cb) and [lo, lo + nst - cb)
+__device__ __forceinline__ uint64_t tile_state(uint64_t v, int cb, int lo) {
+  return (v & ((1ull << cb) - 1)) | ((v >> cb) << lo);
+}
+
 __device__ __forceinline__ uint64_t dep(uint64_t v, const int* pos, int nb) {
   uint64_t g = 0;
   for (int k = 0; k < nb; ++k) g |= ((v >> k) & 1ull) << pos[k];
@@ -80,8 +88,8 @@ __device__ __forceinline__ uint64_t dep(uint64_t v, const int* pos, int nb) {
 // Initial (lastbit pass lb) value of element (aux, r): TMat/tmat.cpp:392-457
 // (DNNI: aux = copy of the top site, site 0 = lb; boundary cases 5 and 9) and
 // :604-612 (BNNNI: aux = copy of the two top sites, sites 0-1 = lb).
-template <class T, int ZB>
-__device__ __forceinline__ T chain_init(const T* __restrict__ x, const double* __restrict__ pre,
+template <class T, int ZB, class IO>
+__device__ __forceinline__ T chain_init(const IO* __restrict__ x, const double* __restrict__ pre,
                                         const uint32_t* __restrict__ smap, int L, int bc, uint64_t r, int aux, int lb,
                                         const AuxCoefT<T>& c) {
   auto u = [&]() -> T {
@@ -89,7 +97,7 @@ __device__ __forceinline__ T chain_init(const T* __restrict__ x, const double* _
       const uint32_t q = smap[r];
       return (T)((double)x[q] * pre[q]);
     }
-    return pre ? (T)((double)x[r] * pre[r]) : x[r];
+    return pre ? (T)((double)x[r] * pre[r]) : (T)x[r];
   };
   if (ZB) {
     if ((int)(r >> (L - 2)) == aux && (int)(r & 3) == lb) return u();
@@ -110,10 +118,10 @@ __device__ __forceinline__ T chain_init(const T* __restrict__ x, const double* _
 //           dir = optdirection); L/2 steps.
 // P: the nlb*2^L*2^NA buffer (in place).  first: tiles built from x; last:
 // y[r] = postc * post[r] * sum_{lb, aux} (one CTA loops the lastbit passes).
-template <class T, int ZB>
-__global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const T* __restrict__ x,
+template <class T, int ZB, class IO>
+__global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
                                                     const double* __restrict__ pre, const uint32_t* __restrict__ smap,
-                                                    T* __restrict__ y, const double* __restrict__ post, double postc,
+                                                    IO* __restrict__ y, const double* __restrict__ post, double postc,
                                                     int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {
   constexpr int NA = ZB ? 2 : 1, KS = ZB ? 2 : 1, GB = NA + KS;  // group bits
   extern __shared__ unsigned char smraw[];
@@ -155,6 +163,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
   const uint64_t ob = blockIdx.x & ((1ull << cp.no) - 1);
   const int lb_outer = (int)(blockIdx.x >> cp.no);
   const uint64_t rbase = dep(ob, cp.opos, cp.no);
+  const int lo = KS * cp.t0;  // lowest site of the pass's steps
   const int nloop = cp.last ? cp.nlb : 1;
   if (cp.last)
     for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) acc[e] = 0.0;
@@ -163,10 +172,10 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
     // load / build the tile
     for (int e = threadIdx.x; e < tile; e += blockDim.x) {
       const int aux = e & ((1 << NA) - 1);
-      const uint64_t r = rbase | dep((uint64_t)(e >> NA), cp.spos, cp.nst);
+      const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, lo);
       T v;
       if (cp.first)
-        v = chain_init<T, ZB>(x, pre, smap, L, bc, r, aux, lb, c);
+        v = chain_init<T, ZB, IO>(x, pre, smap, L, bc, r, aux, lb, c);
       else
         v = P[(((uint64_t)lb << L | r) << NA) | (uint64_t)aux];
       sm[spad(e)] = v;
@@ -183,7 +192,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
         const int lo = rest & ((1 << (sb - NA)) - 1);
         const int hi = rest >> (sb - NA);
         const int ebase = (hi << (sb + KS)) | (lo << NA);
-        const uint64_t r = rbase | dep((uint64_t)(ebase >> NA), cp.spos, cp.nst);
+        const uint64_t r = rbase | tile_state((uint64_t)(ebase >> NA), cp.jbit0, lo);
         if (!ZB) {
           // DNNI: out(a, s) = b1[s^a] b2[nb^s] (b2[s] in(0, a) + b2[s^1] in(1, a)),
           // in(q, s') = value with aux q and site t = s'
@@ -238,7 +247,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
       }
     } else {
       for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-        const uint64_t r = rbase | dep((uint64_t)(e >> NA), cp.spos, cp.nst);
+        const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, lo);
         P[(((uint64_t)lb << L | r) << NA) | (uint64_t)(e & ((1 << NA) - 1))] = sm[spad(e)];
       }
     }
@@ -246,10 +255,10 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
   }
   if (cp.last) {
     for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) {
-      const uint64_t r = rbase | dep((uint64_t)e, cp.spos, cp.nst);
+      const uint64_t r = rbase | tile_state((uint64_t)e, cp.jbit0, lo);
       double v = acc[e];
       if (post) v *= post[r];
-      y[r] = (T)(v * postc);
+      y[r] = (IO)(v * postc);
     }
   }
 }
@@ -320,14 +329,17 @@ void build_aux(Op& op) {
 
 // y = T x (or T^T x for transposed views); scaled: FP32 result divided by the
 // returned factor.
-template <class T>
-double matvec_aux_dir(const Op& op, const T* x, T* y, bool scaled, int dir, cudaStream_t s) {
+// T: arithmetic and pass-buffer type (float, double, or dfloat: FP64-accurate
+// products on the FP32 pipes); IO: element type of x and y.
+template <class T, class IO = T>
+double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cudaStream_t s) {
   const int L = op.L;
   const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
   AuxCoef c64 = coef_of(op);
   const double gb = step_bound(op, c64, dir);
-  const bool norm = (sizeof(T) == 4);
+  // FP32 and double-float steps are normalised (FP32 exponent range)
+  const bool norm = (sizeof(T) == 4) || std::is_same<T, dfloat>::value;
   AuxCoefT<T> c;
   for (int k = 0; k < 2; ++k) {
     c.b1[k] = (T)c64.b1[k];
@@ -344,16 +356,24 @@ double matvec_aux_dir(const Op& op, const T* x, T* y, bool scaled, int dir, cuda
   const int tile_bits = (sizeof(T) == 8) ? 12 : 13;  // 32 KB tiles
   T* P = op.ws_a.as<T>();
   const uint32_t* smap = reduced ? op.smap.as<uint32_t>() : nullptr;
-  T* fold_out = reduced ? op.xp.as<T>() : y;
+  IO* fold_out = reduced ? op.xp.as<IO>() : y;
   const double postc = zb ? sf : (reduced ? sf : op.normfactor * sf);
   const double* post = reduced ? nullptr : op.tvec.as<double>();
-  int t0 = 0;
+  // passes: the first holds up to cap0 steps (its sites start at 0), the
+  // others up to cap1 (they carry a few contiguous low sites for
+  // coalescing); the steps are spread evenly over the passes needed
+  const int cbn = zb ? 2 : 3;
+  const int cap0 = std::max(1, (tile_bits - NA) / KS), cap1 = std::max(1, (tile_bits - NA - cbn) / KS);
+  const int npass = (nsteps <= cap0) ? 1 : 1 + (nsteps - cap0 + cap1 - 1) / cap1;
+  int t0 = 0, pass = 0;
   while (t0 < nsteps) {
     // tile state bits: contiguous low sites for coalescing (none when the
-    // steps start at site 0), then the sites of as many steps as fit
-    const int cb = (t0 == 0) ? 0 : std::min(KS * t0, (zb ? 2 : 3));
-    const int room = tile_bits - NA - cb;
-    const int T_ = std::max(1, std::min(nsteps - t0, room / KS));
+    // steps start at site 0), then the sites of this pass's steps
+    const int cb = (t0 == 0) ? 0 : std::min(KS * t0, cbn);
+    const int left = npass - pass;
+    const int even = (nsteps - t0 + left - 1) / left;
+    const int T_ = std::max(1, std::min(nsteps - t0, std::min(even, t0 == 0 ? cap0 : cap1)));
+    ++pass;
     ChainPass cp{};
     std::vector<int> sp;
     for (int k = 0; k < cb; ++k) sp.push_back(k);
@@ -376,19 +396,19 @@ double matvec_aux_dir(const Op& op, const T* x, T* y, bool scaled, int dir, cuda
     const size_t shm = chain_acc_offset(tile, sizeof(T)) + (cp.last ? (size_t)(tile >> NA) * 8 : 0);
     const int threads = 256;
     if (zb) {
-      raise_smem_limit((const void*)chain_kernel<T, 1>, shm);
-      chain_kernel<T, 1><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
+      raise_smem_limit((const void*)chain_kernel<T, 1, IO>, shm);
+      chain_kernel<T, 1, IO><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
                                                                 postc, L, bc, dir, c, cp);
     } else {
-      raise_smem_limit((const void*)chain_kernel<T, 0>, shm);
-      chain_kernel<T, 0><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
+      raise_smem_limit((const void*)chain_kernel<T, 0, IO>, shm);
+      chain_kernel<T, 0, IO><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
                                                                 postc, L, bc, dir, c, cp);
     }
     TM_CKK("aux_chain");
     t0 += T_;
   }
   if (reduced) {
-    red_contract<T><<<grid_for(op.n), 256, 0, s>>>(fold_out, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),
+    red_contract<IO><<<grid_for(op.n), 256, 0, s>>>(fold_out, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),
                                                    op.tvec.as<double>(), 1.0, y, op.n);
     TM_CKK("red_contract");
   }
@@ -403,5 +423,12 @@ double matvec_aux(const Op& op, const T* x, T* y, bool scaled, cudaStream_t s) {
 
 template double matvec_aux<float>(const Op&, const float*, float*, bool, cudaStream_t);
 template double matvec_aux<double>(const Op&, const double*, double*, bool, cudaStream_t);
+
+// FP64-accurate product in double-float arithmetic (the solver's refinement
+// products for the aux-bit operators)
+void matvec_aux_df(const Op& op, const double* x, double* y, cudaStream_t s) {
+  const Op& base = op.parent ? *op.parent : op;
+  matvec_aux_dir<dfloat, double>(base, x, y, false, op.transposed ? 1 : 0, s);
+}
 
 }  // namespace ltm

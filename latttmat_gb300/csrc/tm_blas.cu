@@ -13,7 +13,7 @@ constexpr int NVMAX = 16;      // vectors per fused pass
 
 int red_blocks(int64_t n) {
   int64_t b = (n + BT * 4 - 1) / (BT * 4);
-  int64_t cap = (int64_t)num_sms() * 4;
+  int64_t cap = (int64_t)num_sms() * kRedBlocksPerSM;
   return (int)std::max<int64_t>(1, std::min(b, cap));
 }
 
@@ -32,7 +32,20 @@ __global__ void __launch_bounds__(BT) mdot_kernel(const double* __restrict__ V, 
   for (int k = 0; k < NV; ++k) acc[k] = 0.0;
   int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * BT;
-  for (; i < n; i += st) {
+  // two elements per iteration: twice the loads in flight per thread
+  for (; i + st < n; i += 2 * st) {
+    const int64_t i2 = i + st;
+    const double wa = W32 ? scale * (double)w32[i] : w[i];
+    const double wb = W32 ? scale * (double)w32[i2] : w[i2];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (k < nv) {
+        const double va = V[k * ldv + i], vb = V[k * ldv + i2];
+        acc[k] = fma(va, wa, acc[k]);
+        acc[k] = fma(vb, wb, acc[k]);
+      }
+  }
+  if (i < n) {
     double wi = W32 ? scale * (double)w32[i] : w[i];
 #pragma unroll
     for (int k = 0; k < NV; ++k)
@@ -78,7 +91,20 @@ __global__ void __launch_bounds__(BT) maxpy_kernel(const double* __restrict__ V,
   __syncthreads();
   int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * BT;
-  for (; i < n; i += st) {
+  for (; i + st < n; i += 2 * st) {
+    const int64_t i2 = i + st;
+    double a = W32 ? scale * (double)w32[i] : w[i];
+    double b = W32 ? scale * (double)w32[i2] : w[i2];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (k < nv) {
+        a = fma(-V[k * ldv + i], hs[k], a);
+        b = fma(-V[k * ldv + i2], hs[k], b);
+      }
+    w[i] = a;
+    w[i2] = b;
+  }
+  if (i < n) {
     double acc = W32 ? scale * (double)w32[i] : w[i];
 #pragma unroll
     for (int k = 0; k < NV; ++k)
@@ -277,7 +303,18 @@ __global__ void __launch_bounds__(BT) mdot_f32_kernel(const float* __restrict__ 
   for (int k = 0; k < NV32; ++k) acc[k] = 0.f;
   int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * BT;
-  for (; i < n; i += st) {
+  for (; i + st < n; i += 2 * st) {
+    const int64_t i2 = i + st;
+    const float wa = w[i], wb = w[i2];
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) {
+        const float va = V[k * ldv + i], vb = V[k * ldv + i2];
+        acc[k] = fmaf(va, wa, acc[k]);
+        acc[k] = fmaf(vb, wb, acc[k]);
+      }
+  }
+  if (i < n) {
     const float wi = w[i];
 #pragma unroll
     for (int k = 0; k < NV32; ++k)
@@ -324,7 +361,21 @@ __global__ void __launch_bounds__(BT) axpy_nrm_f32_kernel(const float* __restric
   float acc[1] = {0.f};
   int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
   const int64_t st = (int64_t)gridDim.x * BT;
-  for (; i < n; i += st) {
+  for (; i + st < n; i += 2 * st) {
+    const int64_t i2 = i + st;
+    float x = w[i], y = w[i2];
+#pragma unroll
+    for (int k = 0; k < NV32; ++k)
+      if (k < nv) {
+        x = fmaf(-V[k * ldv + i], hs[k], x);
+        y = fmaf(-V[k * ldv + i2], hs[k], y);
+      }
+    w[i] = x;
+    w[i2] = y;
+    acc[0] = fmaf(x, x, acc[0]);
+    acc[0] = fmaf(y, y, acc[0]);
+  }
+  if (i < n) {
     float x = w[i];
 #pragma unroll
     for (int k = 0; k < NV32; ++k)
@@ -350,6 +401,115 @@ __global__ void __launch_bounds__(BT) maxpy_f32_kernel(const float* __restrict__
     for (int k = 0; k < NV32; ++k)
       if (k < nv) acc = fmaf(-V[k * ldv + i], hs[k], acc);
     w[i] = acc;
+  }
+}
+
+// Block dots: part[b][k*NW + j] = partial sums of V[k] . W[j] (FP32 data,
+// FP32 per-thread accumulation, FP64 block reduction).  One sweep over KV
+// basis columns serves NW vectors.
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT) mdot_block_f32_kernel(const float* __restrict__ V, int64_t ldv, int kv,
+                                                            F32Cols W, int nw, int64_t n,
+                                                            double* __restrict__ part) {
+  float acc[KV][NW];
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) acc[k][j] = 0.f;
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i + st < n; i += 2 * st) {
+    const int64_t i2 = i + st;
+    float wa[NW], wb[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      wa[j] = (j < nw) ? W.c[j][i] : 0.f;
+      wb[j] = (j < nw) ? W.c[j][i2] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const float va = V[k * ldv + i], vb = V[k * ldv + i2];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+          acc[k][j] = fmaf(va, wa[j], acc[k][j]);
+          acc[k][j] = fmaf(vb, wb[j], acc[k][j]);
+        }
+      }
+  }
+  if (i < n) {
+    float wv[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) wv[j] = (j < nw) ? W.c[j][i] : 0.f;
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const float v = V[k * ldv + i];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) acc[k][j] = fmaf(v, wv[j], acc[k][j]);
+      }
+  }
+  __shared__ double sh[BT / 32][KV * NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      double v = warp_sum((double)acc[k][j]);
+      if (lane == 0) sh[wid][k * NW + j] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    double a = 0.0;
+    for (int q = 0; q < BT / 32; ++q) a += sh[q][t];
+    part[(int64_t)blockIdx.x * (KV * NW) + t] = a;
+  }
+}
+
+// H[(k0 + k) + j * ldh] = sum over blocks of part[b][k*NW + j]
+__global__ void mdot_block_final(const double* __restrict__ part, int nb, int kv, int nw, int stride, int nws,
+                                 double* H, int64_t ldh, int k0) {
+  const int t = blockIdx.x;
+  const int k = t / nw, j = t % nw;
+  if (k >= kv) return;
+  double a = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) a += part[(int64_t)b * stride + k * nws + j];
+  a = warp_sum(a);
+  __shared__ double shr[32];
+  if ((threadIdx.x & 31) == 0) shr[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) r += shr[q];
+    H[(k0 + k) + (int64_t)j * ldh] = r;
+  }
+}
+
+// W[j] -= sum_k V[k] H[k0 + k, j]  (FP32 data and arithmetic)
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT) maxpy_block_f32_kernel(const float* __restrict__ V, int64_t ldv, int kv,
+                                                             const double* __restrict__ H, int64_t ldh, int k0,
+                                                             F32ColsMut W, int nw, int64_t n) {
+  __shared__ float hs[KV][NW];
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    const int k = t / NW, j = t % NW;
+    hs[k][j] = (k < kv && j < nw) ? (float)H[(k0 + k) + (int64_t)j * ldh] : 0.f;
+  }
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    float v[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) v[k] = (k < kv) ? V[k * ldv + i] : 0.f;
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+      if (j < nw) {
+        float w = W.c[j][i];
+#pragma unroll
+        for (int k = 0; k < KV; ++k) w = fmaf(-v[k], hs[k][j], w);
+        W.c[j][i] = w;
+      }
   }
 }
 
@@ -462,6 +622,41 @@ void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, do
     TM_CKK("mdot_final");
   }
 }
+
+void mdot_block_f32(const float* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H,
+                    int64_t ldh, double* part, cudaStream_t s) {
+  if (nw < 1 || nw > kMaxBlockW) fail(TM_ERR_LIMIT, "mdot_block_f32: 1..8 vectors");
+  constexpr int KV = 8;
+  const int nb = red_blocks(n);
+  for (int k0 = 0; k0 < nv; k0 += KV) {
+    const int kv = std::min(KV, nv - k0);
+    if (nw <= 4) {  // half the accumulators when the block is narrow
+      mdot_block_f32_kernel<KV, 4><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+      TM_CKK("mdot_block_f32");
+      mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * 4, 4, H, ldh, k0);
+    } else {
+      mdot_block_f32_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+      TM_CKK("mdot_block_f32");
+      mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * kMaxBlockW, kMaxBlockW, H, ldh, k0);
+    }
+    TM_CKK("mdot_block_final");
+  }
+}
+
+void maxpy_block_f32(const float* V, int64_t ldv, int nv, const double* H, int64_t ldh, const F32ColsMut& W, int nw,
+                     int64_t n, cudaStream_t s) {
+  if (nw < 1 || nw > kMaxBlockW) fail(TM_ERR_LIMIT, "maxpy_block_f32: 1..8 vectors");
+  constexpr int KV = 8;
+  for (int k0 = 0; k0 < nv; k0 += KV) {
+    const int kv = std::min(KV, nv - k0);
+    maxpy_block_f32_kernel<KV, kMaxBlockW><<<red_blocks(n), BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, H, ldh, k0,
+                                                                         W, nw, n);
+    TM_CKK("maxpy_block_f32");
+  }
+}
+
+size_t mdot_block_part_bytes() { return red_part_bytes(8 * kMaxBlockW); }
+size_t red_part_bytes(int width) { return (size_t)num_sms() * kRedBlocksPerSM * width * sizeof(double) + 64; }
 
 void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, cudaStream_t s) {
   for (int k0 = 0; k0 < nv; k0 += NV32) {

@@ -41,6 +41,27 @@ constexpr int NV32 = 16;
 // h[k] = sum_i V[k][i] w[i]
 void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
               cudaStream_t s);
+// Reduction kernels run at most kRedBlocksPerSM blocks of 256 threads per SM;
+// their partial-sum buffers need red_part_bytes(values per block).
+constexpr int kRedBlocksPerSM = 8;
+size_t red_part_bytes(int width);
+
+// Block forms over up to 8 FP32 vectors at once (one sweep over V serves all
+// of them).  H is column-major with leading dimension ldh: H[k + j*ldh] =
+// V[k] . W[j]; part needs mdot_block_part_bytes().
+constexpr int kMaxBlockW = 8;
+struct F32Cols {
+  const float* c[kMaxBlockW];
+};
+struct F32ColsMut {
+  float* c[kMaxBlockW];
+};
+void mdot_block_f32(const float* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H,
+                    int64_t ldh, double* part, cudaStream_t s);
+// W[j] -= sum_k V[k] H[k + j*ldh]
+void maxpy_block_f32(const float* V, int64_t ldv, int nv, const double* H, int64_t ldh, const F32ColsMut& W, int nw,
+                     int64_t n, cudaStream_t s);
+size_t mdot_block_part_bytes();
 // w -= V h (FP32 data and arithmetic), any nv (chunks of NV32)
 void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, cudaStream_t s);
 // wout = win - V h ; h2[k] = sum_i V[k][i] wout[i]   (one pass)

@@ -130,16 +130,20 @@ static bool is_reduced(int kind) {
 static bool bfly_core(int kind) { return kind == K_XAT || kind == K_XAM || kind == K_XAM3; }
 
 void matvec_eo_df(const Op& op, const double* x, double* y, cudaStream_t s);
+void matvec_aux_df(const Op& op, const double* x, double* y, cudaStream_t s);
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s);
 
 // FP64-accurate product for the solver's refinement steps: double-float
-// arithmetic on the FP32 pipes for the even/odd operators (GB300's FP64 rate
-// is a small fraction of its FP32 rate), native FP64 otherwise.
+// arithmetic on the FP32 pipes for the even/odd and aux-bit operators (GB300's
+// FP64 rate is a small fraction of its FP32 rate), native FP64 otherwise.
 void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s) {
   const Op& base = op.parent ? *op.parent : op;
   if (base.eo.active) {
     matvec_eo_df(base, x, y, s);
+    const_cast<Op&>(op).matvecs++;
+  } else if (base.kind == K_XDT || base.kind == K_XDM || base.kind == K_ZBT || base.kind == K_ZBM) {
+    matvec_aux_df(op, x, y, s);
     const_cast<Op&>(op).matvecs++;
   } else {
     apply_internal(op, x, y, nullptr, nullptr, false, s);
@@ -582,22 +586,12 @@ tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, 
     }
   } else {
     std::vector<double> th(nev);
-    std::vector<double> vint;
-    if (vecs) vint.resize((size_t)nev * b.n);
-    st = lanczos_solve(b, nev, ncv, tol, seed, mode, th.data(), vecs ? vint.data() : nullptr, info);
+    // vectors come back in the reference's order (lanczos_solve scatters
+    // pi-ordered operators on the device)
+    st = lanczos_solve(b, nev, ncv, tol, seed, mode, th.data(), vecs, info);
     for (int i = 0; i < nev; ++i) {
       vals_re[i] = th[i] / b.normfactor;
       if (vals_im) vals_im[i] = 0.0;
-    }
-    if (vecs) {
-      if (b.has_pi) {
-        std::vector<uint32_t> pi((size_t)b.n);
-        TM_CK(cudaMemcpy(pi.data(), b.pi.p, (size_t)b.n * 4, cudaMemcpyDeviceToHost));
-        for (int c = 0; c < nev; ++c)
-          for (int64_t k = 0; k < b.n; ++k) vecs[(size_t)c * b.n + pi[k]] = vint[(size_t)c * b.n + k];
-      } else {
-        std::memcpy(vecs, vint.data(), vint.size() * 8);
-      }
     }
     if (vecl) {
       // symmetric operators have no separate left vector (TMat/pfunc.hpp:33-44)

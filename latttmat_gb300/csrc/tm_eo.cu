@@ -208,11 +208,9 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A);
-  // Output.  w1 is stored transposed with class-sorted rows: e goes to row
-  // colmap[e] (every H-class of e one contiguous block of rows), column
-  // `tile`.  Pass 2 then reads its whole input as one contiguous block of
-  // |class| rows.  The column writes of concurrently running tiles fill
-  // adjacent words of each row, which L2 merges into full sectors.
+  // Output.  w1 is stored transposed: e goes to row colmap[e], column
+  // `tile`.  The column writes of concurrently running tiles fill adjacent
+  // words of each row, which L2 merges into full sectors.
   T* wcol = w1 + tile;
   if (A.c > 0) cl.sync();
   for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) {
@@ -431,20 +429,13 @@ void build_eo_plan(Op& op) {
   }
   std::vector<uint32_t> t2(M);
   for (uint32_t o = 0; o < M; ++o) t2[o] = (otile[orep[o]] << 8) | (uint32_t)og[o];
-  // w1 column order: the H-class of each e-representative as one contiguous
-  // block (members ascending), classes in representative order
-  std::vector<uint32_t> colmap(M, 0xffffffffu);
-  {
-    uint32_t pos = 0;
-    for (uint32_t er : elist) {
-      std::vector<uint32_t> mem;
-      for (int g = 0; g < P.ng; ++g) mem.push_back(act_e(g, er, m));
-      std::sort(mem.begin(), mem.end());
-      mem.erase(std::unique(mem.begin(), mem.end()), mem.end());
-      for (uint32_t e : mem) colmap[e] = pos++;
-    }
-    if (pos != M) fail(TM_ERR_ARG, "even/odd plan: H-classes do not cover the even patterns");
-  }
+  // w1 row of each even pattern e.  Rows in e order: pass 1's column writes
+  // then walk the rows in order (consecutive threads, consecutive rows), and
+  // pass 2 reads the |class| rows of its tile's H-class.  (Grouping each
+  // H-class into contiguous rows was measured slower: 2.48 against 1.99 ms for
+  // pass 1 at L=32, pass 2 unchanged.)
+  std::vector<uint32_t> colmap(M);
+  for (uint32_t e = 0; e < M; ++e) colmap[e] = e;
   P.n_orep = (int)olist.size();
   P.n_erep = (int)elist.size();
   P.c32 = cluster_bits_for(m, 4);

@@ -197,7 +197,7 @@ struct Lanczos {
     W.alloc((size_t)n * sizeof(double));
     h1.alloc(64 * 8);
     h2.alloc(64 * 8);
-    part.alloc((size_t)num_sms() * 4 * 16 * 8 + 64);
+    part.alloc(red_part_bytes(16));
     nsq.alloc(8);
     Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
     wd.alloc(64 * 8);
@@ -388,7 +388,7 @@ struct Lanczos32 {
     Y.alloc((size_t)n * 4);
     h1.alloc(64 * 8);
     h2.alloc(64 * 8);
-    part.alloc((size_t)num_sms() * 4 * 16 * 8 + 64);
+    part.alloc(red_part_bytes(16));
     nsq.alloc(8);
     Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
     wd.alloc(64 * 8);
@@ -632,8 +632,11 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   const int64_t n = lz.n;
   const int cap = std::min(48, nx + 5 * nev);
   const int gblocks = blocks_for(n);
-  DBuf AX0, B32, AB32, R32, Xo, AXo, Yd, thd, part;
-  AX0.alloc((size_t)nev * n * 8);
+  DBuf XA, B32, AB32, R32, Xo, AXo, Yd, thd, part, bpart, Hd;
+  // XA = [X0 | A X0] (FP64, contiguous so one sweep gives both coupling rows)
+  XA.alloc((size_t)2 * nev * n * 8);
+  bpart.alloc(mdot_block_part_bytes());
+  Hd.alloc((size_t)48 * 2 * kMaxBlockW * 8);
   B32.alloc((size_t)cap * n * 4);
   AB32.alloc((size_t)cap * n * 4);
   R32.alloc((size_t)nev * n * 4);
@@ -656,13 +659,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     ++lz.matvecs;
     ++lz.matvecs64;
   };
-  auto dots32 = [&](const DBuf& V, int nv, const float* w) {
-    std::vector<double> h(nv);
-    mdot_f32(V.as<float>(), n, nv, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-    TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nv * 8, cudaMemcpyDeviceToHost, s));
-    host_sync();
-    return h;
-  };
+
   // projected matrix G = B^T A B and Gram matrix M = B^T B of B = [X0 | C].
   // The X0 rows take FP64 dots against the exact FP32 values of C (A X0 and
   // X0 in FP64): C is orthogonal to X0 only to FP32 accuracy (~1e-7), the
@@ -671,36 +668,51 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   std::vector<double> G((size_t)cap * cap, 0.0), M((size_t)cap * cap, 0.0);
   auto g = [&](int i, int j) -> double& { return G[(size_t)j * cap + i]; };
   auto mm = [&](int i, int j) -> double& { return M[(size_t)j * cap + i]; };
-  auto dots64 = [&](const double* V, int nv, const float* w) {
-    std::vector<double> h(nv);
-    mdot32(V, n, nv, w, 1.0, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-    TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nv * 8, cudaMemcpyDeviceToHost, s));
+  // X0 rows of C column j (FP64 dots against the FP32 values): one sweep
+  // over XA gives X0 . c (Gram) and A X0 . c (projected matrix)
+  auto x0_rows = [&](int j) {
+    std::vector<double> h(2 * nev);
+    mdot32(XA.as<double>(), n, 2 * nev, f32col(B32, j), 1.0, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+    TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, 2 * nev * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
-    return h;
-  };
-  auto x0_rows = [&](int j) {  // X0 rows of column j >= nev
-    std::vector<double> ga = dots64(AX0.as<double>(), nev, f32col(B32, j));
-    std::vector<double> mb = dots64(lz.v(0), nev, f32col(B32, j));
     for (int i = 0; i < nev; ++i) {
-      g(i, j) = g(j, i) = ga[i];
-      mm(i, j) = mm(j, i) = mb[i];
+      mm(i, j) = mm(j, i) = h[i];
+      g(i, j) = g(j, i) = h[nev + i];
     }
   };
-  auto add_gcol = [&](int j) {  // column j >= nev against columns 0..j
-    std::vector<double> gl = dots32(B32, j + 1, f32col(AB32, j));  // b_i . A b_j / S
-    std::vector<double> gr = dots32(AB32, j + 1, f32col(B32, j));  // (A b_i / S) . b_j
-    std::vector<double> mc = dots32(B32, j + 1, f32col(B32, j));
-    for (int i = nev; i <= j; ++i) {
-      g(i, j) = g(j, i) = S * 0.5 * (gl[i] + gr[i]);
-      mm(i, j) = mm(j, i) = mc[i];
+  // C columns j0 .. j0+cnt-1 (cnt <= 4) against columns 0 .. j0+cnt-1: one
+  // sweep over B32 (b . A w and b . w for the whole block), one over AB32
+  auto add_gcols = [&](int j0, int cnt) {
+    const int nv = j0 + cnt;
+    F32Cols w1{}, w2{};
+    for (int c = 0; c < cnt; ++c) {
+      w1.c[c] = f32col(AB32, j0 + c);
+      w1.c[cnt + c] = f32col(B32, j0 + c);
+      w2.c[c] = f32col(B32, j0 + c);
     }
-    x0_rows(j);
+    mdot_block_f32(B32.as<float>(), n, nv, w1, 2 * cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+    mdot_block_f32(AB32.as<float>(), n, nv, w2, cnt, n, Hd.as<double>() + 48 * 2 * cnt, 48, bpart.as<double>(), s);
+    std::vector<double> h((size_t)48 * 3 * cnt);
+    TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
+    host_sync();
+    for (int c = 0; c < cnt; ++c) {
+      const int j = j0 + c;
+      const double* gl = &h[(size_t)48 * c];             // b_i . A b_j / S
+      const double* mc = &h[(size_t)48 * (cnt + c)];     // b_i . b_j
+      const double* gr = &h[(size_t)48 * (2 * cnt + c)]; // (A b_i / S) . b_j
+      for (int i = nev; i <= j; ++i) {
+        g(i, j) = g(j, i) = S * 0.5 * (gl[i] + gr[i]);
+        mm(i, j) = mm(j, i) = mc[i];
+      }
+      x0_rows(j);
+    }
   };
   // X0 block (FP64 products and dots) and its rows against every C column
   auto set_x0 = [&](int nb) {
+    TM_CK(cudaMemcpyAsync(XA.p, lz.v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
     for (int j = 0; j < nev; ++j) {
       std::vector<double> h(nev), q(nev);
-      mdot(lz.v(0), n, nev, AX0.as<double>() + (int64_t)j * n, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+      mdot(lz.v(0), n, nev, (XA.as<double>() + (int64_t)nev * n) + (int64_t)j * n, n, lz.h1.as<double>(), lz.part.as<double>(), s);
       TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nev * 8, cudaMemcpyDeviceToHost, s));
       mdot(lz.v(0), n, nev, lz.v(j), n, lz.h2.as<double>(), lz.part.as<double>(), s);
       TM_CK(cudaMemcpyAsync(q.data(), lz.h2.p, nev * 8, cudaMemcpyDeviceToHost, s));
@@ -737,10 +749,10 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   }
   for (int j = nev; j < nx; ++j) prod32(f32col(B32, j), f32col(AB32, j));
   if (S == 0.0) prod32(f32col(B32, 0), f32col(AB32, 0));  // only its scale is used; set_x0 overwrites it
-  for (int i = 0; i < nev; ++i) prod64(lz.v(i), AX0.as<double>() + (int64_t)i * n);
+  for (int i = 0; i < nev; ++i) prod64(lz.v(i), (XA.as<double>() + (int64_t)nev * n) + (int64_t)i * n);
   int nb = nx;
   set_x0(nev);
-  for (int j = nev; j < nb; ++j) add_gcol(j);
+  for (int j = nev; j < nb; j += 4) add_gcols(j, std::min(4, nb - j));
   int verified = 0;
   bool have_x = false;
   // after a failed verification: grow before verifying again, and accept
@@ -767,8 +779,10 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     TM_CK(cudaMemcpyAsync(Yd.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
     TM_CK(cudaMemcpyAsync(thd.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
     // wanted Ritz vectors (FP64) and residuals (FP32 copy, norms in FP64)
-    ritz_resid_kernel<kMaxRefineNev><<<gblocks, 256, 0, s>>>(
-        lz.v(0), AX0.as<double>(), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(), nev,
+    auto ritz_kernel = (nev <= 4) ? ritz_resid_kernel<4> : ritz_resid_kernel<kMaxRefineNev>;
+    const int pstride = (nev <= 4) ? 4 : kMaxRefineNev;  // the kernel's per-block stride
+    ritz_kernel<<<gblocks, 256, 0, s>>>(
+        lz.v(0), (XA.as<double>() + (int64_t)nev * n), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(), nev,
         thd.as<double>(), S, R32.as<float>(), Xo.as<double>(), n, part.as<double>());
     TM_CKK("ritz_resid");
     std::vector<double> ph((size_t)gblocks * kMaxRefineNev), rn(nev, 0.0);
@@ -776,7 +790,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     host_sync();
     have_x = true;
     for (int b = 0; b < gblocks; ++b)
-      for (int c = 0; c < nev; ++c) rn[c] += ph[(size_t)b * kMaxRefineNev + c];
+      for (int c = 0; c < nev; ++c) rn[c] += ph[(size_t)b * pstride + c];
     // The estimate differs from the true residual of x only through the
     // FP32 products in the C block: |r - r_est| <= eps32 ||A|| ||y_c||, with
     // eps32 = (2L + 8) 2^-24 per FP32 product (one rounding per butterfly
@@ -833,7 +847,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       info.refine_true = max_resid;
       // the verified vectors become X0 either way
       TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
-      TM_CK(cudaMemcpyAsync(AX0.p, AXo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(XA.as<double>() + (int64_t)nev * n, AXo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
       if (ok_all) {
         info.refine_outcome = 2;
         return true;
@@ -841,11 +855,11 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       // re-orthonormalise X0 (its products follow linearly) and rebuild its rows
       for (int i = 0; i < nev; ++i) {
         double* xi = lz.v(i);
-        double* ai = AX0.as<double>() + (int64_t)i * n;
+        double* ai = (XA.as<double>() + (int64_t)nev * n) + (int64_t)i * n;
         for (int pass = 0; pass < 2 && i > 0; ++pass) {
           mdot(lz.v(0), n, i, xi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
           maxpy(lz.v(0), n, i, lz.h1.as<double>(), xi, n, s);
-          maxpy(AX0.as<double>(), n, i, lz.h1.as<double>(), ai, n, s);
+          maxpy((XA.as<double>() + (int64_t)nev * n), n, i, lz.h1.as<double>(), ai, n, s);
         }
         double q = 0.0;
         nrm2sq(xi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
@@ -862,26 +876,50 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
     force_grow = false;
     if (verified >= 3 || round + 1 >= 3 * kRefineRounds || nb + nev > cap) break;
-    // grow: the wanted residual block, FP32 Gram-Schmidt (two passes) against
-    // the subspace, FP32 products; a column that vanishes is dropped
-    for (int c = 0; c < nev; ++c) {
-      float* w = f32col(B32, nb);
-      TM_CK(cudaMemcpyAsync(w, R32.as<float>() + (int64_t)c * n, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-      double q0 = 0.0, q = 0.0;
-      nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-      TM_CK(cudaMemcpyAsync(&q0, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-      for (int pass = 0; pass < 2; ++pass) {
-        mdot_f32(B32.as<float>(), n, nb, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-        maxpy_f32(B32.as<float>(), n, nb, lz.h1.as<double>(), w, n, s);
+    // grow: the wanted residual block, block FP32 Gram-Schmidt (two passes)
+    // against the subspace, then within the block; FP32 products; a column
+    // that vanishes is dropped
+    {
+      float* wb = f32col(B32, nb);
+      TM_CK(cudaMemcpyAsync(wb, R32.p, (size_t)nev * n * 4, cudaMemcpyDeviceToDevice, s));
+      std::vector<double> q0(nev, 0.0);
+      for (int c = 0; c < nev; ++c) {
+        nrm2sq_f32(f32col(B32, nb + c), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q0[c], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
       }
-      nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-      TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+      F32Cols wc{};
+      F32ColsMut wm{};
+      for (int c = 0; c < nev; ++c) {
+        wc.c[c] = f32col(B32, nb + c);
+        wm.c[c] = f32col(B32, nb + c);
+      }
+      for (int pass = 0; pass < 2; ++pass) {
+        mdot_block_f32(B32.as<float>(), n, nb, wc, nev, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+        maxpy_block_f32(B32.as<float>(), n, nb, Hd.as<double>(), 48, wm, nev, n, s);
+      }
       host_sync();
-      if (!(q0 > 0.0) || !(q > 1e-10 * q0)) continue;
-      normalize_f32(w, lz.nsq.as<double>(), w, n, s);
-      prod32(w, f32col(AB32, nb));
-      add_gcol(nb);
-      ++nb;
+      int pos = nb;
+      for (int c = 0; c < nev; ++c) {
+        float* w = f32col(B32, nb + c);
+        if (pos < nb + c) {
+          TM_CK(cudaMemcpyAsync(f32col(B32, pos), w, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+          w = f32col(B32, pos);
+        }
+        for (int pass = 0; pass < 2 && pos > nb; ++pass) {
+          mdot_f32(f32col(B32, nb), n, pos - nb, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+          maxpy_f32(f32col(B32, nb), n, pos - nb, lz.h1.as<double>(), w, n, s);
+        }
+        double q = 0.0;
+        nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        host_sync();
+        if (!(q0[c] > 0.0) || !(q > 1e-10 * q0[c])) continue;
+        normalize_f32(w, lz.nsq.as<double>(), w, n, s);
+        ++pos;
+      }
+      for (int j = nb; j < pos; ++j) prod32(f32col(B32, j), f32col(AB32, j));
+      if (pos > nb) add_gcols(nb, pos - nb);
+      nb = pos;
     }
   }
   if (have_x) TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
@@ -1020,8 +1058,19 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
   info.max_resid = max_resid;
   for (int i = 0; i < nev && i < (int)theta.size(); ++i) vals[i] = theta[i];
   if (vecs_host && Lz) {
-    TM_CK(cudaMemcpyAsync(vecs_host, Lz->v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToHost, s));
-    TM_CK(cudaStreamSynchronize(s));
+    // eigenvectors in the reference's order: the pi -> reference scatter
+    // runs on the device, then one copy to the host
+    if (op.has_pi) {
+      DBuf ref;
+      ref.alloc((size_t)nev * n * 8);
+      for (int c = 0; c < nev; ++c)
+        scatter_f64(Lz->v(c), op.pi.as<uint32_t>(), ref.as<double>() + (int64_t)c * n, n, s);
+      TM_CK(cudaMemcpyAsync(vecs_host, ref.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost, s));
+      TM_CK(cudaStreamSynchronize(s));
+    } else {
+      TM_CK(cudaMemcpyAsync(vecs_host, Lz->v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToHost, s));
+      TM_CK(cudaStreamSynchronize(s));
+    }
   }
   const_cast<Op&>(op).matvecs += info.matvecs;
   info.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
