@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
   const uint64_t ob = blockIdx.x & ((1ull << cp.no) - 1);
   const int lb_outer = (int)(blockIdx.x >> cp.no);
   const uint64_t rbase = dep(ob, cp.opos, cp.no);
-  const int lo = KS * cp.t0;  // lowest site of the pass's steps
+  const int site0 = KS * cp.t0;  // lowest site of the pass's steps
   const int nloop = cp.last ? cp.nlb : 1;
   if (cp.last)
     for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) acc[e] = 0.0;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
     // load / build the tile
     for (int e = threadIdx.x; e < tile; e += blockDim.x) {
       const int aux = e & ((1 << NA) - 1);
-      const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, lo);
+      const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, site0);
       T v;
       if (cp.first)
         v = chain_init<T, ZB, IO>(x, pre, smap, L, bc, r, aux, lb, c);
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
         const int lo = rest & ((1 << (sb - NA)) - 1);
         const int hi = rest >> (sb - NA);
         const int ebase = (hi << (sb + KS)) | (lo << NA);
-        const uint64_t r = rbase | tile_state((uint64_t)(ebase >> NA), cp.jbit0, lo);
+        const uint64_t r = rbase | tile_state((uint64_t)(ebase >> NA), cp.jbit0, site0);
         if (!ZB) {
           // DNNI: out(a, s) = b1[s^a] b2[nb^s] (b2[s] in(0, a) + b2[s^1] in(1, a)),
           // in(q, s') = value with aux q and site t = s'
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
       }
     } else {
       for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-        const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, lo);
+        const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, site0);
         P[(((uint64_t)lb << L | r) << NA) | (uint64_t)(e & ((1 << NA) - 1))] = sm[spad(e)];
       }
     }
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const 
   }
   if (cp.last) {
     for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) {
-      const uint64_t r = rbase | tile_state((uint64_t)e, cp.jbit0, lo);
+      const uint64_t r = rbase | tile_state((uint64_t)e, cp.jbit0, site0);
       double v = acc[e];
       if (post) v *= post[r];
       y[r] = (IO)(v * postc);
