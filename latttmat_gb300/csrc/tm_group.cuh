@@ -139,7 +139,29 @@ TM_HD int group_order(const GroupDev& g) {
   return 1;
 }
 
+// X-2D periodic group on L <= 32 bits in 32-bit arithmetic: the same images
+// as for_each_image (rotations, their reflections, and the flips of both),
+// tested in rotation order with an early exit.  The orbit-table build spends
+// its time here (2^L states at L = 32).
+TM_HD bool is_rep_x2d32(uint32_t s, int L, int flip) {
+  const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
+  uint32_t a = s;
+  for (int k = 0; k < L; ++k) {
+#if defined(__CUDA_ARCH__)
+    const uint32_t b = __brev(a) >> (32 - L);
+#else
+    uint32_t b = 0;
+    for (int i = 0; i < L; ++i) b |= ((a >> i) & 1u) << (L - 1 - i);
+#endif
+    if (a < s || b < s) return false;
+    if (flip && ((~a & mask) < s || (~b & mask) < s)) return false;
+    a = ((a >> 1) | (a << (L - 1))) & mask;  // rotate right by one site
+  }
+  return true;
+}
+
 TM_HD bool is_rep(const GroupDev& g, uint64_t s) {
+  if (g.kind == G_X2D && g.periodic && g.L <= 32) return is_rep_x2d32((uint32_t)s, g.L, g.flip);
   bool rep = true;
   for_each_image(g, s, [&](uint64_t im) {
     if (im < s) {
