@@ -466,6 +466,48 @@ __global__ void __launch_bounds__(BT) mdot_block_f32_kernel(const float* __restr
   }
 }
 
+// FP64 block dots of FP64 columns against FP32 vectors (exact FP32 values,
+// FP64 products and sums): part[b][k*NW + j] partial sums of V[k] . W[j].
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT) mdot64_block_kernel(const double* __restrict__ V, int64_t ldv, int kv,
+                                                          F32Cols W, int nw, int64_t n, double* __restrict__ part) {
+  double acc[KV][NW];
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) acc[k][j] = 0.0;
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (; i < n; i += st) {
+    double wv[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) wv[j] = (j < nw) ? (double)W.c[j][i] : 0.0;
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const double v = V[k * ldv + i];
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+          if (j < nw) acc[k][j] = fma(v, wv[j], acc[k][j]);
+      }
+  }
+  __shared__ double sh[BT / 32][KV * NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      double v = warp_sum(acc[k][j]);
+      if (lane == 0) sh[wid][k * NW + j] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    double a = 0.0;
+    for (int q = 0; q < BT / 32; ++q) a += sh[q][t];
+    part[(int64_t)blockIdx.x * (KV * NW) + t] = a;
+  }
+}
+
 // H[(k0 + k) + j * ldh] = sum over blocks of part[b][k*NW + j]
 __global__ void mdot_block_final(const double* __restrict__ part, int nb, int kv, int nw, int stride, int nws,
                                  double* H, int64_t ldh, int k0) {
@@ -652,6 +694,20 @@ void maxpy_block_f32(const float* V, int64_t ldv, int nv, const double* H, int64
     maxpy_block_f32_kernel<KV, kMaxBlockW><<<red_blocks(n), BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, H, ldh, k0,
                                                                          W, nw, n);
     TM_CKK("maxpy_block_f32");
+  }
+}
+
+void mdot64_block(const double* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H,
+                  int64_t ldh, double* part, cudaStream_t s) {
+  if (nw < 1 || nw > 4) fail(TM_ERR_LIMIT, "mdot64_block: 1..4 vectors");
+  constexpr int KV = 8, NW = 4;
+  const int nb = red_blocks(n);
+  for (int k0 = 0; k0 < nv; k0 += KV) {
+    const int kv = std::min(KV, nv - k0);
+    mdot64_block_kernel<KV, NW><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+    TM_CKK("mdot64_block");
+    mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * NW, NW, H, ldh, k0);
+    TM_CKK("mdot_block_final");
   }
 }
 

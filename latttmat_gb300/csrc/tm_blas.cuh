@@ -62,6 +62,10 @@ void mdot_block_f32(const float* V, int64_t ldv, int nv, const F32Cols& W, int n
 void maxpy_block_f32(const float* V, int64_t ldv, int nv, const double* H, int64_t ldh, const F32ColsMut& W, int nw,
                      int64_t n, cudaStream_t s);
 size_t mdot_block_part_bytes();
+// H[k + j*ldh] = V[k] . W[j] with FP64 columns V and up to 4 FP32 vectors W,
+// in FP64 (the FP32 values are exact in FP64)
+void mdot64_block(const double* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H,
+                  int64_t ldh, double* part, cudaStream_t s);
 // w -= V h (FP32 data and arithmetic), any nv (chunks of NV32)
 void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, cudaStream_t s);
 // wout = win - V h ; h2[k] = sum_i V[k][i] wout[i]   (one pass)

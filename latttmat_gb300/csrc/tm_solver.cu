@@ -668,16 +668,22 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   std::vector<double> G((size_t)cap * cap, 0.0), M((size_t)cap * cap, 0.0);
   auto g = [&](int i, int j) -> double& { return G[(size_t)j * cap + i]; };
   auto mm = [&](int i, int j) -> double& { return M[(size_t)j * cap + i]; };
-  // X0 rows of C column j (FP64 dots against the FP32 values): one sweep
-  // over XA gives X0 . c (Gram) and A X0 . c (projected matrix)
-  auto x0_rows = [&](int j) {
-    std::vector<double> h(2 * nev);
-    mdot32(XA.as<double>(), n, 2 * nev, f32col(B32, j), 1.0, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-    TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, 2 * nev * 8, cudaMemcpyDeviceToHost, s));
+  // X0 rows of C columns j0 .. j0+cnt-1 (cnt <= 4; FP64 dots against the
+  // FP32 values): one sweep over XA gives X0 . c (Gram) and A X0 . c
+  // (projected matrix) for the whole block
+  auto x0_rows = [&](int j0, int cnt) {
+    F32Cols w{};
+    for (int c = 0; c < cnt; ++c) w.c[c] = f32col(B32, j0 + c);
+    mdot64_block(XA.as<double>(), n, 2 * nev, w, cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+    std::vector<double> h((size_t)48 * cnt);
+    TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
-    for (int i = 0; i < nev; ++i) {
-      mm(i, j) = mm(j, i) = h[i];
-      g(i, j) = g(j, i) = h[nev + i];
+    for (int c = 0; c < cnt; ++c) {
+      const int j = j0 + c;
+      for (int i = 0; i < nev; ++i) {
+        mm(i, j) = mm(j, i) = h[(size_t)48 * c + i];
+        g(i, j) = g(j, i) = h[(size_t)48 * c + nev + i];
+      }
     }
   };
   // C columns j0 .. j0+cnt-1 (cnt <= 4) against columns 0 .. j0+cnt-1: one
@@ -704,8 +710,8 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
         g(i, j) = g(j, i) = S * 0.5 * (gl[i] + gr[i]);
         mm(i, j) = mm(j, i) = mc[i];
       }
-      x0_rows(j);
     }
+    x0_rows(j0, cnt);
   };
   // X0 block (FP64 products and dots) and its rows against every C column
   auto set_x0 = [&](int nb) {
@@ -731,7 +737,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
       TM_CKK("to_f32");
     }
-    for (int j = nev; j < nb; ++j) x0_rows(j);
+    for (int j = nev; j < nb; j += 4) x0_rows(j, std::min(4, nb - j));
   };
   // start: the extra Ritz vectors to FP32 with FP32 products, the wanted ones
   // with FP64-accurate products
