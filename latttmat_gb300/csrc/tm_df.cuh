@@ -45,6 +45,19 @@ __device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
   return df_renorm(p, e);
 }
 
+// a * b + c with one renormalisation (TwoProduct by FMA, then TwoSum)
+__device__ __forceinline__ dfloat df_fma(dfloat a, dfloat b, dfloat c) {
+  float p = a.hi * b.hi;
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  float s = p + c.hi;
+  float bb = s - p;
+  float se = (p - (s - bb)) + (c.hi - bb);
+  se += pe + c.lo;
+  return df_renorm(s, se);
+}
+
 __device__ __forceinline__ dfloat& operator+=(dfloat& a, dfloat b) {
   a = a + b;
   return a;

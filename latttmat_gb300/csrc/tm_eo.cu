@@ -17,20 +17,37 @@
 //   pass 2: z = Th_O w needs only tiles with e = e_rep, one per H-class of e.
 //           Each w value is read from its H-image in a pass-1 tile.  The output
 //           is the value at one designated state of every orbit.
-// Work and HBM traffic are about 2^(L+1)/|H| elements instead of 2^L * L.  The
-// reduced vector is kept in "pi order" (pass-2 tile order) so the output
-// stores are contiguous; pi maps back to the reference's idxlist order.
+// Work and HBM traffic are about 2^(L+1)/|H| elements instead of 2^L * L.
+//
+// Memory layout.  Both passes walk a tile in an "iteration order" of the
+// m-bit patterns: grouped by the top ct bits (the cluster split, below), then
+// by H-class.  A warp's 32 elements are then a few whole H-classes, and
+//   - the reduced vector is kept in "pi order": per pass-2 tile, the
+//     designated outputs in pass 2's iteration order, so pass 1's gathers of
+//     one class land in a few contiguous runs of the vector, and each CTA of
+//     pass 2 writes one contiguous range (pi maps back to idxlist order);
+//   - w1 is class-major: the block of e-class C holds, for each pass-1 tile,
+//     the |C| values of C's members, so pass 1 writes and pass 2 reads whole
+//     runs, and pass 2 reads one contiguous block per tile.
+// Gathers go straight to shared memory with cp.async.
+//
+// Arithmetic.  The butterfly [[a, b], [b, a]] is applied as x0 + r x1,
+// x1 + r x0 with r = min(a, b) / max(a, b): one FMA per element and level.
+// The input is scaled by (1 + r)^-L so magnitudes match the normalised
+// operator, and the output factor stays (e^K + e^-K)^L.
 //
 // A tile of 2^m elements is split over a cluster of 2^c CTAs (FP32 m=16: two
-// CTAs x 2^15 elements in 135 KB of shared memory).  The butterflies on the
-// top c tile bits combine the CTAs' shared memory through DSMEM.  Inside a CTA
-// each thread owns 2^KB elements in registers: KB butterfly levels per round,
-// with a padded shared-memory transpose between rounds.
+// CTAs x 2^15 elements in 135 KB of shared memory), CTA `rank` holding the
+// patterns whose top c bits are `rank`.  The butterflies on those top bits
+// combine the CTAs' tiles through DSMEM once all local rounds are done.
+// Inside a CTA each thread owns 2^KB elements per round: KB butterfly levels
+// in registers, with a padded shared-memory transpose between rounds.
 #include <cooperative_groups.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "tm_df.cuh"
@@ -94,56 +111,90 @@ namespace {
 
 struct EOArgs {
   int m, c, n, p;       // tile bits, cluster bits, local bits, thread bits
+  int ct;               // top bits grouping the iteration orders (c <= ct)
   int ng;               // H elements
-  int64_t n_orep;       // pass-1 tiles (row length of the transposed w1)
-  float a32, b32;       // normalised butterfly coefficients
-  double a64, b64;
+  int64_t n_orep;       // pass-1 tiles
+  // Butterfly [[a, b], [b, a]] / max(a, b) on every site: with r = min/max,
+  // x0' = x0 + r x1, x1' = x1 + r x0 (swap = 0, a >= b) or the outputs
+  // exchanged (swap = 1).  The factor max(a, b)^L is applied at the output.
+  float r32;
+  double r64;
+  int swap;
 };
 
 __device__ __forceinline__ int spad(int e) { return e + (e >> 5); }
 
 template <class T>
-__device__ __forceinline__ T ca(const EOArgs& A);
+__device__ __forceinline__ T coef_r(const EOArgs& A);
 template <>
-__device__ __forceinline__ float ca<float>(const EOArgs& A) { return A.a32; }
+__device__ __forceinline__ float coef_r<float>(const EOArgs& A) { return A.r32; }
 template <>
-__device__ __forceinline__ double ca<double>(const EOArgs& A) { return A.a64; }
-template <class T>
-__device__ __forceinline__ T cb(const EOArgs& A);
+__device__ __forceinline__ double coef_r<double>(const EOArgs& A) { return A.r64; }
 template <>
-__device__ __forceinline__ float cb<float>(const EOArgs& A) { return A.b32; }
-template <>
-__device__ __forceinline__ double cb<double>(const EOArgs& A) { return A.b64; }
-template <>
-__device__ __forceinline__ dfloat ca<dfloat>(const EOArgs& A) { return dfloat(A.a64); }
-template <>
-__device__ __forceinline__ dfloat cb<dfloat>(const EOArgs& A) { return dfloat(A.b64); }
+__device__ __forceinline__ dfloat coef_r<dfloat>(const EOArgs& A) { return dfloat(A.r64); }
+
+// r * x + y in the engine's arithmetic
+__device__ __forceinline__ float fma_t(float r, float x, float y) { return fmaf(r, x, y); }
+__device__ __forceinline__ double fma_t(double r, double x, double y) { return fma(r, x, y); }
+__device__ __forceinline__ dfloat fma_t(dfloat r, dfloat x, dfloat y) { return df_fma(r, x, y); }
 
 // in-register butterflies over the 2^NB elements held by one thread
 template <class T, int NB>
-__device__ __forceinline__ void reg_bfly(T (&v)[1 << NB], int nb, T a, T b) {
+__device__ __forceinline__ void reg_bfly(T (&v)[1 << NB], int nb, T r, int swap) {
+  if (!swap) {
 #pragma unroll
-  for (int lv = 0; lv < NB; ++lv) {
-    if (lv < nb) {
+    for (int lv = 0; lv < NB; ++lv) {
+      if (lv < nb) {
 #pragma unroll
-      for (int i = 0; i < (1 << NB); ++i) {
-        if (!(i & (1 << lv))) {
-          T x0 = v[i], x1 = v[i | (1 << lv)];
-          v[i] = a * x0 + b * x1;
-          v[i | (1 << lv)] = b * x0 + a * x1;
+        for (int i = 0; i < (1 << NB); ++i) {
+          if (!(i & (1 << lv))) {
+            const T x0 = v[i], x1 = v[i | (1 << lv)];
+            v[i] = fma_t(r, x1, x0);
+            v[i | (1 << lv)] = fma_t(r, x0, x1);
+          }
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int lv = 0; lv < NB; ++lv) {
+      if (lv < nb) {
+#pragma unroll
+        for (int i = 0; i < (1 << NB); ++i) {
+          if (!(i & (1 << lv))) {
+            const T x0 = v[i], x1 = v[i | (1 << lv)];
+            v[i] = fma_t(r, x0, x1);
+            v[i | (1 << lv)] = fma_t(r, x1, x0);
+          }
         }
       }
     }
   }
 }
 
-// butterflies on local bits [0, p) of the shared-memory tile, KB bits per round
+// asynchronous global->shared copy of one element (cp.async, sm_80+): the
+// gathers of a tile are all in flight at once without holding registers
+template <int SZ>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src);
+template <>
+__device__ __forceinline__ void cp_async_elem<4>(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+template <>
+__device__ __forceinline__ void cp_async_elem<8>(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// butterflies on local bits [0, nbits) of the shared-memory tile, KB bits per round
 template <class T, int KB>
-__device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A) {
-  const T a = ca<T>(A), b = cb<T>(A);
-  const int n = A.n, p = A.p;
-  for (int g0 = 0; g0 < p; g0 += KB) {
-    const int gs = min(KB, p - g0);
+__device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A, int nbits) {
+  const T r = coef_r<T>(A);
+  const int n = A.n;
+  for (int g0 = 0; g0 < nbits; g0 += KB) {
+    const int gs = min(KB, nbits - g0);
     const int nfree = 1 << (n - gs);
     for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
       int j0 = (f & ((1 << g0) - 1)) | ((f >> g0) << (g0 + gs));
@@ -151,7 +202,7 @@ __device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A) {
 #pragma unroll
       for (int i = 0; i < (1 << KB); ++i)
         if (i < (1 << gs)) v[i] = sm[spad(j0 | (i << g0))];
-      reg_bfly<T, KB>(v, gs, a, b);
+      reg_bfly<T, KB>(v, gs, r, A.swap);
 #pragma unroll
       for (int i = 0; i < (1 << KB); ++i)
         if (i < (1 << gs)) sm[spad(j0 | (i << g0))] = v[i];
@@ -160,29 +211,52 @@ __device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A) {
   }
 }
 
-// combine the cluster's 2^c partial tiles for local element j (top c bits)
-template <class T>
-__device__ __forceinline__ T cluster_combine(cg::cluster_group& cl, T* sm, int rank, int j,
-                                             const EOArgs& A) {
-  const T a = ca<T>(A), b = cb<T>(A);
-  T acc = 0;
+// Combine the cluster's 2^c partial tiles (butterflies on the top c tile
+// bits) in place: afterwards sm[spad(j)] holds the final value of local
+// element j.  Each thread reads its own elements j = tid + k*blockDim from
+// every CTA of the cluster (contiguous DSMEM reads), and writes back after a
+// cluster barrier, so no CTA overwrites values another still reads.  After
+// that barrier no CTA reads another's shared memory, so a CTA may exit.
+template <class T, int KB>
+__device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int rank, const EOArgs& A) {
+  const T a = A.swap ? coef_r<T>(A) : T(1), b = A.swap ? T(1) : coef_r<T>(A);
+  const int p = A.p, kb = A.n - A.p;
   const int nc = 1 << A.c;
+  T acc[1 << KB];
+#pragma unroll
+  for (int k = 0; k < (1 << KB); ++k) acc[k] = T(0);
+  cl.sync();
   for (int r = 0; r < nc; ++r) {
-    T coef = 1;
-    for (int bit = 0; bit < A.c; ++bit) coef *= (((r ^ rank) >> bit) & 1) ? b : a;
+    T coef = T(1);
+    for (int bit = 0; bit < A.c; ++bit) coef = coef * ((((r ^ rank) >> bit) & 1) ? b : a);
     const T* src = (r == rank) ? sm : cl.map_shared_rank(sm, r);
-    acc += coef * src[spad(j)];
+#pragma unroll
+    for (int k = 0; k < (1 << KB); ++k)
+      if (k < (1 << kb)) acc[k] = acc[k] + coef * src[spad(threadIdx.x + (k << p))];
   }
-  return acc;
+  cl.sync();
+#pragma unroll
+  for (int k = 0; k < (1 << KB); ++k)
+    if (k < (1 << kb)) sm[spad(threadIdx.x + (k << p))] = acc[k];
+  // only this CTA reads its combined tile from here on
+  __syncthreads();
 }
 
-// pass 1: w1[t][e] = (Th_E v)[(e, o_rep(t))],  v[(e,o_rep)] = u[map1[t][e]]
-// (InT: element type of u; T: arithmetic / storage type of the tile and w1)
+// elements per batch of the output loops (independent loads in flight per thread)
+constexpr int kOutBatch = 8;
+
+// pass 1: w1(t, e) = (Th_E v)[(e, o_rep(t))],  v[(e,o_rep)] = u[map1[t][P]]
+// where P runs over the iteration order of e (it_e).  CTA `rank` of the
+// cluster owns the e with top c bits = rank, iteration positions
+// [rank*2^n, (rank+1)*2^n).  (InT: element type of u, the same size as T;
+// T: arithmetic / storage type of the tile and w1)
 template <class T, int KB, class InT>
 __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restrict__ u,
                                                     const uint32_t* __restrict__ map1,
-                                                    const uint32_t* __restrict__ colmap,
-                                                    T* __restrict__ w1) {
+                                                    const uint16_t* __restrict__ it_e,
+                                                    const uint32_t* __restrict__ wbase,
+                                                    const uint8_t* __restrict__ wsz, T* __restrict__ w1) {
+  static_assert(sizeof(T) == sizeof(InT), "u and the tile share the element size");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   cg::cluster_group cl = cg::this_cluster();
@@ -190,44 +264,74 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   const int64_t tile = blockIdx.x >> A.c;
   const int n = A.n, p = A.p;
   const int kb = n - p;
-  const uint32_t* mrow = map1 + (tile << A.m) + ((int64_t)rank << n);
-  // round A: gather straight into registers; register bits are local bits [p, n)
+  const uint32_t lmask = (1u << n) - 1u;
+  const uint32_t base = (uint32_t)rank << n;
+  const uint32_t* mrow = map1 + (tile << A.m);
+  // gather the tile: index loads, then one asynchronous copy per element.
+  // A warp's elements are one or two symmetry classes of e, whose orbits sit
+  // in a few contiguous runs of u.
   {
-    T v[1 << KB];
+    uint32_t idx[1 << KB];
+    uint16_t ev[1 << KB];
 #pragma unroll
     for (int i = 0; i < (1 << KB); ++i) {
       if (i < (1 << kb)) {
-        int j = threadIdx.x + (i << p);
-        v[i] = T(u[__ldg(mrow + j)]);
+        const uint32_t P = base + threadIdx.x + (i << p);
+        idx[i] = __ldg(mrow + P);
+        ev[i] = __ldg(it_e + P);
       }
     }
-    reg_bfly<T, KB>(v, kb, ca<T>(A), cb<T>(A));
 #pragma unroll
     for (int i = 0; i < (1 << KB); ++i)
-      if (i < (1 << kb)) sm[spad(threadIdx.x + (i << p))] = v[i];
+      if (i < (1 << kb)) cp_async_elem<sizeof(T)>(sm + spad(ev[i] & lmask), u + idx[i]);
+    cp_async_wait_all();
+    if constexpr (!std::is_same<T, InT>::value) {
+      // each thread converts the elements it copied
+#pragma unroll
+      for (int i = 0; i < (1 << KB); ++i) {
+        if (i < (1 << kb)) {
+          T* slot = sm + spad(ev[i] & lmask);
+          *slot = T(*reinterpret_cast<const InT*>(slot));
+        }
+      }
+    }
   }
   __syncthreads();
-  smem_rounds<T, KB>(sm, A);
-  // Output.  w1 is stored transposed: e goes to row colmap[e], column
-  // `tile`.  The column writes of concurrently running tiles fill adjacent
-  // words of each row, which L2 merges into full sectors.
-  T* wcol = w1 + tile;
-  if (A.c > 0) cl.sync();
-  for (int j = threadIdx.x; j < (1 << n); j += blockDim.x) {
-    T val = (A.c == 0) ? sm[spad(j)] : cluster_combine<T>(cl, sm, rank, j, A);
-    uint32_t row = __ldg(colmap + (((uint32_t)rank << n) | (uint32_t)j));
-    wcol[(int64_t)row * A.n_orep] = val;
+  smem_rounds<T, KB>(sm, A, n);
+  if (A.c > 0) cluster_reduce<T, KB>(cl, sm, rank, A);
+  // Output.  w1 is class-major: the block of e-class C holds, for each tile,
+  // the |C| values of C's members, so a warp writes a few contiguous runs.
+  for (int k0 = 0; k0 < (1 << kb); k0 += kOutBatch) {
+    uint32_t wb[kOutBatch], ws[kOutBatch];
+    uint16_t ev[kOutBatch];
+#pragma unroll
+    for (int q = 0; q < kOutBatch; ++q) {
+      if (k0 + q < (1 << kb)) {
+        const uint32_t P = base + threadIdx.x + ((k0 + q) << p);
+        ev[q] = __ldg(it_e + P);
+        wb[q] = __ldg(wbase + P);
+        ws[q] = __ldg(wsz + P);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kOutBatch; ++q)
+      if (k0 + q < (1 << kb)) w1[(int64_t)wb[q] + tile * ws[q]] = sm[spad(ev[q] & lmask)];
   }
-  if (A.c > 0) cl.sync();
 }
 
-// pass 2: z[(e_rep, o)] = (Th_O w)[(e_rep, o)]; emit designated outputs
+// pass 2: z[(e_rep, o)] = (Th_O w)[(e_rep, o)]; emit designated outputs.
+// The w value at (e_rep, o) is the pass-1 value at the H-image
+// (act_e(g, e_rep), o_rep) with act_o(g, o) = o_rep.  CTA `rank` owns the o
+// with top c bits = rank (iteration positions of it_o as in pass 1).
 // (OutT: element type of y)
 template <class T, int KB, bool F64SCALE, class OutT>
 __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restrict__ w1,
+                                                    const uint16_t* __restrict__ it_o,
                                                     const uint32_t* __restrict__ t2,
+                                                    const uint16_t* __restrict__ cf_e,
                                                     const uint32_t* __restrict__ erep,
-                                                    const uint32_t* __restrict__ colmap,
+                                                    const uint32_t* __restrict__ cls_start,
+                                                    const uint32_t* __restrict__ cls_size,
                                                     const uint32_t* __restrict__ out_off,
                                                     const uint16_t* __restrict__ out_o,
                                                     const double* __restrict__ sout64,
@@ -241,41 +345,60 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
   const int64_t tile = blockIdx.x >> A.c;
   const int n = A.n, p = A.p;
   const int kb = n - p;
+  const uint32_t lmask = (1u << n) - 1u;
+  const uint32_t base = (uint32_t)rank << n;
   const uint32_t e_rep = erep[tile];
-  // w1 rows of this tile's H-class (one contiguous block of rows)
-  for (int g = threadIdx.x; g < A.ng; g += blockDim.x) he[g] = __ldg(colmap + act_e(g, e_rep, A.m));
+  // this tile's w1 block (class-major): member offsets of the H-images of e_rep
+  const uint32_t hb = cls_start[tile], hs = cls_size[tile];
+  for (int g = threadIdx.x; g < A.ng; g += blockDim.x)
+    he[g] = hb * (uint32_t)A.n_orep + (__ldg(cf_e + act_e(g, e_rep, A.m)) - hb);
   __syncthreads();
   {
-    T v[1 << KB];
+    uint32_t code[1 << KB];
+    uint16_t ov[1 << KB];
 #pragma unroll
     for (int i = 0; i < (1 << KB); ++i) {
       if (i < (1 << kb)) {
-        int j = threadIdx.x + (i << p);
-        uint32_t o = ((uint32_t)rank << n) | (uint32_t)j;
-        uint32_t code = __ldg(t2 + o);
-        v[i] = w1[(int64_t)he[code & 255u] * A.n_orep + (code >> 8)];
+        const uint32_t P = base + threadIdx.x + (i << p);
+        code[i] = __ldg(t2 + P);
+        ov[i] = __ldg(it_o + P);
       }
     }
-    reg_bfly<T, KB>(v, kb, ca<T>(A), cb<T>(A));
 #pragma unroll
     for (int i = 0; i < (1 << KB); ++i)
-      if (i < (1 << kb)) sm[spad(threadIdx.x + (i << p))] = v[i];
+      if (i < (1 << kb))
+        cp_async_elem<sizeof(T)>(sm + spad(ov[i] & lmask),
+                                 w1 + he[code[i] & 255u] + (int64_t)(code[i] >> 8) * hs);
+    cp_async_wait_all();
   }
   __syncthreads();
-  smem_rounds<T, KB>(sm, A);
-  const int part = (int)(tile << A.c) + rank;
-  const uint32_t k0 = out_off[part], k1 = out_off[part + 1];
-  const int lmask = (1 << n) - 1;
-  if (A.c > 0) cl.sync();
-  for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-    int j = out_o[k] & lmask;
-    T val = (A.c == 0) ? sm[spad(j)] : cluster_combine<T>(cl, sm, rank, j, A);
-    if (F64SCALE)
-      y[k] = (OutT)((double)val * sout64[k] * post);
-    else
-      y[k] = (OutT)(val * T(sout32[k]));
+  smem_rounds<T, KB>(sm, A, n);
+  if (A.c > 0) cluster_reduce<T, KB>(cl, sm, rank, A);
+  // Designated outputs of this tile.  They are ordered like it_o, so the
+  // outputs whose o this CTA holds form one contiguous range: groups
+  // [rank, rank + 1) * 2^(ct - c) of the tile's 2^ct output groups.
+  const int64_t g0 = (tile << A.ct) + ((int64_t)rank << (A.ct - A.c));
+  const uint32_t k0 = out_off[g0], k1 = out_off[g0 + (1 << (A.ct - A.c))];
+  const uint32_t step = blockDim.x * kOutBatch;
+  for (uint32_t kk = k0 + threadIdx.x; kk < k1; kk += step) {
+    uint16_t ov[kOutBatch];
+#pragma unroll
+    for (int q = 0; q < kOutBatch; ++q) {
+      const uint32_t k = kk + q * blockDim.x;
+      ov[q] = (k < k1) ? out_o[k] : (uint16_t)0;
+    }
+#pragma unroll
+    for (int q = 0; q < kOutBatch; ++q) {
+      const uint32_t k = kk + q * blockDim.x;
+      if (k < k1) {
+        const T val = sm[spad(ov[q] & lmask)];
+        if (F64SCALE)
+          y[k] = (OutT)((double)val * sout64[k] * post);
+        else
+          y[k] = (OutT)(val * T(sout32[k]));
+      }
+    }
   }
-  if (A.c > 0) cl.sync();
 }
 
 // ---------------------------------------------------------------- plan kernels
@@ -292,10 +415,11 @@ __device__ __forceinline__ uint32_t rank_of(const PlanDev& P, uint64_t c) {
 }
 
 // designated output key per representative: min over orbit images whose even
-// part is an H-representative of (tile << m | o)
+// part is an H-representative of (tile << m | pos_o(o)); pos_o is the
+// position of o in pass 2's iteration order
 __global__ void eo_key_kernel(PlanDev P, const uint32_t* __restrict__ idx, int64_t R,
-                              const uint32_t* __restrict__ e_tile, uint32_t* __restrict__ key,
-                              uint32_t* __restrict__ dbits) {
+                              const uint32_t* __restrict__ e_tile, const uint16_t* __restrict__ pos_o,
+                              uint32_t* __restrict__ key, uint32_t* __restrict__ dbits) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < R; i += st) {
@@ -305,7 +429,7 @@ __global__ void eo_key_kernel(PlanDev P, const uint32_t* __restrict__ idx, int64
       uint32_t e = gather16((uint32_t)im), o = gather16((uint32_t)(im >> 1));
       uint32_t t = e_tile[e];
       if (t != 0xffffffffu) {
-        uint32_t k = (t << P.m) | o;
+        uint32_t k = (t << P.m) | pos_o[o];
         if (k < best) best = k;
       }
       return true;
@@ -322,8 +446,9 @@ __global__ void popc_kernel(const uint32_t* __restrict__ bits, uint32_t* __restr
 }
 
 __global__ void eo_perm_kernel(const uint32_t* __restrict__ key, int64_t R, const uint32_t* __restrict__ dbits,
-                               const uint32_t* __restrict__ dpre, int m, uint32_t* __restrict__ pi,
-                               uint32_t* __restrict__ pinv, uint16_t* __restrict__ out_o) {
+                               const uint32_t* __restrict__ dpre, int m, const uint16_t* __restrict__ o_of_pos,
+                               uint32_t* __restrict__ pi, uint32_t* __restrict__ pinv,
+                               uint16_t* __restrict__ out_o) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < R; i += st) {
@@ -332,17 +457,18 @@ __global__ void eo_perm_kernel(const uint32_t* __restrict__ key, int64_t R, cons
     uint32_t pos = dpre[w] + __popc(dbits[w] & ((1u << (k & 31)) - 1u));
     pi[pos] = (uint32_t)i;
     pinv[i] = pos;
-    out_o[pos] = (uint16_t)(k & ((1u << m) - 1u));
+    out_o[pos] = o_of_pos[k & ((1u << m) - 1u)];
   }
 }
 
 __global__ void eo_map1_kernel(PlanDev P, const uint32_t* __restrict__ olist, int n_orep,
-                               const uint32_t* __restrict__ pinv, uint32_t* __restrict__ map1) {
+                               const uint16_t* __restrict__ it_e, const uint32_t* __restrict__ pinv,
+                               uint32_t* __restrict__ map1) {
   const int64_t total = (int64_t)n_orep << P.m;
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < total; i += st) {
-    uint32_t t = (uint32_t)(i >> P.m), e = (uint32_t)(i & ((1 << P.m) - 1));
+    uint32_t t = (uint32_t)(i >> P.m), e = it_e[i & ((1 << P.m) - 1)];
     uint32_t s = join_eo(e, olist[t]);
     uint64_t c = canon(P.g, s);
     map1[i] = pinv[rank_of(P, c)];
@@ -389,6 +515,25 @@ static int cluster_bits_for(int m, size_t elem) {
   return c;
 }
 
+// Orders of the m-bit patterns used by the passes.  cls: H-class index of
+// each pattern; ct: top bits that split a tile over a cluster.
+//   iteration order: (top ct bits, class, pattern) -- a CTA of a 2^c-CTA
+//     cluster (c <= ct) owns one contiguous range, and a warp's elements are
+//     one or two classes;
+//   class-first order: (class, top ct bits, pattern) -- each class contiguous.
+static std::vector<uint32_t> pattern_order(const std::vector<uint32_t>& cls, int m, int ct, bool class_first) {
+  const uint32_t M = 1u << m;
+  std::vector<uint64_t> k(M);
+  for (uint32_t x = 0; x < M; ++x) {
+    const uint64_t top = x >> (m - ct);
+    k[x] = class_first ? ((uint64_t)cls[x] << 40 | top << 20 | x) : (top << 40 | (uint64_t)cls[x] << 20 | x);
+  }
+  std::sort(k.begin(), k.end());
+  std::vector<uint32_t> ord(M);
+  for (uint32_t i = 0; i < M; ++i) ord[i] = (uint32_t)(k[i] & 0xfffffu);
+  return ord;
+}
+
 void build_eo_plan(Op& op) {
   EOPlan& P = op.eo;
   const int L = op.L, m = L / 2;
@@ -412,6 +557,11 @@ void build_eo_plan(Op& op) {
     orep[o] = best;
     og[o] = bg;
   }
+  for (uint32_t e = 0; e < M; ++e) {
+    uint32_t best = e;
+    for (int g = 0; g < P.ng; ++g) best = std::min(best, act_e(g, e, m));
+    erep_of[e] = best;
+  }
   std::vector<uint32_t> olist, elist;
   std::vector<uint32_t> otile(M, 0xffffffffu), etile(M, 0xffffffffu);
   for (uint32_t o = 0; o < M; ++o)
@@ -419,39 +569,76 @@ void build_eo_plan(Op& op) {
       otile[o] = (uint32_t)olist.size();
       olist.push_back(o);
     }
-  for (uint32_t e = 0; e < M; ++e) {
-    uint32_t best = e;
-    for (int g = 0; g < P.ng; ++g) best = std::min(best, act_e(g, e, m));
-    if (best == e) {
+  for (uint32_t e = 0; e < M; ++e)
+    if (erep_of[e] == e) {
       etile[e] = (uint32_t)elist.size();
       elist.push_back(e);
     }
-  }
-  std::vector<uint32_t> t2(M);
-  for (uint32_t o = 0; o < M; ++o) t2[o] = (otile[orep[o]] << 8) | (uint32_t)og[o];
-  // w1 row of each even pattern e.  Rows in e order: pass 1's column writes
-  // then walk the rows in order (consecutive threads, consecutive rows), and
-  // pass 2 reads the |class| rows of its tile's H-class.  (Grouping each
-  // H-class into contiguous rows was measured slower: 2.48 against 1.99 ms for
-  // pass 1 at L=32, pass 2 unchanged.)
-  std::vector<uint32_t> colmap(M);
-  for (uint32_t e = 0; e < M; ++e) colmap[e] = e;
   P.n_orep = (int)olist.size();
   P.n_erep = (int)elist.size();
   P.c32 = cluster_bits_for(m, 4);
   P.c64 = cluster_bits_for(m, 8);
+  const int ct = std::max(P.c32, P.c64);
+  if (ct > 2) fail(TM_ERR_LIMIT, "even/odd tile split over more than 4 CTAs");
+  std::vector<uint32_t> ecls(M), ocls(M);
+  for (uint32_t x = 0; x < M; ++x) {
+    ecls[x] = etile[erep_of[x]];
+    ocls[x] = otile[orep[x]];
+  }
+  // pass 1 walks e in iteration order and stores w1 class-major; pass 2
+  // walks o in iteration order, and the designated outputs of a pass-2 tile
+  // follow the same order (so a CTA's outputs are contiguous)
+  const std::vector<uint32_t> e_it = pattern_order(ecls, m, ct, false);
+  const std::vector<uint32_t> e_cf = pattern_order(ecls, m, ct, true);
+  const std::vector<uint32_t> o_it = pattern_order(ocls, m, ct, false);
+  std::vector<uint16_t> h_it_e(M), h_cf_e(M), h_it_o(M), h_pos_o(M);
+  std::vector<uint32_t> t2(M), h_wbase(M), cls_start(P.n_erep, M), cls_size(P.n_erep, 0);
+  std::vector<uint8_t> h_wsz(M);
+  for (uint32_t i = 0; i < M; ++i) {
+    h_cf_e[e_cf[i]] = (uint16_t)i;
+    h_pos_o[o_it[i]] = (uint16_t)i;
+  }
+  for (uint32_t x = 0; x < M; ++x) {
+    cls_start[ecls[x]] = std::min<uint32_t>(cls_start[ecls[x]], h_cf_e[x]);
+    cls_size[ecls[x]] += 1;
+  }
+  // w1 is class-major: element (t, e) of e-class C at
+  // start(C) * n_orep + t * |C| + (cf(e) - start(C))
+  for (uint32_t i = 0; i < M; ++i) {
+    const uint32_t e = e_it[i], C = ecls[e];
+    h_it_e[i] = (uint16_t)e;
+    h_wbase[i] = cls_start[C] * (uint32_t)P.n_orep + (h_cf_e[e] - cls_start[C]);
+    h_wsz[i] = (uint8_t)cls_size[C];
+    const uint32_t o = o_it[i];
+    h_it_o[i] = (uint16_t)o;
+    t2[i] = (otile[orep[o]] << 8) | (uint32_t)og[o];
+  }
 
   cudaStream_t s = op.stream;
-  DBuf d_olist, d_etile;
+  DBuf d_olist, d_etile, d_pos_o;
   d_olist.alloc(olist.size() * 4);
   d_etile.alloc(M * 4);
+  d_pos_o.alloc(M * 2);
   P.t2.alloc(M * 4);
+  P.it_e.alloc(M * 2);
+  P.wbase.alloc(M * 4);
+  P.wsz.alloc(M);
+  P.cls_start.alloc(cls_start.size() * 4);
+  P.cls_size.alloc(cls_size.size() * 4);
+  P.cf_e.alloc(M * 2);
+  P.it_o.alloc(M * 2);
   P.erep.alloc(elist.size() * 4);
-  P.colmap.alloc(M * 4);
-  TM_CK(cudaMemcpyAsync(P.colmap.p, colmap.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_olist.p, olist.data(), olist.size() * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_etile.p, etile.data(), M * 4, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(d_pos_o.p, h_pos_o.data(), M * 2, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.t2.p, t2.data(), M * 4, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.it_e.p, h_it_e.data(), M * 2, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.wbase.p, h_wbase.data(), M * 4, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.wsz.p, h_wsz.data(), M, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.cls_start.p, cls_start.data(), cls_start.size() * 4, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.cls_size.p, cls_size.data(), cls_size.size() * 4, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.cf_e.p, h_cf_e.data(), M * 2, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(P.it_o.p, h_it_o.data(), M * 2, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.erep.p, elist.data(), elist.size() * 4, cudaMemcpyHostToDevice, s));
 
   PlanDev pd;
@@ -469,7 +656,7 @@ void build_eo_plan(Op& op) {
   dpre.alloc(nwords * 4);
   TM_CK(cudaMemsetAsync(dbits.p, 0, nwords * 4, s));
   eo_key_kernel<<<grid_for(R), 256, 0, s>>>(pd, op.idx.as<uint32_t>(), R, d_etile.as<uint32_t>(),
-                                            key.as<uint32_t>(), dbits.as<uint32_t>());
+                                            d_pos_o.as<uint16_t>(), key.as<uint32_t>(), dbits.as<uint32_t>());
   TM_CKK("eo_key");
   popc_kernel<<<grid_for(nwords), 256, 0, s>>>(dbits.as<uint32_t>(), dpre.as<uint32_t>(), nwords);
   TM_CKK("popc");
@@ -477,27 +664,24 @@ void build_eo_plan(Op& op) {
   op.pi.alloc(R * 4);
   op.pinv.alloc(R * 4);
   P.out_o.alloc(R * 2);
-  eo_perm_kernel<<<grid_for(R), 256, 0, s>>>(key.as<uint32_t>(), R, dbits.as<uint32_t>(),
-                                             dpre.as<uint32_t>(), m, op.pi.as<uint32_t>(),
+  eo_perm_kernel<<<grid_for(R), 256, 0, s>>>(key.as<uint32_t>(), R, dbits.as<uint32_t>(), dpre.as<uint32_t>(), m,
+                                             P.it_o.as<uint16_t>(), op.pi.as<uint32_t>(),
                                              op.pinv.as<uint32_t>(), P.out_o.as<uint16_t>());
   TM_CKK("eo_perm");
-  // per-part output offsets for both cluster splits
-  auto offsets = [&](int c, DBuf& dst) {
-    int nparts = P.n_erep << c;
-    int part_bits = m - c;
-    int part_words = (1 << part_bits) / 32;
-    dst.alloc((size_t)(nparts + 1) * 4);
-    eo_offsets_kernel<<<(nparts + 1 + 255) / 256, 256, 0, s>>>(dpre.as<uint32_t>(), dbits.as<uint32_t>(),
-                                                               nwords, nparts, part_words, dst.as<uint32_t>());
-    TM_CKK("eo_offsets");
-  };
-  offsets(P.c64, P.out_off);
-  offsets(P.c32, P.out_off32);
+  // designated-output offsets per group of 2^(m-ct) iteration positions
+  // of each pass-2 tile
+  P.ct = ct;
+  const int ngroups = P.n_erep << ct;
+  P.out_off.alloc((size_t)(ngroups + 1) * 4);
+  eo_offsets_kernel<<<(ngroups + 1 + 255) / 256, 256, 0, s>>>(dpre.as<uint32_t>(), dbits.as<uint32_t>(), nwords,
+                                                              ngroups, (int)((M >> ct) / 32),
+                                                              P.out_off.as<uint32_t>());
+  TM_CKK("eo_offsets");
   // map1
   const int64_t n1 = (int64_t)P.n_orep << m;
   P.map1.alloc(n1 * 4);
-  eo_map1_kernel<<<grid_for(n1), 256, 0, s>>>(pd, d_olist.as<uint32_t>(), P.n_orep, op.pinv.as<uint32_t>(),
-                                              P.map1.as<uint32_t>());
+  eo_map1_kernel<<<grid_for(n1), 256, 0, s>>>(pd, d_olist.as<uint32_t>(), P.n_orep, P.it_e.as<uint16_t>(),
+                                              op.pinv.as<uint32_t>(), P.map1.as<uint32_t>());
   TM_CKK("eo_map1");
   // scales in pi order
   op.sin64.alloc(R * 8);
@@ -516,17 +700,25 @@ void build_eo_plan(Op& op) {
 // ------------------------------------------------------------------ launch
 namespace {
 
+// u = x * sin * gin.  gin = (1 + r)^-L keeps the magnitudes of the
+// unnormalised butterflies x0 + r x1 those of the normalised operator.
 template <class T>
 __global__ void eo_scale_in(const T* __restrict__ x, const double* __restrict__ s64,
-                            const float* __restrict__ s32, T* __restrict__ u, int64_t n) {
+                            const float* __restrict__ s32, T* __restrict__ u, int64_t n, double gin) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t st = (int64_t)gridDim.x * blockDim.x;
+  const float gin32 = (float)gin;
   for (; i < n; i += st) {
     if (sizeof(T) == 8)
-      u[i] = (T)((double)x[i] * s64[i]);
+      u[i] = (T)((double)x[i] * s64[i] * gin);
     else
-      u[i] = x[i] * (T)s32[i];
+      u[i] = x[i] * ((T)s32[i] * gin32);
   }
+}
+
+// input factor of the unnormalised butterflies: (1 + r)^-L, r = e^-2|K|
+double eo_gin(const Op& op) {
+  return std::pow(1.0 + std::exp(-2.0 * std::fabs(op.mp.betaJ)), -(double)op.L);
 }
 
 // element types around each engine: FP32 and FP64 read and write their own
@@ -543,8 +735,8 @@ struct EoIO<dfloat> {
 };
 
 template <class T, int KB>
-void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, const uint32_t* map1,
-                  const uint32_t* colmap, T* w1, cudaStream_t s) {
+void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, const EOPlan& P, T* w1,
+                  cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
   auto kfn = eo_pass1<T, KB, typename EoIO<T>::In>;
   raise_smem_limit((const void*)kfn, shm);
@@ -560,13 +752,13 @@ void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, co
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, map1, colmap, w1));
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(), P.wbase.as<uint32_t>(),
+                           P.wsz.as<uint8_t>(), w1));
 }
 
 template <class T, int KB, bool F64S>
-void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, const uint32_t* off,
-                  const double* sout64, const float* sout32, double post, typename EoIO<T>::Out* y,
-                  cudaStream_t s) {
+void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, const double* sout64,
+                  const float* sout32, double post, typename EoIO<T>::Out* y, cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
   auto kfn = eo_pass2<T, KB, F64S, typename EoIO<T>::Out>;
   raise_smem_limit((const void*)kfn, shm);
@@ -582,8 +774,9 @@ void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, con
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.t2.as<uint32_t>(), P.erep.as<uint32_t>(),
-                           P.colmap.as<uint32_t>(), off, P.out_o.as<uint16_t>(), sout64, sout32, post, y));
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.it_o.as<uint16_t>(), P.t2.as<uint32_t>(), P.cf_e.as<uint16_t>(),
+                           P.erep.as<uint32_t>(), P.cls_start.as<uint32_t>(), P.cls_size.as<uint32_t>(),
+                           P.out_off.as<uint32_t>(), P.out_o.as<uint16_t>(), sout64, sout32, post, y));
 }
 
 template <class T>
@@ -591,6 +784,7 @@ EOArgs make_args(const Op& op, int c) {
   EOArgs A;
   A.m = op.eo.m;
   A.c = c;
+  A.ct = op.eo.ct;
   A.n = A.m - c;
   const int KB = (sizeof(T) == 8) ? 4 : 5;
   int kb = std::min(KB, std::max(1, A.n - 5));
@@ -599,11 +793,9 @@ EOArgs make_args(const Op& op, int c) {
   A.ng = op.eo.ng;
   A.n_orep = op.eo.n_orep;
   const double K = op.mp.betaJ;
-  double ea = std::exp(K), eb = std::exp(-K);
-  A.a64 = ea / (ea + eb);
-  A.b64 = eb / (ea + eb);
-  A.a32 = (float)A.a64;
-  A.b32 = (float)A.b64;
+  A.r64 = std::exp(-2.0 * std::fabs(K));
+  A.r32 = (float)A.r64;
+  A.swap = K < 0 ? 1 : 0;
   return A;
 }
 
@@ -616,18 +808,18 @@ void eo_dispatch(const Op& op, const EOArgs& A, const typename EoIO<T>::In* x, t
   In* u = static_cast<In*>(op.ws_c.p);
   T* w1 = (sizeof(T) == 8) ? static_cast<T*>(P.w1_64.p) : static_cast<T*>(P.w1_32.p);
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[0], s));
-  eo_scale_in<In><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R);
+  eo_scale_in<In><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R,
+                                               eo_gin(op));
   TM_CKK("eo_scale_in");
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[1], s));
-  launch_pass1<T, KB>(A, P.n_orep, u, P.map1.as<uint32_t>(), P.colmap.as<uint32_t>(), w1, s);
+  launch_pass1<T, KB>(A, P.n_orep, u, P, w1, s);
   TM_CKK("eo_pass1");
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[2], s));
-  const uint32_t* off = (sizeof(T) == 8) ? P.out_off.as<uint32_t>() : P.out_off32.as<uint32_t>();
   const double S = std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);
   if (scaled32)
-    launch_pass2<T, KB, false>(A, P.n_erep, w1, P, off, op.sout64.as<double>(), op.sout32.as<float>(), 1.0, y, s);
+    launch_pass2<T, KB, false>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), 1.0, y, s);
   else
-    launch_pass2<T, KB, true>(A, P.n_erep, w1, P, off, op.sout64.as<double>(), op.sout32.as<float>(), S, y, s);
+    launch_pass2<T, KB, true>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), S, y, s);
   TM_CKK("eo_pass2");
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[3], s));
 }
@@ -677,16 +869,17 @@ void matvec_eo_f64_into(const Op& op, const double* x, double* y, double* u, dou
   const int64_t R = op.n;
   EOArgs A = make_args<double>(op, P.c64);
   if (A.n - A.p > 4) fail(TM_ERR_LIMIT, "even/odd tile too large for the FP64 engine");
-  eo_scale_in<double><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R);
+  eo_scale_in<double><<<grid_for(R), 256, 0, s>>>(x, op.sin64.as<double>(), op.sin32.as<float>(), u, R,
+                                                   eo_gin(op));
   TM_CKK("eo_scale_in");
   const double S = std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);
   switch (A.n - A.p) {
 #define TM_EO_INTO(KBV)                                                                                      \
   case KBV:                                                                                                  \
-    launch_pass1<double, KBV>(A, P.n_orep, u, P.map1.as<uint32_t>(), P.colmap.as<uint32_t>(), w1, s);       \
+    launch_pass1<double, KBV>(A, P.n_orep, u, P, w1, s);                                                     \
     TM_CKK("eo_pass1");                                                                                      \
-    launch_pass2<double, KBV, true>(A, P.n_erep, w1, P, P.out_off.as<uint32_t>(), op.sout64.as<double>(),    \
-                                    op.sout32.as<float>(), S, y, s);                                        \
+    launch_pass2<double, KBV, true>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), S, y, \
+                                    s);                                                                      \
     TM_CKK("eo_pass2");                                                                                      \
     break;
     TM_EO_INTO(1)

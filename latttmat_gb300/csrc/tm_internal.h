@@ -91,16 +91,20 @@ struct EOPlan {
   bool active = false;
   int m = 0;          // bits per pass (L/2)
   int c32 = 0, c64 = 0;  // cluster bits for the FP32 / FP64 passes
+  int ct = 0;         // top bits grouping the iteration orders: max(c32, c64)
   int n_orep = 0;     // pass-1 tiles
   int n_erep = 0;     // pass-2 tiles
   int ng = 0;         // H elements enumerated
-  DBuf map1;          // u32 [n_orep][2^m]: pi-index of the orbit of (e, o_rep)
-  DBuf t2;            // u32 [2^m]: (o-tile << 8) | g  mapping o -> its pass-1 tile
+  DBuf map1;          // u32 [n_orep][2^m]: pi-index of the orbit of (it_e[P], o_rep)
+  DBuf it_e;          // u16 [2^m]: e at each pass-1 iteration position P
+  DBuf wbase, wsz;    // u32 / u8 [2^m]: w1 offset of (tile 0, it_e[P]) and the size of its e-class
+  DBuf cls_start, cls_size;  // u32 [n_erep]: class-first start and size of each e-class
+  DBuf cf_e;          // u16 [2^m]: class-first position of each e
+  DBuf it_o;          // u16 [2^m]: o at each pass-2 iteration position
+  DBuf t2;            // u32 [2^m]: (o-tile << 8) | g for it_o[P]: its pass-1 tile and H element
   DBuf erep;          // u32 [n_erep]: e representative of each pass-2 tile
-  DBuf colmap;        // u32 [2^m]: column of even pattern e in w1 (H-classes of e contiguous)
-  DBuf out_off;       // u32 [n_erep*(2^c)+1]: designated-output offsets per tile part
+  DBuf out_off;       // u32 [n_erep*2^ct+1]: designated-output offsets per tile and top-ct-bit group
   DBuf out_o;         // u16 [R]: o of each designated output (pi order)
-  DBuf out_off32;     // offsets for the FP32 cluster split
   DBuf w1_32, w1_64;  // pass-1 intermediates
   cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // stage timing (diagnostics)
   bool prof_on = false;
