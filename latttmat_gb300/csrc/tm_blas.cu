@@ -651,18 +651,591 @@ __global__ void nrm_f32_kernel(const float* __restrict__ w, int64_t n, double* _
   block_reduce_store<1>(acc, 1, part);
 }
 
+// ------------------------------------------------------- 16-byte vector forms
+// Used when every column starts on a 16-byte boundary (ldv a multiple of 4
+// floats / 2 doubles).  Each thread moves float4 / double2 per column, with
+// U of them per column in flight for narrow bases; the n % 4 (n % 2) tail
+// elements go to block 0.  Widths NVT are matched to the basis so the
+// accumulators and loads in flight fit the registers.
+__device__ __forceinline__ float dot4(const float4& a, const float4& b, float c) {
+  c = fmaf(a.x, b.x, c);
+  c = fmaf(a.y, b.y, c);
+  c = fmaf(a.z, b.z, c);
+  return fmaf(a.w, b.w, c);
+}
+__device__ __forceinline__ void sub4(float4& x, const float4& v, float h) {
+  x.x = fmaf(-v.x, h, x.x);
+  x.y = fmaf(-v.y, h, x.y);
+  x.z = fmaf(-v.z, h, x.z);
+  x.w = fmaf(-v.w, h, x.w);
+}
+__device__ __forceinline__ const float4* col4(const float* V, int64_t ldv, int k) {
+  return reinterpret_cast<const float4*>(V + (int64_t)k * ldv);
+}
+
+template <int NVT, int U>
+__global__ void __launch_bounds__(BT) mdot_f32v_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                       const float* __restrict__ w, int64_t n,
+                                                       double* __restrict__ part) {
+  float acc[NVT];
+#pragma unroll
+  for (int k = 0; k < NVT; ++k) acc[k] = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  for (; i + (U - 1) * st < n4; i += U * st) {
+    float4 wv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) wv[u] = w4[i + u * st];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        const float4* vk = col4(V, ldv, k);
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc[k] = dot4(vk[i + u * st], wv[u], acc[k]);
+      }
+  }
+  for (; i < n4; i += st) {
+    const float4 wv = w4[i];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) acc[k] = dot4(col4(V, ldv, k)[i], wv, acc[k]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) acc[k] = fmaf(V[(int64_t)k * ldv + t], w[t], acc[k]);
+  }
+  block_reduce_store<NVT>(acc, nv, part);
+}
+
+// wout = win - V h ; part <- V . wout  (the V values stay in registers)
+template <int NVT>
+__global__ void __launch_bounds__(BT) axpy_dot_f32v_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                           const double* __restrict__ h,
+                                                           const float* __restrict__ win, float* __restrict__ wout,
+                                                           int64_t n, double* __restrict__ part) {
+  __shared__ float hs[NVT];
+  if (threadIdx.x < NVT) hs[threadIdx.x] = (threadIdx.x < nv) ? (float)h[threadIdx.x] : 0.f;
+  __syncthreads();
+  float acc[NVT];
+#pragma unroll
+  for (int k = 0; k < NVT; ++k) acc[k] = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    float4 v[NVT];
+    float4 x = reinterpret_cast<const float4*>(win)[i];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        v[k] = col4(V, ldv, k)[i];
+        sub4(x, v[k], hs[k]);
+      }
+    reinterpret_cast<float4*>(wout)[i] = x;
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) acc[k] = dot4(v[k], x, acc[k]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+    float x = win[t];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) x = fmaf(-V[(int64_t)k * ldv + t], hs[k], x);
+    wout[t] = x;
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) acc[k] = fmaf(V[(int64_t)k * ldv + t], x, acc[k]);
+  }
+  block_reduce_store<NVT>(acc, nv, part);
+}
+
+// w -= V h in place; with NRM, part <- ||w||^2
+template <int NVT, int U, bool NRM>
+__global__ void __launch_bounds__(BT) axpy_f32v_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                       const double* __restrict__ h, float* __restrict__ w,
+                                                       int64_t n, double* __restrict__ part) {
+  __shared__ float hs[NVT];
+  if (threadIdx.x < NVT) hs[threadIdx.x] = (threadIdx.x < nv) ? (float)h[threadIdx.x] : 0.f;
+  __syncthreads();
+  float acc[1] = {0.f};
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  float4* w4 = reinterpret_cast<float4*>(w);
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  for (; i + (U - 1) * st < n4; i += U * st) {
+    float4 x[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) x[u] = w4[i + u * st];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        const float4* vk = col4(V, ldv, k);
+#pragma unroll
+        for (int u = 0; u < U; ++u) sub4(x[u], vk[i + u * st], hs[k]);
+      }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      w4[i + u * st] = x[u];
+      if (NRM) acc[0] = dot4(x[u], x[u], acc[0]);
+    }
+  }
+  for (; i < n4; i += st) {
+    float4 x = w4[i];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) sub4(x, col4(V, ldv, k)[i], hs[k]);
+    w4[i] = x;
+    if (NRM) acc[0] = dot4(x, x, acc[0]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+    float x = w[t];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) x = fmaf(-V[(int64_t)k * ldv + t], hs[k], x);
+    w[t] = x;
+    if (NRM) acc[0] = fmaf(x, x, acc[0]);
+  }
+  if (NRM) block_reduce_store<1>(acc, 1, part);
+}
+
+// part[b][k*NW + j] = partial sums of V[k] . W[j]
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT) mdot_block_f32v_kernel(const float* __restrict__ V, int64_t ldv, int kv,
+                                                             F32Cols W, int nw, int64_t n,
+                                                             double* __restrict__ part) {
+  float acc[KV][NW];
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) acc[k][j] = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    float4 wv[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) wv[j] = (j < nw) ? reinterpret_cast<const float4*>(W.c[j])[i] : make_float4(0, 0, 0, 0);
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const float4 v = col4(V, ldv, k)[i];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) acc[k][j] = dot4(v, wv[j], acc[k][j]);
+      }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const float v = V[(int64_t)k * ldv + t];
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+          if (j < nw) acc[k][j] = fmaf(v, W.c[j][t], acc[k][j]);
+      }
+  }
+  __shared__ double sh[BT / 32][KV * NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      double v = warp_sum((double)acc[k][j]);
+      if (lane == 0) sh[wid][k * NW + j] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    double a = 0.0;
+    for (int q = 0; q < BT / 32; ++q) a += sh[q][t];
+    part[(int64_t)blockIdx.x * (KV * NW) + t] = a;
+  }
+}
+
+// W[j] -= sum_k V[k] H[k0 + k, j]
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT) maxpy_block_f32v_kernel(const float* __restrict__ V, int64_t ldv, int kv,
+                                                              const double* __restrict__ H, int64_t ldh, int k0,
+                                                              F32ColsMut W, int nw, int64_t n) {
+  __shared__ float hs[KV][NW];
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    const int k = t / NW, j = t % NW;
+    hs[k][j] = (k < kv && j < nw) ? (float)H[(k0 + k) + (int64_t)j * ldh] : 0.f;
+  }
+  __syncthreads();
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    float4 v[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) v[k] = (k < kv) ? col4(V, ldv, k)[i] : make_float4(0, 0, 0, 0);
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+      if (j < nw) {
+        float4* wj = reinterpret_cast<float4*>(W.c[j]);
+        float4 x = wj[i];
+#pragma unroll
+        for (int k = 0; k < KV; ++k) sub4(x, v[k], hs[k][j]);
+        wj[i] = x;
+      }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+    for (int j = 0; j < nw; ++j) {
+      float x = W.c[j][t];
+      for (int k = 0; k < kv; ++k) x = fmaf(-V[(int64_t)k * ldv + t], hs[k][j], x);
+      W.c[j][t] = x;
+    }
+  }
+}
+
+__global__ void normalize_f32v_kernel(const float* __restrict__ w, const double* __restrict__ nsq,
+                                      float* __restrict__ v, int64_t n) {
+  const float inv = (float)(1.0 / sqrt(*nsq));
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    float4 x = reinterpret_cast<const float4*>(w)[i];
+    x.x *= inv;
+    x.y *= inv;
+    x.z *= inv;
+    x.w *= inv;
+    reinterpret_cast<float4*>(v)[i] = x;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+    v[t] = w[t] * inv;
+  }
+}
+
+__global__ void nrm_f32v_kernel(const float* __restrict__ w, int64_t n, double* __restrict__ part) {
+  float acc[1] = {0.f};
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    const float4 x = reinterpret_cast<const float4*>(w)[i];
+    acc[0] = dot4(x, x, acc[0]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const float x = w[(n4 << 2) + threadIdx.x];
+    acc[0] = fmaf(x, x, acc[0]);
+  }
+  block_reduce_store<1>(acc, 1, part);
+}
+
+// out[:, c] = V[:, 0..m) Y[:, c] for c < k (in place when out == V: every
+// row is read before any is written), m <= MM; FP32 or FP64 output
+template <int MM, class OutT>
+__global__ void __launch_bounds__(BT) combine_f32v_kernel(const float* V, int64_t ldv, int m,
+                                                          const double* __restrict__ Y, int k, OutT* out,
+                                                          int64_t ldo, int64_t n) {
+  using AccT = OutT;
+  __shared__ AccT Ys[MM * MM];
+  for (int t = threadIdx.x; t < m * k; t += BT) Ys[t] = (AccT)Y[t];
+  __syncthreads();
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    float4 row[MM];
+#pragma unroll
+    for (int j = 0; j < MM; ++j) row[j] = (j < m) ? col4(V, ldv, j)[i] : make_float4(0, 0, 0, 0);
+    for (int c = 0; c < k; ++c) {
+      AccT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+      for (int j = 0; j < MM; ++j)
+        if (j < m) {
+          const AccT y = Ys[c * m + j];
+          a0 = fma((AccT)row[j].x, y, a0);
+          a1 = fma((AccT)row[j].y, y, a1);
+          a2 = fma((AccT)row[j].z, y, a2);
+          a3 = fma((AccT)row[j].w, y, a3);
+        }
+      OutT* o = out + (int64_t)c * ldo + (i << 2);
+      if (sizeof(OutT) == 4) {
+        *reinterpret_cast<float4*>(o) = make_float4((float)a0, (float)a1, (float)a2, (float)a3);
+      } else {
+        reinterpret_cast<double2*>(o)[0] = make_double2((double)a0, (double)a1);
+        reinterpret_cast<double2*>(o)[1] = make_double2((double)a2, (double)a3);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+    AccT row[MM];
+    for (int j = 0; j < m; ++j) row[j] = (AccT)V[(int64_t)j * ldv + t];
+    for (int c = 0; c < k; ++c) {
+      AccT a = 0;
+      for (int j = 0; j < m; ++j) a = fma(row[j], Ys[c * m + j], a);
+      out[(int64_t)c * ldo + t] = (OutT)a;
+    }
+  }
+}
+
+// ---- FP64 columns, double2 loads
+__device__ __forceinline__ const double2* col2(const double* V, int64_t ldv, int k) {
+  return reinterpret_cast<const double2*>(V + (int64_t)k * ldv);
+}
+
+// part <- V . w  (w FP64, or scale * w32 with W32)
+template <int NVT, int U, bool W32>
+__global__ void __launch_bounds__(BT) mdot_v2_kernel(const double* __restrict__ V, int64_t ldv, int nv,
+                                                     const double* __restrict__ w, const float* __restrict__ w32,
+                                                     double scale, int64_t n, double* __restrict__ part) {
+  double acc[NVT];
+#pragma unroll
+  for (int k = 0; k < NVT; ++k) acc[k] = 0.0;
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  auto wload = [&](int64_t i) -> double2 {
+    if (W32) {
+      const float2 f = reinterpret_cast<const float2*>(w32)[i];
+      return make_double2(scale * (double)f.x, scale * (double)f.y);
+    }
+    return reinterpret_cast<const double2*>(w)[i];
+  };
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  for (; i + (U - 1) * st < n2; i += U * st) {
+    double2 wv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) wv[u] = wload(i + u * st);
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        const double2* vk = col2(V, ldv, k);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const double2 v = vk[i + u * st];
+          acc[k] = fma(v.x, wv[u].x, acc[k]);
+          acc[k] = fma(v.y, wv[u].y, acc[k]);
+        }
+      }
+  }
+  for (; i < n2; i += st) {
+    const double2 wv = wload(i);
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        const double2 v = col2(V, ldv, k)[i];
+        acc[k] = fma(v.x, wv.x, acc[k]);
+        acc[k] = fma(v.y, wv.y, acc[k]);
+      }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
+    const int64_t t = n - 1;
+    const double wt = W32 ? scale * (double)w32[t] : w[t];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) acc[k] = fma(V[(int64_t)k * ldv + t], wt, acc[k]);
+  }
+  __shared__ double sh[BT / 32][NVT];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NVT; ++k) {
+    const double v = warp_sum(acc[k]);
+    if (lane == 0) sh[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NVT) {
+    double t = 0.0;
+    for (int q = 0; q < BT / 32; ++q) t += sh[q][threadIdx.x];
+    part[(int64_t)blockIdx.x * NVT + threadIdx.x] = t;
+  }
+}
+
+// w = (W32 ? scale * w32 : w) - V h
+template <int NVT, int U, bool W32>
+__global__ void __launch_bounds__(BT) maxpy_v2_kernel(const double* __restrict__ V, int64_t ldv, int nv,
+                                                      const double* __restrict__ h, const float* __restrict__ w32,
+                                                      double scale, double* __restrict__ w, int64_t n) {
+  __shared__ double hs[NVT];
+  if (threadIdx.x < NVT) hs[threadIdx.x] = (threadIdx.x < nv) ? h[threadIdx.x] : 0.0;
+  __syncthreads();
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  double2* w2 = reinterpret_cast<double2*>(w);
+  int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x;
+  for (; i + (U - 1) * st < n2; i += U * st) {
+    double2 x[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (W32) {
+        const float2 f = reinterpret_cast<const float2*>(w32)[i + u * st];
+        x[u] = make_double2(scale * (double)f.x, scale * (double)f.y);
+      } else {
+        x[u] = w2[i + u * st];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        const double2* vk = col2(V, ldv, k);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const double2 v = vk[i + u * st];
+          x[u].x = fma(-v.x, hs[k], x[u].x);
+          x[u].y = fma(-v.y, hs[k], x[u].y);
+        }
+      }
+#pragma unroll
+    for (int u = 0; u < U; ++u) w2[i + u * st] = x[u];
+  }
+  for (; i < n2; i += st) {
+    double2 x;
+    if (W32) {
+      const float2 f = reinterpret_cast<const float2*>(w32)[i];
+      x = make_double2(scale * (double)f.x, scale * (double)f.y);
+    } else {
+      x = w2[i];
+    }
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) {
+        const double2 v = col2(V, ldv, k)[i];
+        x.x = fma(-v.x, hs[k], x.x);
+        x.y = fma(-v.y, hs[k], x.y);
+      }
+    w2[i] = x;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
+    const int64_t t = n - 1;
+    double x = W32 ? scale * (double)w32[t] : w[t];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) x = fma(-V[(int64_t)k * ldv + t], hs[k], x);
+    w[t] = x;
+  }
+}
+
+// part[b][k*NW + j] = partial sums of V[k] . W[j], V FP64, W FP32 (exact in FP64)
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT) mdot64_block_v2_kernel(const double* __restrict__ V, int64_t ldv, int kv,
+                                                             F32Cols W, int nw, int64_t n,
+                                                             double* __restrict__ part) {
+  double acc[KV][NW];
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) acc[k][j] = 0.0;
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n2; i += st) {
+    double2 wv[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      if (j < nw) {
+        const float2 f = reinterpret_cast<const float2*>(W.c[j])[i];
+        wv[j] = make_double2((double)f.x, (double)f.y);
+      } else {
+        wv[j] = make_double2(0.0, 0.0);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const double2 v = col2(V, ldv, k)[i];
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+          if (j < nw) {
+            acc[k][j] = fma(v.x, wv[j].x, acc[k][j]);
+            acc[k][j] = fma(v.y, wv[j].y, acc[k][j]);
+          }
+      }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
+    const int64_t t = n - 1;
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv)
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+          if (j < nw) acc[k][j] = fma(V[(int64_t)k * ldv + t], (double)W.c[j][t], acc[k][j]);
+  }
+  __shared__ double sh[BT / 32][KV * NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      const double v = warp_sum(acc[k][j]);
+      if (lane == 0) sh[wid][k * NW + j] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    double a = 0.0;
+    for (int q = 0; q < BT / 32; ++q) a += sh[q][t];
+    part[(int64_t)blockIdx.x * (KV * NW) + t] = a;
+  }
+}
+
+__global__ void nrm_v2_kernel(const double* __restrict__ w, int64_t n, double* __restrict__ part) {
+  double acc = 0.0;
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n2; i += st) {
+    const double2 x = reinterpret_cast<const double2*>(w)[i];
+    acc = fma(x.x, x.x, acc);
+    acc = fma(x.y, x.y, acc);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) acc = fma(w[n - 1], w[n - 1], acc);
+  __shared__ double sh[BT / 32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < BT / 32; ++q) t += sh[q];
+    part[blockIdx.x] = t;
+  }
+}
+
+inline bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+inline bool al8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
+// every column of a float basis on a 16-byte boundary
+inline bool cols4(const float* V, int64_t ldv) { return al16(V) && (ldv & 3) == 0; }
+inline bool cols2(const double* V, int64_t ldv) { return al16(V) && (ldv & 1) == 0; }
+
 }  // namespace
 
 void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
               cudaStream_t s) {
+  const bool vec = cols4(V, ldv) && al16(w);
   for (int k0 = 0; k0 < nv; k0 += NV32) {
     const int kk = std::min(NV32, nv - k0);
-    int nb = red_blocks(n);
-    mdot_f32_kernel<<<nb, BT, 0, s>>>(V + k0 * ldv, ldv, kk, w, n, part);
+    const int nb = red_blocks(n);
+    const float* Vk = V + (int64_t)k0 * ldv;
+    int stride = NV32;
+    if (!vec) {
+      mdot_f32_kernel<<<nb, BT, 0, s>>>(Vk, ldv, kk, w, n, part);
+    } else if (kk <= 3) {
+      mdot_f32v_kernel<4, 2><<<nb, BT, 0, s>>>(Vk, ldv, kk, w, n, part);
+      stride = 4;
+    } else if (kk <= 8) {
+      mdot_f32v_kernel<8, 2><<<nb, BT, 0, s>>>(Vk, ldv, kk, w, n, part);
+      stride = 8;
+    } else if (kk <= 12) {
+      mdot_f32v_kernel<12, 1><<<nb, BT, 0, s>>>(Vk, ldv, kk, w, n, part);
+      stride = 12;
+    } else {
+      mdot_f32v_kernel<16, 1><<<nb, BT, 0, s>>>(Vk, ldv, kk, w, n, part);
+    }
     TM_CKK("mdot_f32");
-    mdot_final<<<kk, 256, 0, s>>>(part, nb, kk, NV32, h + k0);
+    mdot_final<<<kk, 256, 0, s>>>(part, nb, kk, stride, h + k0);
     TM_CKK("mdot_final");
   }
+}
+
+static bool cols_al16(const float* const* c, int nw) {
+  for (int j = 0; j < nw; ++j)
+    if (!al16(c[j])) return false;
+  return true;
+}
+static bool cols_al8(const float* const* c, int nw) {
+  for (int j = 0; j < nw; ++j)
+    if (!al8(c[j])) return false;
+  return true;
 }
 
 void mdot_block_f32(const float* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H,
@@ -670,14 +1243,22 @@ void mdot_block_f32(const float* V, int64_t ldv, int nv, const F32Cols& W, int n
   if (nw < 1 || nw > kMaxBlockW) fail(TM_ERR_LIMIT, "mdot_block_f32: 1..8 vectors");
   constexpr int KV = 8;
   const int nb = red_blocks(n);
+  const bool vec = cols4(V, ldv) && cols_al16(W.c, nw);
   for (int k0 = 0; k0 < nv; k0 += KV) {
     const int kv = std::min(KV, nv - k0);
+    const float* Vk = V + (int64_t)k0 * ldv;
     if (nw <= 4) {  // half the accumulators when the block is narrow
-      mdot_block_f32_kernel<KV, 4><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+      if (vec)
+        mdot_block_f32v_kernel<KV, 4><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
+      else
+        mdot_block_f32_kernel<KV, 4><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
       TM_CKK("mdot_block_f32");
       mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * 4, 4, H, ldh, k0);
     } else {
-      mdot_block_f32_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+      if (vec)
+        mdot_block_f32v_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
+      else
+        mdot_block_f32_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
       TM_CKK("mdot_block_f32");
       mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * kMaxBlockW, kMaxBlockW, H, ldh, k0);
     }
@@ -689,10 +1270,16 @@ void maxpy_block_f32(const float* V, int64_t ldv, int nv, const double* H, int64
                      int64_t n, cudaStream_t s) {
   if (nw < 1 || nw > kMaxBlockW) fail(TM_ERR_LIMIT, "maxpy_block_f32: 1..8 vectors");
   constexpr int KV = 8;
+  const bool vec = cols4(V, ldv) && cols_al16(W.c, nw);
   for (int k0 = 0; k0 < nv; k0 += KV) {
     const int kv = std::min(KV, nv - k0);
-    maxpy_block_f32_kernel<KV, kMaxBlockW><<<red_blocks(n), BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, H, ldh, k0,
-                                                                         W, nw, n);
+    const float* Vk = V + (int64_t)k0 * ldv;
+    if (vec && nw <= 4)
+      maxpy_block_f32v_kernel<KV, 4><<<red_blocks(n), BT, 0, s>>>(Vk, ldv, kv, H, ldh, k0, W, nw, n);
+    else if (vec)
+      maxpy_block_f32v_kernel<KV, kMaxBlockW><<<red_blocks(n), BT, 0, s>>>(Vk, ldv, kv, H, ldh, k0, W, nw, n);
+    else
+      maxpy_block_f32_kernel<KV, kMaxBlockW><<<red_blocks(n), BT, 0, s>>>(Vk, ldv, kv, H, ldh, k0, W, nw, n);
     TM_CKK("maxpy_block_f32");
   }
 }
@@ -702,9 +1289,13 @@ void mdot64_block(const double* V, int64_t ldv, int nv, const F32Cols& W, int nw
   if (nw < 1 || nw > 4) fail(TM_ERR_LIMIT, "mdot64_block: 1..4 vectors");
   constexpr int KV = 8, NW = 4;
   const int nb = red_blocks(n);
+  const bool vec = cols2(V, ldv) && cols_al8(W.c, nw);
   for (int k0 = 0; k0 < nv; k0 += KV) {
     const int kv = std::min(KV, nv - k0);
-    mdot64_block_kernel<KV, NW><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+    if (vec)
+      mdot64_block_v2_kernel<KV, NW><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
+    else
+      mdot64_block_kernel<KV, NW><<<nb, BT, 0, s>>>(V + (int64_t)k0 * ldv, ldv, kv, W, nw, n, part);
     TM_CKK("mdot64_block");
     mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * NW, NW, H, ldh, k0);
     TM_CKK("mdot_block_final");
@@ -715,9 +1306,19 @@ size_t mdot_block_part_bytes() { return red_part_bytes(8 * kMaxBlockW); }
 size_t red_part_bytes(int width) { return (size_t)num_sms() * kRedBlocksPerSM * width * sizeof(double) + 64; }
 
 void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, cudaStream_t s) {
+  const bool vec = cols4(V, ldv) && al16(w);
   for (int k0 = 0; k0 < nv; k0 += NV32) {
     const int kk = std::min(NV32, nv - k0);
-    maxpy_f32_kernel<<<red_blocks(n), BT, 0, s>>>(V + k0 * ldv, ldv, kk, h + k0, w, n);
+    const float* Vk = V + (int64_t)k0 * ldv;
+    const int nb = red_blocks(n);
+    if (!vec)
+      maxpy_f32_kernel<<<nb, BT, 0, s>>>(Vk, ldv, kk, h + k0, w, n);
+    else if (kk <= 4)
+      axpy_f32v_kernel<4, 2, false><<<nb, BT, 0, s>>>(Vk, ldv, kk, h + k0, w, n, nullptr);
+    else if (kk <= 8)
+      axpy_f32v_kernel<8, 1, false><<<nb, BT, 0, s>>>(Vk, ldv, kk, h + k0, w, n, nullptr);
+    else
+      axpy_f32v_kernel<16, 1, false><<<nb, BT, 0, s>>>(Vk, ldv, kk, h + k0, w, n, nullptr);
     TM_CKK("maxpy_f32");
   }
 }
@@ -725,30 +1326,56 @@ void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, i
 void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const float* win, float* wout, int64_t n,
                   double* h2, double* part, cudaStream_t s) {
   if (nv > NV32) fail(TM_ERR_LIMIT, "axpy_dot_f32: too many vectors");
-  int nb = red_blocks(n);
-  axpy_dot_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+  const int nb = red_blocks(n);
+  int stride = NV32;
+  if (!(cols4(V, ldv) && al16(win) && al16(wout))) {
+    axpy_dot_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+  } else if (nv <= 4) {
+    axpy_dot_f32v_kernel<4><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+    stride = 4;
+  } else if (nv <= 8) {
+    axpy_dot_f32v_kernel<8><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+    stride = 8;
+  } else if (nv <= 12) {
+    axpy_dot_f32v_kernel<12><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+    stride = 12;
+  } else {
+    axpy_dot_f32v_kernel<16><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+  }
   TM_CKK("axpy_dot_f32");
-  mdot_final<<<nv, 256, 0, s>>>(part, nb, nv, NV32, h2);
+  mdot_final<<<nv, 256, 0, s>>>(part, nb, nv, stride, h2);
   TM_CKK("mdot_final");
 }
 
 void axpy_nrm_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, int64_t n, double* nsq,
                   double* part, cudaStream_t s) {
   if (nv > NV32) fail(TM_ERR_LIMIT, "axpy_nrm_f32: too many vectors");
-  int nb = red_blocks(n);
-  axpy_nrm_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, w, n, part);
+  const int nb = red_blocks(n);
+  if (!(cols4(V, ldv) && al16(w)))
+    axpy_nrm_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, w, n, part);
+  else if (nv <= 4)
+    axpy_f32v_kernel<4, 2, true><<<nb, BT, 0, s>>>(V, ldv, nv, h, w, n, part);
+  else if (nv <= 8)
+    axpy_f32v_kernel<8, 1, true><<<nb, BT, 0, s>>>(V, ldv, nv, h, w, n, part);
+  else
+    axpy_f32v_kernel<16, 1, true><<<nb, BT, 0, s>>>(V, ldv, nv, h, w, n, part);
   TM_CKK("axpy_nrm_f32");
   mdot_final<<<1, 256, 0, s>>>(part, nb, 1, 1, nsq);
   TM_CKK("mdot_final");
 }
 
 void normalize_f32(const float* w, const double* nsq, float* v, int64_t n, cudaStream_t s) {
-  normalize_f32_kernel<<<red_blocks(n), BT, 0, s>>>(w, nsq, v, n);
+  if (al16(w) && al16(v))
+    normalize_f32v_kernel<<<red_blocks(n), BT, 0, s>>>(w, nsq, v, n);
+  else
+    normalize_f32_kernel<<<red_blocks(n), BT, 0, s>>>(w, nsq, v, n);
   TM_CKK("normalize_f32");
 }
 
 void rotate_f32(float* V, int64_t ldv, int m, const double* Y, int k, int64_t n, cudaStream_t s) {
-  if (m <= 16)
+  if (m <= 16 && cols4(V, ldv))
+    combine_f32v_kernel<16, float><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, V, ldv, n);
+  else if (m <= 16)
     rotate_f32_kernel<16><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, n);
   else if (m <= 32)
     rotate_f32_kernel<32><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, n);
@@ -759,7 +1386,9 @@ void rotate_f32(float* V, int64_t ldv, int m, const double* Y, int k, int64_t n,
 
 void combine_f32_f64(const float* V, int64_t ldv, int m, const double* Y, int k, double* out, int64_t ldo, int64_t n,
                      cudaStream_t s) {
-  if (m <= 16)
+  if (m <= 16 && cols4(V, ldv) && al16(out) && (ldo & 1) == 0)
+    combine_f32v_kernel<16, double><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  else if (m <= 16)
     combine_f32_f64_kernel<16><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
   else if (m <= 32)
     combine_f32_f64_kernel<32><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
@@ -770,7 +1399,9 @@ void combine_f32_f64(const float* V, int64_t ldv, int m, const double* Y, int k,
 
 void combine_f32(const float* V, int64_t ldv, int m, const double* Y, int k, float* out, int64_t ldo, int64_t n,
                  cudaStream_t s) {
-  if (m <= 16)
+  if (m <= 16 && cols4(V, ldv) && cols4(out, ldo))
+    combine_f32v_kernel<16, float><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
+  else if (m <= 16)
     combine_f32_f32_kernel<16><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
   else if (m <= 32)
     combine_f32_f32_kernel<32><<<red_blocks(n), BT, 0, s>>>(V, ldv, m, Y, k, out, ldo, n);
@@ -786,7 +1417,10 @@ void fill_uniform_f32(float* v, int64_t n, uint64_t seed, cudaStream_t s) {
 
 void nrm2sq_f32(const float* w, int64_t n, double* out, double* part, cudaStream_t s) {
   int nb = red_blocks(n);
-  nrm_f32_kernel<<<nb, BT, 0, s>>>(w, n, part);
+  if (al16(w))
+    nrm_f32v_kernel<<<nb, BT, 0, s>>>(w, n, part);
+  else
+    nrm_f32_kernel<<<nb, BT, 0, s>>>(w, n, part);
   TM_CKK("nrm_f32");
   mdot_final<<<1, 256, 0, s>>>(part, nb, 1, 1, out);
   TM_CKK("mdot_final");
@@ -794,15 +1428,35 @@ void nrm2sq_f32(const float* w, int64_t n, double* out, double* part, cudaStream
 
 static void mdot_impl(const double* V, int64_t ldv, int nv, const double* w, const float* w32, double scale,
                       int64_t n, double* h, double* part, cudaStream_t s) {
+  const bool vec = cols2(V, ldv) && (w32 ? al8(w32) : al16(w));
   for (int k0 = 0; k0 < nv; k0 += NVMAX) {
-    int kk = std::min(NVMAX, nv - k0);
-    int nb = red_blocks(n);
-    if (w32)
-      mdot_kernel<NVMAX, true><<<nb, BT, 0, s>>>(V + k0 * ldv, ldv, kk, nullptr, w32, scale, n, part);
-    else
-      mdot_kernel<NVMAX, false><<<nb, BT, 0, s>>>(V + k0 * ldv, ldv, kk, w, nullptr, 1.0, n, part);
+    const int kk = std::min(NVMAX, nv - k0);
+    const int nb = red_blocks(n);
+    const double* Vk = V + (int64_t)k0 * ldv;
+    int stride = NVMAX;
+    if (vec) {
+#define TM_MDOT_V(NVT, U)                                                                            \
+  do {                                                                                                \
+    if (w32)                                                                                          \
+      mdot_v2_kernel<NVT, U, true><<<nb, BT, 0, s>>>(Vk, ldv, kk, nullptr, w32, scale, n, part);      \
+    else                                                                                              \
+      mdot_v2_kernel<NVT, U, false><<<nb, BT, 0, s>>>(Vk, ldv, kk, w, nullptr, 1.0, n, part);         \
+    stride = NVT;                                                                                     \
+  } while (0)
+      if (kk <= 4)
+        TM_MDOT_V(4, 2);
+      else if (kk <= 8)
+        TM_MDOT_V(8, 1);
+      else
+        TM_MDOT_V(16, 1);
+#undef TM_MDOT_V
+    } else if (w32) {
+      mdot_kernel<NVMAX, true><<<nb, BT, 0, s>>>(Vk, ldv, kk, nullptr, w32, scale, n, part);
+    } else {
+      mdot_kernel<NVMAX, false><<<nb, BT, 0, s>>>(Vk, ldv, kk, w, nullptr, 1.0, n, part);
+    }
     TM_CKK("mdot");
-    mdot_final<<<kk, 256, 0, s>>>(part, nb, kk, NVMAX, h + k0);
+    mdot_final<<<kk, 256, 0, s>>>(part, nb, kk, stride, h + k0);
     TM_CKK("mdot_final");
   }
 }
@@ -816,25 +1470,50 @@ void mdot32(const double* V, int64_t ldv, int nv, const float* w32, double scale
   mdot_impl(V, ldv, nv, nullptr, w32, scale, n, h, part, s);
 }
 
-void maxpy(const double* V, int64_t ldv, int nv, const double* h, double* w, int64_t n, cudaStream_t s) {
-  for (int k0 = 0; k0 < nv; k0 += NVMAX) {
-    int kk = std::min(NVMAX, nv - k0);
-    maxpy_kernel<NVMAX, false><<<red_blocks(n), BT, 0, s>>>(V + k0 * ldv, ldv, kk, h + k0, nullptr, 1.0, w, n);
-    TM_CKK("maxpy");
+// w = (w32 ? scale * w32 : w) - V h over one chunk of <= NVMAX columns
+static void maxpy_chunk(const double* V, int64_t ldv, int kk, const double* h, const float* w32, double scale,
+                        double* w, int64_t n, cudaStream_t s) {
+  const int nb = red_blocks(n);
+  if (cols2(V, ldv) && al16(w) && (!w32 || al8(w32))) {
+#define TM_MAXPY_V(NVT, U)                                                                           \
+  do {                                                                                                \
+    if (w32)                                                                                          \
+      maxpy_v2_kernel<NVT, U, true><<<nb, BT, 0, s>>>(V, ldv, kk, h, w32, scale, w, n);               \
+    else                                                                                              \
+      maxpy_v2_kernel<NVT, U, false><<<nb, BT, 0, s>>>(V, ldv, kk, h, nullptr, 1.0, w, n);            \
+  } while (0)
+    if (kk <= 4)
+      TM_MAXPY_V(4, 2);
+    else if (kk <= 8)
+      TM_MAXPY_V(8, 1);
+    else
+      TM_MAXPY_V(16, 1);
+#undef TM_MAXPY_V
+  } else if (w32) {
+    maxpy_kernel<NVMAX, true><<<nb, BT, 0, s>>>(V, ldv, kk, h, w32, scale, w, n);
+  } else {
+    maxpy_kernel<NVMAX, false><<<nb, BT, 0, s>>>(V, ldv, kk, h, nullptr, 1.0, w, n);
   }
+  TM_CKK("maxpy");
+}
+
+void maxpy(const double* V, int64_t ldv, int nv, const double* h, double* w, int64_t n, cudaStream_t s) {
+  for (int k0 = 0; k0 < nv; k0 += NVMAX)
+    maxpy_chunk(V + (int64_t)k0 * ldv, ldv, std::min(NVMAX, nv - k0), h + k0, nullptr, 1.0, w, n, s);
 }
 
 void maxpy32(const double* V, int64_t ldv, int nv, const double* h, const float* w32, double scale, double* w,
              int64_t n, cudaStream_t s) {
-  int kk = std::min(NVMAX, nv);
-  maxpy_kernel<NVMAX, true><<<red_blocks(n), BT, 0, s>>>(V, ldv, kk, h, w32, scale, w, n);
-  TM_CKK("maxpy32");
+  maxpy_chunk(V, ldv, std::min(NVMAX, nv), h, w32, scale, w, n, s);
   if (nv > NVMAX) maxpy(V + NVMAX * ldv, ldv, nv - NVMAX, h + NVMAX, w, n, s);
 }
 
 void nrm2sq(const double* w, int64_t n, double* out, double* part, cudaStream_t s) {
   int nb = red_blocks(n);
-  nrm_kernel<<<nb, BT, 0, s>>>(w, n, part);
+  if (al16(w))
+    nrm_v2_kernel<<<nb, BT, 0, s>>>(w, n, part);
+  else
+    nrm_kernel<<<nb, BT, 0, s>>>(w, n, part);
   TM_CKK("nrm");
   mdot_final<<<1, 256, 0, s>>>(part, nb, 1, 1, out);
   TM_CKK("nrm_final");

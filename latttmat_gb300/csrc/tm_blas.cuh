@@ -1,5 +1,7 @@
 // Device vector kernels for the Krylov solvers: fused multi-vector dot
-// products and updates over a column-major basis V (ld = n), FP64.
+// products and updates over a column-major basis V (leading dimension ldv).
+// Each entry point runs 16-byte vector forms when every column it touches
+// starts on a 16-byte boundary, and element-wise forms otherwise.
 #pragma once
 #include "tm_internal.h"
 
@@ -34,6 +36,10 @@ void axpby(double a, const double* x, double b, const double* y, double* out, in
 void fill_uniform(double* v, int64_t n, uint64_t seed, cudaStream_t s);
 // count of non-finite entries (device counter)
 void count_nonfinite(const double* v, int64_t n, unsigned int* cnt_dev, cudaStream_t s);
+
+// Leading dimension of a Krylov basis of length-n columns: columns start on
+// 256-byte boundaries, so the 16-byte vector forms of the kernels apply.
+inline int64_t col_ld(int64_t n) { return (n + 63) & ~(int64_t)63; }
 
 // ---- FP32-basis Krylov kernels (nv <= 16): FP32 data, per-thread FP32
 // partial sums, FP64 block/global reductions.

@@ -182,7 +182,7 @@ bool gen_sym_eig_host(const double* G, const double* M, int m, double* w, double
 struct Lanczos {
   const Op& op;
   cudaStream_t s;
-  int64_t n;
+  int64_t n, ld;  // vector length, basis leading dimension
   int m;
   DBuf V, W, x32, y32, h1, h2, part, nsq, Hd, wd, Zd, Ysel;
   int matvecs = 0, matvecs64 = 0, restarts = 0;
@@ -191,9 +191,9 @@ struct Lanczos {
 
   // cols0 > 0: allocate only that many basis columns (the mixed path needs
   // the FP64 basis for the wanted vectors only); ensure_full() grows V.
-  Lanczos(const Op& o, int ncv, cudaStream_t st, int cols0 = 0) : op(o), s(st), n(o.n), m(ncv) {
+  Lanczos(const Op& o, int ncv, cudaStream_t st, int cols0 = 0) : op(o), s(st), n(o.n), ld(col_ld(o.n)), m(ncv) {
     vcols = (cols0 > 0) ? std::min(cols0, m + 1) : m + 1;
-    V.alloc((size_t)vcols * n * sizeof(double));
+    V.alloc((size_t)vcols * ld * sizeof(double));
     W.alloc((size_t)n * sizeof(double));
     h1.alloc(64 * 8);
     h2.alloc(64 * 8);
@@ -204,13 +204,13 @@ struct Lanczos {
     Zd.alloc(64 * 64 * 8);
     Ysel.alloc(64 * 64 * 8);
   }
-  double* v(int j) const { return V.as<double>() + (int64_t)j * n; }
+  double* v(int j) const { return V.as<double>() + (int64_t)j * ld; }
 
   void ensure_full() {
     if (vcols >= m + 1) return;
     DBuf nv;
-    nv.alloc((size_t)(m + 1) * n * sizeof(double));
-    TM_CK(cudaMemcpyAsync(nv.p, V.p, (size_t)vcols * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    nv.alloc((size_t)(m + 1) * ld * sizeof(double));
+    TM_CK(cudaMemcpyAsync(nv.p, V.p, (size_t)vcols * ld * sizeof(double), cudaMemcpyDeviceToDevice, s));
     std::swap(V.p, nv.p);
     std::swap(V.bytes, nv.bytes);
     std::swap(V.st, nv.st);
@@ -231,17 +231,17 @@ struct Lanczos {
       ensure32();
       to_f32(v(j), x32.as<float>(), n, s);
       double S = apply_internal(op, nullptr, nullptr, x32.as<float>(), y32.as<float>(), true, s);
-      mdot32(v(0), n, j + 1, y32.as<float>(), S, n, h1.as<double>(), part.as<double>(), s);
-      maxpy32(v(0), n, j + 1, h1.as<double>(), y32.as<float>(), S, w, n, s);
+      mdot32(v(0), ld, j + 1, y32.as<float>(), S, n, h1.as<double>(), part.as<double>(), s);
+      maxpy32(v(0), ld, j + 1, h1.as<double>(), y32.as<float>(), S, w, n, s);
     } else {
       apply_internal(op, v(j), w, nullptr, nullptr, false, s);
       ++matvecs64;
-      mdot(v(0), n, j + 1, w, n, h1.as<double>(), part.as<double>(), s);
-      maxpy(v(0), n, j + 1, h1.as<double>(), w, n, s);
+      mdot(v(0), ld, j + 1, w, n, h1.as<double>(), part.as<double>(), s);
+      maxpy(v(0), ld, j + 1, h1.as<double>(), w, n, s);
     }
     ++matvecs;
-    mdot(v(0), n, j + 1, w, n, h2.as<double>(), part.as<double>(), s);
-    maxpy(v(0), n, j + 1, h2.as<double>(), w, n, s);
+    mdot(v(0), ld, j + 1, w, n, h2.as<double>(), part.as<double>(), s);
+    maxpy(v(0), ld, j + 1, h2.as<double>(), w, n, s);
     nrm2sq(w, n, nsq.as<double>(), part.as<double>(), s);
     hcol_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m + 1, j, h1.as<double>(), h2.as<double>(), nsq.as<double>(),
                                  1);
@@ -283,7 +283,7 @@ struct Lanczos {
     for (int c = 0; c < k; ++c)
       for (int j = 0; j < m; ++j) Y[(size_t)c * m + j] = r.Z[(size_t)r.order[c] * m + j];
     TM_CK(cudaMemcpyAsync(Ysel.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
-    basis_rotate(V.as<double>(), n, m, Ysel.as<double>(), k, n, s);
+    basis_rotate(V.as<double>(), ld, m, Ysel.as<double>(), k, n, s);
   }
 
   // restart with k kept Ritz vectors; v(k) <- v(m)
@@ -376,14 +376,14 @@ __global__ void hcol32_kernel(double* H, int ld, int j, const double* h1, const 
 struct Lanczos32 {
   const Op& op;
   cudaStream_t s;
-  int64_t n;
+  int64_t n, ld;  // vector length, basis leading dimension
   int m;
   DBuf V, W, Y, h1, h2, part, nsq, Hd, wd, Zd, Ysel;
   int matvecs = 0, restarts = 0;
   bool stagnation_stop = true;
 
-  Lanczos32(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), m(ncv) {
-    V.alloc((size_t)(m + 1) * n * 4);
+  Lanczos32(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), ld(col_ld(o.n)), m(ncv) {
+    V.alloc((size_t)(m + 1) * ld * 4);
     W.alloc((size_t)n * 4);
     Y.alloc((size_t)n * 4);
     h1.alloc(64 * 8);
@@ -395,7 +395,7 @@ struct Lanczos32 {
     Zd.alloc(64 * 64 * 8);
     Ysel.alloc(64 * 64 * 8);
   }
-  float* v(int j) const { return V.as<float>() + (int64_t)j * n; }
+  float* v(int j) const { return V.as<float>() + (int64_t)j * ld; }
 
   void start(uint64_t seed) {
     TM_CK(cudaMemsetAsync(Hd.p, 0, (size_t)(m + 1) * (m + 1) * 8, s));
@@ -407,10 +407,10 @@ struct Lanczos32 {
   void step(int j) {
     double S = apply_internal(op, nullptr, nullptr, v(j), Y.as<float>(), true, s);
     ++matvecs;
-    mdot_f32(v(0), n, j + 1, Y.as<float>(), n, h1.as<double>(), part.as<double>(), s);
-    axpy_dot_f32(v(0), n, j + 1, h1.as<double>(), Y.as<float>(), W.as<float>(), n, h2.as<double>(),
+    mdot_f32(v(0), ld, j + 1, Y.as<float>(), n, h1.as<double>(), part.as<double>(), s);
+    axpy_dot_f32(v(0), ld, j + 1, h1.as<double>(), Y.as<float>(), W.as<float>(), n, h2.as<double>(),
                  part.as<double>(), s);
-    axpy_nrm_f32(v(0), n, j + 1, h2.as<double>(), W.as<float>(), n, nsq.as<double>(), part.as<double>(), s);
+    axpy_nrm_f32(v(0), ld, j + 1, h2.as<double>(), W.as<float>(), n, nsq.as<double>(), part.as<double>(), s);
     hcol32_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m + 1, j, h1.as<double>(), h2.as<double>(), nsq.as<double>(), S);
     TM_CKK("hcol32");
     normalize_f32(W.as<float>(), nsq.as<double>(), v(j + 1), n, s);
@@ -446,7 +446,7 @@ struct Lanczos32 {
   void restart(const Lanczos::CycleResult& r, int k) {
     std::vector<double> Yh = ysel(r, k);
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    rotate_f32(V.as<float>(), n, m, Ysel.as<double>(), k, n, s);
+    rotate_f32(V.as<float>(), ld, m, Ysel.as<double>(), k, n, s);
     TM_CK(cudaMemcpyAsync(v(k), v(m), (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0);
     for (int i = 0; i < k; ++i) {
@@ -459,20 +459,20 @@ struct Lanczos32 {
     ++restarts;
   }
 
-  // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k
-  // Ritz vectors first .. first+k-1 as FP32 columns
+  // Ritz vectors first .. first+k-1 as FP32 columns (leading dimension ld)
   void ritz_f32(const Lanczos::CycleResult& r, int first, int k, float* out) {
     std::vector<double> Yh((size_t)m * k);
     for (int c = 0; c < k; ++c)
       for (int j = 0; j < m; ++j) Yh[(size_t)c * m + j] = r.Z[(size_t)r.order[first + c] * m + j];
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    combine_f32(V.as<float>(), n, m, Ysel.as<double>(), k, out, n, n, s);
+    combine_f32(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ld, n, s);
   }
 
-  void ritz_f64(const Lanczos::CycleResult& r, int k, double* out) {
+  // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k (leading dimension ldo)
+  void ritz_f64(const Lanczos::CycleResult& r, int k, double* out, int64_t ldo) {
     std::vector<double> Yh = ysel(r, k);
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    combine_f32_f64(V.as<float>(), n, m, Ysel.as<double>(), k, out, n, n, s);
+    combine_f32_f64(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ldo, n, s);
   }
 
   template <class Conv>
@@ -523,7 +523,8 @@ constexpr int kMaxRefineNev = 8;
 //   x = X0 y_x + B32 y_b,  ax = AX0 y_x + S AB32 y_b,  r = ax - theta_c x,
 // the B32 part in FP32 arithmetic (its weights are at the FP32 noise level).
 // Writes r as FP32 into R32 (column c), optionally x into Xo (FP64), and the
-// block partial sums of ||r||^2 into part[block * NVW + c].
+// block partial sums of ||r||^2 into part[block * NVW + c].  All column
+// blocks have leading dimension ld.
 template <int NVW>
 __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restrict__ X0,
                                                          const double* __restrict__ AX0, int nx,
@@ -532,7 +533,7 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restric
                                                          const double* __restrict__ Y, int nv,
                                                          const double* __restrict__ theta, double S,
                                                          float* __restrict__ R32, double* __restrict__ Xo,
-                                                         int64_t n, double* __restrict__ part) {
+                                                         int64_t n, int64_t ld, double* __restrict__ part) {
   __shared__ double Yd[48 * NVW];
   __shared__ float Yf[48 * NVW];
   __shared__ double th[NVW];
@@ -554,7 +555,7 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restric
       xs[c] = axs[c] = 0.f;
     }
     for (int j = 0; j < nx; ++j) {
-      const double xv = X0[(int64_t)j * n + i], av = AX0[(int64_t)j * n + i];
+      const double xv = X0[(int64_t)j * ld + i], av = AX0[(int64_t)j * ld + i];
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
@@ -563,7 +564,7 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restric
         }
     }
     for (int j = nx; j < nb; ++j) {
-      const float bv = B32[(int64_t)j * n + i], abv = AB32[(int64_t)j * n + i];
+      const float bv = B32[(int64_t)j * ld + i], abv = AB32[(int64_t)j * ld + i];
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
@@ -576,8 +577,8 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restric
       if (c < nv) {
         const double xx = x[c] + (double)xs[c];
         const double r = fma(S, (double)axs[c], ax[c]) - th[c] * xx;
-        R32[(int64_t)c * n + i] = (float)r;
-        if (Xo) Xo[(int64_t)c * n + i] = xx;
+        R32[(int64_t)c * ld + i] = (float)r;
+        if (Xo) Xo[(int64_t)c * ld + i] = xx;
         acc[c] = fma(r, r, acc[c]);
       }
   }
@@ -629,23 +630,24 @@ __global__ void f64_to_f32_scaled_kernel(const double* __restrict__ in, double s
 bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::vector<double>& thv,
                   double& max_resid, const std::function<void(float*)>& fill_extras, tm_eigs_info& info) {
   cudaStream_t s = lz.s;
-  const int64_t n = lz.n;
+  const int64_t n = lz.n, ld = lz.ld;  // every column block below has leading dimension ld
   const int cap = std::min(48, nx + 5 * nev);
   const int gblocks = blocks_for(n);
   DBuf XA, B32, AB32, R32, Xo, AXo, Yd, thd, part, bpart, Hd;
   // XA = [X0 | A X0] (FP64, contiguous so one sweep gives both coupling rows)
-  XA.alloc((size_t)2 * nev * n * 8);
+  XA.alloc((size_t)2 * nev * ld * 8);
   bpart.alloc(mdot_block_part_bytes());
   Hd.alloc((size_t)48 * 2 * kMaxBlockW * 8);
-  B32.alloc((size_t)cap * n * 4);
-  AB32.alloc((size_t)cap * n * 4);
-  R32.alloc((size_t)nev * n * 4);
-  Xo.alloc((size_t)nev * n * 8);
-  AXo.alloc((size_t)nev * n * 8);
+  B32.alloc((size_t)cap * ld * 4);
+  AB32.alloc((size_t)cap * ld * 4);
+  R32.alloc((size_t)nev * ld * 4);
+  Xo.alloc((size_t)nev * ld * 8);
+  AXo.alloc((size_t)nev * ld * 8);
   Yd.alloc((size_t)48 * kMaxRefineNev * 8);
   thd.alloc(kMaxRefineNev * 8);
   part.alloc((size_t)gblocks * kMaxRefineNev * 8);
-  auto f32col = [&](const DBuf& b, int j) { return b.as<float>() + (int64_t)j * n; };
+  auto f32col = [&](const DBuf& b, int j) { return b.as<float>() + (int64_t)j * ld; };
+  auto ax0 = [&](int j) { return XA.as<double>() + (int64_t)(nev + j) * ld; };  // A X0 column j
   auto host_sync = [&]() { TM_CK(cudaStreamSynchronize(s)); };
   double S = 0.0;
   auto prod32 = [&](const float* x, float* y) {
@@ -674,7 +676,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   auto x0_rows = [&](int j0, int cnt) {
     F32Cols w{};
     for (int c = 0; c < cnt; ++c) w.c[c] = f32col(B32, j0 + c);
-    mdot64_block(XA.as<double>(), n, 2 * nev, w, cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+    mdot64_block(XA.as<double>(), ld, 2 * nev, w, cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
     std::vector<double> h((size_t)48 * cnt);
     TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
@@ -696,8 +698,8 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       w1.c[cnt + c] = f32col(B32, j0 + c);
       w2.c[c] = f32col(B32, j0 + c);
     }
-    mdot_block_f32(B32.as<float>(), n, nv, w1, 2 * cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
-    mdot_block_f32(AB32.as<float>(), n, nv, w2, cnt, n, Hd.as<double>() + 48 * 2 * cnt, 48, bpart.as<double>(), s);
+    mdot_block_f32(B32.as<float>(), ld, nv, w1, 2 * cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+    mdot_block_f32(AB32.as<float>(), ld, nv, w2, cnt, n, Hd.as<double>() + 48 * 2 * cnt, 48, bpart.as<double>(), s);
     std::vector<double> h((size_t)48 * 3 * cnt);
     TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
@@ -715,12 +717,12 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   };
   // X0 block (FP64 products and dots) and its rows against every C column
   auto set_x0 = [&](int nb) {
-    TM_CK(cudaMemcpyAsync(XA.p, lz.v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+    TM_CK(cudaMemcpyAsync(XA.p, lz.v(0), (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
     for (int j = 0; j < nev; ++j) {
       std::vector<double> h(nev), q(nev);
-      mdot(lz.v(0), n, nev, (XA.as<double>() + (int64_t)nev * n) + (int64_t)j * n, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+      mdot(lz.v(0), ld, nev, ax0(j), n, lz.h1.as<double>(), lz.part.as<double>(), s);
       TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nev * 8, cudaMemcpyDeviceToHost, s));
-      mdot(lz.v(0), n, nev, lz.v(j), n, lz.h2.as<double>(), lz.part.as<double>(), s);
+      mdot(lz.v(0), ld, nev, lz.v(j), n, lz.h2.as<double>(), lz.part.as<double>(), s);
       TM_CK(cudaMemcpyAsync(q.data(), lz.h2.p, nev * 8, cudaMemcpyDeviceToHost, s));
       host_sync();
       for (int i = 0; i < nev; ++i) {
@@ -755,7 +757,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   }
   for (int j = nev; j < nx; ++j) prod32(f32col(B32, j), f32col(AB32, j));
   if (S == 0.0) prod32(f32col(B32, 0), f32col(AB32, 0));  // only its scale is used; set_x0 overwrites it
-  for (int i = 0; i < nev; ++i) prod64(lz.v(i), (XA.as<double>() + (int64_t)nev * n) + (int64_t)i * n);
+  for (int i = 0; i < nev; ++i) prod64(lz.v(i), ax0(i));
   int nb = nx;
   set_x0(nev);
   for (int j = nev; j < nb; j += 4) add_gcols(j, std::min(4, nb - j));
@@ -788,8 +790,8 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     auto ritz_kernel = (nev <= 4) ? ritz_resid_kernel<4> : ritz_resid_kernel<kMaxRefineNev>;
     const int pstride = (nev <= 4) ? 4 : kMaxRefineNev;  // the kernel's per-block stride
     ritz_kernel<<<gblocks, 256, 0, s>>>(
-        lz.v(0), (XA.as<double>() + (int64_t)nev * n), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(), nev,
-        thd.as<double>(), S, R32.as<float>(), Xo.as<double>(), n, part.as<double>());
+        lz.v(0), ax0(0), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(), nev, thd.as<double>(), S,
+        R32.as<float>(), Xo.as<double>(), n, ld, part.as<double>());
     TM_CKK("ritz_resid");
     std::vector<double> ph((size_t)gblocks * kMaxRefineNev), rn(nev, 0.0);
     TM_CK(cudaMemcpyAsync(ph.data(), part.p, ph.size() * 8, cudaMemcpyDeviceToHost, s));
@@ -819,7 +821,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
     info.refine_est = max_resid;
     if (est_ok && certified && trust_bound) {
-      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
       info.refine_outcome = 1;
       return true;
     }
@@ -829,11 +831,11 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       bool ok_all = true;
       max_resid = 0.0;
       for (int c = 0; c < nev; ++c) {
-        double* xc = Xo.as<double>() + (int64_t)c * n;
-        double* axc = AXo.as<double>() + (int64_t)c * n;
+        double* xc = Xo.as<double>() + (int64_t)c * ld;
+        double* axc = AXo.as<double>() + (int64_t)c * ld;
         prod64(xc, axc);
         double q[2];
-        mdot(xc, n, 1, axc, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+        mdot(xc, ld, 1, axc, n, lz.h1.as<double>(), lz.part.as<double>(), s);
         nrm2sq(xc, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
         TM_CK(cudaMemcpyAsync(&q[0], lz.h1.p, 8, cudaMemcpyDeviceToHost, s));
         TM_CK(cudaMemcpyAsync(&q[1], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
@@ -852,8 +854,8 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       ++info.refine_checks;
       info.refine_true = max_resid;
       // the verified vectors become X0 either way
-      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
-      TM_CK(cudaMemcpyAsync(XA.as<double>() + (int64_t)nev * n, AXo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(ax0(0), AXo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
       if (ok_all) {
         info.refine_outcome = 2;
         return true;
@@ -861,11 +863,11 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       // re-orthonormalise X0 (its products follow linearly) and rebuild its rows
       for (int i = 0; i < nev; ++i) {
         double* xi = lz.v(i);
-        double* ai = (XA.as<double>() + (int64_t)nev * n) + (int64_t)i * n;
+        double* ai = ax0(i);
         for (int pass = 0; pass < 2 && i > 0; ++pass) {
-          mdot(lz.v(0), n, i, xi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-          maxpy(lz.v(0), n, i, lz.h1.as<double>(), xi, n, s);
-          maxpy((XA.as<double>() + (int64_t)nev * n), n, i, lz.h1.as<double>(), ai, n, s);
+          mdot(lz.v(0), ld, i, xi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+          maxpy(lz.v(0), ld, i, lz.h1.as<double>(), xi, n, s);
+          maxpy(ax0(0), ld, i, lz.h1.as<double>(), ai, n, s);
         }
         double q = 0.0;
         nrm2sq(xi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
@@ -887,7 +889,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     // that vanishes is dropped
     {
       float* wb = f32col(B32, nb);
-      TM_CK(cudaMemcpyAsync(wb, R32.p, (size_t)nev * n * 4, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(wb, R32.p, (size_t)nev * ld * 4, cudaMemcpyDeviceToDevice, s));
       std::vector<double> q0(nev, 0.0);
       for (int c = 0; c < nev; ++c) {
         nrm2sq_f32(f32col(B32, nb + c), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
@@ -900,8 +902,8 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
         wm.c[c] = f32col(B32, nb + c);
       }
       for (int pass = 0; pass < 2; ++pass) {
-        mdot_block_f32(B32.as<float>(), n, nb, wc, nev, n, Hd.as<double>(), 48, bpart.as<double>(), s);
-        maxpy_block_f32(B32.as<float>(), n, nb, Hd.as<double>(), 48, wm, nev, n, s);
+        mdot_block_f32(B32.as<float>(), ld, nb, wc, nev, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+        maxpy_block_f32(B32.as<float>(), ld, nb, Hd.as<double>(), 48, wm, nev, n, s);
       }
       host_sync();
       int pos = nb;
@@ -912,8 +914,8 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
           w = f32col(B32, pos);
         }
         for (int pass = 0; pass < 2 && pos > nb; ++pass) {
-          mdot_f32(f32col(B32, nb), n, pos - nb, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-          maxpy_f32(f32col(B32, nb), n, pos - nb, lz.h1.as<double>(), w, n, s);
+          mdot_f32(f32col(B32, nb), ld, pos - nb, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+          maxpy_f32(f32col(B32, nb), ld, pos - nb, lz.h1.as<double>(), w, n, s);
         }
         double q = 0.0;
         nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
@@ -928,7 +930,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       nb = pos;
     }
   }
-  if (have_x) TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, s));
+  if (have_x) TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
   info.refine_outcome = 3;
   return false;
 }
@@ -977,12 +979,12 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         r = l32->run(nev, 200, conv32);
         // wanted Ritz vectors in FP64, re-orthonormalised (CGS2): the FP32
         // basis is orthonormal to FP32 accuracy only
-        l32->ritz_f64(r, nev, lz.v(0));
+        l32->ritz_f64(r, nev, lz.v(0), lz.ld);
         for (int i = 0; i < nev; ++i) {
           double* bi = lz.v(i);
           for (int pass = 0; pass < 2 && i > 0; ++pass) {
-            mdot(lz.v(0), n, i, bi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-            maxpy(lz.v(0), n, i, lz.h1.as<double>(), bi, n, s);
+            mdot(lz.v(0), lz.ld, i, bi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
+            maxpy(lz.v(0), lz.ld, i, lz.h1.as<double>(), bi, n, s);
           }
           nrm2sq(bi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
           normalize(bi, lz.nsq.as<double>(), bi, nullptr, n, s);
@@ -1074,7 +1076,8 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       TM_CK(cudaMemcpyAsync(vecs_host, ref.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost, s));
       TM_CK(cudaStreamSynchronize(s));
     } else {
-      TM_CK(cudaMemcpyAsync(vecs_host, Lz->v(0), (size_t)nev * n * 8, cudaMemcpyDeviceToHost, s));
+      TM_CK(cudaMemcpy2DAsync(vecs_host, (size_t)n * 8, Lz->v(0), (size_t)Lz->ld * 8, (size_t)n * 8, nev,
+                              cudaMemcpyDeviceToHost, s));
       TM_CK(cudaStreamSynchronize(s));
     }
   }
