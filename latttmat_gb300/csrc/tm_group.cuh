@@ -160,6 +160,72 @@ TM_HD bool is_rep_x2d32(uint32_t s, int L, int flip) {
   return true;
 }
 
+#if defined(__CUDACC__)
+// ---- warp-cooperative forms for the X-2D periodic group on L <= 32 bits.
+// Lane k < L takes the images of rotation k (a = rotr(s, k), b = its
+// reflection, and their flips), so one warp covers the whole group list in
+// one step.  All 32 lanes must call these with the same s.
+
+// rotate right by k within L bits, 1 <= k <= L - 1
+__device__ __forceinline__ uint32_t rotr_l32(uint32_t x, int L, int k, uint32_t mask) {
+  return ((x >> k) | (x << (L - k))) & mask;
+}
+
+// true iff the L-bit word y has a cyclic run of ones of length >= k (1 <= k <= L)
+__device__ __forceinline__ bool has_run32(uint32_t y, int L, int k, uint32_t mask) {
+  uint32_t t = y;
+  int len = 1;
+  while (2 * len <= k && len < L) {
+    t &= rotr_l32(t, L, len, mask);
+    len *= 2;
+  }
+  if (k > len) t &= rotr_l32(t, L, k - len, mask);
+  return t != 0;
+}
+
+// Necessary condition for s to be its orbit's minimum: no cyclic run of
+// zeros longer than s's leading zeros (rotating it to the front gives a
+// smaller image), and with the spin flip no such run of ones either.
+__device__ __forceinline__ bool rep_candidate_x2d32(uint32_t s, int L, int flip) {
+  if (s == 0) return true;
+  const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
+  const int z = __clz(s) - (32 - L);  // leading zeros within L bits
+  if (z + 1 > L) return true;
+  if (has_run32(~s & mask, L, z + 1, mask)) return false;
+  if (flip && has_run32(s, L, z + 1, mask)) return false;
+  return true;
+}
+
+// s is its orbit's minimum (the whole group list, as is_rep)
+__device__ __forceinline__ bool warp_is_rep_x2d32(uint32_t s, int L, int flip) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
+  bool smaller = false;
+  if (lane < L) {
+    const uint32_t a = lane ? rotr_l32(s, L, lane, mask) : s;
+    const uint32_t b = __brev(a) >> (32 - L);
+    smaller = (a < s) || (b < s);
+    if (flip) smaller = smaller || ((~a & mask) < s) || ((~b & mask) < s);
+  }
+  return __ballot_sync(0xffffffffu, smaller) == 0;
+}
+
+// orbit size: group order / number of list elements fixing s (as orbit_size)
+__device__ __forceinline__ int warp_orbit_size_x2d32(uint32_t s, int L, int flip) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
+  unsigned fix = 0;
+  if (lane < L) {
+    const uint32_t a = lane ? rotr_l32(s, L, lane, mask) : s;
+    const uint32_t b = __brev(a) >> (32 - L);
+    fix = (a == s) + (b == s);
+    if (flip) fix += ((~a & mask) == s) + ((~b & mask) == s);
+  }
+  fix = __reduce_add_sync(0xffffffffu, fix);
+  return (int)((2u * L * (flip ? 2u : 1u)) / fix);
+}
+#endif
+
 TM_HD bool is_rep(const GroupDev& g, uint64_t s) {
   if (g.kind == G_X2D && g.periodic && g.L <= 32) return is_rep_x2d32((uint32_t)s, g.L, g.flip);
   bool rep = true;

@@ -133,6 +133,53 @@ __global__ void rep_bits_kernel(GroupDev g, uint64_t nstate, uint32_t* bits, uin
   }
 }
 
+// X-2D periodic group, L <= 32: a cheap necessary test per lane, then each
+// candidate of the word tested by the whole warp (one rotation per lane), so
+// the lanes do not wait on one another's early exits.
+__global__ void rep_bits_x2d32_kernel(int L, int flip, uint64_t nstate, uint32_t* bits, uint32_t* cnt,
+                                      int64_t nwords) {
+  const int lane = threadIdx.x & 31;
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp; w < nwords; w += nwarps) {
+    const uint64_t s = (uint64_t)w * 32 + lane;
+    uint32_t cand = __ballot_sync(0xffffffffu, s < nstate && rep_candidate_x2d32((uint32_t)s, L, flip));
+    uint32_t word = 0;
+    while (cand) {
+      const int b = __ffs(cand) - 1;
+      cand &= cand - 1;
+      if (warp_is_rep_x2d32((uint32_t)(w * 32 + b), L, flip)) word |= 1u << b;
+    }
+    if (lane == 0) {
+      bits[w] = word;
+      cnt[w] = __popc(word);
+    }
+  }
+}
+
+// compaction with warp-cooperative orbit sizes (X-2D periodic, L <= 32)
+__global__ void compact_x2d32_kernel(int L, int flip, const uint32_t* bits, const uint32_t* prefix,
+                                     int64_t nwords, uint32_t* idx, uint16_t* dup) {
+  const int lane = threadIdx.x & 31;
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp; w < nwords; w += nwarps) {
+    uint32_t word = bits[w];
+    uint32_t pos = prefix[w];
+    while (word) {
+      const int b = __ffs(word) - 1;
+      word &= word - 1;
+      const uint32_t s = (uint32_t)(w * 32 + b);
+      const int osz = warp_orbit_size_x2d32(s, L, flip);
+      if (lane == 0) {
+        idx[pos] = s;
+        dup[pos] = (uint16_t)osz;
+      }
+      ++pos;
+    }
+  }
+}
+
 __global__ void compact_kernel(GroupDev g, const uint32_t* bits, const uint32_t* prefix,
                                int64_t nwords, uint32_t* idx, uint16_t* dup) {
   const int lane = threadIdx.x & 31;
@@ -188,7 +235,11 @@ void build_orbit_table(Op& op) {
   const int threads = 256;
   int64_t want = (nwords * 32 + threads - 1) / threads;
   int blocks = (int)std::min<int64_t>(want, (int64_t)num_sms() * 64);
-  rep_bits_kernel<<<blocks, threads, 0, op.stream>>>(g, nstate, bits, pre, nwords);
+  const bool x2d32 = g.kind == G_X2D && g.periodic && g.L <= 32 && !op.grp.nbits;
+  if (x2d32)
+    rep_bits_x2d32_kernel<<<blocks, threads, 0, op.stream>>>(g.L, g.flip, nstate, bits, pre, nwords);
+  else
+    rep_bits_kernel<<<blocks, threads, 0, op.stream>>>(g, nstate, bits, pre, nwords);
   TM_CKK("rep_bits");
   uint32_t last_cnt = 0, last_bits = 0;
   TM_CK(cudaMemcpyAsync(&last_bits, bits + nwords - 1, 4, cudaMemcpyDeviceToHost, op.stream));
@@ -199,8 +250,12 @@ void build_orbit_table(Op& op) {
   op.n = R;
   op.idx.alloc(R * sizeof(uint32_t));
   op.dup.alloc(R * sizeof(uint16_t));
-  compact_kernel<<<blocks, threads, 0, op.stream>>>(g, bits, pre, nwords, op.idx.as<uint32_t>(),
-                                                    op.dup.as<uint16_t>());
+  if (x2d32)
+    compact_x2d32_kernel<<<blocks, threads, 0, op.stream>>>(g.L, g.flip, bits, pre, nwords, op.idx.as<uint32_t>(),
+                                                            op.dup.as<uint16_t>());
+  else
+    compact_kernel<<<blocks, threads, 0, op.stream>>>(g, bits, pre, nwords, op.idx.as<uint32_t>(),
+                                                      op.dup.as<uint16_t>());
   TM_CKK("compact");
   TM_CK(cudaStreamSynchronize(op.stream));
 }
@@ -218,7 +273,11 @@ void ensure_state_map(Op& op) {
   bits.alloc(nwords * 4);
   pre.alloc(nwords * 4);
   int blocks = (int)std::min<int64_t>((nwords * 32 + 255) / 256, (int64_t)num_sms() * 64);
-  rep_bits_kernel<<<blocks, 256, 0, op.stream>>>(g, nstate, bits.as<uint32_t>(), pre.as<uint32_t>(), nwords);
+  if (g.kind == G_X2D && g.periodic && g.L <= 32 && !op.grp.nbits)
+    rep_bits_x2d32_kernel<<<blocks, 256, 0, op.stream>>>(g.L, g.flip, nstate, bits.as<uint32_t>(),
+                                                        pre.as<uint32_t>(), nwords);
+  else
+    rep_bits_kernel<<<blocks, 256, 0, op.stream>>>(g, nstate, bits.as<uint32_t>(), pre.as<uint32_t>(), nwords);
   TM_CKK("rep_bits");
   exclusive_scan_u32(pre.as<uint32_t>(), pre.as<uint32_t>(), nwords, op.stream);
   op.smap.alloc(nstate * sizeof(uint32_t));

@@ -524,7 +524,7 @@ constexpr int kMaxRefineNev = 8;
 // the B32 part in FP32 arithmetic (its weights are at the FP32 noise level).
 // Writes r as FP32 into R32 (column c), optionally x into Xo (FP64), and the
 // block partial sums of ||r||^2 into part[block * NVW + c].  All column
-// blocks have leading dimension ld.
+// blocks have an even leading dimension ld and 16-byte aligned columns.
 template <int NVW>
 __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restrict__ X0,
                                                          const double* __restrict__ AX0, int nx,
@@ -543,50 +543,85 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restric
   }
   if (threadIdx.x < nv) th[threadIdx.x] = theta[threadIdx.x];
   __syncthreads();
-  double acc[NVW];
+  // ||r||^2 per thread in FP32: the estimate needs a few digits only
+  float acc[NVW];
 #pragma unroll
-  for (int c = 0; c < NVW; ++c) acc[c] = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double x[NVW], ax[NVW];
-    float xs[NVW], axs[NVW];
+  for (int c = 0; c < NVW; ++c) acc[c] = 0.f;
+  // two elements per thread and step: 16-byte FP64 and 8-byte FP32 loads
+  // (ld is even and every column 16-byte aligned); an odd n leaves one
+  // element for block 0
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += st) {
+    double2 x[NVW], ax[NVW];
+    float2 xs[NVW], axs[NVW];
 #pragma unroll
     for (int c = 0; c < NVW; ++c) {
-      x[c] = ax[c] = 0.0;
-      xs[c] = axs[c] = 0.f;
+      x[c] = ax[c] = make_double2(0.0, 0.0);
+      xs[c] = axs[c] = make_float2(0.f, 0.f);
     }
     for (int j = 0; j < nx; ++j) {
-      const double xv = X0[(int64_t)j * ld + i], av = AX0[(int64_t)j * ld + i];
+      const double2 xv = reinterpret_cast<const double2*>(X0 + (int64_t)j * ld)[i];
+      const double2 av = reinterpret_cast<const double2*>(AX0 + (int64_t)j * ld)[i];
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
-          x[c] = fma(xv, Yd[c * nb + j], x[c]);
-          ax[c] = fma(av, Yd[c * nb + j], ax[c]);
+          const double y = Yd[c * nb + j];
+          x[c].x = fma(xv.x, y, x[c].x);
+          x[c].y = fma(xv.y, y, x[c].y);
+          ax[c].x = fma(av.x, y, ax[c].x);
+          ax[c].y = fma(av.y, y, ax[c].y);
         }
     }
     for (int j = nx; j < nb; ++j) {
-      const float bv = B32[(int64_t)j * ld + i], abv = AB32[(int64_t)j * ld + i];
+      const float2 bv = reinterpret_cast<const float2*>(B32 + (int64_t)j * ld)[i];
+      const float2 abv = reinterpret_cast<const float2*>(AB32 + (int64_t)j * ld)[i];
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
-          xs[c] = fmaf(bv, Yf[c * nb + j], xs[c]);
-          axs[c] = fmaf(abv, Yf[c * nb + j], axs[c]);
+          const float y = Yf[c * nb + j];
+          xs[c].x = fmaf(bv.x, y, xs[c].x);
+          xs[c].y = fmaf(bv.y, y, xs[c].y);
+          axs[c].x = fmaf(abv.x, y, axs[c].x);
+          axs[c].y = fmaf(abv.y, y, axs[c].y);
         }
     }
 #pragma unroll
     for (int c = 0; c < NVW; ++c)
       if (c < nv) {
-        const double xx = x[c] + (double)xs[c];
-        const double r = fma(S, (double)axs[c], ax[c]) - th[c] * xx;
-        R32[(int64_t)c * ld + i] = (float)r;
-        if (Xo) Xo[(int64_t)c * ld + i] = xx;
-        acc[c] = fma(r, r, acc[c]);
+        const double x0 = x[c].x + (double)xs[c].x, x1 = x[c].y + (double)xs[c].y;
+        const float r0 = (float)(fma(S, (double)axs[c].x, ax[c].x) - th[c] * x0);
+        const float r1 = (float)(fma(S, (double)axs[c].y, ax[c].y) - th[c] * x1);
+        reinterpret_cast<float2*>(R32 + (int64_t)c * ld)[i] = make_float2(r0, r1);
+        if (Xo) reinterpret_cast<double2*>(Xo + (int64_t)c * ld)[i] = make_double2(x0, x1);
+        acc[c] = fmaf(r0, r0, fmaf(r1, r1, acc[c]));
       }
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int64_t i = n - 1;
+    for (int c = 0; c < nv; ++c) {
+      double x = 0.0, ax = 0.0;
+      float xs = 0.f, axs = 0.f;
+      for (int j = 0; j < nx; ++j) {
+        x = fma(X0[(int64_t)j * ld + i], Yd[c * nb + j], x);
+        ax = fma(AX0[(int64_t)j * ld + i], Yd[c * nb + j], ax);
+      }
+      for (int j = nx; j < nb; ++j) {
+        xs = fmaf(B32[(int64_t)j * ld + i], Yf[c * nb + j], xs);
+        axs = fmaf(AB32[(int64_t)j * ld + i], Yf[c * nb + j], axs);
+      }
+      const double xx = x + (double)xs;
+      const float r = (float)(fma(S, (double)axs, ax) - th[c] * xx);
+      R32[(int64_t)c * ld + i] = r;
+      if (Xo) Xo[(int64_t)c * ld + i] = xx;
+      acc[c] = fmaf(r, r, acc[c]);
+    }
   }
   __shared__ double sh[8][NVW];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < NVW; ++c) {
-    double v = acc[c];
+    double v = (double)acc[c];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) sh[wid][c] = v;
   }
@@ -786,7 +821,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
     TM_CK(cudaMemcpyAsync(Yd.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
     TM_CK(cudaMemcpyAsync(thd.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
-    // wanted Ritz vectors (FP64) and residuals (FP32 copy, norms in FP64)
+    // wanted Ritz vectors (FP64) and residuals (FP32 copy and norms)
     auto ritz_kernel = (nev <= 4) ? ritz_resid_kernel<4> : ritz_resid_kernel<kMaxRefineNev>;
     const int pstride = (nev <= 4) ? 4 : kMaxRefineNev;  // the kernel's per-block stride
     ritz_kernel<<<gblocks, 256, 0, s>>>(
