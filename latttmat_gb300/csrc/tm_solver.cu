@@ -404,8 +404,10 @@ struct Lanczos32 {
     normalize_f32(W.as<float>(), nsq.as<double>(), v(0), n, s);
   }
 
+  double S = 0.0;  // scale of the FP32 products: y = T v / S
+
   void step(int j) {
-    double S = apply_internal(op, nullptr, nullptr, v(j), Y.as<float>(), true, s);
+    S = apply_internal(op, nullptr, nullptr, v(j), Y.as<float>(), true, s);
     ++matvecs;
     mdot_f32(v(0), ld, j + 1, Y.as<float>(), n, h1.as<double>(), part.as<double>(), s);
     axpy_dot_f32(v(0), ld, j + 1, h1.as<double>(), Y.as<float>(), W.as<float>(), n, h2.as<double>(),
@@ -466,6 +468,23 @@ struct Lanczos32 {
       for (int j = 0; j < m; ++j) Yh[(size_t)c * m + j] = r.Z[(size_t)r.order[first + c] * m + j];
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
     combine_f32(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ld, n, s);
+  }
+
+  // Products of Ritz vectors first .. first+k-1 from the Lanczos relation
+  // A V_m = V_m H + beta v_m e_m^T: A x = theta x + beta (e_m^T y) v_m, so
+  // A x / S = V_{m+1} [theta y; beta y_m] / S with no product of the
+  // operator (FP32 columns, leading dimension ld).
+  void ritz_f32_prod(const Lanczos::CycleResult& r, int first, int k, float* out) {
+    const int m1 = m + 1;
+    std::vector<double> Yh((size_t)m1 * k);
+    for (int c = 0; c < k; ++c) {
+      const int col = r.order[first + c];
+      const double th = r.theta[first + c];
+      for (int j = 0; j < m; ++j) Yh[(size_t)c * m1 + j] = th * r.Z[(size_t)col * m + j] / S;
+      Yh[(size_t)c * m1 + m] = r.beta * r.Z[(size_t)col * m + (m - 1)] / S;
+    }
+    TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
+    combine_f32(V.as<float>(), ld, m1, Ysel.as<double>(), k, out, ld, n, s);
   }
 
   // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k (leading dimension ldo)
@@ -659,11 +678,13 @@ __global__ void f64_to_f32_scaled_kernel(const double* __restrict__ in, double s
 // verified vectors become the new X0 and the rounds go on.
 //
 // In: lz.v(0..nev-1) the wanted Ritz vectors (FP64, orthonormal); the other
-// nx - nev Ritz vectors from fill_extras (FP32 columns) or, without it, from
+// nx - nev Ritz vectors from fill_extras (FP32 columns, and their FP32
+// products A x / S when it returns the scale S > 0) or, without it, from
 // lz.v(nev..nx-1).
 // Out: lz.v(0..nev-1) the best Ritz vectors; thv, max_resid; true when accepted.
 bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::vector<double>& thv,
-                  double& max_resid, const std::function<void(float*)>& fill_extras, tm_eigs_info& info) {
+                  double& max_resid, const std::function<double(float*, float*)>& fill_extras,
+                  tm_eigs_info& info) {
   cudaStream_t s = lz.s;
   const int64_t n = lz.n, ld = lz.ld;  // every column block below has leading dimension ld
   const int cap = std::min(48, nx + 5 * nev);
@@ -782,15 +803,23 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
     TM_CKK("to_f32");
   }
+  bool extras_prod = false;
   if (fill_extras) {
-    if (nx > nev) fill_extras(f32col(B32, nev));
+    if (nx > nev) {
+      const double Se = fill_extras(f32col(B32, nev), f32col(AB32, nev));
+      if (Se > 0.0) {
+        S = Se;
+        extras_prod = true;
+      }
+    }
   } else {
     for (int j = nev; j < nx; ++j) {
       f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
       TM_CKK("to_f32");
     }
   }
-  for (int j = nev; j < nx; ++j) prod32(f32col(B32, j), f32col(AB32, j));
+  if (!extras_prod)
+    for (int j = nev; j < nx; ++j) prod32(f32col(B32, j), f32col(AB32, j));
   if (S == 0.0) prod32(f32col(B32, 0), f32col(AB32, 0));  // only its scale is used; set_x0 overwrites it
   for (int i = 0; i < nev; ++i) prod64(lz.v(i), ax0(i));
   int nb = nx;
@@ -1006,7 +1035,7 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         return true;
       };
       std::unique_ptr<Lanczos32> l32;
-      std::function<void(float*)> extras;
+      std::function<double(float*, float*)> extras;
       if (ncv <= NV32) {
         // FP32 Krylov basis (half the bytes of the FP64 basis per sweep)
         l32.reset(new Lanczos32(op, ncv, s));
@@ -1026,7 +1055,11 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         }
         // the other Ritz vectors stay FP32
         Lanczos32* lp = l32.get();
-        extras = [lp, &r, nev, nb0](float* out) { lp->ritz_f32(r, nev, nb0 - nev, out); };
+        extras = [lp, &r, nev, nb0](float* out, float* aout) {
+          lp->ritz_f32(r, nev, nb0 - nev, out);
+          lp->ritz_f32_prod(r, nev, nb0 - nev, aout);
+          return lp->S;
+        };
         lz.matvecs += l32->matvecs;
         lz.restarts += l32->restarts;
       } else {
