@@ -892,6 +892,53 @@ __global__ void __launch_bounds__(BT) maxpy_block_f32v_kernel(const float* __res
   }
 }
 
+// W[j] -= sum_{k < nv} V[k] H[k, j] in one sweep (nv <= 48): each W element
+// is loaded and stored once however many basis columns there are
+template <int NW>
+__global__ void __launch_bounds__(BT) maxpy_block_all_f32v_kernel(const float* __restrict__ V, int64_t ldv, int nv,
+                                                                  const double* __restrict__ H, int64_t ldh,
+                                                                  F32ColsMut W, int nw, int64_t n) {
+  __shared__ float hs[48][NW];
+  for (int t = threadIdx.x; t < 48 * NW; t += BT) {
+    const int k = t / NW, j = t % NW;
+    hs[k][j] = (k < nv && j < nw) ? (float)H[k + (int64_t)j * ldh] : 0.f;
+  }
+  __syncthreads();
+  const int64_t n4 = n >> 2;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
+    float4 x[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) x[j] = (j < nw) ? reinterpret_cast<const float4*>(W.c[j])[i] : make_float4(0, 0, 0, 0);
+    int k = 0;
+    for (; k + 4 <= nv; k += 4) {
+      float4 v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = col4(V, ldv, k + q)[i];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < NW; ++j) sub4(x[j], v[q], hs[k + q][j]);
+    }
+    for (; k < nv; ++k) {
+      const float4 v = col4(V, ldv, k)[i];
+#pragma unroll
+      for (int j = 0; j < NW; ++j) sub4(x[j], v, hs[k][j]);
+    }
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+      if (j < nw) reinterpret_cast<float4*>(W.c[j])[i] = x[j];
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = (n4 << 2) + threadIdx.x;
+    for (int j = 0; j < nw; ++j) {
+      float x = W.c[j][t];
+      for (int k = 0; k < nv; ++k) x = fmaf(-V[(int64_t)k * ldv + t], hs[k][j], x);
+      W.c[j][t] = x;
+    }
+  }
+}
+
 __global__ void normalize_f32v_kernel(const float* __restrict__ w, const double* __restrict__ nsq,
                                       float* __restrict__ v, int64_t n) {
   const float inv = (float)(1.0 / sqrt(*nsq));
@@ -1271,6 +1318,14 @@ void maxpy_block_f32(const float* V, int64_t ldv, int nv, const double* H, int64
   if (nw < 1 || nw > kMaxBlockW) fail(TM_ERR_LIMIT, "maxpy_block_f32: 1..8 vectors");
   constexpr int KV = 8;
   const bool vec = cols4(V, ldv) && cols_al16(W.c, nw);
+  if (vec && nv <= 48) {
+    if (nw <= 4)
+      maxpy_block_all_f32v_kernel<4><<<red_blocks(n), BT, 0, s>>>(V, ldv, nv, H, ldh, W, nw, n);
+    else
+      maxpy_block_all_f32v_kernel<kMaxBlockW><<<red_blocks(n), BT, 0, s>>>(V, ldv, nv, H, ldh, W, nw, n);
+    TM_CKK("maxpy_block_f32");
+    return;
+  }
   for (int k0 = 0; k0 < nv; k0 += KV) {
     const int kv = std::min(KV, nv - k0);
     const float* Vk = V + (int64_t)k0 * ldv;

@@ -965,9 +965,22 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
         wc.c[c] = f32col(B32, nb + c);
         wm.c[c] = f32col(B32, nb + c);
       }
+      // second pass only when the first removed a large part of a column
+      // ("twice is enough": a norm ratio below 1/sqrt(2))
       for (int pass = 0; pass < 2; ++pass) {
         mdot_block_f32(B32.as<float>(), ld, nb, wc, nev, n, Hd.as<double>(), 48, bpart.as<double>(), s);
         maxpy_block_f32(B32.as<float>(), ld, nb, Hd.as<double>(), 48, wm, nev, n, s);
+        if (pass == 1) break;
+        std::vector<double> q1(nev, 0.0);
+        for (int c = 0; c < nev; ++c) {
+          nrm2sq_f32(f32col(B32, nb + c), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+          TM_CK(cudaMemcpyAsync(&q1[c], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        }
+        host_sync();
+        bool again = false;
+        for (int c = 0; c < nev; ++c)
+          if (!(q1[c] >= 0.5 * q0[c])) again = true;
+        if (!again) break;
       }
       host_sync();
       int pos = nb;
