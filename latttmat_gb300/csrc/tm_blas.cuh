@@ -3,6 +3,7 @@
 // Each entry point runs 16-byte vector forms when every column it touches
 // starts on a 16-byte boundary, and element-wise forms otherwise.
 #pragma once
+#include "tm_df.cuh"
 #include "tm_internal.h"
 
 namespace ltm {
@@ -94,6 +95,32 @@ void combine_f32(const float* V, int64_t ldv, int m, const double* Y, int k, flo
 void fill_uniform_f32(float* v, int64_t n, uint64_t seed, cudaStream_t s);
 // ||w||^2 of an FP32 vector (FP64 result on device)
 void nrm2sq_f32(const float* w, int64_t n, double* out, double* part, cudaStream_t s);
+
+// ---- double-float vectors ((hi, lo) FP32 pairs, 8 bytes per element;
+// columns 16-byte aligned, leading dimension even).  Dot products return
+// FP64; part needs dd_part_bytes(8).
+size_t dd_part_bytes(int width);
+// h[k] = V[k] . w, k < nv <= 8
+void mdot_dd(const dfloat* V, int64_t ldv, int nv, const dfloat* w, int64_t n, double* h, double* part,
+             cudaStream_t s);
+// w -= V h  (nv <= 8, h FP64 on the device)
+void maxpy_dd(const dfloat* V, int64_t ldv, int nv, const double* h, dfloat* w, int64_t n, cudaStream_t s);
+// *out = ||w||^2
+void nrm2sq_dd(const dfloat* w, int64_t n, double* out, double* part, cudaStream_t s);
+// out = a x + b y  (b = 0: y unused; out may alias x)
+void axpby_dd(double a, const dfloat* x, double b, const dfloat* y, dfloat* out, int64_t n, cudaStream_t s);
+// w /= sqrt(*nsq)
+void normalize_dd(dfloat* w, const double* nsq, int64_t n, cudaStream_t s);
+// out[:, c] = V32[:, 0..m) Y[:, c], c < k <= 8, in double-float (Y FP64 on the device)
+void combine_f32_dd(const float* V, int64_t ldv, int m, const double* Y, int k, dfloat* out, int64_t ldo, int64_t n,
+                    cudaStream_t s);
+// H[k + j*ldh] = V[k] . W[j]: V double-float columns, up to 4 FP32 vectors W
+void mdot_dd_block(const dfloat* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H, int64_t ldh,
+                   double* part, cudaStream_t s);
+// conversions: out = fl32(x); out = x * scale (FP64); out = x * scale (double-float)
+void df_to_f32(const dfloat* x, float* out, int64_t n, cudaStream_t s);
+void df_to_f64(const dfloat* x, double scale, double* out, int64_t n, cudaStream_t s);
+void f64_to_df(const double* x, double scale, dfloat* out, int64_t n, cudaStream_t s);
 
 // small dense symmetric eigenproblem on device (one warp, cyclic Jacobi, m <= 48):
 // A (m x m column-major, symmetric) -> eigenvalues w[m], eigenvectors Z (m x m, column-major)

@@ -150,6 +150,27 @@ void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s) {
   }
 }
 
+void matvec_eo_dd(const Op& op, const dfloat* x, dfloat* y, cudaStream_t s);
+
+// y = A x / S in double-float storage, FP64-accurate: the even/odd engine
+// reads and writes double-float directly (its output scale is S); other
+// operators go through FP64 storage around apply_refine.
+void apply_refine_dd(const Op& op, const dfloat* x, dfloat* y, double S, cudaStream_t s) {
+  const Op& base = op.parent ? *op.parent : op;
+  if (base.eo.active && S == eo_scale32(base)) {
+    matvec_eo_dd(base, x, y, s);
+    const_cast<Op&>(op).matvecs++;
+    return;
+  }
+  const int64_t n = base.n;
+  DBuf x64, y64;
+  x64.alloc((size_t)n * 8);
+  y64.alloc((size_t)n * 8);
+  df_to_f64(x, 1.0, x64.as<double>(), n, s);
+  apply_refine(op, x64.as<double>(), y64.as<double>(), s);
+  f64_to_df(y64.as<double>(), 1.0 / S, y, n, s);
+}
+
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s) {
   const Op& base = op.parent ? *op.parent : op;

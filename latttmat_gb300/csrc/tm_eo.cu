@@ -319,12 +319,16 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   }
 }
 
+// Output modes of pass 2: y = val * sout32 (FP32), val * sout64 * post
+// (FP64), or val * soutdf in double-float (double-float storage).
+enum { kOutF32 = 0, kOutF64 = 1, kOutDF = 2 };
+
 // pass 2: z[(e_rep, o)] = (Th_O w)[(e_rep, o)]; emit designated outputs.
 // The w value at (e_rep, o) is the pass-1 value at the H-image
 // (act_e(g, e_rep), o_rep) with act_o(g, o) = o_rep.  CTA `rank` owns the o
 // with top c bits = rank (iteration positions of it_o as in pass 1).
 // (OutT: element type of y)
-template <class T, int KB, bool F64SCALE, class OutT>
+template <class T, int KB, int OSC, class OutT>
 __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restrict__ w1,
                                                     const uint16_t* __restrict__ it_o,
                                                     const uint32_t* __restrict__ t2,
@@ -335,7 +339,8 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
                                                     const uint32_t* __restrict__ out_off,
                                                     const uint16_t* __restrict__ out_o,
                                                     const double* __restrict__ sout64,
-                                                    const float* __restrict__ sout32, double post,
+                                                    const float* __restrict__ sout32,
+                                                    const dfloat* __restrict__ soutdf, double post,
                                                     OutT* __restrict__ y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
@@ -392,7 +397,9 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
       const uint32_t k = kk + q * blockDim.x;
       if (k < k1) {
         const T val = sm[spad(ov[q] & lmask)];
-        if (F64SCALE)
+        if constexpr (OSC == kOutDF)
+          y[k] = val * soutdf[k];
+        else if constexpr (OSC == kOutF64)
           y[k] = (OutT)((double)val * sout64[k] * post);
         else
           y[k] = (OutT)(val * T(sout32[k]));
@@ -476,8 +483,8 @@ __global__ void eo_map1_kernel(PlanDev P, const uint32_t* __restrict__ olist, in
 }
 
 __global__ void eo_scale_kernel(const uint32_t* __restrict__ pi, const double* __restrict__ tv,
-                                const uint16_t* __restrict__ dup, int64_t R, double* sin64, double* sout64,
-                                float* sin32, float* sout32) {
+                                const uint16_t* __restrict__ dup, int64_t R, double gin, double* sin64,
+                                double* sout64, float* sin32, float* sout32, dfloat* sindf, dfloat* soutdf) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < R; i += st) {
@@ -488,6 +495,8 @@ __global__ void eo_scale_kernel(const uint32_t* __restrict__ pi, const double* _
     sout64[i] = so;
     sin32[i] = (float)t;
     sout32[i] = (float)so;
+    sindf[i] = dfloat(t * gin);
+    soutdf[i] = dfloat(so);
   }
 }
 
@@ -688,9 +697,15 @@ void build_eo_plan(Op& op) {
   op.sout64.alloc(R * 8);
   op.sin32.alloc(R * 4);
   op.sout32.alloc(R * 4);
+  op.sindf.alloc(R * 8);
+  op.soutdf.alloc(R * 8);
+  // double-float input scale with the (1 + r)^-L factor of the
+  // unnormalised butterflies folded in
+  const double gin = std::pow(1.0 + std::exp(-2.0 * std::fabs(op.mp.betaJ)), -(double)op.L);
   eo_scale_kernel<<<grid_for(R), 256, 0, s>>>(op.pi.as<uint32_t>(), op.tvec.as<double>(), op.dup.as<uint16_t>(),
-                                              R, op.sin64.as<double>(), op.sout64.as<double>(),
-                                              op.sin32.as<float>(), op.sout32.as<float>());
+                                              R, gin, op.sin64.as<double>(), op.sout64.as<double>(),
+                                              op.sin32.as<float>(), op.sout32.as<float>(), op.sindf.as<dfloat>(),
+                                              op.soutdf.as<dfloat>());
   TM_CKK("eo_scale");
   TM_CK(cudaStreamSynchronize(s));
   op.has_pi = true;
@@ -756,11 +771,11 @@ void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, co
                            P.wsz.as<uint8_t>(), w1));
 }
 
-template <class T, int KB, bool F64S>
+template <class T, int KB, int OSC, class OutT = typename EoIO<T>::Out>
 void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, const double* sout64,
-                  const float* sout32, double post, typename EoIO<T>::Out* y, cudaStream_t s) {
+                  const float* sout32, const dfloat* soutdf, double post, OutT* y, cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
-  auto kfn = eo_pass2<T, KB, F64S, typename EoIO<T>::Out>;
+  auto kfn = eo_pass2<T, KB, OSC, OutT>;
   raise_smem_limit((const void*)kfn, shm);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
@@ -776,7 +791,7 @@ void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, con
   cfg.numAttrs = 1;
   TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.it_o.as<uint16_t>(), P.t2.as<uint32_t>(), P.cf_e.as<uint16_t>(),
                            P.erep.as<uint32_t>(), P.cls_start.as<uint32_t>(), P.cls_size.as<uint32_t>(),
-                           P.out_off.as<uint32_t>(), P.out_o.as<uint16_t>(), sout64, sout32, post, y));
+                           P.out_off.as<uint32_t>(), P.out_o.as<uint16_t>(), sout64, sout32, soutdf, post, y));
 }
 
 template <class T>
@@ -817,9 +832,11 @@ void eo_dispatch(const Op& op, const EOArgs& A, const typename EoIO<T>::In* x, t
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[2], s));
   const double S = std::pow(std::exp(op.mp.betaJ) + std::exp(-op.mp.betaJ), (double)op.L);
   if (scaled32)
-    launch_pass2<T, KB, false>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), 1.0, y, s);
+    launch_pass2<T, KB, kOutF32>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), nullptr, 1.0,
+                                 y, s);
   else
-    launch_pass2<T, KB, true>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), S, y, s);
+    launch_pass2<T, KB, kOutF64>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), nullptr, S, y,
+                                 s);
   TM_CKK("eo_pass2");
   if (P.prof_on) TM_CK(cudaEventRecord(P.prof_ev[3], s));
 }
@@ -861,6 +878,58 @@ void matvec_eo_df(const Op& op, const double* x, double* y, cudaStream_t s) {
   matvec_eo_engine<dfloat>(op, x, y, false, s);
 }
 
+namespace {
+__global__ void eo_scale_in_dd(const dfloat* __restrict__ x, const dfloat* __restrict__ sdf, dfloat* __restrict__ u,
+                               int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    u[i] = x[i] * sdf[i];
+}
+
+template <int KB>
+void eo_dispatch_dd(const Op& op, const EOArgs& A, const dfloat* x, dfloat* y, cudaStream_t s) {
+  const EOPlan& P = op.eo;
+  const int64_t R = op.n;
+  dfloat* u = static_cast<dfloat*>(op.ws_c.p);
+  dfloat* w1 = static_cast<dfloat*>(P.w1_64.p);
+  eo_scale_in_dd<<<grid_for(R), 256, 0, s>>>(x, op.sindf.as<dfloat>(), u, R);
+  TM_CKK("eo_scale_in_dd");
+  const size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(dfloat);
+  auto k1 = eo_pass1<dfloat, KB, dfloat>;
+  raise_smem_limit((const void*)k1, shm);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(P.n_orep << A.c));
+  cfg.blockDim = dim3(1u << A.p);
+  cfg.dynamicSmemBytes = shm;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 1u << A.c;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  TM_CK(cudaLaunchKernelEx(&cfg, k1, A, (const dfloat*)u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(),
+                           P.wbase.as<uint32_t>(), P.wsz.as<uint8_t>(), w1));
+  TM_CKK("eo_pass1_dd");
+  launch_pass2<dfloat, KB, kOutDF, dfloat>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(),
+                                           op.soutdf.as<dfloat>(), 1.0, y, s);
+  TM_CKK("eo_pass2_dd");
+}
+}  // namespace
+
+// Double-float in/out: y = T x / S with S = eo_scale32 (the FP32 products'
+// scale), so values stay in the FP32 exponent range.
+void matvec_eo_dd(const Op& op, const dfloat* x, dfloat* y, cudaStream_t s) {
+  EOArgs A = make_args<dfloat>(op, op.eo.c64);
+  switch (A.n - A.p) {
+    case 1: eo_dispatch_dd<1>(op, A, x, y, s); break;
+    case 2: eo_dispatch_dd<2>(op, A, x, y, s); break;
+    case 3: eo_dispatch_dd<3>(op, A, x, y, s); break;
+    case 4: eo_dispatch_dd<4>(op, A, x, y, s); break;
+    default: fail(TM_ERR_LIMIT, "even/odd tile too large for the 8-byte engines");
+  }
+}
+
 // FP64 even/odd product in pi order with caller-provided scratch: u (R
 // doubles) and w1 (n_orep * 2^m doubles).  Used by the entry point whose
 // scratch lives in a fixed device array.
@@ -878,8 +947,8 @@ void matvec_eo_f64_into(const Op& op, const double* x, double* y, double* u, dou
   case KBV:                                                                                                  \
     launch_pass1<double, KBV>(A, P.n_orep, u, P, w1, s);                                                     \
     TM_CKK("eo_pass1");                                                                                      \
-    launch_pass2<double, KBV, true>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(), S, y, \
-                                    s);                                                                      \
+    launch_pass2<double, KBV, kOutF64>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(),   \
+                                       nullptr, S, y, s);                                                    \
     TM_CKK("eo_pass2");                                                                                      \
     break;
     TM_EO_INTO(1)

@@ -144,6 +144,7 @@ struct Op {
   DBuf pi, pinv;   // u32 [n]
   DBuf sin64, sout64;  // f64 [n] input/output scales in pi order
   DBuf sin32, sout32;  // f32 copies
+  DBuf sindf, soutdf;  // double-float [n]: input scale times (1 + r)^-L, output scale
   EOPlan eo;
 
   // workspace

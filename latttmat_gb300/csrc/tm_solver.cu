@@ -34,6 +34,9 @@ namespace ltm {
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s);
 void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s);
+// y = A x / S in double-float storage with FP64-accurate arithmetic (S: the
+// FP32 products' scale)
+void apply_refine_dd(const Op& op, const dfloat* x, dfloat* y, double S, cudaStream_t s);
 
 namespace {
 
@@ -487,6 +490,13 @@ struct Lanczos32 {
     combine_f32(V.as<float>(), ld, m1, Ysel.as<double>(), k, out, ld, n, s);
   }
 
+  // double-float Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k <= 8
+  void ritz_dd(const Lanczos::CycleResult& r, int k, dfloat* out, int64_t ldo) {
+    std::vector<double> Yh = ysel(r, k);
+    TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
+    combine_f32_dd(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ldo, n, s);
+  }
+
   // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k (leading dimension ldo)
   void ritz_f64(const Lanczos::CycleResult& r, int k, double* out, int64_t ldo) {
     std::vector<double> Yh = ysel(r, k);
@@ -536,60 +546,64 @@ struct EigOut {
 // Symmetric solve.  vecs_host may be null.
 constexpr int kMaxRefineNev = 8;
 
-// Ritz pairs of the refinement subspace [X0 | B32] (X0: nx FP64 columns with
-// FP64-accurate products AX0; B32: FP32 columns nx..nb-1 with FP32 products
-// AB32 = A b / S).  For each wanted pair c < nv with coefficients Y(:, c):
-//   x = X0 y_x + B32 y_b,  ax = AX0 y_x + S AB32 y_b,  r = ax - theta_c x,
-// the B32 part in FP32 arithmetic (its weights are at the FP32 noise level).
-// Writes r as FP32 into R32 (column c), optionally x into Xo (FP64), and the
-// block partial sums of ||r||^2 into part[block * NVW + c].  All column
-// blocks have an even leading dimension ld and 16-byte aligned columns.
+// Ritz pairs of the refinement subspace [X0 | B32] (X0: nx double-float
+// columns with FP64-accurate products AX0 = A X0 / S; B32: FP32 columns
+// nx..nb-1 with FP32 products AB32 = A b / S).  For each wanted pair c < nv
+// with coefficients Y(:, c) and ts = theta_c / S:
+//   x = X0 y_x + B32 y_b,  ax/S = AX0 y_x + AB32 y_b,  r/S = ax/S - ts x,
+// the X0 part in double-float, the B32 part in FP32 (its weights are at the
+// FP32 noise level).  Writes r / S as FP32 into R32 (column c), x into Xo
+// (double-float), and the block partial sums of ||r/S||^2 (FP32 per thread)
+// into part[block * NVW + c].  All column blocks have an even leading
+// dimension ld and 16-byte aligned columns; a thread takes two elements.
 template <int NVW>
-__global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restrict__ X0,
-                                                         const double* __restrict__ AX0, int nx,
+__global__ void __launch_bounds__(256) ritz_resid_kernel(const dfloat* __restrict__ X0,
+                                                         const dfloat* __restrict__ AX0, int nx,
                                                          const float* __restrict__ B32,
                                                          const float* __restrict__ AB32, int nb,
                                                          const double* __restrict__ Y, int nv,
-                                                         const double* __restrict__ theta, double S,
-                                                         float* __restrict__ R32, double* __restrict__ Xo,
+                                                         const double* __restrict__ theta_s,
+                                                         float* __restrict__ R32, dfloat* __restrict__ Xo,
                                                          int64_t n, int64_t ld, double* __restrict__ part) {
-  __shared__ double Yd[48 * NVW];
+  __shared__ dfloat Yd[48 * NVW];
   __shared__ float Yf[48 * NVW];
-  __shared__ double th[NVW];
+  __shared__ dfloat th[NVW];
   for (int t = threadIdx.x; t < nb * nv; t += blockDim.x) {
-    Yd[t] = Y[t];
+    Yd[t] = dfloat(Y[t]);
     Yf[t] = (float)Y[t];
   }
-  if (threadIdx.x < nv) th[threadIdx.x] = theta[threadIdx.x];
+  if (threadIdx.x < nv) th[threadIdx.x] = dfloat(-theta_s[threadIdx.x]);
   __syncthreads();
-  // ||r||^2 per thread in FP32: the estimate needs a few digits only
   float acc[NVW];
 #pragma unroll
   for (int c = 0; c < NVW; ++c) acc[c] = 0.f;
-  // two elements per thread and step: 16-byte FP64 and 8-byte FP32 loads
-  // (ld is even and every column 16-byte aligned); an odd n leaves one
-  // element for block 0
+  auto ld2 = [](const dfloat* p, int64_t i, dfloat& a, dfloat& b) {
+    const float4 v = reinterpret_cast<const float4*>(p)[i];
+    a = dfloat(v.x, v.y);
+    b = dfloat(v.z, v.w);
+  };
   const int64_t n2 = n >> 1;
   const int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += st) {
-    double2 x[NVW], ax[NVW];
+    dfloat x0[NVW], x1[NVW], a0[NVW], a1[NVW];
     float2 xs[NVW], axs[NVW];
 #pragma unroll
     for (int c = 0; c < NVW; ++c) {
-      x[c] = ax[c] = make_double2(0.0, 0.0);
+      x0[c] = x1[c] = a0[c] = a1[c] = dfloat(0.f, 0.f);
       xs[c] = axs[c] = make_float2(0.f, 0.f);
     }
     for (int j = 0; j < nx; ++j) {
-      const double2 xv = reinterpret_cast<const double2*>(X0 + (int64_t)j * ld)[i];
-      const double2 av = reinterpret_cast<const double2*>(AX0 + (int64_t)j * ld)[i];
+      dfloat xa, xb, aa, ab;
+      ld2(X0 + (int64_t)j * ld, i, xa, xb);
+      ld2(AX0 + (int64_t)j * ld, i, aa, ab);
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
-          const double y = Yd[c * nb + j];
-          x[c].x = fma(xv.x, y, x[c].x);
-          x[c].y = fma(xv.y, y, x[c].y);
-          ax[c].x = fma(av.x, y, ax[c].x);
-          ax[c].y = fma(av.y, y, ax[c].y);
+          const dfloat y = Yd[c * nb + j];
+          x0[c] = df_fma(xa, y, x0[c]);
+          x1[c] = df_fma(xb, y, x1[c]);
+          a0[c] = df_fma(aa, y, a0[c]);
+          a1[c] = df_fma(ab, y, a1[c]);
         }
     }
     for (int j = nx; j < nb; ++j) {
@@ -608,32 +622,34 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const double* __restric
 #pragma unroll
     for (int c = 0; c < NVW; ++c)
       if (c < nv) {
-        const double x0 = x[c].x + (double)xs[c].x, x1 = x[c].y + (double)xs[c].y;
-        const float r0 = (float)(fma(S, (double)axs[c].x, ax[c].x) - th[c] * x0);
-        const float r1 = (float)(fma(S, (double)axs[c].y, ax[c].y) - th[c] * x1);
-        reinterpret_cast<float2*>(R32 + (int64_t)c * ld)[i] = make_float2(r0, r1);
-        if (Xo) reinterpret_cast<double2*>(Xo + (int64_t)c * ld)[i] = make_double2(x0, x1);
-        acc[c] = fmaf(r0, r0, fmaf(r1, r1, acc[c]));
+        const dfloat xx0 = x0[c] + dfloat(xs[c].x, 0.f), xx1 = x1[c] + dfloat(xs[c].y, 0.f);
+        const dfloat r0 = df_fma(th[c], xx0, a0[c] + dfloat(axs[c].x, 0.f));
+        const dfloat r1 = df_fma(th[c], xx1, a1[c] + dfloat(axs[c].y, 0.f));
+        const float f0 = r0.hi + r0.lo, f1 = r1.hi + r1.lo;
+        reinterpret_cast<float2*>(R32 + (int64_t)c * ld)[i] = make_float2(f0, f1);
+        reinterpret_cast<float4*>(Xo + (int64_t)c * ld)[i] = make_float4(xx0.hi, xx0.lo, xx1.hi, xx1.lo);
+        acc[c] = fmaf(f0, f0, fmaf(f1, f1, acc[c]));
       }
   }
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
     const int64_t i = n - 1;
     for (int c = 0; c < nv; ++c) {
-      double x = 0.0, ax = 0.0;
+      dfloat x(0.f, 0.f), ax(0.f, 0.f);
       float xs = 0.f, axs = 0.f;
       for (int j = 0; j < nx; ++j) {
-        x = fma(X0[(int64_t)j * ld + i], Yd[c * nb + j], x);
-        ax = fma(AX0[(int64_t)j * ld + i], Yd[c * nb + j], ax);
+        x = df_fma(X0[(int64_t)j * ld + i], Yd[c * nb + j], x);
+        ax = df_fma(AX0[(int64_t)j * ld + i], Yd[c * nb + j], ax);
       }
       for (int j = nx; j < nb; ++j) {
         xs = fmaf(B32[(int64_t)j * ld + i], Yf[c * nb + j], xs);
         axs = fmaf(AB32[(int64_t)j * ld + i], Yf[c * nb + j], axs);
       }
-      const double xx = x + (double)xs;
-      const float r = (float)(fma(S, (double)axs, ax) - th[c] * xx);
-      R32[(int64_t)c * ld + i] = r;
-      if (Xo) Xo[(int64_t)c * ld + i] = xx;
-      acc[c] = fmaf(r, r, acc[c]);
+      const dfloat xx = x + dfloat(xs, 0.f);
+      const dfloat r = df_fma(th[c], xx, ax + dfloat(axs, 0.f));
+      const float f = r.hi + r.lo;
+      R32[(int64_t)c * ld + i] = f;
+      Xo[(int64_t)c * ld + i] = xx;
+      acc[c] = fmaf(f, f, acc[c]);
     }
   }
   __shared__ double sh[8][NVW];
@@ -662,48 +678,60 @@ __global__ void f64_to_f32_scaled_kernel(const double* __restrict__ in, double s
 // FP64-accurate refinement of the FP32 phase's Ritz pairs.
 //
 // On GB300 FP64 arithmetic runs at a small fraction of the FP32 rate, so the
-// refinement keeps FP64 where the result needs it and nowhere else.  The
-// subspace is [X0 | C]: X0 = the nev wanted Ritz vectors (FP64, with
-// FP64-accurate products), C = the other FP32 Ritz vectors and, each round,
-// the wanted residual block (FP32 storage, FP32 products, FP32 Gram-Schmidt).
-// C's weight in a wanted Ritz vector is at the FP32 noise level (~1e-7), so
-// FP32 errors in C, in A C and in the C-rows of the projected matrix reach
-// the wanted pairs only at ~1e-14 relative.  The projected matrix takes each
-// entry from the side whose product is the more accurate one (A X0 for the
-// X0 rows).  The extra Ritz vectors carry the eigenvectors next to the wanted
-// ones, which residual blocks alone resolve slowly.  When the estimated
-// residuals meet tol, the Ritz vectors get FP64-accurate products and are
-// accepted on the test of the FP64 path and of Spectra's SymEigsSolver,
-// ||A x - theta x|| <= tol |theta|, with theta the Rayleigh quotient; else the
-// verified vectors become the new X0 and the rounds go on.
+// refinement keeps FP64-level accuracy where the result needs it, in
+// double-float storage and arithmetic (FP32 pipes), and FP32 everywhere
+// else.  The subspace is [X0 | C]: X0 = the nev wanted Ritz vectors
+// (double-float, with FP64-accurate products), C = the other FP32 Ritz vectors
+// and, each round, the wanted residual block (FP32 storage, FP32 products,
+// FP32 Gram-Schmidt).  C's weight in a wanted Ritz vector is at the FP32 noise
+// level (~1e-7), so FP32 errors in C, in A C and in the C-rows of the projected
+// matrix reach the wanted pairs only at ~1e-14 relative.  The projected matrix
+// takes each entry from the side whose product is the more accurate one (A X0
+// for the X0 rows).  The extra Ritz vectors carry the eigenvectors next to
+// the wanted ones, which residual blocks alone resolve slowly.  When the
+// estimated residuals meet tol, the Ritz vectors get FP64-accurate products
+// and are accepted on the test of the FP64 path and of Spectra's
+// SymEigsSolver, ||A x - theta x|| <= tol |theta|, with theta the Rayleigh
+// quotient; else the verified vectors become the new X0 and the rounds go on.
+// All products are kept divided by S, the FP32 products' scale, so they stay
+// in the FP32 exponent range.
 //
-// In: lz.v(0..nev-1) the wanted Ritz vectors (FP64, orthonormal); the other
-// nx - nev Ritz vectors from fill_extras (FP32 columns, and their FP32
+// In: fill_x0 writes the wanted Ritz vectors (orthonormal, double-float,
+// leading dimension lz.ld) into the nev columns it is given; the other
+// nx - nev Ritz vectors come from fill_extras (FP32 columns, and their FP32
 // products A x / S when it returns the scale S > 0) or, without it, from
 // lz.v(nev..nx-1).
-// Out: lz.v(0..nev-1) the best Ritz vectors; thv, max_resid; true when accepted.
+// Out: lz.v(0..nev-1) the best Ritz vectors (FP64); thv, max_resid; true when
+// accepted.
 bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::vector<double>& thv,
-                  double& max_resid, const std::function<double(float*, float*)>& fill_extras,
-                  tm_eigs_info& info) {
+                  double& max_resid, const std::function<void(dfloat*)>& fill_x0,
+                  const std::function<double(float*, float*)>& fill_extras, tm_eigs_info& info) {
   cudaStream_t s = lz.s;
   const int64_t n = lz.n, ld = lz.ld;  // every column block below has leading dimension ld
   const int cap = std::min(48, nx + 5 * nev);
   const int gblocks = blocks_for(n);
-  DBuf XA, B32, AB32, R32, Xo, AXo, Yd, thd, part, bpart, Hd;
-  // XA = [X0 | A X0] (FP64, contiguous so one sweep gives both coupling rows)
+  DBuf XA, B32, AB32, R32, Xo, AXo, Wd, Yd, thd, part, bpart, dpart, Hd, hd;
+  // XA = [X0 | A X0 / S] (double-float, contiguous so one sweep gives both
+  // coupling rows)
   XA.alloc((size_t)2 * nev * ld * 8);
   bpart.alloc(mdot_block_part_bytes());
+  dpart.alloc(dd_part_bytes(kMaxBlockW * 4));
   Hd.alloc((size_t)48 * 2 * kMaxBlockW * 8);
+  hd.alloc(64 * 8);
   B32.alloc((size_t)cap * ld * 4);
   AB32.alloc((size_t)cap * ld * 4);
   R32.alloc((size_t)nev * ld * 4);
   Xo.alloc((size_t)nev * ld * 8);
   AXo.alloc((size_t)nev * ld * 8);
+  Wd.alloc((size_t)ld * 8);
   Yd.alloc((size_t)48 * kMaxRefineNev * 8);
   thd.alloc(kMaxRefineNev * 8);
   part.alloc((size_t)gblocks * kMaxRefineNev * 8);
   auto f32col = [&](const DBuf& b, int j) { return b.as<float>() + (int64_t)j * ld; };
-  auto ax0 = [&](int j) { return XA.as<double>() + (int64_t)(nev + j) * ld; };  // A X0 column j
+  auto x0 = [&](int j) { return XA.as<dfloat>() + (int64_t)j * ld; };          // X0 column j
+  auto ax0 = [&](int j) { return XA.as<dfloat>() + (int64_t)(nev + j) * ld; };  // A X0 / S column j
+  auto xo = [&](int c) { return Xo.as<dfloat>() + (int64_t)c * ld; };
+  auto axo = [&](int c) { return AXo.as<dfloat>() + (int64_t)c * ld; };
   auto host_sync = [&]() { TM_CK(cudaStreamSynchronize(s)); };
   double S = 0.0;
   auto prod32 = [&](const float* x, float* y) {
@@ -712,27 +740,30 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     if (S == 0.0) S = Sj;
     if (Sj != S) fail(TM_ERR_CUDA, "inconsistent FP32 product scale");
   };
-  auto prod64 = [&](const double* x, double* y) {
-    apply_refine(op, x, y, s);
+  auto proddd = [&](const dfloat* x, dfloat* y) {
+    apply_refine_dd(op, x, y, S, s);
     ++lz.matvecs;
     ++lz.matvecs64;
   };
+  // the final vectors back to the FP64 basis
+  auto to_lz = [&](const dfloat* X) {
+    for (int c = 0; c < nev; ++c) df_to_f64(X + (int64_t)c * ld, 1.0, lz.v(c), n, s);
+  };
 
   // projected matrix G = B^T A B and Gram matrix M = B^T B of B = [X0 | C].
-  // The X0 rows take FP64 dots against the exact FP32 values of C (A X0 and
-  // X0 in FP64): C is orthogonal to X0 only to FP32 accuracy (~1e-7), the
-  // size of the couplings that carry the correction, so those entries and
-  // the Gram block must be exact.  The C-C block is FP32 (second order).
+  // The X0 rows take FP64-accurate dots against the exact FP32 values of C: C
+  // is orthogonal to X0 only to FP32 accuracy (~1e-7), the size of the
+  // couplings that carry the correction, so those entries and the Gram block
+  // must be exact.  The C-C block is FP32 (second order).
   std::vector<double> G((size_t)cap * cap, 0.0), M((size_t)cap * cap, 0.0);
   auto g = [&](int i, int j) -> double& { return G[(size_t)j * cap + i]; };
   auto mm = [&](int i, int j) -> double& { return M[(size_t)j * cap + i]; };
-  // X0 rows of C columns j0 .. j0+cnt-1 (cnt <= 4; FP64 dots against the
-  // FP32 values): one sweep over XA gives X0 . c (Gram) and A X0 . c
-  // (projected matrix) for the whole block
+  // X0 rows of C columns j0 .. j0+cnt-1 (cnt <= 4): one sweep over XA gives
+  // X0 . c (Gram) and (A X0 / S) . c (projected matrix) for the whole block
   auto x0_rows = [&](int j0, int cnt) {
     F32Cols w{};
     for (int c = 0; c < cnt; ++c) w.c[c] = f32col(B32, j0 + c);
-    mdot64_block(XA.as<double>(), ld, 2 * nev, w, cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+    mdot_dd_block(XA.as<dfloat>(), ld, 2 * nev, w, cnt, n, Hd.as<double>(), 48, dpart.as<double>(), s);
     std::vector<double> h((size_t)48 * cnt);
     TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
@@ -740,7 +771,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       const int j = j0 + c;
       for (int i = 0; i < nev; ++i) {
         mm(i, j) = mm(j, i) = h[(size_t)48 * c + i];
-        g(i, j) = g(j, i) = h[(size_t)48 * c + nev + i];
+        g(i, j) = g(j, i) = S * h[(size_t)48 * c + nev + i];
       }
     }
   };
@@ -771,18 +802,19 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
     x0_rows(j0, cnt);
   };
-  // X0 block (FP64 products and dots) and its rows against every C column
+  // X0 block (FP64-accurate products and dots) and its rows against every C
+  // column
   auto set_x0 = [&](int nb) {
-    TM_CK(cudaMemcpyAsync(XA.p, lz.v(0), (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
     for (int j = 0; j < nev; ++j) {
       std::vector<double> h(nev), q(nev);
-      mdot(lz.v(0), ld, nev, ax0(j), n, lz.h1.as<double>(), lz.part.as<double>(), s);
-      TM_CK(cudaMemcpyAsync(h.data(), lz.h1.p, nev * 8, cudaMemcpyDeviceToHost, s));
-      mdot(lz.v(0), ld, nev, lz.v(j), n, lz.h2.as<double>(), lz.part.as<double>(), s);
-      TM_CK(cudaMemcpyAsync(q.data(), lz.h2.p, nev * 8, cudaMemcpyDeviceToHost, s));
+      mdot_dd(x0(0), ld, nev, ax0(j), n, hd.as<double>(), dpart.as<double>(), s);
+      TM_CK(cudaMemcpyAsync(h.data(), hd.p, nev * 8, cudaMemcpyDeviceToHost, s));
+      host_sync();
+      mdot_dd(x0(0), ld, nev, x0(j), n, hd.as<double>(), dpart.as<double>(), s);
+      TM_CK(cudaMemcpyAsync(q.data(), hd.p, nev * 8, cudaMemcpyDeviceToHost, s));
       host_sync();
       for (int i = 0; i < nev; ++i) {
-        g(i, j) = h[i];
+        g(i, j) = S * h[i];
         mm(i, j) = q[i];
       }
     }
@@ -791,18 +823,14 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
         g(i, j) = g(j, i) = 0.5 * (g(i, j) + g(j, i));
         mm(i, j) = mm(j, i) = 0.5 * (mm(i, j) + mm(j, i));
       }
-    for (int j = 0; j < nev; ++j) {  // FP32 copy of X0 for the FP32 Gram-Schmidt of C
-      f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
-      TM_CKK("to_f32");
-    }
+    for (int j = 0; j < nev; ++j)  // FP32 copy of X0 for the FP32 Gram-Schmidt of C
+      df_to_f32(x0(j), f32col(B32, j), n, s);
     for (int j = nev; j < nb; j += 4) x0_rows(j, std::min(4, nb - j));
   };
   // start: the extra Ritz vectors to FP32 with FP32 products, the wanted ones
   // with FP64-accurate products
-  for (int j = 0; j < nev; ++j) {
-    f64_to_f32_scaled_kernel<<<gblocks, 256, 0, s>>>(lz.v(j), 1.0, f32col(B32, j), n);
-    TM_CKK("to_f32");
-  }
+  fill_x0(x0(0));
+  for (int j = 0; j < nev; ++j) df_to_f32(x0(j), f32col(B32, j), n, s);
   bool extras_prod = false;
   if (fill_extras) {
     if (nx > nev) {
@@ -821,7 +849,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   if (!extras_prod)
     for (int j = nev; j < nx; ++j) prod32(f32col(B32, j), f32col(AB32, j));
   if (S == 0.0) prod32(f32col(B32, 0), f32col(AB32, 0));  // only its scale is used; set_x0 overwrites it
-  for (int i = 0; i < nev; ++i) prod64(lz.v(i), ax0(i));
+  for (int i = 0; i < nev; ++i) proddd(x0(i), ax0(i));
   int nb = nx;
   set_x0(nev);
   for (int j = nev; j < nb; j += 4) add_gcols(j, std::min(4, nb - j));
@@ -843,19 +871,20 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     std::vector<int> ord(nb);
     std::iota(ord.begin(), ord.end(), 0);
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(gw[a]) > std::fabs(gw[b]); });
-    std::vector<double> Y((size_t)nb * nev), tha(nev);
+    std::vector<double> Y((size_t)nb * nev), tha(nev), ths(nev);
     for (int c = 0; c < nev; ++c) {
       tha[c] = gw[ord[c]];
+      ths[c] = tha[c] / S;
       for (int j = 0; j < nb; ++j) Y[(size_t)c * nb + j] = gz[(size_t)ord[c] * nb + j];
     }
     TM_CK(cudaMemcpyAsync(Yd.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
-    TM_CK(cudaMemcpyAsync(thd.p, tha.data(), nev * 8, cudaMemcpyHostToDevice, s));
-    // wanted Ritz vectors (FP64) and residuals (FP32 copy and norms)
+    TM_CK(cudaMemcpyAsync(thd.p, ths.data(), nev * 8, cudaMemcpyHostToDevice, s));
+    // wanted Ritz vectors (double-float) and residuals (FP32 copy and norms)
     auto ritz_kernel = (nev <= 4) ? ritz_resid_kernel<4> : ritz_resid_kernel<kMaxRefineNev>;
     const int pstride = (nev <= 4) ? 4 : kMaxRefineNev;  // the kernel's per-block stride
-    ritz_kernel<<<gblocks, 256, 0, s>>>(
-        lz.v(0), ax0(0), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(), nev, thd.as<double>(), S,
-        R32.as<float>(), Xo.as<double>(), n, ld, part.as<double>());
+    ritz_kernel<<<gblocks, 256, 0, s>>>(x0(0), ax0(0), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(),
+                                        nev, thd.as<double>(), R32.as<float>(), Xo.as<dfloat>(), n, ld,
+                                        part.as<double>());
     TM_CKK("ritz_resid");
     std::vector<double> ph((size_t)gblocks * kMaxRefineNev), rn(nev, 0.0);
     TM_CK(cudaMemcpyAsync(ph.data(), part.p, ph.size() * 8, cudaMemcpyDeviceToHost, s));
@@ -874,7 +903,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     max_resid = 0.0;
     ++info.refine_rounds;
     for (int c = 0; c < nev; ++c) {
-      rn[c] = std::sqrt(std::max(rn[c], 0.0));
+      rn[c] = S * std::sqrt(std::max(rn[c], 0.0));
       thv[c] = tha[c];
       max_resid = std::max(max_resid, rn[c] / std::fabs(tha[c]));
       double yc2 = 0.0;
@@ -885,7 +914,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
     info.refine_est = max_resid;
     if (est_ok && certified && trust_bound) {
-      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
+      to_lz(xo(0));
       info.refine_outcome = 1;
       return true;
     }
@@ -895,22 +924,21 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       bool ok_all = true;
       max_resid = 0.0;
       for (int c = 0; c < nev; ++c) {
-        double* xc = Xo.as<double>() + (int64_t)c * ld;
-        double* axc = AXo.as<double>() + (int64_t)c * ld;
-        prod64(xc, axc);
+        proddd(xo(c), axo(c));
         double q[2];
-        mdot(xc, ld, 1, axc, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-        nrm2sq(xc, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&q[0], lz.h1.p, 8, cudaMemcpyDeviceToHost, s));
-        TM_CK(cudaMemcpyAsync(&q[1], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        mdot_dd(xo(c), ld, 1, axo(c), n, hd.as<double>(), dpart.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q[0], hd.p, 8, cudaMemcpyDeviceToHost, s));
+        nrm2sq_dd(xo(c), n, hd.as<double>() + 1, dpart.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q[1], hd.as<double>() + 1, 8, cudaMemcpyDeviceToHost, s));
         host_sync();
-        const double th = q[0] / q[1];
-        axpby(1.0, axc, -th, xc, lz.W.as<double>(), n, s);
-        nrm2sq(lz.W.as<double>(), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        const double ts = q[0] / q[1];  // theta / S
+        axpby_dd(1.0, axo(c), -ts, xo(c), Wd.as<dfloat>(), n, s);
         double rr = 0.0;
-        TM_CK(cudaMemcpyAsync(&rr, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        nrm2sq_dd(Wd.as<dfloat>(), n, hd.as<double>(), dpart.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&rr, hd.p, 8, cudaMemcpyDeviceToHost, s));
         host_sync();
-        const double res = std::sqrt(std::max(rr, 0.0) / q[1]);
+        const double th = S * ts;
+        const double res = S * std::sqrt(std::max(rr, 0.0) / q[1]);
         thv[c] = th;
         max_resid = std::max(max_resid, res / std::fabs(th));
         if (!(res <= tol * std::max(std::fabs(th), 1e-300))) ok_all = false;
@@ -918,28 +946,27 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       ++info.refine_checks;
       info.refine_true = max_resid;
       // the verified vectors become X0 either way
-      TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
+      TM_CK(cudaMemcpyAsync(x0(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
       TM_CK(cudaMemcpyAsync(ax0(0), AXo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
       if (ok_all) {
+        to_lz(x0(0));
         info.refine_outcome = 2;
         return true;
       }
       // re-orthonormalise X0 (its products follow linearly) and rebuild its rows
       for (int i = 0; i < nev; ++i) {
-        double* xi = lz.v(i);
-        double* ai = ax0(i);
         for (int pass = 0; pass < 2 && i > 0; ++pass) {
-          mdot(lz.v(0), ld, i, xi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-          maxpy(lz.v(0), ld, i, lz.h1.as<double>(), xi, n, s);
-          maxpy(ax0(0), ld, i, lz.h1.as<double>(), ai, n, s);
+          mdot_dd(x0(0), ld, i, x0(i), n, hd.as<double>(), dpart.as<double>(), s);
+          maxpy_dd(x0(0), ld, i, hd.as<double>(), x0(i), n, s);
+          maxpy_dd(ax0(0), ld, i, hd.as<double>(), ax0(i), n, s);
         }
         double q = 0.0;
-        nrm2sq(xi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        nrm2sq_dd(x0(i), n, hd.as<double>(), dpart.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q, hd.p, 8, cudaMemcpyDeviceToHost, s));
         host_sync();
         const double inv = 1.0 / std::sqrt(q);
-        axpby(inv, xi, 0.0, xi, xi, n, s);
-        axpby(inv, ai, 0.0, ai, ai, n, s);
+        axpby_dd(inv, x0(i), 0.0, x0(i), x0(i), n, s);
+        axpby_dd(inv, ax0(i), 0.0, ax0(i), ax0(i), n, s);
       }
       set_x0(nb);
       force_grow = true;
@@ -1007,7 +1034,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       nb = pos;
     }
   }
-  if (have_x) TM_CK(cudaMemcpyAsync(lz.v(0), Xo.p, (size_t)nev * ld * 8, cudaMemcpyDeviceToDevice, s));
+  to_lz(have_x ? xo(0) : x0(0));
   info.refine_outcome = 3;
   return false;
 }
@@ -1049,25 +1076,47 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       };
       std::unique_ptr<Lanczos32> l32;
       std::function<double(float*, float*)> extras;
+      std::function<void(dfloat*)> fill_x0;
+      std::function<void()> x0_f64;
       if (ncv <= NV32) {
         // FP32 Krylov basis (half the bytes of the FP64 basis per sweep)
         l32.reset(new Lanczos32(op, ncv, s));
         l32->start(seed);
         r = l32->run(nev, 200, conv32);
-        // wanted Ritz vectors in FP64, re-orthonormalised (CGS2): the FP32
-        // basis is orthonormal to FP32 accuracy only
-        l32->ritz_f64(r, nev, lz.v(0), lz.ld);
-        for (int i = 0; i < nev; ++i) {
-          double* bi = lz.v(i);
-          for (int pass = 0; pass < 2 && i > 0; ++pass) {
-            mdot(lz.v(0), lz.ld, i, bi, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-            maxpy(lz.v(0), lz.ld, i, lz.h1.as<double>(), bi, n, s);
-          }
-          nrm2sq(bi, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-          normalize(bi, lz.nsq.as<double>(), bi, nullptr, n, s);
-        }
-        // the other Ritz vectors stay FP32
+        // the wanted Ritz vectors in double-float for the refinement,
+        // re-orthonormalised (CGS2): the FP32 basis is orthonormal to FP32
+        // accuracy only
         Lanczos32* lp = l32.get();
+        Lanczos* lzp = &lz;
+        fill_x0 = [lp, lzp, &r, nev](dfloat* X) {
+          const int64_t ld = lzp->ld, nn = lzp->n;
+          lp->ritz_dd(r, nev, X, ld);
+          for (int i = 0; i < nev; ++i) {
+            dfloat* xi = X + (int64_t)i * ld;
+            for (int pass = 0; pass < 2 && i > 0; ++pass) {
+              mdot_dd(X, ld, i, xi, nn, lzp->h1.as<double>(), lzp->part.as<double>(), lzp->s);
+              maxpy_dd(X, ld, i, lzp->h1.as<double>(), xi, nn, lzp->s);
+            }
+            nrm2sq_dd(xi, nn, lzp->nsq.as<double>(), lzp->part.as<double>(), lzp->s);
+            normalize_dd(xi, lzp->nsq.as<double>(), nn, lzp->s);
+          }
+        };
+        // the same in FP64 in V, for the FP64 continuation when the
+        // refinement does not run
+        x0_f64 = [lp, lzp, &r, nev]() {
+          const int64_t nn = lzp->n;
+          lp->ritz_f64(r, nev, lzp->v(0), lzp->ld);
+          for (int i = 0; i < nev; ++i) {
+            double* bi = lzp->v(i);
+            for (int pass = 0; pass < 2 && i > 0; ++pass) {
+              mdot(lzp->v(0), lzp->ld, i, bi, nn, lzp->h1.as<double>(), lzp->part.as<double>(), lzp->s);
+              maxpy(lzp->v(0), lzp->ld, i, lzp->h1.as<double>(), bi, nn, lzp->s);
+            }
+            nrm2sq(bi, nn, lzp->nsq.as<double>(), lzp->part.as<double>(), lzp->s);
+            normalize(bi, lzp->nsq.as<double>(), bi, nullptr, nn, lzp->s);
+          }
+        };
+        // the other Ritz vectors stay FP32
         extras = [lp, &r, nev, nb0](float* out, float* aout) {
           lp->ritz_f32(r, nev, nb0 - nev, out);
           lp->ritz_f32_prod(r, nev, nb0 - nev, aout);
@@ -1081,6 +1130,10 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         r = lz.run(nev, true, 200, conv32, &ok);
         lz.stagnation_stop = false;
         lz.rotate(r, nb0);
+        Lanczos* lzp = &lz;
+        fill_x0 = [lzp, nev](dfloat* X) {
+          for (int i = 0; i < nev; ++i) f64_to_df(lzp->v(i), 1.0, X + (int64_t)i * lzp->ld, lzp->n, lzp->s);
+        };
       }
       // FP64-accurate refinement (refine_mixed); leaves the best Ritz
       // vectors in V's leading columns either way
@@ -1088,8 +1141,9 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       bool cluster = false;
       for (int i = 0; i < nev && i + 1 < (int)r.theta.size(); ++i)
         if (std::fabs(r.theta[i] - r.theta[i + 1]) < 1e-5 * std::fabs(r.theta[i])) cluster = true;
-      const bool refined = !cluster && nev <= kMaxRefineNev && (int64_t)(nb0 + 6 * nev) * 4 <= n &&
-                           refine_mixed(op, lz, nev, nb0, tol, thv, max_resid, extras, info);
+      const bool run_refine = !cluster && nev <= kMaxRefineNev && (int64_t)(nb0 + 6 * nev) * 4 <= n;
+      const bool refined = run_refine && refine_mixed(op, lz, nev, nb0, tol, thv, max_resid, fill_x0, extras, info);
+      if (!run_refine && x0_f64) x0_f64();
       if (!refined && info.refine_outcome == 0) info.refine_outcome = 3;
       if (refined) {
         theta = thv;
