@@ -7,6 +7,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <future>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -304,11 +305,15 @@ static void build_op(Op& op) {
   }
   op.nstate = 1ll << op.L;
   if (is_reduced(op.kind)) {
+    const bool eo_ok = (op.kind == K_XAM) && op.grp.periodic && (op.L % 2 == 0) && op.L >= 12 && op.L <= 32;
+    // the even/odd plan's host tables depend on L and the flip only: build
+    // them on a host thread while the GPU builds the orbit table
+    std::future<std::shared_ptr<EOHostTables>> eo_host;
+    if (eo_ok) eo_host = std::async(std::launch::async, eo_host_tables, op.L / 2, op.grp.flip);
     build_orbit_table(op);
     build_tvec(op);
-    const bool eo_ok = (op.kind == K_XAM) && op.grp.periodic && (op.L % 2 == 0) && op.L >= 12 && op.L <= 32;
     if (eo_ok) {
-      build_eo_plan(op);
+      build_eo_plan(op, eo_host.get().get());
       op.ws_a.release();
       op.ws_b.release();
       op.ws_c.alloc((size_t)op.n * 8);

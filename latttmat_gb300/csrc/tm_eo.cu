@@ -47,6 +47,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <type_traits>
 #include <vector>
 
@@ -525,103 +526,172 @@ static int cluster_bits_for(int m, size_t elem) {
 }
 
 // Orders of the m-bit patterns used by the passes.  cls: H-class index of
-// each pattern; ct: top bits that split a tile over a cluster.
+// each pattern (ncls classes); ct: top bits that split a tile over a cluster.
 //   iteration order: (top ct bits, class, pattern) -- a CTA of a 2^c-CTA
 //     cluster (c <= ct) owns one contiguous range, and a warp's elements are
 //     one or two classes;
 //   class-first order: (class, top ct bits, pattern) -- each class contiguous.
-static std::vector<uint32_t> pattern_order(const std::vector<uint32_t>& cls, int m, int ct, bool class_first) {
-  const uint32_t M = 1u << m;
-  std::vector<uint64_t> k(M);
-  for (uint32_t x = 0; x < M; ++x) {
-    const uint64_t top = x >> (m - ct);
-    k[x] = class_first ? ((uint64_t)cls[x] << 40 | top << 20 | x) : (top << 40 | (uint64_t)cls[x] << 20 | x);
-  }
-  std::sort(k.begin(), k.end());
+// A counting sort over the (top, class) buckets, patterns ascending within.
+static std::vector<uint32_t> pattern_order(const std::vector<uint32_t>& cls, uint32_t ncls, int m, int ct,
+                                           bool class_first) {
+  const uint32_t M = 1u << m, ntop = 1u << ct;
+  const size_t nb = (size_t)ncls * ntop;
+  auto bucket = [&](uint32_t x) -> size_t {
+    const uint32_t top = x >> (m - ct);
+    return class_first ? (size_t)cls[x] * ntop + top : (size_t)top * ncls + cls[x];
+  };
+  std::vector<uint32_t> start(nb + 1, 0);
+  for (uint32_t x = 0; x < M; ++x) ++start[bucket(x) + 1];
+  for (size_t b = 0; b < nb; ++b) start[b + 1] += start[b];
   std::vector<uint32_t> ord(M);
-  for (uint32_t i = 0; i < M; ++i) ord[i] = (uint32_t)(k[i] & 0xfffffu);
+  for (uint32_t x = 0; x < M; ++x) ord[start[bucket(x)]++] = x;
   return ord;
 }
 
-void build_eo_plan(Op& op) {
-  EOPlan& P = op.eo;
-  const int L = op.L, m = L / 2;
-  P.m = m;
-  const int flip = op.grp.flip;
-  P.ng = 2 * m * (flip ? 2 : 1);
-  const uint32_t M = 1u << m;
-  // host tables over m-bit patterns
+// Host tables of the even/odd plan.  They depend on m and the spin flip only,
+// so they are computed on a host thread while the orbit table is built.
+struct EOHostTables {
+  int m = 0, ng = 0, c32 = 0, c64 = 0, ct = 0, n_orep = 0, n_erep = 0;
+  std::vector<uint32_t> olist, elist, etile, t2, wbase, cls_start, cls_size;
+  std::vector<uint16_t> it_e, cf_e, it_o, pos_o;
+  std::vector<uint8_t> wsz;
+};
+
+std::shared_ptr<EOHostTables> eo_host_tables(int m, int flip) {
+  auto H = std::make_shared<EOHostTables>();
+  H->m = m;
+  H->ng = 2 * m * (flip ? 2 : 1);
+  const uint32_t M = 1u << m, mask = M - 1u;
+  // bit reversal of m-bit patterns through a byte table
+  uint8_t rev8[256];
+  for (int x = 0; x < 256; ++x) {
+    int r = 0;
+    for (int i = 0; i < 8; ++i) r |= ((x >> i) & 1) << (7 - i);
+    rev8[x] = (uint8_t)r;
+  }
+  auto brev = [&](uint32_t x) { return (((uint32_t)rev8[x & 255u] << 8) | rev8[(x >> 8) & 255u]) >> (16 - m); };
+  auto rot1 = [&](uint32_t x) { return ((x >> 1) | (x << (m - 1))) & mask; };  // rotate right by one
+  // orbit minima under H and, for odd patterns, the first H element (in the
+  // order g = j + m*refl + 2m*flip of act_o) reaching it
   std::vector<uint32_t> orep(M), erep_of(M);
   std::vector<int> og(M);
   for (uint32_t o = 0; o < M; ++o) {
-    uint32_t best = o;
+    uint32_t best = o, r = o;
     int bg = 0;
-    for (int g = 0; g < P.ng; ++g) {
-      uint32_t im = act_o(g, o, m);
-      if (im < best) {
-        best = im;
-        bg = g;
+    for (int j = 0; j < m; ++j, r = rot1(r)) {
+      const uint32_t b = brev(r);
+      const uint32_t im[4] = {r, b, r ^ mask, b ^ mask};
+      for (int q = 0; q < (flip ? 4 : 2); ++q) {
+        const int g = j + m * q;
+        if (im[q] < best || (im[q] == best && g < bg)) {
+          best = im[q];
+          bg = g;
+        }
       }
     }
     orep[o] = best;
-    og[o] = bg;
+    og[o] = (best == o) ? 0 : bg;
   }
   for (uint32_t e = 0; e < M; ++e) {
-    uint32_t best = e;
-    for (int g = 0; g < P.ng; ++g) best = std::min(best, act_e(g, e, m));
+    uint32_t best = e, r = e;
+    for (int j = 0; j < m; ++j, r = rot1(r)) {
+      const uint32_t b = ((brev(r) << 1) | (brev(r) >> (m - 1))) & mask;  // rotl(brev(r), 1)
+      best = std::min(best, std::min(r, b));
+      if (flip) best = std::min(best, std::min(r ^ mask, b ^ mask));
+    }
     erep_of[e] = best;
   }
-  std::vector<uint32_t> olist, elist;
-  std::vector<uint32_t> otile(M, 0xffffffffu), etile(M, 0xffffffffu);
+  std::vector<uint32_t> otile(M, 0xffffffffu);
+  H->etile.assign(M, 0xffffffffu);
   for (uint32_t o = 0; o < M; ++o)
     if (orep[o] == o) {
-      otile[o] = (uint32_t)olist.size();
-      olist.push_back(o);
+      otile[o] = (uint32_t)H->olist.size();
+      H->olist.push_back(o);
     }
   for (uint32_t e = 0; e < M; ++e)
     if (erep_of[e] == e) {
-      etile[e] = (uint32_t)elist.size();
-      elist.push_back(e);
+      H->etile[e] = (uint32_t)H->elist.size();
+      H->elist.push_back(e);
     }
-  P.n_orep = (int)olist.size();
-  P.n_erep = (int)elist.size();
-  P.c32 = cluster_bits_for(m, 4);
-  P.c64 = cluster_bits_for(m, 8);
-  const int ct = std::max(P.c32, P.c64);
+  H->n_orep = (int)H->olist.size();
+  H->n_erep = (int)H->elist.size();
+  H->c32 = cluster_bits_for(m, 4);
+  H->c64 = cluster_bits_for(m, 8);
+  const int ct = H->ct = std::max(H->c32, H->c64);
   if (ct > 2) fail(TM_ERR_LIMIT, "even/odd tile split over more than 4 CTAs");
   std::vector<uint32_t> ecls(M), ocls(M);
   for (uint32_t x = 0; x < M; ++x) {
-    ecls[x] = etile[erep_of[x]];
+    ecls[x] = H->etile[erep_of[x]];
     ocls[x] = otile[orep[x]];
   }
   // pass 1 walks e in iteration order and stores w1 class-major; pass 2
   // walks o in iteration order, and the designated outputs of a pass-2 tile
   // follow the same order (so a CTA's outputs are contiguous)
-  const std::vector<uint32_t> e_it = pattern_order(ecls, m, ct, false);
-  const std::vector<uint32_t> e_cf = pattern_order(ecls, m, ct, true);
-  const std::vector<uint32_t> o_it = pattern_order(ocls, m, ct, false);
-  std::vector<uint16_t> h_it_e(M), h_cf_e(M), h_it_o(M), h_pos_o(M);
-  std::vector<uint32_t> t2(M), h_wbase(M), cls_start(P.n_erep, M), cls_size(P.n_erep, 0);
-  std::vector<uint8_t> h_wsz(M);
+  const std::vector<uint32_t> e_it = pattern_order(ecls, H->n_erep, m, ct, false);
+  const std::vector<uint32_t> e_cf = pattern_order(ecls, H->n_erep, m, ct, true);
+  const std::vector<uint32_t> o_it = pattern_order(ocls, H->n_orep, m, ct, false);
+  H->it_e.resize(M);
+  H->cf_e.resize(M);
+  H->it_o.resize(M);
+  H->pos_o.resize(M);
+  H->t2.resize(M);
+  H->wbase.resize(M);
+  H->wsz.resize(M);
+  H->cls_start.assign(H->n_erep, M);
+  H->cls_size.assign(H->n_erep, 0);
   for (uint32_t i = 0; i < M; ++i) {
-    h_cf_e[e_cf[i]] = (uint16_t)i;
-    h_pos_o[o_it[i]] = (uint16_t)i;
+    H->cf_e[e_cf[i]] = (uint16_t)i;
+    H->pos_o[o_it[i]] = (uint16_t)i;
   }
   for (uint32_t x = 0; x < M; ++x) {
-    cls_start[ecls[x]] = std::min<uint32_t>(cls_start[ecls[x]], h_cf_e[x]);
-    cls_size[ecls[x]] += 1;
+    H->cls_start[ecls[x]] = std::min<uint32_t>(H->cls_start[ecls[x]], H->cf_e[x]);
+    H->cls_size[ecls[x]] += 1;
   }
   // w1 is class-major: element (t, e) of e-class C at
   // start(C) * n_orep + t * |C| + (cf(e) - start(C))
   for (uint32_t i = 0; i < M; ++i) {
     const uint32_t e = e_it[i], C = ecls[e];
-    h_it_e[i] = (uint16_t)e;
-    h_wbase[i] = cls_start[C] * (uint32_t)P.n_orep + (h_cf_e[e] - cls_start[C]);
-    h_wsz[i] = (uint8_t)cls_size[C];
+    H->it_e[i] = (uint16_t)e;
+    H->wbase[i] = H->cls_start[C] * (uint32_t)H->n_orep + (H->cf_e[e] - H->cls_start[C]);
+    H->wsz[i] = (uint8_t)H->cls_size[C];
     const uint32_t o = o_it[i];
-    h_it_o[i] = (uint16_t)o;
-    t2[i] = (otile[orep[o]] << 8) | (uint32_t)og[o];
+    H->it_o[i] = (uint16_t)o;
+    H->t2[i] = (otile[orep[o]] << 8) | (uint32_t)og[o];
   }
+  return H;
+}
+
+void build_eo_plan(Op& op, const EOHostTables* Hp) {
+  std::shared_ptr<EOHostTables> own;
+  if (!Hp) {
+    own = eo_host_tables(op.L / 2, op.grp.flip);
+    Hp = own.get();
+  }
+  const EOHostTables& H = *Hp;
+  EOPlan& P = op.eo;
+  const int L = op.L, m = L / 2;
+  if (H.m != m) fail(TM_ERR_ARG, "even/odd host tables for another L");
+  const int flip = op.grp.flip;
+  const uint32_t M = 1u << m;
+  P.m = m;
+  P.ng = H.ng;
+  P.n_orep = H.n_orep;
+  P.n_erep = H.n_erep;
+  P.c32 = H.c32;
+  P.c64 = H.c64;
+  const int ct = H.ct;
+  const std::vector<uint32_t>& olist = H.olist;
+  const std::vector<uint32_t>& elist = H.elist;
+  const std::vector<uint32_t>& etile = H.etile;
+  const std::vector<uint32_t>& t2 = H.t2;
+  const std::vector<uint32_t>& cls_start = H.cls_start;
+  const std::vector<uint32_t>& cls_size = H.cls_size;
+  const std::vector<uint16_t>& h_pos_o = H.pos_o;
+  const std::vector<uint16_t>& h_it_e = H.it_e;
+  const std::vector<uint16_t>& h_cf_e = H.cf_e;
+  const std::vector<uint16_t>& h_it_o = H.it_o;
+  const std::vector<uint32_t>& h_wbase = H.wbase;
+  const std::vector<uint8_t>& h_wsz = H.wsz;
 
   cudaStream_t s = op.stream;
   DBuf d_olist, d_etile, d_pos_o;

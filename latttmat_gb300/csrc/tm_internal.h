@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -165,7 +166,9 @@ void build_group(Op& op);
 void build_orbit_table(Op& op);          // idx, dup (reference order)
 void build_tvec(Op& op);                 // Tvec for the operator
 void build_state_map(Op& op);            // smap for the generic reduced path
-void build_eo_plan(Op& op);              // even/odd plan for K_XAM
+struct EOHostTables;                     // host-side even/odd plan tables (tm_eo.cu)
+std::shared_ptr<EOHostTables> eo_host_tables(int m, int flip);
+void build_eo_plan(Op& op, const EOHostTables* host = nullptr);  // even/odd plan for K_XAM
 void build_two_layer(Op& op);            // tables of K_YAT / K_Y2AT / K_YAM
 // y = T x (or T^T x for a transposed view) of a two-layer operator, FP64
 void matvec_two_layer(const Op& op, const double* x, double* y, cudaStream_t s);

@@ -9,6 +9,7 @@
 //  * Tvec per operator, restating each reference genTvec.
 #include <cmath>
 #include <cstdio>
+#include <vector>
 
 #include "tm_group.cuh"
 #include "tm_internal.h"
@@ -451,6 +452,31 @@ __global__ void tvec_full_kernel(TvecParams p, int64_t n, double* tv) {
   for (; i < n; i += st) tv[i] = tv_eval(p, (uint64_t)i);
 }
 
+// Reduced x-ANNNI weights from a table over the bond counts: tv_xam's
+// exponent takes (L+1)^3 values (n1, n2, n0 in [0, L]), so its exponentials
+// are evaluated once on the host with the same expression.
+__global__ void tvec_xam_tab_kernel(int L, int boundary, int64_t n, const uint32_t* __restrict__ idx,
+                                    const uint16_t* __restrict__ dup, const double* __restrict__ tab,
+                                    double* __restrict__ tv) {
+  const uint64_t mask = (1ull << L) - 1;
+  const int w = L + 1;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) {
+    const uint64_t s = idx[i];
+    int n1, n2;
+    if (!boundary) {
+      n1 = popc64(s ^ rotr(s, L, 1));
+      n2 = popc64(s ^ rotr(s, L, 2));
+    } else {
+      n1 = popc64((s & (mask >> 1)) ^ (s >> 1));
+      n2 = popc64((s & (mask >> 2)) ^ (s >> 2));
+    }
+    const int n0 = popc64(s);
+    tv[i] = __ldg(tab + ((int64_t)n1 * w + n2) * w + n0) / sqrt((double)dup[i]);
+  }
+}
+
 __global__ void tvec_red_kernel(TvecParams p, int64_t n, const uint32_t* idx, const uint16_t* dup,
                                 double* tv) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -478,11 +504,28 @@ void build_tvec(Op& op) {
   op.tvec.alloc(n * sizeof(double));
   int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 16);
   if (blocks < 1) blocks = 1;
-  if (reduced)
+  DBuf tab;
+  if (reduced && op.kind == K_XAM && op.L <= 32) {
+    // tv_xam's exponentials over all bond counts, same expression
+    const int L = op.L, w = L + 1;
+    const double hb = 0.5 * p.betaJ;
+    const double J1 = -hb, J2 = hb * p.kappa, hJ = -hb * p.h, Jn = hb * p.nfexp;
+    std::vector<double> T((size_t)w * w * w);
+    for (int n1 = 0; n1 <= L; ++n1)
+      for (int n2 = 0; n2 <= L; ++n2)
+        for (int n0 = 0; n0 <= L; ++n0)
+          T[((size_t)n1 * w + n2) * w + n0] = std::exp(J1 * (2 * n1 - L) + J2 * (2 * n2 - L) + hJ * (2 * n0 - L) + Jn);
+    tab.alloc(T.size() * 8);
+    TM_CK(cudaMemcpyAsync(tab.p, T.data(), T.size() * 8, cudaMemcpyHostToDevice, op.stream));
+    tvec_xam_tab_kernel<<<blocks, 256, 0, op.stream>>>(L, p.boundary, n, op.idx.as<uint32_t>(),
+                                                       op.dup.as<uint16_t>(), tab.as<double>(),
+                                                       op.tvec.as<double>());
+  } else if (reduced) {
     tvec_red_kernel<<<blocks, 256, 0, op.stream>>>(p, n, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),
                                                    op.tvec.as<double>());
-  else
+  } else {
     tvec_full_kernel<<<blocks, 256, 0, op.stream>>>(p, n, op.tvec.as<double>());
+  }
   TM_CKK("tvec");
   TM_CK(cudaStreamSynchronize(op.stream));
 }
