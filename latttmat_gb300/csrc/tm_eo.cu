@@ -410,6 +410,8 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
 }
 
 // ---------------------------------------------------------------- plan kernels
+
+
 struct PlanDev {
   GroupDev g;
   int m;
@@ -422,26 +424,48 @@ __device__ __forceinline__ uint32_t rank_of(const PlanDev& P, uint64_t c) {
   return P.prefix[w] + __popc(P.bits[w] & ((1u << (c & 31)) - 1u));
 }
 
-// designated output key per representative: min over orbit images whose even
-// part is an H-representative of (tile << m | pos_o(o)); pos_o is the
-// position of o in pass 2's iteration order
-__global__ void eo_key_kernel(PlanDev P, const uint32_t* __restrict__ idx, int64_t R,
-                              const uint32_t* __restrict__ e_tile, const uint16_t* __restrict__ pos_o,
+// Designated output key of a state's orbit: the minimum of (tile << m |
+// pos_o(o)) over the orbit images whose even part is an H-representative
+// (pass-2 tile `tile`); pos_o is the position of o in pass 2's iteration
+// order.  The layer group is H u H.tau with tau = rotation by one site, which
+// maps (e, o) to (o, rotr_m(e, 1)); within a coset the images with a
+// representative even part are those of the H elements taking e to its
+// representative, usually one (einfo), so the key takes two lookups per coset
+// instead of a walk over the whole group.
+__device__ __forceinline__ uint32_t coset_key(uint32_t e, uint32_t o, int m, int ng,
+                                              const uint32_t* __restrict__ einfo,
+                                              const uint16_t* __restrict__ pos_o) {
+  const uint32_t inf = __ldg(einfo + e);
+  const uint32_t t = inf & 0xffffu, j = (inf >> 16) & 31u, nst = inf >> 24;
+  const uint32_t mask = (1u << m) - 1u;
+  // act_o of the decoded element: rotate right by j, reflect, flip
+  uint32_t r = j ? (((o >> j) | (o << (m - j))) & mask) : o;
+  if (inf & (1u << 21)) r = __brev(r) >> (32 - m);
+  if (inf & (1u << 22)) r ^= mask;
+  uint32_t best = (t << m) | __ldg(pos_o + r);
+  if (nst > 1) {  // e has a nontrivial stabiliser in H: every element reaching its representative
+    const int g0 = (int)j + m * (int)(((inf >> 21) & 1u) + 2u * ((inf >> 22) & 1u));
+    const uint32_t rep = act_e(g0, e, m);
+    for (int g = g0 + 1; g < ng; ++g)
+      if (act_e(g, e, m) == rep) best = min(best, (t << m) | __ldg(pos_o + act_o(g, o, m)));
+  }
+  return best;
+}
+
+__device__ __forceinline__ uint32_t designated_key(uint32_t s, int m, int ng, const uint32_t* __restrict__ einfo,
+                                                   const uint16_t* __restrict__ pos_o) {
+  const uint32_t e = gather16(s), o = gather16(s >> 1);
+  const uint32_t e1 = ((e >> 1) | (e << (m - 1))) & ((1u << m) - 1u);  // rotr_m(e, 1)
+  return min(coset_key(e, o, m, ng, einfo, pos_o), coset_key(o, e1, m, ng, einfo, pos_o));
+}
+
+__global__ void eo_key_kernel(int m, int ng, const uint32_t* __restrict__ idx, int64_t R,
+                              const uint32_t* __restrict__ einfo, const uint16_t* __restrict__ pos_o,
                               uint32_t* __restrict__ key, uint32_t* __restrict__ dbits) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < R; i += st) {
-    uint64_t s = idx[i];
-    uint32_t best = 0xffffffffu;
-    for_each_image(P.g, s, [&](uint64_t im) {
-      uint32_t e = gather16((uint32_t)im), o = gather16((uint32_t)(im >> 1));
-      uint32_t t = e_tile[e];
-      if (t != 0xffffffffu) {
-        uint32_t k = (t << P.m) | pos_o[o];
-        if (k < best) best = k;
-      }
-      return true;
-    });
+    const uint32_t best = designated_key(idx[i], m, ng, einfo, pos_o);
     key[i] = best;
     atomicOr(dbits + (best >> 5), 1u << (best & 31));
   }
@@ -469,6 +493,8 @@ __global__ void eo_perm_kernel(const uint32_t* __restrict__ key, int64_t R, cons
   }
 }
 
+// map1: pi position of the orbit of (it_e[P], o_rep(t)): its minimum by a
+// walk over the group, then the orbit rank (rep bitset and word prefix)
 __global__ void eo_map1_kernel(PlanDev P, const uint32_t* __restrict__ olist, int n_orep,
                                const uint16_t* __restrict__ it_e, const uint32_t* __restrict__ pinv,
                                uint32_t* __restrict__ map1) {
@@ -553,6 +579,10 @@ static std::vector<uint32_t> pattern_order(const std::vector<uint32_t>& cls, uin
 struct EOHostTables {
   int m = 0, ng = 0, c32 = 0, c64 = 0, ct = 0, n_orep = 0, n_erep = 0;
   std::vector<uint32_t> olist, elist, etile, t2, wbase, cls_start, cls_size;
+  // per m-bit pattern x: e-tile of its H-representative (bits 0-15), the first
+  // H element g = j + m (refl + 2 flip) with act_e(g, x) = rep, decoded (j in
+  // bits 16-20, refl bit 21, flip bit 22), and how many reach it (bits 24-31)
+  std::vector<uint32_t> einfo;
   std::vector<uint16_t> it_e, cf_e, it_o, pos_o;
   std::vector<uint8_t> wsz;
 };
@@ -615,6 +645,26 @@ std::shared_ptr<EOHostTables> eo_host_tables(int m, int flip) {
     }
   H->n_orep = (int)H->olist.size();
   H->n_erep = (int)H->elist.size();
+  if (H->n_erep > 0xffff) fail(TM_ERR_LIMIT, "even/odd plan: too many even tiles");
+  H->einfo.resize(M);
+  for (uint32_t e = 0; e < M; ++e) {
+    const uint32_t rep = erep_of[e];
+    int g0 = -1, cnt = 0;
+    uint32_t r = e;
+    // act_e(g, e) for g = j + m * q, q = reflection + 2 * flip
+    for (int j = 0; j < m; ++j, r = rot1(r)) {
+      const uint32_t b = ((brev(r) << 1) | (brev(r) >> (m - 1))) & mask;
+      const uint32_t im[4] = {r, b, r ^ mask, b ^ mask};
+      for (int q = 0; q < (flip ? 4 : 2); ++q)
+        if (im[q] == rep) {
+          const int g = j + m * q;
+          if (g0 < 0 || g < g0) g0 = g;
+          ++cnt;
+        }
+    }
+    const uint32_t j0 = (uint32_t)(g0 % m), q0 = (uint32_t)(g0 / m);
+    H->einfo[e] = H->etile[rep] | (j0 << 16) | ((q0 & 1u) << 21) | ((q0 >> 1) << 22) | ((uint32_t)cnt << 24);
+  }
   H->c32 = cluster_bits_for(m, 4);
   H->c64 = cluster_bits_for(m, 8);
   const int ct = H->ct = std::max(H->c32, H->c64);
@@ -682,7 +732,6 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   const int ct = H.ct;
   const std::vector<uint32_t>& olist = H.olist;
   const std::vector<uint32_t>& elist = H.elist;
-  const std::vector<uint32_t>& etile = H.etile;
   const std::vector<uint32_t>& t2 = H.t2;
   const std::vector<uint32_t>& cls_start = H.cls_start;
   const std::vector<uint32_t>& cls_size = H.cls_size;
@@ -694,9 +743,9 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   const std::vector<uint8_t>& h_wsz = H.wsz;
 
   cudaStream_t s = op.stream;
-  DBuf d_olist, d_etile, d_pos_o;
+  DBuf d_olist, d_einfo, d_pos_o;
   d_olist.alloc(olist.size() * 4);
-  d_etile.alloc(M * 4);
+  d_einfo.alloc(M * 4);
   d_pos_o.alloc(M * 2);
   P.t2.alloc(M * 4);
   P.it_e.alloc(M * 2);
@@ -708,7 +757,7 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   P.it_o.alloc(M * 2);
   P.erep.alloc(elist.size() * 4);
   TM_CK(cudaMemcpyAsync(d_olist.p, olist.data(), olist.size() * 4, cudaMemcpyHostToDevice, s));
-  TM_CK(cudaMemcpyAsync(d_etile.p, etile.data(), M * 4, cudaMemcpyHostToDevice, s));
+  TM_CK(cudaMemcpyAsync(d_einfo.p, H.einfo.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_pos_o.p, h_pos_o.data(), M * 2, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.t2.p, t2.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.it_e.p, h_it_e.data(), M * 2, cudaMemcpyHostToDevice, s));
@@ -720,11 +769,6 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   TM_CK(cudaMemcpyAsync(P.it_o.p, h_it_o.data(), M * 2, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.erep.p, elist.data(), elist.size() * 4, cudaMemcpyHostToDevice, s));
 
-  PlanDev pd;
-  pd.g = to_dev(op.grp);
-  pd.m = m;
-  pd.bits = op.ws_a.as<uint32_t>();
-  pd.prefix = op.ws_b.as<uint32_t>();
   const int64_t R = op.n;
   // designated outputs -> pi
   const int64_t nkeybits = (int64_t)P.n_erep << m;
@@ -734,7 +778,7 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   dbits.alloc(nwords * 4);
   dpre.alloc(nwords * 4);
   TM_CK(cudaMemsetAsync(dbits.p, 0, nwords * 4, s));
-  eo_key_kernel<<<grid_for(R), 256, 0, s>>>(pd, op.idx.as<uint32_t>(), R, d_etile.as<uint32_t>(),
+  eo_key_kernel<<<grid_for(R), 256, 0, s>>>(m, P.ng, op.idx.as<uint32_t>(), R, d_einfo.as<uint32_t>(),
                                             d_pos_o.as<uint16_t>(), key.as<uint32_t>(), dbits.as<uint32_t>());
   TM_CKK("eo_key");
   popc_kernel<<<grid_for(nwords), 256, 0, s>>>(dbits.as<uint32_t>(), dpre.as<uint32_t>(), nwords);
@@ -759,6 +803,11 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   // map1
   const int64_t n1 = (int64_t)P.n_orep << m;
   P.map1.alloc(n1 * 4);
+  PlanDev pd;
+  pd.g = to_dev(op.grp);
+  pd.m = m;
+  pd.bits = op.ws_a.as<uint32_t>();
+  pd.prefix = op.ws_b.as<uint32_t>();
   eo_map1_kernel<<<grid_for(n1), 256, 0, s>>>(pd, d_olist.as<uint32_t>(), P.n_orep, P.it_e.as<uint16_t>(),
                                               op.pinv.as<uint32_t>(), P.map1.as<uint32_t>());
   TM_CKK("eo_map1");

@@ -776,27 +776,26 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
   };
   // C columns j0 .. j0+cnt-1 (cnt <= 4) against columns 0 .. j0+cnt-1: one
-  // sweep over B32 (b . A w and b . w for the whole block), one over AB32
+  // sweep over B32 gives b . A w and b . w for the whole block.  The C-C
+  // block enters the wanted pairs at second order, so one side of the
+  // symmetric product suffices.
   auto add_gcols = [&](int j0, int cnt) {
     const int nv = j0 + cnt;
-    F32Cols w1{}, w2{};
+    F32Cols w1{};
     for (int c = 0; c < cnt; ++c) {
       w1.c[c] = f32col(AB32, j0 + c);
       w1.c[cnt + c] = f32col(B32, j0 + c);
-      w2.c[c] = f32col(B32, j0 + c);
     }
     mdot_block_f32(B32.as<float>(), ld, nv, w1, 2 * cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
-    mdot_block_f32(AB32.as<float>(), ld, nv, w2, cnt, n, Hd.as<double>() + 48 * 2 * cnt, 48, bpart.as<double>(), s);
-    std::vector<double> h((size_t)48 * 3 * cnt);
+    std::vector<double> h((size_t)48 * 2 * cnt);
     TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
     for (int c = 0; c < cnt; ++c) {
       const int j = j0 + c;
-      const double* gl = &h[(size_t)48 * c];             // b_i . A b_j / S
-      const double* mc = &h[(size_t)48 * (cnt + c)];     // b_i . b_j
-      const double* gr = &h[(size_t)48 * (2 * cnt + c)]; // (A b_i / S) . b_j
+      const double* gl = &h[(size_t)48 * c];          // b_i . A b_j / S
+      const double* mc = &h[(size_t)48 * (cnt + c)];  // b_i . b_j
       for (int i = nev; i <= j; ++i) {
-        g(i, j) = g(j, i) = S * 0.5 * (gl[i] + gr[i]);
+        g(i, j) = g(j, i) = S * gl[i];
         mm(i, j) = mm(j, i) = mc[i];
       }
     }
