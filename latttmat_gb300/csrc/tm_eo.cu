@@ -212,33 +212,66 @@ __device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A, int nbits) {
   }
 }
 
+// acc += c * v over the 16 / sizeof(T) elements of a 16-byte chunk
+template <class T>
+__device__ __forceinline__ void axpy16(float4& acc, const float4& v, T c);
+template <>
+__device__ __forceinline__ void axpy16<float>(float4& acc, const float4& v, float c) {
+  acc.x = fmaf(c, v.x, acc.x);
+  acc.y = fmaf(c, v.y, acc.y);
+  acc.z = fmaf(c, v.z, acc.z);
+  acc.w = fmaf(c, v.w, acc.w);
+}
+template <>
+__device__ __forceinline__ void axpy16<double>(float4& acc, const float4& v, double c) {
+  double2 a = *reinterpret_cast<double2*>(&acc);
+  const double2 x = *reinterpret_cast<const double2*>(&v);
+  a.x = fma(c, x.x, a.x);
+  a.y = fma(c, x.y, a.y);
+  acc = *reinterpret_cast<float4*>(&a);
+}
+template <>
+__device__ __forceinline__ void axpy16<dfloat>(float4& acc, const float4& v, dfloat c) {
+  const dfloat a0 = df_fma(c, dfloat(v.x, v.y), dfloat(acc.x, acc.y));
+  const dfloat a1 = df_fma(c, dfloat(v.z, v.w), dfloat(acc.z, acc.w));
+  acc = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
+}
+
 // Combine the cluster's 2^c partial tiles (butterflies on the top c tile
 // bits) in place: afterwards sm[spad(j)] holds the final value of local
-// element j.  Each thread reads its own elements j = tid + k*blockDim from
-// every CTA of the cluster (contiguous DSMEM reads), and writes back after a
+// element j.  The combination is elementwise at equal positions of the
+// padded tiles, so it runs over raw 16-byte chunks of the buffer (the padding
+// slots carry values nobody reads): every thread reads its chunks from every
+// CTA of the cluster with 16-byte DSMEM loads, and writes back after a
 // cluster barrier, so no CTA overwrites values another still reads.  After
 // that barrier no CTA reads another's shared memory, so a CTA may exit.
 template <class T, int KB>
 __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int rank, const EOArgs& A) {
   const T a = A.swap ? coef_r<T>(A) : T(1), b = A.swap ? T(1) : coef_r<T>(A);
-  const int p = A.p, kb = A.n - A.p;
+  constexpr int kMaxChunks = ((1 << KB) * 33 * (int)sizeof(T) + 511) / 512;  // ceil(2^KB * 33/32 * sizeof(T) / 16)
+  const int nchunks = (((1 << A.n) + (1 << (A.n - 5))) * (int)sizeof(T)) / 16;
   const int nc = 1 << A.c;
-  T acc[1 << KB];
+  float4 acc[kMaxChunks];
 #pragma unroll
-  for (int k = 0; k < (1 << KB); ++k) acc[k] = T(0);
+  for (int k = 0; k < kMaxChunks; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   cl.sync();
   for (int r = 0; r < nc; ++r) {
     T coef = T(1);
     for (int bit = 0; bit < A.c; ++bit) coef = coef * ((((r ^ rank) >> bit) & 1) ? b : a);
-    const T* src = (r == rank) ? sm : cl.map_shared_rank(sm, r);
+    const float4* src = reinterpret_cast<const float4*>((r == rank) ? sm : cl.map_shared_rank(sm, r));
 #pragma unroll
-    for (int k = 0; k < (1 << KB); ++k)
-      if (k < (1 << kb)) acc[k] = acc[k] + coef * src[spad(threadIdx.x + (k << p))];
+    for (int k = 0; k < kMaxChunks; ++k) {
+      const int q = (int)threadIdx.x + k * (int)blockDim.x;
+      if (q < nchunks) axpy16<T>(acc[k], src[q], coef);
+    }
   }
   cl.sync();
+  float4* dst = reinterpret_cast<float4*>(sm);
 #pragma unroll
-  for (int k = 0; k < (1 << KB); ++k)
-    if (k < (1 << kb)) sm[spad(threadIdx.x + (k << p))] = acc[k];
+  for (int k = 0; k < kMaxChunks; ++k) {
+    const int q = (int)threadIdx.x + k * (int)blockDim.x;
+    if (q < nchunks) dst[q] = acc[k];
+  }
   // only this CTA reads its combined tile from here on
   __syncthreads();
 }
