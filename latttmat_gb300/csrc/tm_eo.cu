@@ -248,6 +248,29 @@ __device__ __forceinline__ void axpy16<dfloat>(float4& acc, const float4& v, dfl
 template <class T, int KB>
 __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int rank, const EOArgs& A) {
   const T a = A.swap ? coef_r<T>(A) : T(1), b = A.swap ? T(1) : coef_r<T>(A);
+  if constexpr (std::is_same<T, double>::value) {
+    // native FP64: element-wise (the chunk accumulators and FP64 temporaries
+    // together would spill)
+    const int p = A.p, kb = A.n - A.p;
+    T acc[1 << KB];
+#pragma unroll
+    for (int k = 0; k < (1 << KB); ++k) acc[k] = T(0);
+    cl.sync();
+    for (int r = 0; r < (1 << A.c); ++r) {
+      T coef = T(1);
+      for (int bit = 0; bit < A.c; ++bit) coef = coef * ((((r ^ rank) >> bit) & 1) ? b : a);
+      const T* src = (r == rank) ? sm : cl.map_shared_rank(sm, r);
+#pragma unroll
+      for (int k = 0; k < (1 << KB); ++k)
+        if (k < (1 << kb)) acc[k] = acc[k] + coef * src[spad(threadIdx.x + (k << p))];
+    }
+    cl.sync();
+#pragma unroll
+    for (int k = 0; k < (1 << KB); ++k)
+      if (k < (1 << kb)) sm[spad(threadIdx.x + (k << p))] = acc[k];
+    __syncthreads();
+    return;
+  }
   constexpr int kMaxChunks = ((1 << KB) * 33 * (int)sizeof(T) + 511) / 512;  // ceil(2^KB * 33/32 * sizeof(T) / 16)
   const int nchunks = (((1 << A.n) + (1 << (A.n - 5))) * (int)sizeof(T)) / 16;
   const int nc = 1 << A.c;
