@@ -119,7 +119,7 @@ __device__ __forceinline__ T chain_init(const IO* __restrict__ x, const double* 
 // P: the nlb*2^L*2^NA buffer (in place).  first: tiles built from x; last:
 // y[r] = postc * post[r] * sum_{lb, aux} (one CTA loops the lastbit passes).
 template <class T, int ZB, class IO>
-__global__ void __launch_bounds__(256, 2) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
+__global__ void __launch_bounds__(256, 3) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
                                                     const double* __restrict__ pre, const uint32_t* __restrict__ smap,
                                                     IO* __restrict__ y, const double* __restrict__ post, double postc,
                                                     int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {

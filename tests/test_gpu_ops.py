@@ -157,3 +157,27 @@ def test_double_float_refinement_product(L, ec):
     valsm, _, _, infom = op.eigs(3, tol=1e-12, mode=lt.TM_EIGS_MIXED)
     np.testing.assert_allclose(valsm, vals64, rtol=1e-10)
     assert infom["matvecs_f64"] < info64["matvecs_f64"]
+
+
+@pytest.mark.parametrize("L,ec,bj", [(12, 2, -0.4), (14, 0, -0.35), (16, 2, -0.6), (20, 2, -0.3)])
+def test_even_odd_negative_coupling(L, ec, bj):
+    """betaJ < 0 swaps the roles of the butterfly coefficients in the even/odd
+    engines (x0' = x1 + r x0): the FP64 and FP32 products against the oracle,
+    and the mixed solve (FP32 and double-float engines) against the FP64 one."""
+    torch = pytest.importorskip("torch")
+    oracle = pytest.importorskip("oracle.oracle")
+    op = lt.TMatOp("A", 2, 5, bj, 0.5, 0.0, L, 0.0, ec)
+    ref = oracle.OracleOp("A", 2, 5, bj, 0.5, 0.0, L, 0.0, ec)
+    x = seeded_input(op.rows(), 5)
+    yr = ref.perform_op(x)
+    assert rel_err(op.perform_op(x), yr) < 1e-12
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.empty_like(xd)
+    op.perform_op_dev(xd.data_ptr(), yd.data_ptr(), lt.TM_F32, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rel_err(yd.double().cpu().numpy(), yr) < 2e-5
+    nev = 3
+    vals64, _, _, _ = op.eigs(nev, tol=1e-12, mode=lt.TM_EIGS_F64)
+    valsm, _, _, infom = op.eigs(nev, tol=1e-12, mode=lt.TM_EIGS_MIXED)
+    np.testing.assert_allclose(valsm, vals64, rtol=1e-10)
+    assert infom["nconv"] == nev
