@@ -119,7 +119,7 @@ __device__ __forceinline__ T chain_init(const IO* __restrict__ x, const double* 
 // P: the nlb*2^L*2^NA buffer (in place).  first: tiles built from x; last:
 // y[r] = postc * post[r] * sum_{lb, aux} (one CTA loops the lastbit passes).
 template <class T, int ZB, class IO>
-__global__ void __launch_bounds__(256, 3) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3)) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
                                                     const double* __restrict__ pre, const uint32_t* __restrict__ smap,
                                                     IO* __restrict__ y, const double* __restrict__ post, double postc,
                                                     int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {
@@ -213,27 +213,43 @@ __global__ void __launch_bounds__(256, 3) chain_kernel(T* __restrict__ P, const 
           const int fl = lastst ? (lb >> 1) : (int)((r >> (2 * t + 3)) & 1);
           const int fr = lastst ? (lb & 1) : (int)((r >> (2 * t + 2)) & 1);
           const T* vf = vt + ((fl << 1) | fr) * 16;
-          T in[4][4], out[4][4];
+          T in[4][4];
 #pragma unroll
           for (int q = 0; q < 4; ++q)
 #pragma unroll
             for (int sp = 0; sp < 4; ++sp) in[q][sp] = sm[spad(ebase | q | (sp << sb))];
+          if constexpr (sizeof(T) == 4) {
+            // every input is read before any output is written, so each
+            // output is stored as soon as it is formed (fewer live registers)
 #pragma unroll
-          for (int sv = 0; sv < 4; ++sv) {
-            const T w0 = wt[sv * 4], w1 = wt[sv * 4 + 1], w2 = wt[sv * 4 + 2], w3 = wt[sv * 4 + 3];
+            for (int aux = 0; aux < 4; ++aux)
 #pragma unroll
-            for (int aux = 0; aux < 4; ++aux) {
-              T d = in[0][aux] * w0;
-              d += in[1][aux] * w1;
-              d += in[2][aux] * w2;
-              d += in[3][aux] * w3;
-              out[aux][sv] = vf[aux * 4 + sv] * d;
+              for (int sv = 0; sv < 4; ++sv) {
+                T d = in[0][aux] * wt[sv * 4];
+                d += in[1][aux] * wt[sv * 4 + 1];
+                d += in[2][aux] * wt[sv * 4 + 2];
+                d += in[3][aux] * wt[sv * 4 + 3];
+                sm[spad(ebase | aux | (sv << sb))] = vf[aux * 4 + sv] * d;
+              }
+          } else {
+            T out[4][4];
+#pragma unroll
+            for (int sv = 0; sv < 4; ++sv) {
+              const T w0 = wt[sv * 4], w1 = wt[sv * 4 + 1], w2 = wt[sv * 4 + 2], w3 = wt[sv * 4 + 3];
+#pragma unroll
+              for (int aux = 0; aux < 4; ++aux) {
+                T d = in[0][aux] * w0;
+                d += in[1][aux] * w1;
+                d += in[2][aux] * w2;
+                d += in[3][aux] * w3;
+                out[aux][sv] = vf[aux * 4 + sv] * d;
+              }
             }
+#pragma unroll
+            for (int aux = 0; aux < 4; ++aux)
+#pragma unroll
+              for (int sv = 0; sv < 4; ++sv) sm[spad(ebase | aux | (sv << sb))] = out[aux][sv];
           }
-#pragma unroll
-          for (int aux = 0; aux < 4; ++aux)
-#pragma unroll
-            for (int sv = 0; sv < 4; ++sv) sm[spad(ebase | aux | (sv << sb))] = out[aux][sv];
         }
       }
       __syncthreads();
