@@ -301,13 +301,15 @@ __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int
 
 // elements per batch of the output loops (independent loads in flight per thread)
 constexpr int kOutBatch = 8;
+// elements per chunk of the gather loops
+constexpr int kGatherChunk = 16;
 
 // pass 1: w1(t, e) = (Th_E v)[(e, o_rep(t))],  v[(e,o_rep)] = u[map1[t][P]]
 // where P runs over the iteration order of e (it_e).  CTA `rank` of the
 // cluster owns the e with top c bits = rank, iteration positions
 // [rank*2^n, (rank+1)*2^n).  (InT: element type of u, the same size as T;
 // T: arithmetic / storage type of the tile and w1)
-template <class T, int KB, class InT>
+template <class T, int KB, class InT, bool CL>
 __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restrict__ u,
                                                     const uint32_t* __restrict__ map1,
                                                     const uint16_t* __restrict__ it_e,
@@ -317,7 +319,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   cg::cluster_group cl = cg::this_cluster();
-  const int rank = (A.c > 0) ? (int)cl.block_rank() : 0;
+  const int rank = CL ? (int)cl.block_rank() : 0;
   const int64_t tile = blockIdx.x >> A.c;
   const int n = A.n, p = A.p;
   const int kb = n - p;
@@ -327,27 +329,32 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   // gather the tile: index loads, then one asynchronous copy per element.
   // A warp's elements are one or two symmetry classes of e, whose orbits sit
   // in a few contiguous runs of u.
+  // (in chunks of kGatherChunk per thread: the copies are asynchronous, so
+  // the chunks overlap while holding fewer registers)
   {
-    uint32_t idx[1 << KB];
-    uint16_t ev[1 << KB];
 #pragma unroll
-    for (int i = 0; i < (1 << KB); ++i) {
-      if (i < (1 << kb)) {
-        const uint32_t P = base + threadIdx.x + (i << p);
-        idx[i] = __ldg(mrow + P);
-        ev[i] = __ldg(it_e + P);
+    for (int c0 = 0; c0 < (1 << KB); c0 += kGatherChunk) {
+      uint32_t idx[kGatherChunk];
+      uint16_t ev[kGatherChunk];
+#pragma unroll
+      for (int i = 0; i < kGatherChunk; ++i) {
+        if (c0 + i < (1 << kb)) {
+          const uint32_t P = base + threadIdx.x + ((c0 + i) << p);
+          idx[i] = __ldg(mrow + P);
+          ev[i] = __ldg(it_e + P);
+        }
       }
-    }
 #pragma unroll
-    for (int i = 0; i < (1 << KB); ++i)
-      if (i < (1 << kb)) cp_async_elem<sizeof(T)>(sm + spad(ev[i] & lmask), u + idx[i]);
+      for (int i = 0; i < kGatherChunk; ++i)
+        if (c0 + i < (1 << kb)) cp_async_elem<sizeof(T)>(sm + spad(ev[i] & lmask), u + idx[i]);
+    }
     cp_async_wait_all();
     if constexpr (!std::is_same<T, InT>::value) {
       // each thread converts the elements it copied
 #pragma unroll
       for (int i = 0; i < (1 << KB); ++i) {
         if (i < (1 << kb)) {
-          T* slot = sm + spad(ev[i] & lmask);
+          T* slot = sm + spad(__ldg(it_e + base + threadIdx.x + (i << p)) & lmask);
           *slot = T(*reinterpret_cast<const InT*>(slot));
         }
       }
@@ -355,7 +362,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A, n);
-  if (A.c > 0) cluster_reduce<T, KB>(cl, sm, rank, A);
+  if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A);
   // Output.  w1 is class-major: the block of e-class C holds, for each tile,
   // the |C| values of C's members, so a warp writes a few contiguous runs.
   for (int k0 = 0; k0 < (1 << kb); k0 += kOutBatch) {
@@ -385,7 +392,7 @@ enum { kOutF32 = 0, kOutF64 = 1, kOutDF = 2 };
 // (act_e(g, e_rep), o_rep) with act_o(g, o) = o_rep.  CTA `rank` owns the o
 // with top c bits = rank (iteration positions of it_o as in pass 1).
 // (OutT: element type of y)
-template <class T, int KB, int OSC, class OutT>
+template <class T, int KB, int OSC, class OutT, bool CL>
 __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restrict__ w1,
                                                     const uint16_t* __restrict__ it_o,
                                                     const uint32_t* __restrict__ t2,
@@ -403,7 +410,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
   T* sm = reinterpret_cast<T*>(smem_raw);
   __shared__ uint32_t he[128];
   cg::cluster_group cl = cg::this_cluster();
-  const int rank = (A.c > 0) ? (int)cl.block_rank() : 0;
+  const int rank = CL ? (int)cl.block_rank() : 0;
   const int64_t tile = blockIdx.x >> A.c;
   const int n = A.n, p = A.p;
   const int kb = n - p;
@@ -416,26 +423,29 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
     he[g] = hb * (uint32_t)A.n_orep + (__ldg(cf_e + act_e(g, e_rep, A.m)) - hb);
   __syncthreads();
   {
-    uint32_t code[1 << KB];
-    uint16_t ov[1 << KB];
 #pragma unroll
-    for (int i = 0; i < (1 << KB); ++i) {
-      if (i < (1 << kb)) {
-        const uint32_t P = base + threadIdx.x + (i << p);
-        code[i] = __ldg(t2 + P);
-        ov[i] = __ldg(it_o + P);
+    for (int c0 = 0; c0 < (1 << KB); c0 += kGatherChunk) {
+      uint32_t code[kGatherChunk];
+      uint16_t ov[kGatherChunk];
+#pragma unroll
+      for (int i = 0; i < kGatherChunk; ++i) {
+        if (c0 + i < (1 << kb)) {
+          const uint32_t P = base + threadIdx.x + ((c0 + i) << p);
+          code[i] = __ldg(t2 + P);
+          ov[i] = __ldg(it_o + P);
+        }
       }
-    }
 #pragma unroll
-    for (int i = 0; i < (1 << KB); ++i)
-      if (i < (1 << kb))
-        cp_async_elem<sizeof(T)>(sm + spad(ov[i] & lmask),
-                                 w1 + he[code[i] & 255u] + (int64_t)(code[i] >> 8) * hs);
+      for (int i = 0; i < kGatherChunk; ++i)
+        if (c0 + i < (1 << kb))
+          cp_async_elem<sizeof(T)>(sm + spad(ov[i] & lmask),
+                                   w1 + he[code[i] & 255u] + (int64_t)(code[i] >> 8) * hs);
+    }
     cp_async_wait_all();
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A, n);
-  if (A.c > 0) cluster_reduce<T, KB>(cl, sm, rank, A);
+  if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A);
   // Designated outputs of this tile.  They are ordered like it_o, so the
   // outputs whose o this CTA holds form one contiguous range: groups
   // [rank, rank + 1) * 2^(ct - c) of the tile's 2^ct output groups.
@@ -928,7 +938,7 @@ template <class T, int KB>
 void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, const EOPlan& P, T* w1,
                   cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
-  auto kfn = eo_pass1<T, KB, typename EoIO<T>::In>;
+  auto kfn = (A.c > 0) ? eo_pass1<T, KB, typename EoIO<T>::In, true> : eo_pass1<T, KB, typename EoIO<T>::In, false>;
   raise_smem_limit((const void*)kfn, shm);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
@@ -950,7 +960,7 @@ template <class T, int KB, int OSC, class OutT = typename EoIO<T>::Out>
 void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, const double* sout64,
                   const float* sout32, const dfloat* soutdf, double post, OutT* y, cudaStream_t s) {
   size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(T);
-  auto kfn = eo_pass2<T, KB, OSC, OutT>;
+  auto kfn = (A.c > 0) ? eo_pass2<T, KB, OSC, OutT, true> : eo_pass2<T, KB, OSC, OutT, false>;
   raise_smem_limit((const void*)kfn, shm);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ntiles << A.c));
@@ -1069,7 +1079,7 @@ void eo_dispatch_dd(const Op& op, const EOArgs& A, const dfloat* x, dfloat* y, c
   eo_scale_in_dd<<<grid_for(R), 256, 0, s>>>(x, op.sindf.as<dfloat>(), u, R);
   TM_CKK("eo_scale_in_dd");
   const size_t shm = (size_t)((1 << A.n) + (1 << A.n) / 32 + 1) * sizeof(dfloat);
-  auto k1 = eo_pass1<dfloat, KB, dfloat>;
+  auto k1 = (A.c > 0) ? eo_pass1<dfloat, KB, dfloat, true> : eo_pass1<dfloat, KB, dfloat, false>;
   raise_smem_limit((const void*)k1, shm);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(P.n_orep << A.c));
