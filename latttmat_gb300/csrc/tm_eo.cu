@@ -313,8 +313,7 @@ template <class T, int KB, class InT, bool CL>
 __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restrict__ u,
                                                     const uint32_t* __restrict__ map1,
                                                     const uint16_t* __restrict__ it_e,
-                                                    const uint32_t* __restrict__ wbase,
-                                                    const uint8_t* __restrict__ wsz, T* __restrict__ w1) {
+                                                    const uint2* __restrict__ wout, T* __restrict__ w1) {
   static_assert(sizeof(T) == sizeof(InT), "u and the tile share the element size");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
@@ -372,9 +371,10 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
     for (int q = 0; q < kOutBatch; ++q) {
       if (k0 + q < (1 << kb)) {
         const uint32_t P = base + threadIdx.x + ((k0 + q) << p);
-        ev[q] = __ldg(it_e + P);
-        wb[q] = __ldg(wbase + P);
-        ws[q] = __ldg(wsz + P);
+        const uint2 w = __ldg(wout + P);  // (w1 offset, it_e | class size << 16)
+        wb[q] = w.x;
+        ev[q] = (uint16_t)(w.y & 0xffffu);
+        ws[q] = w.y >> 16;
       }
     }
 #pragma unroll
@@ -394,8 +394,7 @@ enum { kOutF32 = 0, kOutF64 = 1, kOutDF = 2 };
 // (OutT: element type of y)
 template <class T, int KB, int OSC, class OutT, bool CL>
 __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restrict__ w1,
-                                                    const uint16_t* __restrict__ it_o,
-                                                    const uint32_t* __restrict__ t2,
+                                                    const uint2* __restrict__ t2o,
                                                     const uint16_t* __restrict__ cf_e,
                                                     const uint32_t* __restrict__ erep,
                                                     const uint32_t* __restrict__ cls_start,
@@ -431,8 +430,9 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
       for (int i = 0; i < kGatherChunk; ++i) {
         if (c0 + i < (1 << kb)) {
           const uint32_t P = base + threadIdx.x + ((c0 + i) << p);
-          code[i] = __ldg(t2 + P);
-          ov[i] = __ldg(it_o + P);
+          const uint2 w = __ldg(t2o + P);  // (t2 code, it_o)
+          code[i] = w.x;
+          ov[i] = (uint16_t)w.y;
         }
       }
 #pragma unroll
@@ -813,10 +813,7 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   d_olist.alloc(olist.size() * 4);
   d_einfo.alloc(M * 4);
   d_pos_o.alloc(M * 2);
-  P.t2.alloc(M * 4);
   P.it_e.alloc(M * 2);
-  P.wbase.alloc(M * 4);
-  P.wsz.alloc(M);
   P.cls_start.alloc(cls_start.size() * 4);
   P.cls_size.alloc(cls_size.size() * 4);
   P.cf_e.alloc(M * 2);
@@ -825,14 +822,25 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   TM_CK(cudaMemcpyAsync(d_olist.p, olist.data(), olist.size() * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_einfo.p, H.einfo.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(d_pos_o.p, h_pos_o.data(), M * 2, cudaMemcpyHostToDevice, s));
-  TM_CK(cudaMemcpyAsync(P.t2.p, t2.data(), M * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.it_e.p, h_it_e.data(), M * 2, cudaMemcpyHostToDevice, s));
-  TM_CK(cudaMemcpyAsync(P.wbase.p, h_wbase.data(), M * 4, cudaMemcpyHostToDevice, s));
-  TM_CK(cudaMemcpyAsync(P.wsz.p, h_wsz.data(), M, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.cls_start.p, cls_start.data(), cls_start.size() * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.cls_size.p, cls_size.data(), cls_size.size() * 4, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.cf_e.p, h_cf_e.data(), M * 2, cudaMemcpyHostToDevice, s));
   TM_CK(cudaMemcpyAsync(P.it_o.p, h_it_o.data(), M * 2, cudaMemcpyHostToDevice, s));
+  {
+    // per-position pairs read together by the passes
+    std::vector<uint32_t> wo(2 * (size_t)M), to(2 * (size_t)M);
+    for (uint32_t i = 0; i < M; ++i) {
+      wo[2 * i] = h_wbase[i];
+      wo[2 * i + 1] = (uint32_t)h_it_e[i] | ((uint32_t)h_wsz[i] << 16);
+      to[2 * i] = t2[i];
+      to[2 * i + 1] = h_it_o[i];
+    }
+    P.wout.alloc((size_t)M * 8);
+    P.t2o.alloc((size_t)M * 8);
+    TM_CK(cudaMemcpyAsync(P.wout.p, wo.data(), (size_t)M * 8, cudaMemcpyHostToDevice, s));
+    TM_CK(cudaMemcpyAsync(P.t2o.p, to.data(), (size_t)M * 8, cudaMemcpyHostToDevice, s));
+  }
   TM_CK(cudaMemcpyAsync(P.erep.p, elist.data(), elist.size() * 4, cudaMemcpyHostToDevice, s));
 
   const int64_t R = op.n;
@@ -952,8 +960,7 @@ void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, co
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(), P.wbase.as<uint32_t>(),
-                           P.wsz.as<uint8_t>(), w1));
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(), P.wout.as<uint2>(), w1));
 }
 
 template <class T, int KB, int OSC, class OutT = typename EoIO<T>::Out>
@@ -974,7 +981,7 @@ void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, con
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.it_o.as<uint16_t>(), P.t2.as<uint32_t>(), P.cf_e.as<uint16_t>(),
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.t2o.as<uint2>(), P.cf_e.as<uint16_t>(),
                            P.erep.as<uint32_t>(), P.cls_start.as<uint32_t>(), P.cls_size.as<uint32_t>(),
                            P.out_off.as<uint32_t>(), P.out_o.as<uint16_t>(), sout64, sout32, soutdf, post, y));
 }
@@ -1094,7 +1101,7 @@ void eo_dispatch_dd(const Op& op, const EOArgs& A, const dfloat* x, dfloat* y, c
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   TM_CK(cudaLaunchKernelEx(&cfg, k1, A, (const dfloat*)u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(),
-                           P.wbase.as<uint32_t>(), P.wsz.as<uint8_t>(), w1));
+                           P.wout.as<uint2>(), w1));
   TM_CKK("eo_pass1_dd");
   launch_pass2<dfloat, KB, kOutDF, dfloat>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(),
                                            op.soutdf.as<dfloat>(), 1.0, y, s);

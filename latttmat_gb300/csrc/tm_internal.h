@@ -98,11 +98,11 @@ struct EOPlan {
   int ng = 0;         // H elements enumerated
   DBuf map1;          // u32 [n_orep][2^m]: pi-index of the orbit of (it_e[P], o_rep)
   DBuf it_e;          // u16 [2^m]: e at each pass-1 iteration position P
-  DBuf wbase, wsz;    // u32 / u8 [2^m]: w1 offset of (tile 0, it_e[P]) and the size of its e-class
   DBuf cls_start, cls_size;  // u32 [n_erep]: class-first start and size of each e-class
+  DBuf wout;          // uint2 [2^m]: (w1 offset of (tile 0, it_e[P]), it_e[P] | e-class size << 16)
+  DBuf t2o;           // uint2 [2^m]: ((o-tile << 8) | H element g, it_o[P]) per pass-2 position
   DBuf cf_e;          // u16 [2^m]: class-first position of each e
   DBuf it_o;          // u16 [2^m]: o at each pass-2 iteration position
-  DBuf t2;            // u32 [2^m]: (o-tile << 8) | g for it_o[P]: its pass-1 tile and H element
   DBuf erep;          // u32 [n_erep]: e representative of each pass-2 tile
   DBuf out_off;       // u32 [n_erep*2^ct+1]: designated-output offsets per tile and top-ct-bit group
   DBuf out_o;         // u16 [R]: o of each designated output (pi order)
