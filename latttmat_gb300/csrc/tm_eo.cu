@@ -189,27 +189,40 @@ __device__ __forceinline__ void cp_async_elem<8>(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// butterflies on local bits [0, nbits) of the shared-memory tile, KB bits per round
-template <class T, int KB>
-__device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A, int nbits) {
-  const T r = coef_r<T>(A);
-  const int n = A.n;
-  for (int g0 = 0; g0 < nbits; g0 += KB) {
-    const int gs = min(KB, nbits - g0);
-    const int nfree = 1 << (n - gs);
-    for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
-      int j0 = (f & ((1 << g0) - 1)) | ((f >> g0) << (g0 + gs));
-      T v[1 << KB];
+// Tile bits covered by the unrolled butterfly rounds (the largest tile is
+// 2^15 elements in FP32 and 2^14 in 8-byte types).
+constexpr int kMaxTileBits = 16;
+
+// One butterfly round on local bits [G0, G0 + gs) of the shared-memory tile.
+// G0 is a compile-time constant, so each of a thread's 2^KB slots is the
+// thread's base slot plus a constant: j0 and i << G0 have disjoint bits, and
+// spad(a | b) = spad(a) + spad(b) for disjoint a, b (no carry reaches bit 5).
+template <class T, int KB, int G0>
+__device__ __forceinline__ void smem_round(T* sm, int n, int gs, T r, int swap) {
+  const int nfree = 1 << (n - gs);
+  for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
+    const int j0 = (f & ((1 << G0) - 1)) | ((f >> G0) << (G0 + gs));
+    T* b = sm + spad(j0);
+    T v[1 << KB];
 #pragma unroll
-      for (int i = 0; i < (1 << KB); ++i)
-        if (i < (1 << gs)) v[i] = sm[spad(j0 | (i << g0))];
-      reg_bfly<T, KB>(v, gs, r, A.swap);
+    for (int i = 0; i < (1 << KB); ++i)
+      if (i < (1 << gs)) v[i] = b[spad(i << G0)];
+    reg_bfly<T, KB>(v, gs, r, swap);
 #pragma unroll
-      for (int i = 0; i < (1 << KB); ++i)
-        if (i < (1 << gs)) sm[spad(j0 | (i << g0))] = v[i];
-    }
-    __syncthreads();
+    for (int i = 0; i < (1 << KB); ++i)
+      if (i < (1 << gs)) b[spad(i << G0)] = v[i];
   }
+}
+
+// butterflies on local bits [0, nbits) of the shared-memory tile, KB bits per
+// round (nbits <= kMaxTileBits)
+template <class T, int KB, int R = 0>
+__device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A, int nbits) {
+  constexpr int G0 = R * KB;
+  if (G0 >= nbits) return;
+  smem_round<T, KB, G0>(sm, A.n, min(KB, nbits - G0), coef_r<T>(A), A.swap);
+  __syncthreads();
+  if constexpr ((R + 1) * KB < kMaxTileBits) smem_rounds<T, KB, R + 1>(sm, A, nbits);
 }
 
 // acc += c * v over the 16 / sizeof(T) elements of a 16-byte chunk
@@ -993,6 +1006,7 @@ EOArgs make_args(const Op& op, int c) {
   A.c = c;
   A.ct = op.eo.ct;
   A.n = A.m - c;
+  if (A.n > kMaxTileBits) fail(TM_ERR_LIMIT, "even/odd tile larger than 2^16 elements");
   const int KB = (sizeof(T) == 8) ? 4 : 5;
   int kb = std::min(KB, std::max(1, A.n - 5));
   A.p = A.n - kb;

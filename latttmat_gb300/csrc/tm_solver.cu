@@ -592,6 +592,8 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const dfloat* __restric
       x0[c] = x1[c] = a0[c] = a1[c] = dfloat(0.f, 0.f);
       xs[c] = axs[c] = make_float2(0.f, 0.f);
     }
+    // unrolled so that several columns' loads are in flight per thread
+#pragma unroll 4
     for (int j = 0; j < nx; ++j) {
       dfloat xa, xb, aa, ab;
       ld2(X0 + (int64_t)j * ld, i, xa, xb);
@@ -606,6 +608,7 @@ __global__ void __launch_bounds__(256) ritz_resid_kernel(const dfloat* __restric
           a1[c] = df_fma(ab, y, a1[c]);
         }
     }
+#pragma unroll 4
     for (int j = nx; j < nb; ++j) {
       const float2 bv = reinterpret_cast<const float2*>(B32 + (int64_t)j * ld)[i];
       const float2 abv = reinterpret_cast<const float2*>(AB32 + (int64_t)j * ld)[i];
