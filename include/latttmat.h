@@ -44,7 +44,9 @@ enum {
 };
 
 /* TM_F64_DF: FP64 values computed in double-float (FP32 pair) arithmetic,
- * the solver's refinement product; accepted by tm_profile_matvec. */
+ * the solver's refinement product: FP64 accuracy (relative error ~1e-14 per
+ * product) on the FP32 pipes, for the even/odd x-ANNNI and aux-bit (DNNI,
+ * BNNNI) operators; other operators compute it in native FP64. */
 typedef enum { TM_F64 = 0, TM_F32 = 1, TM_F64_DF = 2 } tm_dtype;
 
 /* Model parameters; mirrors MParameter (TMat/commondef.hpp:18-24).  For dim=3
@@ -115,9 +117,10 @@ int64_t tm_matvec_count(const tm_op* op);  /* OpCounter::get() (TMat/utility.hpp
  * (TMat/tmat.hpp:89).  Copies in, computes in FP64 on the GPU, copies out. */
 tm_status tm_perform_op(const tm_op* op, const double* x_host, double* y_host);
 
-/* y = T x on device buffers (dtype TM_F64 or TM_F32, length cols()), on the
- * given CUDA stream (cudaStream_t, or NULL for the library's stream).
- * Asynchronous with respect to the host. */
+/* y = T x on device buffers (dtype TM_F64, TM_F32 or TM_F64_DF; length
+ * cols()), on the given CUDA stream (cudaStream_t, or NULL for the library's
+ * stream).  TM_F64_DF buffers hold doubles.  Asynchronous with respect to the
+ * host. */
 tm_status tm_perform_op_dev(const tm_op* op, const void* x_dev, void* y_dev, tm_dtype dtype,
                             void* stream);
 

@@ -199,9 +199,18 @@ double apply_internal(const Op& op, const double* x, double* y, const float* x32
 void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStream_t s) {
   const Op& base = op.parent ? *op.parent : op;
   const int64_t n = base.n;
+  const bool aux_df = base.kind == K_XDT || base.kind == K_XDM || base.kind == K_ZBT || base.kind == K_ZBM;
+  // TM_F64_DF: FP64 values in double-float arithmetic where an engine for it
+  // exists (even/odd and aux-bit operators), native FP64 otherwise
+  if (dt == TM_F64_DF && !base.eo.active && !aux_df) dt = TM_F64;
   if (is_two_layer(base.kind)) {
     if (dt != TM_F64) fail(TM_ERR_UNSUPPORTED, "two-layer operators run in FP64 only");
     matvec_two_layer(op, (const double*)x, (double*)y, s);
+  } else if (dt == TM_F64_DF && !base.has_pi) {
+    if (base.eo.active)
+      matvec_eo_df(base, (const double*)x, (double*)y, s);
+    else
+      matvec_aux_df(op, (const double*)x, (double*)y, s);
   } else if (!base.has_pi) {
     if (dt == TM_F64) {
       if (base.eo.active) {
@@ -219,9 +228,12 @@ void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStr
     }
   } else {
     const uint32_t* pi = base.pi.as<uint32_t>();
-    if (dt == TM_F64) {
+    if (dt != TM_F32) {
       gather_f64((const double*)x, pi, base.xp.as<double>(), n, s);
-      matvec_eo<double>(base, base.xp.as<double>(), base.yp.as<double>(), false, s);
+      if (dt == TM_F64_DF)
+        matvec_eo_df(base, base.xp.as<double>(), base.yp.as<double>(), s);
+      else
+        matvec_eo<double>(base, base.xp.as<double>(), base.yp.as<double>(), false, s);
       scatter_f64(base.yp.as<double>(), pi, (double*)y, n, s);
     } else {
       gather_f32((const float*)x, pi, base.xp.as<float>(), n, s);
@@ -534,7 +546,7 @@ tm_status tm_perform_op(const tm_op* op, const double* x, double* y) {
 tm_status tm_perform_op_dev(const tm_op* op, const void* x, void* y, tm_dtype dt, void* stream) {
   TM_API_BEGIN
   if (!op || !x || !y) fail(TM_ERR_ARG, "null argument");
-  if (dt != TM_F64 && dt != TM_F32) fail(TM_ERR_ARG, "dtype must be TM_F64 or TM_F32");
+  if (dt != TM_F64 && dt != TM_F32 && dt != TM_F64_DF) fail(TM_ERR_ARG, "unknown dtype");
   Op& o = *op->impl;
   const Op& b = o.parent ? *o.parent : o;
   cudaStream_t s = stream ? (cudaStream_t)stream : b.stream;

@@ -58,6 +58,25 @@ __device__ __forceinline__ dfloat df_fma(dfloat a, dfloat b, dfloat c) {
   return df_renorm(s, se);
 }
 
+// df_fma without the final renormalisation: hi + lo still carries the exact
+// TwoSum error, but |lo| may exceed ulp(hi)/2 by a few ulps.  For chains of
+// a few such steps (the butterfly levels of one round) followed by df_norm;
+// the operands' lo enter only as correction terms, so accuracy is unchanged
+// up to a few units of 2^-48.
+__device__ __forceinline__ dfloat df_fma_unnorm(dfloat a, dfloat b, dfloat c) {
+  float p = a.hi * b.hi;
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  float s = p + c.hi;
+  float bb = s - p;
+  float se = (p - (s - bb)) + (c.hi - bb);
+  se += pe + c.lo;
+  return dfloat(s, se);
+}
+
+__device__ __forceinline__ dfloat df_norm(dfloat a) { return df_renorm(a.hi, a.lo); }
+
 __device__ __forceinline__ dfloat& operator+=(dfloat& a, dfloat b) {
   a = a + b;
   return a;

@@ -137,7 +137,7 @@ __device__ __forceinline__ dfloat coef_r<dfloat>(const EOArgs& A) { return dfloa
 // r * x + y in the engine's arithmetic
 __device__ __forceinline__ float fma_t(float r, float x, float y) { return fmaf(r, x, y); }
 __device__ __forceinline__ double fma_t(double r, double x, double y) { return fma(r, x, y); }
-__device__ __forceinline__ dfloat fma_t(dfloat r, dfloat x, dfloat y) { return df_fma(r, x, y); }
+__device__ __forceinline__ dfloat fma_t(dfloat r, dfloat x, dfloat y) { return df_fma_unnorm(r, x, y); }
 
 // in-register butterflies over the 2^NB elements held by one thread
 template <class T, int NB>
@@ -208,6 +208,11 @@ __device__ __forceinline__ void smem_round(T* sm, int n, int gs, T r, int swap) 
     for (int i = 0; i < (1 << KB); ++i)
       if (i < (1 << gs)) v[i] = b[spad(i << G0)];
     reg_bfly<T, KB>(v, gs, r, swap);
+    if constexpr (std::is_same<T, dfloat>::value) {
+      // the double-float levels skip renormalisation; once per round here
+#pragma unroll
+      for (int i = 0; i < (1 << KB); ++i) v[i] = df_norm(v[i]);
+    }
 #pragma unroll
     for (int i = 0; i < (1 << KB); ++i)
       if (i < (1 << gs)) b[spad(i << G0)] = v[i];

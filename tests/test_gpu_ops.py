@@ -1,7 +1,7 @@
 """GPU parity: operators through the C ABI against the reference's own outputs.
 
-Bars: orbit tables bit-exact; FP64 matvec within 1e-12 of the reference
-(relative to max|y|); FP32 device matvec within 2e-5; eigenvalues within
+Bars: orbit tables bit-exact; FP64 matvec (native or double-float) within
+1e-12 of the reference (relative to max|y|); FP32 device matvec within 2e-5; eigenvalues within
 1e-10 relative of the reference (ARPACK on the reference perform_op).
 """
 import numpy as np
@@ -75,6 +75,38 @@ def test_matvec_fp32_device(name):
     op.perform_op_dev(xd64.data_ptr(), yd64.data_ptr(), lt.TM_F64, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert rel_err(yd64.cpu().numpy(), ref) < 1e-12
+
+
+@pytest.mark.parametrize("name", case_names(["xat", "xam", "x3d", "xdt", "xdm", "zbt", "zbm"]))
+def test_matvec_double_float_device(name):
+    """TM_F64_DF device product (double-float engines for the even/odd and
+    aux-bit operators, native FP64 for the rest) within the FP64 bar, for
+    the operator and, where it has one, its transpose."""
+    torch = pytest.importorskip("torch")
+    f = fixture(name)
+    op = _skip_if_unavailable(lambda: make_op(name))
+    n = op.rows()
+    x = seeded_input(n, 1)
+
+    def dev_df(o):
+        xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+        yd = torch.empty_like(xd)
+        o.perform_op_dev(xd.data_ptr(), yd.data_ptr(), lt.TM_F64_DF, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return yd.cpu().numpy()
+
+    y = dev_df(op)
+    if "y" in f:
+        assert rel_err(y, f["y"]) < 1e-12
+    w = checksum_weights(n)
+    np.testing.assert_allclose([np.dot(w, y), np.linalg.norm(y)], f["y_chk"], rtol=1e-12)
+    try:
+        t = op.get_t_instance()
+    except lt.TMError as e:
+        if e.code == lt.TM_ERR_NOTRANSPOSE:
+            return
+        raise
+    assert rel_err(dev_df(t), t.perform_op(x)) < 1e-12
 
 
 @pytest.mark.parametrize("name", case_names(["yat", "y2at", "yam", "ybm"]))
@@ -176,6 +208,11 @@ def test_even_odd_negative_coupling(L, ec, bj):
     op.perform_op_dev(xd.data_ptr(), yd.data_ptr(), lt.TM_F32, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert rel_err(yd.double().cpu().numpy(), yr) < 2e-5
+    xd64 = torch.tensor(x, dtype=torch.float64, device="cuda")
+    yd64 = torch.empty_like(xd64)
+    op.perform_op_dev(xd64.data_ptr(), yd64.data_ptr(), lt.TM_F64_DF, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rel_err(yd64.cpu().numpy(), yr) < 1e-12
     nev = 3
     vals64, _, _, _ = op.eigs(nev, tol=1e-12, mode=lt.TM_EIGS_F64)
     valsm, _, _, infom = op.eigs(nev, tol=1e-12, mode=lt.TM_EIGS_MIXED)
