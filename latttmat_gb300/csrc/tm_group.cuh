@@ -196,6 +196,32 @@ __device__ __forceinline__ bool rep_candidate_x2d32(uint32_t s, int L, int flip)
   return true;
 }
 
+// true iff y has a (non-cyclic) run of ones of length >= k (1 <= k <= 32)
+__device__ __forceinline__ bool has_run_linear32(uint32_t y, int k) {
+  uint32_t t = y;
+  int len = 1;
+  while (2 * len <= k) {
+    t &= t >> len;
+    len *= 2;
+  }
+  if (k > len) t &= t >> (k - len);
+  return t != 0;
+}
+
+// The 32 states w*32 + b (b < 32) share bits [5, L), and for w > 0 their
+// leading-zero count z.  A run of more than z zeros inside those bits (or,
+// with the spin flip, of more than z ones) fails rep_candidate_x2d32 for every
+// state of the word, so the word holds no representative.
+__device__ __forceinline__ bool word_rejected_x2d32(uint64_t w, int L, int flip) {
+  if (w == 0 || L <= 6) return false;
+  const uint32_t up = (uint32_t)(w << 5);  // w < 2^(L-5), so this fits in L bits
+  const int z = __clz(up) - (32 - L);
+  if (z + 1 > L - 5) return false;
+  const uint32_t umask = ((L == 32) ? 0xffffffffu : ((1u << L) - 1u)) & ~31u;
+  if (has_run_linear32(~up & umask, z + 1)) return true;
+  return flip && has_run_linear32(up & umask, z + 1);
+}
+
 // s is its orbit's minimum (the whole group list, as is_rep)
 __device__ __forceinline__ bool warp_is_rep_x2d32(uint32_t s, int L, int flip) {
   const int lane = threadIdx.x & 31;

@@ -134,49 +134,75 @@ __global__ void rep_bits_kernel(GroupDev g, uint64_t nstate, uint32_t* bits, uin
   }
 }
 
-// X-2D periodic group, L <= 32: a cheap necessary test per lane, then each
-// candidate of the word tested by the whole warp (one rotation per lane), so
-// the lanes do not wait on one another's early exits.
+// Representative bitset for the periodic X-2D group, L <= 32.  A warp takes
+// 32 consecutive words: words that word_rejected_x2d32 rules out cost a few
+// uniform operations; in the others each lane tests one state against the
+// necessary condition and the warp checks the survivors one by one, a lane
+// per group element.  Lane j stores word j, so the stores coalesce.
 __global__ void rep_bits_x2d32_kernel(int L, int flip, uint64_t nstate, uint32_t* bits, uint32_t* cnt,
                                       int64_t nwords) {
   const int lane = threadIdx.x & 31;
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = warp; w < nwords; w += nwarps) {
-    const uint64_t s = (uint64_t)w * 32 + lane;
-    uint32_t cand = __ballot_sync(0xffffffffu, s < nstate && rep_candidate_x2d32((uint32_t)s, L, flip));
-    uint32_t word = 0;
-    while (cand) {
-      const int b = __ffs(cand) - 1;
-      cand &= cand - 1;
-      if (warp_is_rep_x2d32((uint32_t)(w * 32 + b), L, flip)) word |= 1u << b;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w0 = warp * 32; w0 < nwords; w0 += nwarps * 32) {
+    const int nw = (int)((nwords - w0 < 32) ? nwords - w0 : 32);
+    uint32_t mine = 0;
+    for (int j = 0; j < nw; ++j) {
+      const int64_t w = w0 + j;
+      if (word_rejected_x2d32((uint64_t)w, L, flip)) continue;
+      const uint64_t s = (uint64_t)w * 32 + lane;
+      uint32_t cand = __ballot_sync(0xffffffffu, s < nstate && rep_candidate_x2d32((uint32_t)s, L, flip));
+      uint32_t word = 0;
+      while (cand) {
+        const int b = __ffs(cand) - 1;
+        cand &= cand - 1;
+        if (warp_is_rep_x2d32((uint32_t)(w * 32 + b), L, flip)) word |= 1u << b;
+      }
+      if (lane == j) mine = word;
     }
-    if (lane == 0) {
-      bits[w] = word;
-      cnt[w] = __popc(word);
+    if (lane < nw) {
+      bits[w0 + lane] = mine;
+      cnt[w0 + lane] = __popc(mine);
     }
   }
 }
 
-// compaction with warp-cooperative orbit sizes (X-2D periodic, L <= 32)
+// Compaction with warp-cooperative orbit sizes (X-2D periodic, L <= 32).  A
+// warp loads 32 words and their prefixes at once, then takes the non-empty
+// words one by one.  Lane k keeps the k-th representative's state and orbit
+// size, so each word's outputs are stored by consecutive lanes.
 __global__ void compact_x2d32_kernel(int L, int flip, const uint32_t* bits, const uint32_t* prefix,
                                      int64_t nwords, uint32_t* idx, uint16_t* dup) {
   const int lane = threadIdx.x & 31;
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = warp; w < nwords; w += nwarps) {
-    uint32_t word = bits[w];
-    uint32_t pos = prefix[w];
-    while (word) {
-      const int b = __ffs(word) - 1;
-      word &= word - 1;
-      const uint32_t s = (uint32_t)(w * 32 + b);
-      const int osz = warp_orbit_size_x2d32(s, L, flip);
-      if (lane == 0) {
-        idx[pos] = s;
-        dup[pos] = (uint16_t)osz;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w0 = warp * 32; w0 < nwords; w0 += nwarps * 32) {
+    const int64_t wl = w0 + lane;
+    const uint32_t word = (wl < nwords) ? bits[wl] : 0u;
+    const uint32_t pos = (wl < nwords) ? prefix[wl] : 0u;
+    uint32_t nz = __ballot_sync(0xffffffffu, word != 0);
+    while (nz) {
+      const int src = __ffs(nz) - 1;
+      nz &= nz - 1;
+      uint32_t wd = __shfl_sync(0xffffffffu, word, src);
+      const uint32_t p = __shfl_sync(0xffffffffu, pos, src);
+      const uint32_t sb = (uint32_t)((w0 + src) * 32);
+      uint32_t my_s = 0;
+      int my_o = 0, k = 0;
+      while (wd) {
+        const int b = __ffs(wd) - 1;
+        wd &= wd - 1;
+        const int osz = warp_orbit_size_x2d32(sb + (uint32_t)b, L, flip);
+        if (lane == k) {
+          my_s = sb + (uint32_t)b;
+          my_o = osz;
+        }
+        ++k;
       }
-      ++pos;
+      if (lane < k) {
+        idx[p + lane] = my_s;
+        dup[p + lane] = (uint16_t)my_o;
+      }
     }
   }
 }
