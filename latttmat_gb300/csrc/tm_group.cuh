@@ -222,34 +222,55 @@ __device__ __forceinline__ bool word_rejected_x2d32(uint64_t w, int L, int flip)
   return flip && has_run_linear32(up & umask, z + 1);
 }
 
-// s is its orbit's minimum (the whole group list, as is_rep)
-__device__ __forceinline__ bool warp_is_rep_x2d32(uint32_t s, int L, int flip) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
-  bool smaller = false;
-  if (lane < L) {
-    const uint32_t a = lane ? rotr_l32(s, L, lane, mask) : s;
-    const uint32_t b = __brev(a) >> (32 - L);
-    smaller = (a < s) || (b < s);
-    if (flip) smaller = smaller || ((~a & mask) < s) || ((~b & mask) < s);
+// Bit i set iff bits i .. i+k-1 (cyclic, L-bit word) of y are all ones;
+// every bit for k = 0.  (0 <= k < L)
+__device__ __forceinline__ uint32_t run_starts32(uint32_t y, int L, int k, uint32_t mask) {
+  if (k == 0) return mask;
+  uint32_t t = y;
+  int len = 1;
+  while (2 * len <= k) {
+    t &= rotr_l32(t, L, len, mask);
+    len *= 2;
   }
-  return __ballot_sync(0xffffffffu, smaller) == 0;
+  if (k > len) t &= rotr_l32(t, L, k - len, mask);
+  return t;
 }
 
-// orbit size: group order / number of list elements fixing s (as orbit_size)
-__device__ __forceinline__ int warp_orbit_size_x2d32(uint32_t s, int L, int flip) {
-  const int lane = threadIdx.x & 31;
+// One thread's exact test of s against the periodic X-2D group (L <= 32):
+// true iff no image of s is smaller, and then *fix = the number of group
+// elements fixing s (orbit size = group order / *fix).  An image no larger
+// than s starts with at least z zeros (z = s's leading zeros within L bits),
+// so only the rotations that bring a run of z zeros of s or of its mirror
+// image to the front -- or, for the flipped images, a run of z ones -- need a
+// comparison: rotation by k = i + z for each run start i.  Images equal to s
+// are among them too, so the same pass counts the stabiliser.
+__device__ __forceinline__ bool lane_rep_x2d32(uint32_t s, int L, int flip, int* fix) {
   const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
-  unsigned fix = 0;
-  if (lane < L) {
-    const uint32_t a = lane ? rotr_l32(s, L, lane, mask) : s;
-    const uint32_t b = __brev(a) >> (32 - L);
-    fix = (a == s) + (b == s);
-    if (flip) fix += ((~a & mask) == s) + ((~b & mask) == s);
+  if (s == 0) {
+    *fix = 2 * L;  // rotations and reflections; the flip moves 0 to the all-ones state
+    return true;
   }
-  fix = __reduce_add_sync(0xffffffffu, fix);
-  return (int)((2u * L * (flip ? 2u : 1u)) / fix);
+  const int z = __clz(s) - (32 - L);
+  const uint32_t r = __brev(s) >> (32 - L);
+  int f = 0;
+  for (int v4 = 0; v4 < (flip ? 4 : 2); ++v4) {
+    const uint32_t v = (v4 & 1) ? r : s;
+    const bool inv = v4 >= 2;
+    uint32_t t = run_starts32(inv ? v : (~v & mask), L, z, mask);
+    while (t) {
+      const int i = __ffs(t) - 1;
+      t &= t - 1;
+      const int k = (i + z >= L) ? i + z - L : i + z;
+      uint32_t a = k ? rotr_l32(v, L, k, mask) : v;
+      if (inv) a = ~a & mask;
+      if (a < s) return false;
+      f += (a == s);
+    }
+  }
+  *fix = f;
+  return true;
 }
+
 #endif
 
 TM_HD bool is_rep(const GroupDev& g, uint64_t s) {

@@ -135,10 +135,10 @@ __global__ void rep_bits_kernel(GroupDev g, uint64_t nstate, uint32_t* bits, uin
 }
 
 // Representative bitset for the periodic X-2D group, L <= 32.  A warp takes
-// 32 consecutive words: words that word_rejected_x2d32 rules out cost a few
-// uniform operations; in the others each lane tests one state against the
-// necessary condition and the warp checks the survivors one by one, a lane
-// per group element.  Lane j stores word j, so the stores coalesce.
+// 32 consecutive words, lane j screening word j with word_rejected_x2d32; in
+// each surviving word every lane tests its own state, first against the
+// necessary condition, then exactly (lane_rep_x2d32).  Lane j stores word j,
+// so the stores coalesce.
 __global__ void rep_bits_x2d32_kernel(int L, int flip, uint64_t nstate, uint32_t* bits, uint32_t* cnt,
                                       int64_t nwords) {
   const int lane = threadIdx.x & 31;
@@ -146,18 +146,17 @@ __global__ void rep_bits_x2d32_kernel(int L, int flip, uint64_t nstate, uint32_t
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t w0 = warp * 32; w0 < nwords; w0 += nwarps * 32) {
     const int nw = (int)((nwords - w0 < 32) ? nwords - w0 : 32);
+    uint32_t todo = __ballot_sync(0xffffffffu, lane < nw && !word_rejected_x2d32((uint64_t)(w0 + lane), L, flip));
     uint32_t mine = 0;
-    for (int j = 0; j < nw; ++j) {
+    while (todo) {
+      const int j = __ffs(todo) - 1;
+      todo &= todo - 1;
       const int64_t w = w0 + j;
-      if (word_rejected_x2d32((uint64_t)w, L, flip)) continue;
       const uint64_t s = (uint64_t)w * 32 + lane;
-      uint32_t cand = __ballot_sync(0xffffffffu, s < nstate && rep_candidate_x2d32((uint32_t)s, L, flip));
-      uint32_t word = 0;
-      while (cand) {
-        const int b = __ffs(cand) - 1;
-        cand &= cand - 1;
-        if (warp_is_rep_x2d32((uint32_t)(w * 32 + b), L, flip)) word |= 1u << b;
-      }
+      int fix;
+      const bool rep = s < nstate && rep_candidate_x2d32((uint32_t)s, L, flip) &&
+                       lane_rep_x2d32((uint32_t)s, L, flip, &fix);
+      const uint32_t word = __ballot_sync(0xffffffffu, rep);
       if (lane == j) mine = word;
     }
     if (lane < nw) {
@@ -167,15 +166,16 @@ __global__ void rep_bits_x2d32_kernel(int L, int flip, uint64_t nstate, uint32_t
   }
 }
 
-// Compaction with warp-cooperative orbit sizes (X-2D periodic, L <= 32).  A
-// warp loads 32 words and their prefixes at once, then takes the non-empty
-// words one by one.  Lane k keeps the k-th representative's state and orbit
-// size, so each word's outputs are stored by consecutive lanes.
+// Compaction with orbit sizes (X-2D periodic, L <= 32).  A warp loads 32
+// words and their prefixes at once, then takes the non-empty words one by
+// one, a lane per representative: lane b computes its state's stabiliser
+// count and stores at the word's offset plus its rank within the word.
 __global__ void compact_x2d32_kernel(int L, int flip, const uint32_t* bits, const uint32_t* prefix,
                                      int64_t nwords, uint32_t* idx, uint16_t* dup) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int order = 2 * L * (flip ? 2 : 1);
   for (int64_t w0 = warp * 32; w0 < nwords; w0 += nwarps * 32) {
     const int64_t wl = w0 + lane;
     const uint32_t word = (wl < nwords) ? bits[wl] : 0u;
@@ -184,24 +184,15 @@ __global__ void compact_x2d32_kernel(int L, int flip, const uint32_t* bits, cons
     while (nz) {
       const int src = __ffs(nz) - 1;
       nz &= nz - 1;
-      uint32_t wd = __shfl_sync(0xffffffffu, word, src);
+      const uint32_t wd = __shfl_sync(0xffffffffu, word, src);
       const uint32_t p = __shfl_sync(0xffffffffu, pos, src);
-      const uint32_t sb = (uint32_t)((w0 + src) * 32);
-      uint32_t my_s = 0;
-      int my_o = 0, k = 0;
-      while (wd) {
-        const int b = __ffs(wd) - 1;
-        wd &= wd - 1;
-        const int osz = warp_orbit_size_x2d32(sb + (uint32_t)b, L, flip);
-        if (lane == k) {
-          my_s = sb + (uint32_t)b;
-          my_o = osz;
-        }
-        ++k;
-      }
-      if (lane < k) {
-        idx[p + lane] = my_s;
-        dup[p + lane] = (uint16_t)my_o;
+      if ((wd >> lane) & 1u) {
+        const uint32_t s = (uint32_t)((w0 + src) * 32) + (uint32_t)lane;
+        int fix = 1;
+        lane_rep_x2d32(s, L, flip, &fix);
+        const uint32_t at = p + __popc(wd & ((1u << lane) - 1u));
+        idx[at] = s;
+        dup[at] = (uint16_t)(order / fix);
       }
     }
   }
