@@ -231,6 +231,13 @@ tm_status tm_profile_matvec(const tm_op* op, tm_dtype dtype, int iters, double* 
 /* Number of CUDA kernels this library has launched since load (all ops). */
 int64_t tm_launch_count(void);
 
+/* Caps the tile size of the even/odd x-ANNNI passes at 2^bits elements for
+ * operators created afterwards (0 removes the cap).  Operators whose tiles
+ * exceed the cap split them over thread-block clusters, as those with
+ * L >= 30 always do; the cap makes those code paths reachable at small L,
+ * for tests.  Results are the same up to rounding. */
+void tm_debug_set_eo_tile_bits(int bits);
+
 /* ---- misc -------------------------------------------------------------- */
 
 const char* tm_last_error(void);

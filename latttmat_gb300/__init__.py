@@ -44,6 +44,7 @@ EXPORTED_SYMBOLS = (
     "tm_is_symmetric", "tm_suggested_ncv", "tm_matvec_count", "tm_perform_op", "tm_perform_op_dev",
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
     "tm_profile_matvec", "tm_launch_count", "tm_perform_op_dev_noalloc", "tm_eigs_batch",
+    "tm_debug_set_eo_tile_bits",
 )
 
 
@@ -105,6 +106,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
                                   ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, P, P, P, P]
     lib.tm_eigs_batch.restype = ctypes.c_int
     lib.tm_launch_count.restype = ctypes.c_int64
+    lib.tm_debug_set_eo_tile_bits.argtypes = [ctypes.c_int]
+    lib.tm_debug_set_eo_tile_bits.restype = None
     lib.tm_last_error.restype = ctypes.c_char_p
     lib.tm_version.restype = ctypes.c_char_p
     for f in ("tm_create", "tm_transpose", "tm_destroy", "tm_perform_op", "tm_perform_op_dev", "tm_orbit_table",
@@ -144,6 +147,12 @@ def eigs_batch(model: str, dim: int, axialdir: int, points, nev: int = 2, tol: f
 def launch_count() -> int:
     """Kernels launched by the library since load."""
     return int(load_library().tm_launch_count())
+
+
+def debug_set_eo_tile_bits(bits: int) -> None:
+    """Cap the even/odd passes' tiles at 2^bits elements for operators created
+    afterwards (0: no cap), so small operators take the clustered code paths."""
+    load_library().tm_debug_set_eo_tile_bits(int(bits))
 
 
 def _check(code: int):

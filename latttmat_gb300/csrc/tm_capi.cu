@@ -331,6 +331,7 @@ static void build_op(Op& op) {
       op.ws_c.alloc((size_t)op.n * 8);
       op.eo.w1_32.alloc(((size_t)op.eo.n_orep << op.eo.m) * 4);
       op.eo.w1_64.alloc(((size_t)op.eo.n_orep << op.eo.m) * 8);
+      if (const size_t xb = eo_xchg_bytes(op.eo)) op.eo.xchg.alloc(xb);
       op.xp.alloc((size_t)op.n * 8);
       op.yp.alloc((size_t)op.n * 8);
     } else {
@@ -695,6 +696,8 @@ tm_status tm_phys_extend(const tm_op* op, const double* ql, const double* qr, do
 }
 
 int64_t tm_launch_count(void) { return g_launches.load(); }
+
+void tm_debug_set_eo_tile_bits(int bits) { ltm::eo_set_tile_bits_cap(bits); }
 
 tm_status tm_profile_matvec(const tm_op* op, tm_dtype dt, int iters, double* ms_out, int cap, int* nstages) {
   TM_API_BEGIN

@@ -42,6 +42,7 @@
 // combine the CTAs' tiles through DSMEM once all local rounds are done.
 // Inside a CTA each thread owns 2^KB elements per round: KB butterfly levels
 // in registers, with a padded shared-memory transpose between rounds.
+#include <atomic>
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -255,16 +256,31 @@ __device__ __forceinline__ void axpy16<dfloat>(float4& acc, const float4& v, dfl
   acc = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
 }
 
+// 16-byte chunks of one CTA's exchange slot: the padded tile rounded up to
+// whole 128-byte lines
+__host__ __device__ __forceinline__ int64_t xchg_slot_chunks(int n, int elem) {
+  const int64_t chunks = ((int64_t)((1 << n) + (1 << n) / 32) * elem) / 16;
+  return (chunks + 7) & ~(int64_t)7;
+}
+
 // Combine the cluster's 2^c partial tiles (butterflies on the top c tile
 // bits) in place: afterwards sm[spad(j)] holds the final value of local
 // element j.  The combination is elementwise at equal positions of the
 // padded tiles, so it runs over raw 16-byte chunks of the buffer (the padding
-// slots carry values nobody reads): every thread reads its chunks from every
-// CTA of the cluster with 16-byte DSMEM loads, and writes back after a
-// cluster barrier, so no CTA overwrites values another still reads.  After
-// that barrier no CTA reads another's shared memory, so a CTA may exit.
+// slots carry values nobody reads).
+//
+// With an exchange buffer (xchg), each CTA first stores its tile to its own
+// slot (CTA index order, 128-byte aligned); after a cluster barrier, whose
+// release/acquire orders those stores before the partners' loads, every
+// thread reads its chunks of the partners' tiles from L2 and of its own tile
+// from shared memory.  A second barrier marks the partners' reads done; each
+// CTA then discards its slot's lines from L2, so the buffer is never written
+// back to DRAM.  Without one, the partners' tiles are read through DSMEM, and
+// the write-back waits for a cluster barrier so no CTA overwrites values
+// another still reads.  The arithmetic is the same either way.
 template <class T, int KB>
-__device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int rank, const EOArgs& A) {
+__device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int rank, const EOArgs& A,
+                                               float4* __restrict__ xchg) {
   const T a = A.swap ? coef_r<T>(A) : T(1), b = A.swap ? T(1) : coef_r<T>(A);
   if constexpr (std::is_same<T, double>::value) {
     // native FP64: element-wise (the chunk accumulators and FP64 temporaries
@@ -292,7 +308,47 @@ __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int
   constexpr int kMaxChunks = ((1 << KB) * 33 * (int)sizeof(T) + 511) / 512;  // ceil(2^KB * 33/32 * sizeof(T) / 16)
   const int nchunks = (((1 << A.n) + (1 << (A.n - 5))) * (int)sizeof(T)) / 16;
   const int nc = 1 << A.c;
+  float4* dst = reinterpret_cast<float4*>(sm);
   float4 acc[kMaxChunks];
+  if (xchg) {
+    const int64_t slot = xchg_slot_chunks(A.n, (int)sizeof(T));
+    const int64_t first = (int64_t)blockIdx.x - rank;  // the cluster's CTAs are consecutive
+    float4* mine = xchg + (int64_t)blockIdx.x * slot;
+#pragma unroll
+    for (int k = 0; k < kMaxChunks; ++k) {
+      const int q = (int)threadIdx.x + k * (int)blockDim.x;
+      if (q < nchunks) __stcg(mine + q, dst[q]);
+      acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    cl.sync();
+    for (int r = 0; r < nc; ++r) {
+      T coef = T(1);
+      for (int bit = 0; bit < A.c; ++bit) coef = coef * ((((r ^ rank) >> bit) & 1) ? b : a);
+      if (r == rank) {
+#pragma unroll
+        for (int k = 0; k < kMaxChunks; ++k) {
+          const int q = (int)threadIdx.x + k * (int)blockDim.x;
+          if (q < nchunks) axpy16<T>(acc[k], dst[q], coef);
+        }
+      } else {
+        const float4* src = xchg + (first + r) * slot;
+#pragma unroll
+        for (int k = 0; k < kMaxChunks; ++k) {
+          const int q = (int)threadIdx.x + k * (int)blockDim.x;
+          if (q < nchunks) axpy16<T>(acc[k], __ldcg(src + q), coef);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxChunks; ++k) {
+      const int q = (int)threadIdx.x + k * (int)blockDim.x;
+      if (q < nchunks) dst[q] = acc[k];
+    }
+    cl.sync();  // the partners' reads of this slot are done (and the tile is complete)
+    for (int64_t line = threadIdx.x; line < slot / 8; line += blockDim.x)
+      asm volatile("discard.global.L2 [%0], 128;\n" ::"l"(mine + line * 8) : "memory");
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < kMaxChunks; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   cl.sync();
@@ -307,7 +363,6 @@ __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, T* sm, int
     }
   }
   cl.sync();
-  float4* dst = reinterpret_cast<float4*>(sm);
 #pragma unroll
   for (int k = 0; k < kMaxChunks; ++k) {
     const int q = (int)threadIdx.x + k * (int)blockDim.x;
@@ -331,7 +386,8 @@ template <class T, int KB, class InT, bool CL>
 __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restrict__ u,
                                                     const uint32_t* __restrict__ map1,
                                                     const uint16_t* __restrict__ it_e,
-                                                    const uint2* __restrict__ wout, T* __restrict__ w1) {
+                                                    const uint2* __restrict__ wout, T* __restrict__ w1,
+                                                    float4* __restrict__ xchg) {
   static_assert(sizeof(T) == sizeof(InT), "u and the tile share the element size");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
@@ -379,7 +435,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A, n);
-  if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A);
+  if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A, xchg);
   // Output.  w1 is class-major: the block of e-class C holds, for each tile,
   // the |C| values of C's members, so a warp writes a few contiguous runs.
   for (int k0 = 0; k0 < (1 << kb); k0 += kOutBatch) {
@@ -422,7 +478,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
                                                     const double* __restrict__ sout64,
                                                     const float* __restrict__ sout32,
                                                     const dfloat* __restrict__ soutdf, double post,
-                                                    OutT* __restrict__ y) {
+                                                    OutT* __restrict__ y, float4* __restrict__ xchg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   __shared__ uint32_t he[128];
@@ -463,7 +519,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
   }
   __syncthreads();
   smem_rounds<T, KB>(sm, A, n);
-  if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A);
+  if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A, xchg);
   // Designated outputs of this tile.  They are ordered like it_o, so the
   // outputs whose o this CTA holds form one contiguous range: groups
   // [rank, rank + 1) * 2^(ct - c) of the tile's 2^ct output groups.
@@ -628,11 +684,29 @@ int grid_for(int64_t n) {
 
 }  // namespace
 
+// Cap on the tile bits of the passes for operators created from now on
+// (0: none).  A diagnostic: it lets small operators run the clustered code
+// paths that otherwise only L >= 30 reaches.
+static std::atomic<int> g_eo_tile_bits_cap{0};
+void eo_set_tile_bits_cap(int bits) { g_eo_tile_bits_cap.store(bits < 0 ? 0 : bits); }
+
 // Decide cluster bits so a CTA's tile part fits in shared memory.
 static int cluster_bits_for(int m, size_t elem) {
   int c = 0;
   while (((size_t)(1 << (m - c)) * elem * 33 / 32) > 200 * 1024) ++c;
+  const int cap = g_eo_tile_bits_cap.load();
+  if (cap > 0 && m - c > cap) c = m - cap;
   return c;
+}
+
+// Bytes of exchange slots the clustered launches of a plan need (0: none;
+// only clusters of 4 or more CTAs use them).
+size_t eo_xchg_bytes(const EOPlan& P) {
+  size_t b = 0;
+  const size_t nt = (size_t)std::max(P.n_orep, P.n_erep);
+  if (P.c32 >= 2) b = std::max(b, (nt << P.c32) * (size_t)xchg_slot_chunks(P.m - P.c32, 4) * 16);
+  if (P.c64 >= 2) b = std::max(b, (nt << P.c64) * (size_t)xchg_slot_chunks(P.m - P.c64, 8) * 16);
+  return b;
 }
 
 // Orders of the m-bit patterns used by the passes.  cls: H-class index of
@@ -960,6 +1034,20 @@ struct EoIO<dfloat> {
   using Out = double;
 };
 
+// The exchange buffer for a clustered launch of `ntiles` tiles (one slot per
+// CTA), or null: the cluster combine then reads the partners' tiles through
+// DSMEM.  Clusters of 4 or more CTAs exchange through L2 (at L = 32 the
+// double-float passes take 4.55 + 3.99 ms that way against 5.05 + 4.62 ms
+// over DSMEM); a 2-CTA cluster reads its one partner through DSMEM, which
+// measured 2-3% faster than the round trip through L2.  Native FP64
+// combines element by element through DSMEM.
+template <class T>
+float4* eo_xchg(const EOArgs& A, const EOPlan& P, int ntiles) {
+  if (A.c < 2 || std::is_same<T, double>::value || !P.xchg.p) return nullptr;
+  const size_t need = ((size_t)ntiles << A.c) * (size_t)xchg_slot_chunks(A.n, (int)sizeof(T)) * 16;
+  return need <= P.xchg.bytes ? P.xchg.as<float4>() : nullptr;
+}
+
 template <class T, int KB>
 void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, const EOPlan& P, T* w1,
                   cudaStream_t s) {
@@ -978,7 +1066,8 @@ void launch_pass1(const EOArgs& A, int ntiles, const typename EoIO<T>::In* u, co
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(), P.wout.as<uint2>(), w1));
+  TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(), P.wout.as<uint2>(), w1,
+                           eo_xchg<T>(A, P, ntiles)));
 }
 
 template <class T, int KB, int OSC, class OutT = typename EoIO<T>::Out>
@@ -1001,7 +1090,8 @@ void launch_pass2(const EOArgs& A, int ntiles, const T* w1, const EOPlan& P, con
   cfg.numAttrs = 1;
   TM_CK(cudaLaunchKernelEx(&cfg, kfn, A, w1, P.t2o.as<uint2>(), P.cf_e.as<uint16_t>(),
                            P.erep.as<uint32_t>(), P.cls_start.as<uint32_t>(), P.cls_size.as<uint32_t>(),
-                           P.out_off.as<uint32_t>(), P.out_o.as<uint16_t>(), sout64, sout32, soutdf, post, y));
+                           P.out_off.as<uint32_t>(), P.out_o.as<uint16_t>(), sout64, sout32, soutdf, post, y,
+                           eo_xchg<T>(A, P, ntiles)));
 }
 
 template <class T>
@@ -1120,7 +1210,7 @@ void eo_dispatch_dd(const Op& op, const EOArgs& A, const dfloat* x, dfloat* y, c
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   TM_CK(cudaLaunchKernelEx(&cfg, k1, A, (const dfloat*)u, P.map1.as<uint32_t>(), P.it_e.as<uint16_t>(),
-                           P.wout.as<uint2>(), w1));
+                           P.wout.as<uint2>(), w1, eo_xchg<dfloat>(A, P, P.n_orep)));
   TM_CKK("eo_pass1_dd");
   launch_pass2<dfloat, KB, kOutDF, dfloat>(A, P.n_erep, w1, P, op.sout64.as<double>(), op.sout32.as<float>(),
                                            op.soutdf.as<dfloat>(), 1.0, y, s);

@@ -107,6 +107,7 @@ struct EOPlan {
   DBuf out_off;       // u32 [n_erep*2^ct+1]: designated-output offsets per tile and top-ct-bit group
   DBuf out_o;         // u16 [R]: o of each designated output (pi order)
   DBuf w1_32, w1_64;  // pass-1 intermediates
+  DBuf xchg;          // cluster-combine exchange slots (one per CTA of a clustered launch), or empty
   cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // stage timing (diagnostics)
   bool prof_on = false;
 };
@@ -169,6 +170,8 @@ void build_state_map(Op& op);            // smap for the generic reduced path
 struct EOHostTables;                     // host-side even/odd plan tables (tm_eo.cu)
 std::shared_ptr<EOHostTables> eo_host_tables(int m, int flip);
 void build_eo_plan(Op& op, const EOHostTables* host = nullptr);  // even/odd plan for K_XAM
+size_t eo_xchg_bytes(const EOPlan& P);
+void eo_set_tile_bits_cap(int bits);
 void build_two_layer(Op& op);            // tables of K_YAT / K_Y2AT / K_YAM
 // y = T x (or T^T x for a transposed view) of a two-layer operator, FP64
 void matvec_two_layer(const Op& op, const double* x, double* y, cudaStream_t s);

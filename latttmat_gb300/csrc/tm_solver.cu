@@ -977,45 +977,54 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
     force_grow = false;
     if (verified >= 3 || round + 1 >= 3 * kRefineRounds || nb + nev > cap) break;
-    // grow: the wanted residual block, block FP32 Gram-Schmidt (two passes)
-    // against the subspace, then within the block; FP32 products; a column
-    // that vanishes is dropped
+    // grow: the residuals of the wanted pairs not yet well converged (all of
+    // them if none is left), block FP32 Gram-Schmidt (two passes) against the
+    // subspace, then within the block; FP32 products; a column that vanishes
+    // is dropped.  A residual already below 5% of the tolerance adds little,
+    // and its product costs as much as any other.
     {
-      float* wb = f32col(B32, nb);
-      TM_CK(cudaMemcpyAsync(wb, R32.p, (size_t)nev * ld * 4, cudaMemcpyDeviceToDevice, s));
-      std::vector<double> q0(nev, 0.0);
-      for (int c = 0; c < nev; ++c) {
-        nrm2sq_f32(f32col(B32, nb + c), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&q0[c], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+      std::vector<int> keep;
+      for (int c = 0; c < nev; ++c)
+        if (!(rn[c] <= 0.05 * tol * std::fabs(thv[c]))) keep.push_back(c);
+      if (keep.empty())
+        for (int c = 0; c < nev; ++c) keep.push_back(c);
+      const int nk = (int)keep.size();
+      for (int k = 0; k < nk; ++k)
+        TM_CK(cudaMemcpyAsync(f32col(B32, nb + k), R32.as<float>() + (size_t)keep[k] * ld, (size_t)n * 4,
+                              cudaMemcpyDeviceToDevice, s));
+      std::vector<double> q0(nk, 0.0);
+      for (int k = 0; k < nk; ++k) {
+        nrm2sq_f32(f32col(B32, nb + k), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+        TM_CK(cudaMemcpyAsync(&q0[k], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
       }
       F32Cols wc{};
       F32ColsMut wm{};
-      for (int c = 0; c < nev; ++c) {
-        wc.c[c] = f32col(B32, nb + c);
-        wm.c[c] = f32col(B32, nb + c);
+      for (int k = 0; k < nk; ++k) {
+        wc.c[k] = f32col(B32, nb + k);
+        wm.c[k] = f32col(B32, nb + k);
       }
       // second pass only when the first removed a large part of a column
       // ("twice is enough": a norm ratio below 1/sqrt(2))
       for (int pass = 0; pass < 2; ++pass) {
-        mdot_block_f32(B32.as<float>(), ld, nb, wc, nev, n, Hd.as<double>(), 48, bpart.as<double>(), s);
-        maxpy_block_f32(B32.as<float>(), ld, nb, Hd.as<double>(), 48, wm, nev, n, s);
+        mdot_block_f32(B32.as<float>(), ld, nb, wc, nk, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+        maxpy_block_f32(B32.as<float>(), ld, nb, Hd.as<double>(), 48, wm, nk, n, s);
         if (pass == 1) break;
-        std::vector<double> q1(nev, 0.0);
-        for (int c = 0; c < nev; ++c) {
-          nrm2sq_f32(f32col(B32, nb + c), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-          TM_CK(cudaMemcpyAsync(&q1[c], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
+        std::vector<double> q1(nk, 0.0);
+        for (int k = 0; k < nk; ++k) {
+          nrm2sq_f32(f32col(B32, nb + k), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
+          TM_CK(cudaMemcpyAsync(&q1[k], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
         }
         host_sync();
         bool again = false;
-        for (int c = 0; c < nev; ++c)
-          if (!(q1[c] >= 0.5 * q0[c])) again = true;
+        for (int k = 0; k < nk; ++k)
+          if (!(q1[k] >= 0.5 * q0[k])) again = true;
         if (!again) break;
       }
       host_sync();
       int pos = nb;
-      for (int c = 0; c < nev; ++c) {
-        float* w = f32col(B32, nb + c);
-        if (pos < nb + c) {
+      for (int k = 0; k < nk; ++k) {
+        float* w = f32col(B32, nb + k);
+        if (pos < nb + k) {
           TM_CK(cudaMemcpyAsync(f32col(B32, pos), w, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
           w = f32col(B32, pos);
         }
@@ -1027,7 +1036,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
         nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
         TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
         host_sync();
-        if (!(q0[c] > 0.0) || !(q > 1e-10 * q0[c])) continue;
+        if (!(q0[k] > 0.0) || !(q > 1e-10 * q0[k])) continue;
         normalize_f32(w, lz.nsq.as<double>(), w, n, s);
         ++pos;
       }

@@ -191,6 +191,37 @@ def test_double_float_refinement_product(L, ec):
     assert infom["matvecs_f64"] < info64["matvecs_f64"]
 
 
+@pytest.mark.parametrize("L,bits,bj", [(20, 9, 0.3), (20, 8, -0.4), (24, 11, 0.45), (24, 10, -0.3)])
+def test_even_odd_cluster_split(L, bits, bj):
+    """Tiles split over 2- and 4-CTA clusters (the layout L >= 30 uses),
+    forced at small L by capping the tile bits: the FP32 and double-float
+    passes combine through the L2 exchange slots, native FP64 through DSMEM.
+    All products against the oracle, and the mixed solve against FP64."""
+    torch = pytest.importorskip("torch")
+    oracle = pytest.importorskip("oracle.oracle")
+    lt.debug_set_eo_tile_bits(bits)
+    try:
+        op = lt.TMatOp("A", 2, 5, bj, 0.5, 0.0, L, 0.0, 2)
+    finally:
+        lt.debug_set_eo_tile_bits(0)
+    ref = oracle.OracleOp("A", 2, 5, bj, 0.5, 0.0, L, 0.0, 2)
+    x = seeded_input(op.rows(), 7)
+    yr = ref.perform_op(x)
+    assert rel_err(op.perform_op(x), yr) < 1e-12
+    stream = torch.cuda.current_stream().cuda_stream
+    for dt, tdt, bar in ((lt.TM_F32, torch.float32, 2e-5), (lt.TM_F64_DF, torch.float64, 1e-12),
+                         (lt.TM_F64, torch.float64, 1e-12)):
+        xd = torch.tensor(x, dtype=tdt, device="cuda")
+        yd = torch.empty_like(xd)
+        op.perform_op_dev(xd.data_ptr(), yd.data_ptr(), dt, stream)
+        torch.cuda.synchronize()
+        assert rel_err(yd.double().cpu().numpy(), yr) < bar, dt
+    vals64, _, _, _ = op.eigs(3, tol=1e-12, mode=lt.TM_EIGS_F64)
+    valsm, _, _, infom = op.eigs(3, tol=1e-12, mode=lt.TM_EIGS_MIXED)
+    np.testing.assert_allclose(valsm, vals64, rtol=1e-10)
+    assert infom["nconv"] == 3
+
+
 @pytest.mark.parametrize("L,ec,bj", [(12, 2, -0.4), (14, 0, -0.35), (16, 2, -0.6), (20, 2, -0.3)])
 def test_even_odd_negative_coupling(L, ec, bj):
     """betaJ < 0 swaps the roles of the butterfly coefficients in the even/odd

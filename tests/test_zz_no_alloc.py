@@ -52,6 +52,7 @@ def test_noalloc_matches_regular_product(L, ec):
     n = op.rows()
     gen = torch.Generator().manual_seed(1000 + L)
     xs = [(torch.rand(n, generator=gen, dtype=torch.float64) - 0.5).cuda() for _ in range(2)]
+    torch.cuda.synchronize()  # the products below run on the library's stream
     refs = []
     for x in xs:
         y = torch.empty_like(x)
