@@ -1212,9 +1212,23 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
   info.max_resid = max_resid;
   for (int i = 0; i < nev && i < (int)theta.size(); ++i) vals[i] = theta[i];
   if (vecs_host && Lz) {
-    // eigenvectors in the reference's order: the pi -> reference scatter
-    // runs on the device, then one copy to the host
-    if (op.has_pi) {
+    // eigenvectors in the reference's order.  Host memory the device can
+    // address (pinned and mapped) is filled by a gather kernel that reads the
+    // pi-order vectors from HBM and stores coalesced over the host link;
+    // other host memory gets the pi -> reference scatter on the device, then
+    // one copy.
+    cudaPointerAttributes pa{};
+    double* hdev = nullptr;
+    if (cudaPointerGetAttributes(&pa, vecs_host) == cudaSuccess) {
+      if (pa.type == cudaMemoryTypeHost && pa.devicePointer) hdev = static_cast<double*>(pa.devicePointer);
+    } else {
+      (void)cudaGetLastError();
+    }
+    if (op.has_pi && hdev) {
+      for (int c = 0; c < nev; ++c)
+        gather_f64(Lz->v(c), op.pinv.as<uint32_t>(), hdev + (int64_t)c * n, n, s);
+      TM_CK(cudaStreamSynchronize(s));
+    } else if (op.has_pi) {
       DBuf ref;
       ref.alloc((size_t)nev * n * 8);
       for (int c = 0; c < nev; ++c)
