@@ -1,6 +1,6 @@
 """Oracle (test infrastructure): CPU restatement of the reference's hot path.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-package, as the checker or as the timed CPU reference.  The GPU product path
-never imports it.
+package: to check the GPU results, or as the timed CPU reference.  The GPU
+product path never imports it.
 """

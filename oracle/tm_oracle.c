@@ -2,8 +2,8 @@
  * tm_oracle.c -- CPU restatement of LattTMat's transfer-matrix hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the tests, smoke() and
- * bench.py's CPU-baseline leg call it as the checker or as the timed CPU
- * reference.  The GPU product path never calls it.
+ * bench.py's CPU-baseline leg call it to check the GPU results or as the
+ * timed CPU reference.  The GPU product path never calls it.
  *
  * Each function restates the reference algorithm it cites (LattTMat TMat/ sources)
  * in plain C99 + OpenMP, with the same loop structure and arithmetic order:

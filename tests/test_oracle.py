@@ -63,7 +63,8 @@ def test_oracle_eigenvalues(name):
 
 
 def test_published_probe_values():
-    """Survey/BASELINE probe numbers for A/1, A/5 at L=12, betaJ=kappa=0.5."""
+    """Leading eigenvalues of the reference run for A/1 and A/5 (flip on and
+    off) at L=12, betaJ=kappa=0.5, as the reference's own probe printed them."""
     full = oracle.OracleOp("A", 2, 1, 0.5, 0.5, 0.0, 12).eigs(2)
     np.testing.assert_allclose(full, [84970.93472621, 59989.6215884], rtol=1e-11)
     nf = oracle.OracleOp("A", 2, 5, 0.5, 0.5, 0.0, 12, 0.0, 2).eigs(2)
