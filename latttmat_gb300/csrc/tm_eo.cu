@@ -583,11 +583,35 @@ __device__ __forceinline__ uint32_t coset_key(uint32_t e, uint32_t o, int m, int
   if (inf & (1u << 21)) r = __brev(r) >> (32 - m);
   if (inf & (1u << 22)) r ^= mask;
   uint32_t best = (t << m) | __ldg(pos_o + r);
-  if (nst > 1) {  // e has a nontrivial stabiliser in H: every element reaching its representative
+  if (nst > 1) {
+    // e has a nontrivial stabiliser in H: the nst elements reaching its
+    // representative, g0 first.  H is walked as (flip, reflection, rotation
+    // j) with the rotations applied one site at a time.
     const int g0 = (int)j + m * (int)(((inf >> 21) & 1u) + 2u * ((inf >> 22) & 1u));
     const uint32_t rep = act_e(g0, e, m);
-    for (int g = g0 + 1; g < ng; ++g)
-      if (act_e(g, e, m) == rep) best = min(best, (t << m) | __ldg(pos_o + act_o(g, o, m)));
+    uint32_t found = 1;
+    for (int fl = 0; fl * 2 * m < ng && found < nst; ++fl)
+      for (int rf = 0; rf < 2 && found < nst; ++rf) {
+        uint32_t ee = e, oo = o;  // rotated right by j2
+        for (int j2 = 0; j2 < m && found < nst; ++j2) {
+          if (j2 + m * (rf + 2 * fl) > g0) {
+            uint32_t ae = ee;
+            if (rf) {
+              ae = brev_m(ee, m);
+              ae = ((ae << 1) | (ae >> (m - 1))) & mask;  // rotate left by one
+            }
+            if (fl) ae ^= mask;
+            if (ae == rep) {
+              uint32_t ao = rf ? brev_m(oo, m) : oo;
+              if (fl) ao ^= mask;
+              best = min(best, (t << m) | __ldg(pos_o + ao));
+              ++found;
+            }
+          }
+          ee = ((ee >> 1) | (ee << (m - 1))) & mask;
+          oo = ((oo >> 1) | (oo << (m - 1))) & mask;
+        }
+      }
   }
   return best;
 }

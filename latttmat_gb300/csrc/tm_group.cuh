@@ -160,6 +160,75 @@ TM_HD bool is_rep_x2d32(uint32_t s, int L, int flip) {
   return true;
 }
 
+// Orbit minimum under the X-2D periodic group, L <= 32, in 32-bit
+// arithmetic.  The smallest image has the most leading zeros: a longest
+// cyclic run of zeros of s (or of its mirror image, which has the same runs)
+// rotated to the front, or with the spin flip a longest run of ones.  Growing
+// the run-start mask one bit at a time gives the longest length and where
+// those runs start, so only a few rotations need comparing.
+TM_HD uint32_t rotr32_l(uint32_t x, int L, int k, uint32_t mask) {
+  return k ? (((x >> k) | (x << (L - k))) & mask) : x;
+}
+TM_HD uint32_t brev32_l(uint32_t x, int L) {
+#if defined(__CUDA_ARCH__)
+  return __brev(x) >> (32 - L);
+#else
+  uint32_t b = 0;
+  for (int i = 0; i < L; ++i) b |= ((x >> i) & 1u) << (L - 1 - i);
+  return b;
+#endif
+}
+// length of the longest cyclic run of ones in y (y != 0, y != mask) and, in
+// *starts, the bits where runs of that length start
+TM_HD int longest_run32(uint32_t y, int L, uint32_t mask, uint32_t* starts) {
+  uint32_t t = y;
+  int k = 1;
+  for (;;) {  // ends with k <= L - 1: y has a zero bit
+    const uint32_t nt = t & rotr32_l(y, L, k, mask);
+    if (!nt) break;
+    t = nt;
+    ++k;
+  }
+  *starts = t;
+  return k;
+}
+TM_HD uint32_t canon_x2d32(uint32_t s, int L, int flip) {
+  const uint32_t mask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
+  if (s == 0 || (flip && s == mask)) return 0;
+  if (s == mask) return s;  // no flip: every image is s
+  const uint32_t r = brev32_l(s, L);
+  uint32_t zs, zr;
+  const int Z = longest_run32(~s & mask, L, mask, &zs);
+  uint32_t os = 0, orr = 0;
+  const int O = flip ? longest_run32(s, L, mask, &os) : -1;
+  uint32_t best = mask;
+  auto scan = [&](uint32_t v, uint32_t t, int k0, bool inv) {
+    while (t) {
+#if defined(__CUDA_ARCH__)
+      const int i = __ffs(t) - 1;
+#else
+      const int i = __builtin_ctz(t);
+#endif
+      t &= t - 1;
+      const int k = (i + k0 >= L) ? i + k0 - L : i + k0;
+      uint32_t a = rotr32_l(v, L, k, mask);
+      if (inv) a = ~a & mask;
+      if (a < best) best = a;
+    }
+  };
+  if (Z >= O) {
+    longest_run32(~r & mask, L, mask, &zr);
+    scan(s, zs, Z, false);
+    scan(r, zr, Z, false);
+  }
+  if (flip && O >= Z) {
+    longest_run32(r, L, mask, &orr);
+    scan(s, os, O, true);
+    scan(r, orr, O, true);
+  }
+  return best;
+}
+
 #if defined(__CUDACC__)
 // ---- warp-cooperative forms for the X-2D periodic group on L <= 32 bits.
 // Lane k < L takes the images of rotation k (a = rotr(s, k), b = its
@@ -287,6 +356,7 @@ TM_HD bool is_rep(const GroupDev& g, uint64_t s) {
 }
 
 TM_HD uint64_t canon(const GroupDev& g, uint64_t s) {
+  if (g.kind == G_X2D && g.periodic && g.L <= 32) return canon_x2d32((uint32_t)s, g.L, g.flip);
   uint64_t m = s;
   for_each_image(g, s, [&](uint64_t im) {
     if (im < m) m = im;

@@ -76,3 +76,109 @@ def test_even_odd_subgroup(L, flip):
             assert s2 in orbit(s, L, flip)
         maps.add(tuple(join(*act(g, *split(s, L), m), m) for s in range(0, 1 << L, max(1, (1 << L) // 4096))))
     assert len(maps) == ng
+
+
+# ---- run-start forms of the periodic X-2D group (L <= 32), as the GPU
+# orbit-table and map kernels compute them: the smallest image starts with a
+# longest run of zeros (or, with the flip, of ones), so only the rotations that
+# bring such a run to the front are compared.
+
+def _rotr_m(x, L, k, mask):
+    return ((x >> k) | (x << (L - k))) & mask if k else x
+
+
+def _run_starts(y, L, k, mask):
+    """bits where a cyclic run of >= k ones of y starts (every bit for k=0)"""
+    t = mask
+    for q in range(k):
+        t &= _rotr_m(y, L, q, mask)
+    return t
+
+
+def _longest_run(y, L, mask):
+    t, k = y, 1
+    while True:
+        nt = t & _rotr_m(y, L, k, mask)
+        if not nt:
+            return k, t
+        t, k = nt, k + 1
+
+
+def _images(s, L, flip):
+    mask = (1 << L) - 1
+    out = []
+    for k in range(L):
+        a = _rotr_m(s, L, k, mask)
+        b = brev(a, L)
+        out += [a, b] + ([a ^ mask, b ^ mask] if flip else [])
+    return out
+
+
+def _canon_runs(s, L, flip):
+    mask = (1 << L) - 1
+    if s == 0 or (flip and s == mask):
+        return 0
+    if s == mask:
+        return s
+    r = brev(s, L)
+    Z, zs = _longest_run(~s & mask, L, mask)
+    O, os_ = _longest_run(s, L, mask) if flip else (-1, 0)
+    best = mask
+    cands = []
+    if Z >= O:
+        cands += [(s, zs, Z, False), (r, _longest_run(~r & mask, L, mask)[1], Z, False)]
+    if flip and O >= Z:
+        cands += [(s, os_, O, True), (r, _longest_run(r, L, mask)[1], O, True)]
+    for v, t, k0, inv in cands:
+        for i in range(L):
+            if (t >> i) & 1:
+                a = _rotr_m(v, L, (i + k0) % L, mask)
+                best = min(best, (a ^ mask) if inv else a)
+    return best
+
+
+def _rep_runs(s, L, flip):
+    """(is the orbit minimum, number of group elements fixing s)"""
+    mask = (1 << L) - 1
+    if s == 0:
+        return True, 2 * L
+    z = L - s.bit_length()
+    r = brev(s, L)
+    f = 0
+    for v, inv in [(s, False), (r, False)] + ([(s, True), (r, True)] if flip else []):
+        t = _run_starts(v if inv else (~v & mask), L, z, mask)
+        for i in range(L):
+            if (t >> i) & 1:
+                a = _rotr_m(v, L, (i + z) % L, mask)
+                if inv:
+                    a ^= mask
+                if a < s:
+                    return False, 0
+                f += a == s
+    return True, f
+
+
+@pytest.mark.parametrize("flip", [0, 1])
+def test_run_start_forms_exhaustive(flip):
+    for L in range(2, 13):
+        for s in range(1 << L):
+            ims = _images(s, L, flip)
+            assert _canon_runs(s, L, flip) == min(ims)
+            rep, fix = _rep_runs(s, L, flip)
+            assert rep == (min(ims) == s)
+            if rep:
+                assert fix == sum(im == s for im in ims)
+
+
+@pytest.mark.parametrize("flip", [0, 1])
+def test_run_start_forms_sampled_l32(flip):
+    rng = random.Random(7 + flip)
+    L = 32
+    for _ in range(3000):
+        s = rng.getrandbits(L) >> rng.randrange(L)
+        ims = _images(s, L, flip)
+        assert _canon_runs(s, L, flip) == min(ims)
+        rep, fix = _rep_runs(s, L, flip)
+        assert rep == (min(ims) == s)
+        if rep:
+            assert fix == sum(im == s for im in ims)
