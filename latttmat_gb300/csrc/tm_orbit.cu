@@ -472,9 +472,14 @@ __global__ void tvec_full_kernel(TvecParams p, int64_t n, double* tv) {
 // Reduced x-ANNNI weights from a table over the bond counts: tv_xam's
 // exponent takes (L+1)^3 values (n1, n2, n0 in [0, L]), so its exponentials
 // are evaluated once on the host with the same expression.
+// tab[(cell) * ndiv + k] = exp(...) / sqrt(d_k) over the bond-count cells
+// (n1, n2, n0) and the divisors d_k of the group order (every orbit size is
+// one), divided on the host in the same double arithmetic; divk[d] = k.  The
+// FP64 square root and division per representative would cost more than the
+// rest of the kernel on GB300's FP64 pipe.
 __global__ void tvec_xam_tab_kernel(int L, int boundary, int64_t n, const uint32_t* __restrict__ idx,
                                     const uint16_t* __restrict__ dup, const double* __restrict__ tab,
-                                    double* __restrict__ tv) {
+                                    const uint8_t* __restrict__ divk, int ndiv, double* __restrict__ tv) {
   const uint64_t mask = (1ull << L) - 1;
   const int w = L + 1;
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -490,7 +495,7 @@ __global__ void tvec_xam_tab_kernel(int L, int boundary, int64_t n, const uint32
       n2 = popc64((s & (mask >> 2)) ^ (s >> 2));
     }
     const int n0 = popc64(s);
-    tv[i] = __ldg(tab + ((int64_t)n1 * w + n2) * w + n0) / sqrt((double)dup[i]);
+    tv[i] = __ldg(tab + (((int64_t)n1 * w + n2) * w + n0) * ndiv + __ldg(divk + dup[i]));
   }
 }
 
@@ -521,22 +526,35 @@ void build_tvec(Op& op) {
   op.tvec.alloc(n * sizeof(double));
   int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 16);
   if (blocks < 1) blocks = 1;
-  DBuf tab;
+  DBuf tab, divk;  // freed after the synchronisation below
   if (reduced && op.kind == K_XAM && op.L <= 32) {
     // tv_xam's exponentials over all bond counts, same expression
     const int L = op.L, w = L + 1;
     const double hb = 0.5 * p.betaJ;
     const double J1 = -hb, J2 = hb * p.kappa, hJ = -hb * p.h, Jn = hb * p.nfexp;
-    std::vector<double> T((size_t)w * w * w);
+    // orbit sizes divide the group order
+    const int G = op.grp.order();
+    std::vector<int> divs;
+    for (int d = 1; d <= G; ++d)
+      if (G % d == 0) divs.push_back(d);
+    const int ndiv = (int)divs.size();
+    std::vector<uint8_t> K((size_t)G + 1, 0);
+    for (int k = 0; k < ndiv; ++k) K[divs[k]] = (uint8_t)k;
+    std::vector<double> T((size_t)w * w * w * ndiv);
     for (int n1 = 0; n1 <= L; ++n1)
       for (int n2 = 0; n2 <= L; ++n2)
-        for (int n0 = 0; n0 <= L; ++n0)
-          T[((size_t)n1 * w + n2) * w + n0] = std::exp(J1 * (2 * n1 - L) + J2 * (2 * n2 - L) + hJ * (2 * n0 - L) + Jn);
+        for (int n0 = 0; n0 <= L; ++n0) {
+          const double e = std::exp(J1 * (2 * n1 - L) + J2 * (2 * n2 - L) + hJ * (2 * n0 - L) + Jn);
+          for (int k = 0; k < ndiv; ++k)
+            T[(((size_t)n1 * w + n2) * w + n0) * ndiv + k] = e / std::sqrt((double)divs[k]);
+        }
     tab.alloc(T.size() * 8);
+    divk.alloc(K.size());
     TM_CK(cudaMemcpyAsync(tab.p, T.data(), T.size() * 8, cudaMemcpyHostToDevice, op.stream));
+    TM_CK(cudaMemcpyAsync(divk.p, K.data(), K.size(), cudaMemcpyHostToDevice, op.stream));
     tvec_xam_tab_kernel<<<blocks, 256, 0, op.stream>>>(L, p.boundary, n, op.idx.as<uint32_t>(),
                                                        op.dup.as<uint16_t>(), tab.as<double>(),
-                                                       op.tvec.as<double>());
+                                                       divk.as<uint8_t>(), ndiv, op.tvec.as<double>());
   } else if (reduced) {
     tvec_red_kernel<<<blocks, 256, 0, op.stream>>>(p, n, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),
                                                    op.tvec.as<double>());
