@@ -525,13 +525,25 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
   // [rank, rank + 1) * 2^(ct - c) of the tile's 2^ct output groups.
   const int64_t g0 = (tile << A.ct) + ((int64_t)rank << (A.ct - A.c));
   const uint32_t k0 = out_off[g0], k1 = out_off[g0 + (1 << (A.ct - A.c))];
+  // the output scales are loaded with the o indices, a batch at a time, so
+  // their loads are in flight together
+  using Scale = typename std::conditional<OSC == kOutDF, dfloat, typename std::conditional<OSC == kOutF64, double, float>::type>::type;
+  const Scale* __restrict__ scale = [&] {
+    if constexpr (OSC == kOutDF) return soutdf;
+    else if constexpr (OSC == kOutF64) return sout64;
+    else return sout32;
+  }();
   const uint32_t step = blockDim.x * kOutBatch;
   for (uint32_t kk = k0 + threadIdx.x; kk < k1; kk += step) {
     uint16_t ov[kOutBatch];
+    Scale sc[kOutBatch];
 #pragma unroll
     for (int q = 0; q < kOutBatch; ++q) {
       const uint32_t k = kk + q * blockDim.x;
-      ov[q] = (k < k1) ? out_o[k] : (uint16_t)0;
+      if (k < k1) {
+        ov[q] = out_o[k];
+        sc[q] = scale[k];
+      }
     }
 #pragma unroll
     for (int q = 0; q < kOutBatch; ++q) {
@@ -539,11 +551,11 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
       if (k < k1) {
         const T val = sm[spad(ov[q] & lmask)];
         if constexpr (OSC == kOutDF)
-          y[k] = val * soutdf[k];
+          y[k] = val * sc[q];
         else if constexpr (OSC == kOutF64)
-          y[k] = (OutT)((double)val * sout64[k] * post);
+          y[k] = (OutT)((double)val * sc[q] * post);
         else
-          y[k] = (OutT)(val * T(sout32[k]));
+          y[k] = (OutT)(val * T(sc[q]));
       }
     }
   }
