@@ -188,6 +188,28 @@ __global__ void gather_kernel(const T* __restrict__ src, const uint32_t* __restr
   int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < n; i += st) dst[i] = src[idx[i]];
 }
+// dst[c*n + i] = src[c*lds + idx[i]] for nvec columns, two consecutive
+// outputs per thread in one 16-byte store where dst allows it (the stores may
+// go to host memory over the host link, where wide stores count)
+__global__ void gather_cols_f64_kernel(const double* __restrict__ src, int64_t lds, const uint32_t* __restrict__ idx,
+                                       double* __restrict__ dst, int64_t n, int nvec) {
+  const int64_t half = (n + 1) >> 1;
+  const int64_t total = half * nvec;
+  const bool pairs = (n % 2 == 0) && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t / half, i = (t - c * half) * 2;
+    const double* sc = src + c * lds;
+    double* dc = dst + c * n;
+    if (pairs) {
+      const double a = sc[idx[i]], b = sc[idx[i + 1]];
+      *reinterpret_cast<double2*>(dc + i) = make_double2(a, b);
+    } else {
+      dc[i] = sc[idx[i]];
+      if (i + 1 < n) dc[i + 1] = sc[idx[i + 1]];
+    }
+  }
+}
+
 template <class T>
 __global__ void scatter_kernel(const T* __restrict__ src, const uint32_t* __restrict__ idx,
                                T* __restrict__ dst, int64_t n) {
@@ -200,6 +222,11 @@ __global__ void scatter_kernel(const T* __restrict__ src, const uint32_t* __rest
 void gather_f64(const double* src, const uint32_t* idx, double* dst, int64_t n, cudaStream_t s) {
   gather_kernel<double><<<grid_for(n), 256, 0, s>>>(src, idx, dst, n);
   TM_CKK("gather");
+}
+void gather_cols_f64(const double* src, int64_t lds, const uint32_t* idx, double* dst, int64_t n, int nvec,
+                     cudaStream_t s) {
+  gather_cols_f64_kernel<<<grid_for(((n + 1) / 2) * nvec), 256, 0, s>>>(src, lds, idx, dst, n, nvec);
+  TM_CKK("gather_cols");
 }
 void scatter_f64(const double* src, const uint32_t* idx, double* dst, int64_t n, cudaStream_t s) {
   scatter_kernel<double><<<grid_for(n), 256, 0, s>>>(src, idx, dst, n);

@@ -197,6 +197,9 @@ int num_sms();
 
 // permutation helpers
 void gather_f64(const double* src, const uint32_t* idx, double* dst, int64_t n, cudaStream_t s);
+// dst[c*n + i] = src[c*lds + idx[i]], c < nvec (dst may be device-mapped host memory)
+void gather_cols_f64(const double* src, int64_t lds, const uint32_t* idx, double* dst, int64_t n, int nvec,
+                     cudaStream_t s);
 void scatter_f64(const double* src, const uint32_t* idx, double* dst, int64_t n, cudaStream_t s);
 void gather_f32(const float* src, const uint32_t* idx, float* dst, int64_t n, cudaStream_t s);
 void scatter_f32(const float* src, const uint32_t* idx, float* dst, int64_t n, cudaStream_t s);

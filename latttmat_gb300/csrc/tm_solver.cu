@@ -1217,16 +1217,20 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
     // pi-order vectors from HBM and stores coalesced over the host link;
     // other host memory gets the pi -> reference scatter on the device, then
     // one copy.
+    // Only page-locked memory (cudaHostGetFlags knows it) takes the direct
+    // path: a system that lets the device reach pageable memory through the
+    // host's page tables reports it as addressable too, but stores through
+    // those translations are far slower than one copy.
     cudaPointerAttributes pa{};
+    unsigned int hflags = 0;
     double* hdev = nullptr;
-    if (cudaPointerGetAttributes(&pa, vecs_host) == cudaSuccess) {
+    if (cudaHostGetFlags(&hflags, vecs_host) == cudaSuccess && cudaPointerGetAttributes(&pa, vecs_host) == cudaSuccess) {
       if (pa.type == cudaMemoryTypeHost && pa.devicePointer) hdev = static_cast<double*>(pa.devicePointer);
     } else {
       (void)cudaGetLastError();
     }
     if (op.has_pi && hdev) {
-      for (int c = 0; c < nev; ++c)
-        gather_f64(Lz->v(c), op.pinv.as<uint32_t>(), hdev + (int64_t)c * n, n, s);
+      gather_cols_f64(Lz->v(0), Lz->ld, op.pinv.as<uint32_t>(), hdev, n, nev, s);
       TM_CK(cudaStreamSynchronize(s));
     } else if (op.has_pi) {
       DBuf ref;

@@ -192,12 +192,13 @@ def test_double_float_refinement_product(L, ec):
 
 
 @pytest.mark.parametrize("mode", [lt.TM_EIGS_F64, lt.TM_EIGS_MIXED])
-def test_eigenvectors_into_pinned_host_memory(mode):
+@pytest.mark.parametrize("L,ec", [(20, 2), (16, 0), (18, 2)])
+def test_eigenvectors_into_pinned_host_memory(mode, L, ec):
     """Eigenvectors written into pinned (device-mapped) host memory come
-    straight from a gather kernel; they equal those copied into pageable
-    memory bit for bit."""
+    straight from a gather kernel (16-byte stores for even row lengths); they
+    equal those copied into pageable memory bit for bit."""
     torch = pytest.importorskip("torch")
-    op = lt.TMatOp("A", 2, 5, 0.3, 0.5, 0.0, 20, 0.0, 2)
+    op = lt.TMatOp("A", 2, 5, 0.3, 0.5, 0.0, L, 0.0, ec)
     nev = 3
     vals_a, vecs_a, _, _ = op.eigs(nev, tol=1e-12, mode=mode, vectors=True)
     pinned = torch.empty((nev, op.rows()), dtype=torch.float64, pin_memory=True).numpy()
@@ -207,7 +208,7 @@ def test_eigenvectors_into_pinned_host_memory(mode):
     np.testing.assert_array_equal(vecs_a, vecs_b)
     # eigenvector check in the reference's order against the oracle
     oracle = pytest.importorskip("oracle.oracle")
-    ref = oracle.OracleOp("A", 2, 5, 0.3, 0.5, 0.0, 20, 0.0, 2)
+    ref = oracle.OracleOp("A", 2, 5, 0.3, 0.5, 0.0, L, 0.0, ec)
     for c in range(nev):
         y = ref.perform_op(vecs_b[c]) / op.getnormfactor()
         assert rel_err(y, vals_b[c] * vecs_b[c]) < 1e-9
