@@ -182,3 +182,49 @@ def test_run_start_forms_sampled_l32(flip):
         assert rep == (min(ims) == s)
         if rep:
             assert fix == sum(im == s for im in ims)
+
+
+def _word_rejected(w, L, flip):
+    """The orbit-table kernel's screen of the 32 states w*32 + b: a run of
+    more than z zeros (with the flip: or ones) inside their shared bits
+    [5, L), z their common leading-zero count, rules the word out."""
+    if w == 0 or L <= 6:
+        return False
+    up = w << 5
+    z = L - up.bit_length()
+    if z + 1 > L - 5:
+        return False
+    umask = ((1 << L) - 1) & ~31
+
+    def run(y, k):
+        t, ln = y, 1
+        while 2 * ln <= k:
+            t &= t >> ln
+            ln *= 2
+        if k > ln:
+            t &= t >> (k - ln)
+        return t != 0
+
+    return run(~up & umask, z + 1) or bool(flip and run(up & umask, z + 1))
+
+
+@pytest.mark.parametrize("flip", [0, 1])
+def test_word_screen_never_drops_a_representative(flip):
+    np = pytest.importorskip("numpy")
+    for L in range(7, 17):
+        mask = (1 << L) - 1
+        s = np.arange(1 << L, dtype=np.int64)
+        rev = np.zeros_like(s)
+        for i in range(L):
+            rev |= ((s >> i) & 1) << (L - 1 - i)
+        best = s.copy()
+        for k in range(L):
+            a = ((s >> k) | (s << (L - k))) & mask
+            b = ((rev >> k) | (rev << (L - k))) & mask
+            for im in [a, b] + ([a ^ mask, b ^ mask] if flip else []):
+                best = np.minimum(best, im)
+        words = set((np.nonzero(best == s)[0] >> 5).tolist())
+        assert not [w for w in words if _word_rejected(w, L, flip)]
+        # and the screen does real work
+        nw = (1 << L) >> 5
+        assert sum(_word_rejected(w, L, flip) for w in range(nw)) > nw // 4
