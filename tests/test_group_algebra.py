@@ -225,6 +225,7 @@ def test_word_screen_never_drops_a_representative(flip):
                 best = np.minimum(best, im)
         words = set((np.nonzero(best == s)[0] >> 5).tolist())
         assert not [w for w in words if _word_rejected(w, L, flip)]
-        # and the screen does real work
-        nw = (1 << L) >> 5
-        assert sum(_word_rejected(w, L, flip) for w in range(nw)) > nw // 4
+        # and the screen does real work (over 60% of the words from L = 12 on)
+        if L >= 12:
+            nw = (1 << L) >> 5
+            assert sum(_word_rejected(w, L, flip) for w in range(nw)) > 0.6 * nw
