@@ -33,30 +33,6 @@ namespace {
 constexpr int MMAX = 48;
 
 // --------------------------------------------------------------- small dense
-// Eigenvalues of a general m x m matrix (column-major, lda), one thread
-// (tm_hqr.cuh: Hessenberg reduction + Francis double-shift QR).
-__global__ void geneigval_kernel(const double* __restrict__ Ain, int m, int lda, double* __restrict__ wr,
-                                 double* __restrict__ wi, int* __restrict__ status) {
-  __shared__ double H[MMAX * MMAX];
-  if (threadIdx.x != 0) return;
-  for (int j = 0; j < m; ++j)
-    for (int i = 0; i < m; ++i) H[i + j * m] = Ain[i + j * lda];
-  *status = geneig_values(H, m, wr, wi);
-}
-
-// Right eigenvectors for selected eigenvalues by complex inverse iteration
-// (tm_hqr.cuh); one thread per eigenvalue.  Output unit-norm columns
-// (Yr, Yi: m x ksel column-major).
-__global__ void geneigvec_kernel(const double* __restrict__ A, int m, int lda, const double* __restrict__ lr,
-                                 const double* __restrict__ li, int ksel, double* __restrict__ scratch,
-                                 double* __restrict__ Yr, double* __restrict__ Yi) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ksel) return;
-  double* Br = scratch + (size_t)t * 2 * m * m;
-  double* Bi = Br + m * m;
-  geneig_vector(A, m, lda, lr[t], li[t], Br, Bi, Yr + (size_t)t * m, Yi + (size_t)t * m);
-}
-
 __global__ void hcolg_kernel(double* H, int ld, int j, const double* h1, const double* h2, const double* nsq) {
   int i = threadIdx.x;
   if (i <= j) H[i + j * ld] = h1[i] + h2[i];

@@ -43,8 +43,6 @@ __device__ __forceinline__ dfloat df_fma_f(float a, dfloat b, dfloat acc) {
   return df_renorm(s, err);
 }
 
-__device__ __forceinline__ dfloat df_neg(dfloat a) { return dfloat(-a.hi, -a.lo); }
-
 // two consecutive elements of a double-float column
 struct df2 {
   dfloat a, b;
@@ -163,10 +161,10 @@ __global__ void __launch_bounds__(BT) nrm_dd_kernel(const dfloat* __restrict__ w
   block_store_df<1>(acc, part);
 }
 
-// out = a x + b y; with nsq != nullptr, a is replaced by a / sqrt(*nsq)
-__global__ void __launch_bounds__(BT) axpby_dd_kernel(double a, const dfloat* __restrict__ x, double b,
-                                                      const dfloat* __restrict__ y, dfloat* __restrict__ out,
-                                                      int64_t n, const double* __restrict__ nsq) {
+// out = a x + b y; with nsq != nullptr, a is replaced by a / sqrt(*nsq).
+// Element-wise, so out may be x or y (in-place updates and normalisation).
+__global__ void __launch_bounds__(BT) axpby_dd_kernel(double a, const dfloat* x, double b, const dfloat* y,
+                                                      dfloat* out, int64_t n, const double* __restrict__ nsq) {
   __shared__ dfloat ab[2];
   if (threadIdx.x == 0) {
     ab[0] = dfloat(nsq ? a / sqrt(*nsq) : a);

@@ -914,8 +914,8 @@ void build_eo_plan(Op& op, const EOHostTables* Hp) {
   const EOHostTables& H = *Hp;
   EOPlan& P = op.eo;
   const int L = op.L, m = L / 2;
-  if (H.m != m) fail(TM_ERR_ARG, "even/odd host tables for another L");
-  const int flip = op.grp.flip;
+  if (H.m != m || H.ng != 2 * m * (op.grp.flip ? 2 : 1))
+    fail(TM_ERR_ARG, "even/odd host tables for another L or spin-flip setting");
   const uint32_t M = 1u << m;
   P.m = m;
   P.ng = H.ng;

@@ -64,21 +64,6 @@ __global__ void copy_kernel(const double* __restrict__ a, double* __restrict__ b
   for (; i < n; i += st) b[i] = a[i];
 }
 
-__global__ void resid_kernel(const double* __restrict__ W, const double* __restrict__ X, int64_t ld, int k,
-                             const double* __restrict__ theta, double* __restrict__ R, int64_t n) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < n; i += st)
-    for (int c = 0; c < k; ++c) R[c * ld + i] = W[c * ld + i] - theta[c] * X[c * ld + i];
-}
-
-// y = S * y32 (an FP32 product that was computed divided by S)
-__global__ void f32_scaled_kernel(const float* __restrict__ y32, double S, double* __restrict__ y, int64_t n) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t st = (int64_t)gridDim.x * blockDim.x;
-  for (; i < n; i += st) y[i] = S * (double)y32[i];
-}
-
 int blocks_for(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8));
 }
