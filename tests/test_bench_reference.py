@@ -47,3 +47,21 @@ def test_reference_arm_two_ranks():
     lines = _json_lines(r.stdout)
     assert len(lines) == 1
     _check(lines[0])
+
+
+def test_cpu_baseline_sample_of_the_gpu_arm():
+    """The GPU arm's cpu_baseline leg: the oracle port timed at a small width
+    and scaled to L=32 by the 2^L*L work ratio."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    sys.path.insert(0, ROOT)
+    try:
+        spec.loader.exec_module(bench)
+        cpu = bench.cpu_baseline_sample(14, 46)
+    finally:
+        sys.path.remove(ROOT)
+    assert set(cpu) == {"value", "unit", "cores", "kind", "sample"}
+    assert cpu["value"] > 0 and cpu["unit"] == "s" and cpu["kind"] == "port" and cpu["cores"] >= 1
+    assert "L=14" in cpu["sample"] and "46 products" in cpu["sample"]
