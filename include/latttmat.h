@@ -22,6 +22,7 @@
 #ifndef LATTTMAT_GB300_H
 #define LATTTMAT_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -179,17 +180,60 @@ tm_status tm_eigs(const tm_op* op, int nev, int ncv, double tol, uint64_t seed, 
                   double* vals_re, double* vals_im, double* vecs, double* vecl, tm_eigs_info* info);
 
 /* Parameter sweep: solve `count` independent operators (params[i], and the
- * same model/dim/axialdir/extend_cond for all) concurrently, each built,
- * solved with tm_eigs (ncv = tm_suggested_ncv, seed 0) and released on its
- * own CUDA stream by a pool of `nthreads` host threads (0 = 16).  Replaces
+ * same model/dim/axialdir/extend_cond for all; widths may differ).  Replaces
  * running the reference tmat once per parameter point (TMat/main.cpp,
- * TMat/pfunc.cpp:16-106).  vals_re/vals_im: host, count*nev; infos: host
- * count or NULL; status: host count or NULL, per-instance codes.  Returns
- * TM_OK if every instance succeeded, else the first failing code (message
- * names the instance). */
+ * TMat/pfunc.cpp:16-106).  Aux-bit operators (models B and D) are solved as
+ * one device batch (tm_sweep_create + tm_sweep_eigs); other families by a pool
+ * of `nthreads` host threads (0 = 16), each point on its own CUDA stream with
+ * tm_eigs (ncv = tm_suggested_ncv, seed 0).  vals_re/vals_im: host, count*nev;
+ * infos: host count or NULL; status: host count or NULL, per-instance codes.
+ * Returns TM_OK if every instance succeeded, else the first failing code
+ * (message names the instance). */
 tm_status tm_eigs_batch(const tm_params* params, int count, char model, int dim, int axialdir,
                         int extend_cond, int nev, double tol, int mode, int nthreads, double* vals_re,
                         double* vals_im, tm_eigs_info* infos, tm_status* status);
+
+/* ---- batched sweeps of aux-bit operators (no reference counterpart) ----- */
+
+/* A sweep: `count` operators of one aux-bit family (model 'B' axialdir 3 or 7,
+ * model 'D' axialdir 1, 2, 5, 6, 17 or 18; params[i] per point, widths may
+ * differ) solved as one batch on the device.  The reference builds one
+ * operator per tmat run (TMat/pfunc.cpp:16-106).  Here each chain pass of the
+ * product is one launch over every member's tiles (an instance table in
+ * device memory), the members run Arnoldi in lockstep with each restart
+ * cycle captured in a CUDA graph, and members are processed in waves that fit
+ * the free device memory (tm_sweep_set_wave_bytes overrides the share). */
+typedef struct tm_sweep tm_sweep;
+tm_status tm_sweep_create(const tm_params* params, int count, char model, int dim, int axialdir,
+                          int extend_cond, tm_sweep** out);
+tm_status tm_sweep_destroy(tm_sweep* sweep);
+int tm_sweep_count(const tm_sweep* sweep);
+int64_t tm_sweep_rows(const tm_sweep* sweep, int i);        /* rows of member i */
+double tm_sweep_normfactor(const tm_sweep* sweep, int i);   /* normfactor of member i */
+tm_status tm_sweep_set_wave_bytes(tm_sweep* sweep, size_t bytes);  /* 0: 60% of free memory */
+
+/* y_i = T_i x_i for every member: host arrays of `count` device pointers to
+ * FP64 vectors (length tm_sweep_rows(i)); dtype TM_F64, TM_F64_DF or TM_F32
+ * (computed in FP32, returned widened).  Synchronous. */
+tm_status tm_sweep_perform_op_dev(tm_sweep* sweep, const double* const* x_dev, double* const* y_dev,
+                                  tm_dtype dtype);
+
+/* Largest-magnitude eigenvalues of every member (Arnoldi; ncv 0 = the
+ * reference's suggested_nev rule; start vector uniform(0,1), seed 0).
+ * vals_re/vals_im: host, count*nev, eigenvalues / normfactor in descending
+ * magnitude; infos, status: host arrays of count or NULL.  Returns TM_OK or
+ * the first failing member's code. */
+tm_status tm_sweep_eigs(tm_sweep* sweep, int nev, int ncv, double tol, int mode, double* vals_re,
+                        double* vals_im, tm_eigs_info* infos, tm_status* status);
+
+/* Autotuner of the aux-bit chain kernels (no reference counterpart): times
+ * the operator's product (TM_F32 or TM_F64_DF) over 2^11..2^14-element tiles
+ * and 128 or 256 threads per block, keeps the fastest for this model, width
+ * and element size in the process-wide tuning table (used by tm_perform_op*,
+ * tm_eigs and sweeps), and returns it with its time per product. */
+tm_status tm_chain_autotune(const tm_op* op, tm_dtype dtype, int* tile_bits, int* threads, double* ms);
+/* Sets one entry of the tuning table (tile_bits 0 / threads 0: the default). */
+tm_status tm_chain_set_tuning(char model, int L, tm_dtype dtype, int tile_bits, int threads);
 
 /* ---- observables ------------------------------------------------------- */
 
@@ -230,6 +274,12 @@ tm_status tm_profile_matvec(const tm_op* op, tm_dtype dtype, int iters, double* 
 
 /* Number of CUDA kernels this library has launched since load (all ops). */
 int64_t tm_launch_count(void);
+
+/* Number of device allocations this library has requested since load (every
+ * device buffer of operators, solvers and products goes through one
+ * allocator).  A diagnostic: tests use it to show that an entry point
+ * allocates nothing. */
+int64_t tm_alloc_count(void);
 
 /* Caps the tile size of the even/odd x-ANNNI passes at 2^bits elements for
  * operators created afterwards (0 removes the cap).  Operators whose tiles

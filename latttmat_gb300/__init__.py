@@ -43,8 +43,10 @@ EXPORTED_SYMBOLS = (
     "tm_create", "tm_transpose", "tm_destroy", "tm_rows", "tm_cols", "tm_normfactor", "tm_layer_size",
     "tm_is_symmetric", "tm_suggested_ncv", "tm_matvec_count", "tm_perform_op", "tm_perform_op_dev",
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
-    "tm_profile_matvec", "tm_launch_count", "tm_perform_op_dev_noalloc", "tm_eigs_batch",
-    "tm_debug_set_eo_tile_bits",
+    "tm_profile_matvec", "tm_launch_count", "tm_alloc_count", "tm_perform_op_dev_noalloc", "tm_eigs_batch",
+    "tm_debug_set_eo_tile_bits", "tm_sweep_create", "tm_sweep_destroy", "tm_sweep_count", "tm_sweep_rows",
+    "tm_sweep_normfactor", "tm_sweep_set_wave_bytes", "tm_sweep_perform_op_dev", "tm_sweep_eigs",
+    "tm_chain_autotune", "tm_chain_set_tuning",
 )
 
 
@@ -106,8 +108,26 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
                                   ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, P, P, P, P]
     lib.tm_eigs_batch.restype = ctypes.c_int
     lib.tm_launch_count.restype = ctypes.c_int64
+    lib.tm_alloc_count.restype = ctypes.c_int64
     lib.tm_debug_set_eo_tile_bits.argtypes = [ctypes.c_int]
     lib.tm_debug_set_eo_tile_bits.restype = None
+    lib.tm_sweep_create.argtypes = [P, ctypes.c_int, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(P)]
+    lib.tm_sweep_destroy.argtypes = [P]
+    lib.tm_sweep_count.argtypes = [P]
+    lib.tm_sweep_rows.argtypes = [P, ctypes.c_int]
+    lib.tm_sweep_rows.restype = ctypes.c_int64
+    lib.tm_sweep_normfactor.argtypes = [P, ctypes.c_int]
+    lib.tm_sweep_normfactor.restype = ctypes.c_double
+    lib.tm_sweep_set_wave_bytes.argtypes = [P, ctypes.c_size_t]
+    lib.tm_sweep_perform_op_dev.argtypes = [P, P, P, ctypes.c_int]
+    lib.tm_sweep_eigs.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, P, P, P, P]
+    lib.tm_chain_autotune.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_double)]
+    lib.tm_chain_set_tuning.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    for f in ("tm_sweep_create", "tm_sweep_destroy", "tm_sweep_set_wave_bytes", "tm_sweep_perform_op_dev",
+              "tm_sweep_eigs", "tm_chain_autotune", "tm_chain_set_tuning"):
+        getattr(lib, f).restype = ctypes.c_int
     lib.tm_last_error.restype = ctypes.c_char_p
     lib.tm_version.restype = ctypes.c_char_p
     for f in ("tm_create", "tm_transpose", "tm_destroy", "tm_perform_op", "tm_perform_op_dev", "tm_orbit_table",
@@ -144,9 +164,95 @@ def eigs_batch(model: str, dim: int, axialdir: int, points, nev: int = 2, tol: f
     return vals, info, st[:count].copy()
 
 
+class Sweep:
+    """A parameter sweep of aux-bit operators (models B and D) solved as one
+    device batch (tm_sweep_*): points are (betaJ, kappa, kappa2, h, size)
+    tuples, widths may differ."""
+
+    def __init__(self, model: str, dim: int, axialdir: int, points, extend_cond: int = 0):
+        lib = load_library()
+        self._lib = lib
+        count = len(points)
+        arr = (tm_params * max(count, 1))()
+        for i, (bj, k, k2, h, size) in enumerate(points):
+            arr[i] = tm_params(float(bj), float(k), float(k2), float(h), int(size))
+        h_ = ctypes.c_void_p()
+        _check(lib.tm_sweep_create(ctypes.byref(arr), count, model.encode()[:1], int(dim), int(axialdir),
+                                   int(extend_cond), ctypes.byref(h_)))
+        self._h = h_
+        self.points = list(points)
+
+    def count(self) -> int:
+        return int(self._lib.tm_sweep_count(self._h))
+
+    def rows(self, i: int) -> int:
+        return int(self._lib.tm_sweep_rows(self._h, int(i)))
+
+    def normfactor(self, i: int) -> float:
+        return float(self._lib.tm_sweep_normfactor(self._h, int(i)))
+
+    def set_wave_bytes(self, nbytes: int) -> None:
+        _check(self._lib.tm_sweep_set_wave_bytes(self._h, int(nbytes)))
+
+    def perform_op_dev(self, x_ptrs, y_ptrs, dtype: int = TM_F64) -> None:
+        """y_i = T_i x_i for every member; x_ptrs / y_ptrs: device pointers to FP64 vectors."""
+        n = self.count()
+        xa = (ctypes.c_void_p * n)(*[ctypes.c_void_p(int(p)) for p in x_ptrs])
+        ya = (ctypes.c_void_p * n)(*[ctypes.c_void_p(int(p)) for p in y_ptrs])
+        _check(self._lib.tm_sweep_perform_op_dev(self._h, ctypes.cast(xa, ctypes.c_void_p),
+                                                 ctypes.cast(ya, ctypes.c_void_p), int(dtype)))
+
+    def eigs(self, nev: int = 2, tol: float = 1e-10, mode: int = TM_EIGS_MIXED, ncv: int = 0):
+        """(vals complex [count, nev] / normfactor, info dicts, status codes)."""
+        n = self.count()
+        vr = np.zeros(n * nev)
+        vi = np.zeros(n * nev)
+        infos = (tm_eigs_info * n)()
+        st = np.zeros(n, dtype=np.int32)
+        code = self._lib.tm_sweep_eigs(self._h, int(nev), int(ncv), float(tol), int(mode), _ptr(vr), _ptr(vi),
+                                       ctypes.byref(infos), _ptr(st))
+        if code != TM_OK and not np.any(st == TM_OK):
+            _check(code)
+        vals = (vr + 1j * vi).reshape(n, nev)
+        info = [{k: getattr(infos[i], k) for k, _ in tm_eigs_info._fields_} for i in range(n)]
+        return vals, info, st.copy()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.tm_sweep_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def chain_autotune(op: "TMatOp", dtype: int = TM_F32):
+    """Time the aux-bit operator's product over the chain kernels' tile and
+    block sizes; the fastest goes into the library's tuning table.
+    Returns (tile_bits, threads, ms per product)."""
+    tb = ctypes.c_int()
+    th = ctypes.c_int()
+    ms = ctypes.c_double()
+    _check(load_library().tm_chain_autotune(op._h, int(dtype), ctypes.byref(tb), ctypes.byref(th), ctypes.byref(ms)))
+    return tb.value, th.value, ms.value
+
+
+def chain_set_tuning(model: str, L: int, dtype: int, tile_bits: int, threads: int) -> None:
+    """Set one entry of the chain tuning table (0, 0: the default)."""
+    _check(load_library().tm_chain_set_tuning(model.encode()[:1], int(L), int(dtype), int(tile_bits), int(threads)))
+
+
 def launch_count() -> int:
     """Kernels launched by the library since load."""
     return int(load_library().tm_launch_count())
+
+
+def alloc_count() -> int:
+    """Device allocations requested by the library since load."""
+    return int(load_library().tm_alloc_count())
 
 
 def debug_set_eo_tile_bits(bits: int) -> None:

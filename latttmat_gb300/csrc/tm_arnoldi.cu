@@ -5,8 +5,9 @@
 // device and thick restarts on an orthonormal basis of the kept Ritz vectors
 // (a Krylov-Schur style restart: A V_k = V_k H_k + f b^T with
 // span(W) H-invariant, so no implicit shifts are needed).  The small dense
-// eigenproblem runs on the device: Householder reduction to Hessenberg form
-// and Francis double-shift QR for the eigenvalues (Golub & Van Loan, Alg. 7.4.2,
+// eigenproblem runs on the host, where the projected matrix comes back each
+// cycle anyway: Householder reduction to Hessenberg form and Francis
+// double-shift QR for the eigenvalues (Golub & Van Loan, Alg. 7.4.2,
 // 7.5.1-7.5.2), complex inverse iteration for the wanted eigenvectors.
 // Mixed mode: FP32 matvecs until the Ritz residuals hit the FP32 floor, then
 // FP64 restart cycles from the same basis until the tolerance is met.
@@ -21,12 +22,120 @@
 #include "tm_blas.cuh"
 #include "tm_hqr.cuh"
 #include "tm_internal.h"
+#include "tm_krylov.h"
 
 namespace ltm {
 
 void apply_refine(const Op& op, const double* x, double* y, cudaStream_t s);
 double apply_internal(const Op& op, const double* x, double* y, const float* x32, float* y32, bool f32,
                       cudaStream_t s);
+
+// ------------------------------------------------------------------ restart algebra (host)
+// The small-matrix side of the Krylov-Schur restart, shared by the single
+// solver below and the batched sweep (tm_sweep.cu).
+
+// Eigen-decompose H_m ((m+1) x (m+1) column-major, leading m x m block; host:
+// the routines of tm_hqr.cuh take microseconds at these sizes): Ritz values by
+// |theta| descending, eigenvectors and residual estimates for the first kvec.
+Ritz krylov_project(const double* Hh, int m, int kvec) {
+  Ritz R;
+  std::vector<double> Hm((size_t)m * m);
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) Hm[i + (size_t)j * m] = Hh[i + (size_t)j * (m + 1)];
+  std::vector<double> er(m), ei(m);
+  if (geneig_values(Hm.data(), m, er.data(), ei.data())) fail(TM_ERR_NOCONV, "small Hessenberg QR did not converge");
+  std::vector<int> ord(m);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+    double ma = std::hypot(er[a], ei[a]), mb = std::hypot(er[b], ei[b]);
+    if (ma != mb) return ma > mb;
+    return ei[a] > ei[b];
+  });
+  R.beta = Hh[m + (size_t)(m - 1) * (m + 1)];
+  kvec = std::min(kvec, m);
+  std::vector<double> yr((size_t)m * kvec), yi((size_t)m * kvec), Br((size_t)m * m), Bi((size_t)m * m);
+  for (int c = 0; c < kvec; ++c)
+    geneig_vector(Hh, m, m + 1, er[ord[c]], ei[ord[c]], Br.data(), Bi.data(), yr.data() + (size_t)c * m,
+                  yi.data() + (size_t)c * m);
+  for (int i = 0; i < m; ++i) R.theta.push_back({er[ord[i]], ei[ord[i]]});
+  for (int c = 0; c < kvec; ++c) {
+    std::vector<std::complex<double>> y(m);
+    for (int i = 0; i < m; ++i) y[i] = {yr[(size_t)c * m + i], yi[(size_t)c * m + i]};
+    R.resid.push_back(std::fabs(R.beta) * std::abs(y[m - 1]));
+    R.y.push_back(y);
+  }
+  return R;
+}
+
+// Ritz vectors computed per projection, and Ritz pairs kept at a restart
+int krylov_kvec(int m, int nev) { return std::min(m - 1, std::max(nev + 2, (m + nev) / 2 + 1)); }
+int krylov_keep(int m, int nev, int nconv, int kvec) {
+  int kk = std::min(kvec, std::max(nev + 1, nev + std::min(nconv, (m - nev) / 2)));
+  return std::max(kk, std::min(kvec, (m + nev) / 2));
+}
+
+// Real orthonormal basis Wm (m x k, column-major) of the span of the first kk
+// Ritz vectors (a complex pair contributes Re and Im); returns k.
+int krylov_basis(const Ritz& R, int m, int kk, std::vector<double>& Wm) {
+  std::vector<std::vector<double>> cols;
+  for (int c = 0; c < kk; ++c) {
+    bool cplx = std::fabs(R.theta[c].imag()) > 0.0;
+    std::vector<double> re(m), im(m);
+    for (int i = 0; i < m; ++i) {
+      re[i] = R.y[c][i].real();
+      im[i] = R.y[c][i].imag();
+    }
+    cols.push_back(re);
+    if (cplx) {
+      cols.push_back(im);
+      ++c;  // skip the conjugate partner
+    }
+  }
+  // modified Gram-Schmidt twice
+  std::vector<std::vector<double>> q;
+  for (auto& cvec : cols) {
+    std::vector<double> w = cvec;
+    for (int pass = 0; pass < 2; ++pass)
+      for (auto& b : q) {
+        double d = 0;
+        for (int i = 0; i < m; ++i) d += b[i] * w[i];
+        for (int i = 0; i < m; ++i) w[i] -= d * b[i];
+      }
+    double nr = 0;
+    for (int i = 0; i < m; ++i) nr += w[i] * w[i];
+    nr = std::sqrt(nr);
+    if (nr < 1e-10) continue;
+    for (int i = 0; i < m; ++i) w[i] /= nr;
+    q.push_back(w);
+  }
+  int k = (int)q.size();
+  Wm.assign((size_t)m * k, 0.0);
+  for (int c = 0; c < k; ++c)
+    for (int i = 0; i < m; ++i) Wm[(size_t)c * m + i] = q[c][i];
+  return k;
+}
+
+// Projected matrix after the restart V_k = V_m W: H_k = W^T H_m W and the
+// coupling row beta * W[m-1, :] below it ((m+1) x (m+1) column-major).
+void krylov_restart_h(const double* Hh, int m, const std::vector<double>& Wm, int k, double beta,
+                      std::vector<double>& Hn) {
+  const int ld = m + 1;
+  std::vector<double> HW((size_t)m * k, 0.0);
+  Hn.assign((size_t)ld * ld, 0.0);
+  for (int c = 0; c < k; ++c)
+    for (int i = 0; i < m; ++i) {
+      double acc = 0;
+      for (int j = 0; j < m; ++j) acc += Hh[i + (size_t)j * ld] * Wm[(size_t)c * m + j];
+      HW[(size_t)c * m + i] = acc;
+    }
+  for (int c = 0; c < k; ++c)
+    for (int r = 0; r < k; ++r) {
+      double acc = 0;
+      for (int i = 0; i < m; ++i) acc += Wm[(size_t)r * m + i] * HW[(size_t)c * m + i];
+      Hn[r + (size_t)c * ld] = acc;
+    }
+  for (int c = 0; c < k; ++c) Hn[k + (size_t)c * ld] = beta * Wm[(size_t)c * m + (m - 1)];
+}
 
 namespace {
 
@@ -47,19 +156,13 @@ __global__ void copyv_kernel(const double* __restrict__ a, double* __restrict__ 
 
 int nblk(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8)); }
 
-struct Ritz {
-  std::vector<std::complex<double>> theta;   // sorted by |theta| desc
-  std::vector<double> resid;
-  std::vector<std::vector<std::complex<double>>> y;  // eigenvectors of H (m)
-  double beta = 0;
-};
 
 struct Arnoldi {
   const Op& op;
   cudaStream_t s;
   int64_t n;
   int m;
-  DBuf V, W, x32, y32, h1, h2, part, nsq, Hd, wr, wi, lr, li, Yr, Yi, scr, Wd, st;
+  DBuf V, W, x32, y32, h1, h2, part, nsq, Hd, Wd;
   int matvecs = 0, matvecs64 = 0, restarts = 0;
   std::vector<double> Hh;  // host copy (m+1)^2
 
@@ -71,15 +174,7 @@ struct Arnoldi {
     part.alloc(red_part_bytes(16));
     nsq.alloc(8);
     Hd.alloc((size_t)(m + 1) * (m + 1) * 8);
-    wr.alloc(64 * 8);
-    wi.alloc(64 * 8);
-    lr.alloc(64 * 8);
-    li.alloc(64 * 8);
-    Yr.alloc((size_t)64 * 64 * 8);
-    Yi.alloc((size_t)64 * 64 * 8);
-    scr.alloc((size_t)64 * 2 * 64 * 64 * 8);
     Wd.alloc((size_t)64 * 64 * 8);
-    st.alloc(16);
   }
   double* v(int j) const { return V.as<double>() + (int64_t)j * n; }
 
@@ -126,81 +221,14 @@ struct Arnoldi {
     normalize(W.as<double>(), nsq.as<double>(), v(0), nullptr, n, s);
   }
 
-  // eigen-decompose H_m (host; the routines of tm_hqr.cuh take microseconds
-  // at these sizes); eigenvectors for the first kvec by |theta|
   Ritz project(int kvec) {
-    Ritz R;
     Hh.assign((size_t)(m + 1) * (m + 1), 0.0);
     TM_CK(cudaMemcpyAsync(Hh.data(), Hd.p, Hh.size() * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaStreamSynchronize(s));
-    std::vector<double> Hm((size_t)m * m);
-    for (int j = 0; j < m; ++j)
-      for (int i = 0; i < m; ++i) Hm[i + (size_t)j * m] = Hh[i + (size_t)j * (m + 1)];
-    std::vector<double> er(m), ei(m);
-    if (geneig_values(Hm.data(), m, er.data(), ei.data())) fail(TM_ERR_NOCONV, "small Hessenberg QR did not converge");
-    std::vector<int> ord(m);
-    std::iota(ord.begin(), ord.end(), 0);
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-      double ma = std::hypot(er[a], ei[a]), mb = std::hypot(er[b], ei[b]);
-      if (ma != mb) return ma > mb;
-      return ei[a] > ei[b];
-    });
-    R.beta = Hh[m + (size_t)(m - 1) * (m + 1)];
-    kvec = std::min(kvec, m);
-    std::vector<double> yr((size_t)m * kvec), yi((size_t)m * kvec), Br((size_t)m * m), Bi((size_t)m * m);
-    for (int c = 0; c < kvec; ++c)
-      geneig_vector(Hh.data(), m, m + 1, er[ord[c]], ei[ord[c]], Br.data(), Bi.data(), yr.data() + (size_t)c * m,
-                    yi.data() + (size_t)c * m);
-    for (int i = 0; i < m; ++i) R.theta.push_back({er[ord[i]], ei[ord[i]]});
-    for (int c = 0; c < kvec; ++c) {
-      std::vector<std::complex<double>> y(m);
-      for (int i = 0; i < m; ++i) y[i] = {yr[(size_t)c * m + i], yi[(size_t)c * m + i]};
-      R.resid.push_back(std::fabs(R.beta) * std::abs(y[m - 1]));
-      R.y.push_back(y);
-    }
-    return R;
+    return krylov_project(Hh.data(), m, kvec);
   }
 
-  // real orthonormal basis W (m x k) of the span of the first kk Ritz vectors
-  // (a complex pair contributes Re and Im); returns k
-  int build_basis(const Ritz& R, int kk, std::vector<double>& Wm) {
-    std::vector<std::vector<double>> cols;
-    for (int c = 0; c < kk; ++c) {
-      bool cplx = std::fabs(R.theta[c].imag()) > 0.0;
-      std::vector<double> re(m), im(m);
-      for (int i = 0; i < m; ++i) {
-        re[i] = R.y[c][i].real();
-        im[i] = R.y[c][i].imag();
-      }
-      cols.push_back(re);
-      if (cplx) {
-        cols.push_back(im);
-        ++c;  // skip the conjugate partner
-      }
-    }
-    // modified Gram-Schmidt twice
-    std::vector<std::vector<double>> q;
-    for (auto& cvec : cols) {
-      std::vector<double> w = cvec;
-      for (int pass = 0; pass < 2; ++pass)
-        for (auto& b : q) {
-          double d = 0;
-          for (int i = 0; i < m; ++i) d += b[i] * w[i];
-          for (int i = 0; i < m; ++i) w[i] -= d * b[i];
-        }
-      double nr = 0;
-      for (int i = 0; i < m; ++i) nr += w[i] * w[i];
-      nr = std::sqrt(nr);
-      if (nr < 1e-10) continue;
-      for (int i = 0; i < m; ++i) w[i] /= nr;
-      q.push_back(w);
-    }
-    int k = (int)q.size();
-    Wm.assign((size_t)m * k, 0.0);
-    for (int c = 0; c < k; ++c)
-      for (int i = 0; i < m; ++i) Wm[(size_t)c * m + i] = q[c][i];
-    return k;
-  }
+  int build_basis(const Ritz& R, int kk, std::vector<double>& Wm) { return krylov_basis(R, m, kk, Wm); }
 
   // restart: V_k = V_m W, H_k = W^T H_m W, coupling row b = beta * W[m-1,:], v_k = v_m
   void restart(const Ritz& R, const std::vector<double>& Wm, int k) {
@@ -208,21 +236,8 @@ struct Arnoldi {
     basis_rotate(V.as<double>(), n, m, Wd.as<double>(), k, n, s);
     copyv_kernel<<<nblk(n), 256, 0, s>>>(v(m), v(k), n);
     TM_CKK("copyv");
-    const int ld = m + 1;
-    std::vector<double> HW((size_t)m * k, 0.0), Hn((size_t)ld * ld, 0.0);
-    for (int c = 0; c < k; ++c)
-      for (int i = 0; i < m; ++i) {
-        double acc = 0;
-        for (int j = 0; j < m; ++j) acc += Hh[i + (size_t)j * ld] * Wm[(size_t)c * m + j];
-        HW[(size_t)c * m + i] = acc;
-      }
-    for (int c = 0; c < k; ++c)
-      for (int r = 0; r < k; ++r) {
-        double acc = 0;
-        for (int i = 0; i < m; ++i) acc += Wm[(size_t)r * m + i] * HW[(size_t)c * m + i];
-        Hn[r + (size_t)c * ld] = acc;
-      }
-    for (int c = 0; c < k; ++c) Hn[k + (size_t)c * ld] = R.beta * Wm[(size_t)c * m + (m - 1)];
+    std::vector<double> Hn;
+    krylov_restart_h(Hh.data(), m, Wm, k, R.beta, Hn);
     TM_CK(cudaMemcpyAsync(Hd.p, Hn.data(), Hn.size() * 8, cudaMemcpyHostToDevice, s));
     ++restarts;
   }
@@ -234,7 +249,7 @@ struct Arnoldi {
     int stall = 0;
     for (int cyc = 0; cyc < max_cycles; ++cyc) {
       for (int j = k; j < m; ++j) step(j, f32);
-      int kvec = std::min(m - 1, std::max(nev + 2, (m + nev) / 2 + 1));
+      const int kvec = krylov_kvec(m, nev);
       R = project(kvec);
       double ref = std::abs(R.theta[0]);
       bool ok = true;
@@ -257,10 +272,8 @@ struct Arnoldi {
           return false;
         }
       }
-      int kk = std::min(kvec, std::max(nev + 1, nev + std::min(nconv, (m - nev) / 2)));
-      kk = std::max(kk, std::min(kvec, (m + nev) / 2));
       std::vector<double> Wm;
-      int knew = build_basis(R, kk, Wm);
+      int knew = build_basis(R, krylov_keep(m, nev, nconv, kvec), Wm);
       if (knew >= m - 1) knew = m - 2;
       restart(R, Wm, knew);
       k = knew;

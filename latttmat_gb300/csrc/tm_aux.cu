@@ -26,25 +26,17 @@
 // state->rank map and contract the full-space result at the representatives.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
+#include "tm_chain.h"
 #include "tm_df.cuh"
 #include "tm_internal.h"
 
 namespace ltm {
 
 namespace {
-
-struct AuxCoef {
-  double b1[2], b2[2], b3[2];
-};
-
-template <class T>
-struct AuxCoefT {
-  T b1[2], b2[2], b3[2];
-  T g;  // step normalisation (multiply)
-};
 
 int grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
@@ -53,25 +45,12 @@ int grid_for(int64_t n) {
 
 __device__ __forceinline__ int spad(int e) { return e + (e >> 5); }
 
+__device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp);
+
 // byte offset of the fold accumulators in chain_kernel's shared memory
 __host__ __device__ __forceinline__ size_t chain_acc_offset(int tile, size_t elem) {
   return (((size_t)(tile + tile / 32 + 1) * elem) + 15) & ~(size_t)15;
 }
-
-// Geometry of one pass.  Element index in HBM: ((lb << L | r) << NA) | aux.
-// Tile index e: bits [0, NA) aux, then tile state bits k -> state position
-// spos[k]; the outer index (blockIdx) deposits into opos[] (state bits) and,
-// when the lastbit pass is outer, into lb.
-struct ChainPass {
-  int nst;         // tile state bits
-  int spos[16];
-  int no;          // outer state bits
-  int opos[32];
-  int t0, T;       // steps [t0, t0 + T)
-  int jbit0;       // tile state bit of step t0's lowest site
-  int first, last; // build from x / fold into y
-  int nlb;         // lastbit passes (DNNI 2 or 1, BNNNI 4)
-};
 
 // tile state index -> state bits: the tile's state bits are the contiguous
 // runs [0, cb) and [lo, lo + nst - cb)
@@ -118,11 +97,12 @@ __device__ __forceinline__ T chain_init(const IO* __restrict__ x, const double* 
 //           dir = optdirection); L/2 steps.
 // P: the nlb*2^L*2^NA buffer (in place).  first: tiles built from x; last:
 // y[r] = postc * post[r] * sum_{lb, aux} (one CTA loops the lastbit passes).
+// (the body of one block: `blk` is its index within the pass's grid)
 template <class T, int ZB, class IO>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3)) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
-                                                    const double* __restrict__ pre, const uint32_t* __restrict__ smap,
-                                                    IO* __restrict__ y, const double* __restrict__ post, double postc,
-                                                    int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {
+__device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restrict__ x,
+                                            const double* __restrict__ pre, const uint32_t* __restrict__ smap,
+                                            IO* __restrict__ y, const double* __restrict__ post, double postc, int L,
+                                            int bc, int dir, const AuxCoefT<T>& c, const ChainPass& cp, uint64_t blk) {
   constexpr int NA = ZB ? 2 : 1, KS = ZB ? 2 : 1, GB = NA + KS;  // group bits
   extern __shared__ unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
@@ -160,8 +140,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3)) chain_kernel(T*
     }
   }
   // outer index: state bits, then (unless last) the lastbit pass
-  const uint64_t ob = blockIdx.x & ((1ull << cp.no) - 1);
-  const int lb_outer = (int)(blockIdx.x >> cp.no);
+  const uint64_t ob = blk & ((1ull << cp.no) - 1);
+  const int lb_outer = (int)(blk >> cp.no);
   const uint64_t rbase = dep(ob, cp.opos, cp.no);
   const int site0 = KS * cp.t0;  // lowest site of the pass's steps
   const int nloop = cp.last ? cp.nlb : 1;
@@ -279,6 +259,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3)) chain_kernel(T*
   }
 }
 
+template <class T, int ZB, class IO>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3)) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
+                                                    const double* __restrict__ pre, const uint32_t* __restrict__ smap,
+                                                    IO* __restrict__ y, const double* __restrict__ post, double postc,
+                                                    int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {
+  chain_block<T, ZB, IO>(P, x, pre, smap, y, post, postc, L, bc, dir, c, cp, blockIdx.x);
+}
+
 // ------------------------------------------------------------------ reduced contract
 template <class T>
 __global__ void red_contract(const T* __restrict__ z, const uint32_t* __restrict__ idx, const uint16_t* __restrict__ dup,
@@ -287,6 +275,93 @@ __global__ void red_contract(const T* __restrict__ z, const uint32_t* __restrict
   const int64_t st = (int64_t)gridDim.x * blockDim.x;
   for (; i < n; i += st) y[i] = (T)((double)z[idx[i]] * post * (double)dup[i] * tv[i]);
 }
+
+// ------------------------------------------------------------------ batched product
+// One pass over every batch member's tiles: the block finds its instance by
+// binary search over the pass's block prefix, then runs the same tile body
+// as chain_kernel on that instance's geometry (copied to shared memory).
+template <class T, int ZB, class IO, int MODE>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3))
+    chain_batch_kernel(const ChainInst* __restrict__ inst, const int2* __restrict__ km, const int64_t* __restrict__ start,
+                       int count, int pass, int j) {
+  __shared__ ChainPass cps;
+  __shared__ int s_i;
+  if (threadIdx.x == 0) {
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (start[mid] <= b)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_i = lo;
+  }
+  __syncthreads();
+  const ChainInst& I = inst[s_i];
+  const int64_t blk = (int64_t)blockIdx.x - start[s_i];
+  const int np = (sizeof(T) == 4) ? I.np4 : I.np8;
+  const int2 kmi = km[s_i];
+  if (kmi.y != MODE || j < kmi.x || pass >= np) return;  // uniform over the block
+  {
+    const int* src = reinterpret_cast<const int*>((sizeof(T) == 4) ? &I.p4[pass] : &I.p8[pass]);
+    int* dst = reinterpret_cast<int*>(&cps);
+    for (int q = threadIdx.x; q < (int)(sizeof(ChainPass) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
+  }
+  __syncthreads();
+  if (blk >= chain_pass_blocks_dev(cps)) return;
+  const IO* x = (MODE == kModeF32) ? reinterpret_cast<const IO*>(I.x32)
+                                   : reinterpret_cast<const IO*>(I.V + (int64_t)j * I.ldv);
+  const AuxCoefT<T>* c;
+  if constexpr (MODE == kModeF32)
+    c = reinterpret_cast<const AuxCoefT<T>*>(&I.c32);
+  else if constexpr (MODE == kModeDF)
+    c = reinterpret_cast<const AuxCoefT<T>*>(&I.cdf);
+  else
+    c = reinterpret_cast<const AuxCoefT<T>*>(&I.c64);
+  chain_block<T, ZB, IO>(reinterpret_cast<T*>(I.P), x, I.tvec, I.smap, reinterpret_cast<IO*>(I.fold), nullptr, 1.0,
+                         I.L, I.bc, I.dir, *c, cps, (uint64_t)blk);
+}
+
+// w[k] = fold[idx[k]] * gs * dup[k] * tvec[k] (reduced) or fold[k] * gs * nf *
+// tvec[k] (full), per instance; kSweepRows rows per block
+template <class IO, int MODE>
+__global__ void __launch_bounds__(256) contract_batch_kernel(const ChainInst* __restrict__ inst,
+                                                             const int2* __restrict__ km,
+                                                             const int64_t* __restrict__ rstart, int count, int j) {
+  __shared__ int s_i;
+  if (threadIdx.x == 0) {
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (rstart[mid] <= b)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_i = lo;
+  }
+  __syncthreads();
+  const ChainInst& I = inst[s_i];
+  const int2 kmi = km[s_i];
+  if (kmi.y != MODE || j < kmi.x) return;
+  const int64_t r0 = ((int64_t)blockIdx.x - rstart[s_i]) * kSweepRows;
+  const int64_t r1 = min(r0 + (int64_t)kSweepRows, I.n);
+  const double gs = (MODE == kModeF32) ? I.gs32 : (MODE == kModeDF ? I.gsdf : I.gs64);
+  const IO* z = reinterpret_cast<const IO*>(I.fold);
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const double f = I.idx ? (double)z[I.idx[r]] * (double)I.dup[r] : (double)z[r] * I.nf;
+    I.w[r] = f * gs * I.tvec[r];
+  }
+}
+
+__device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp) {
+  return (int64_t)(cp.last ? 1 : cp.nlb) << cp.no;
+}
+
+}  // namespace
 
 AuxCoef coef_of(const Op& op) {
   AuxCoef c;
@@ -330,57 +405,93 @@ double step_bound(const Op& op, const AuxCoef& c, int dir) {
   return best;
 }
 
-}  // namespace
+// Batch members keep no product buffers of their own: the batch owns them.
+static thread_local bool g_batch_member = false;
+BatchMemberScope::BatchMemberScope() : prev(g_batch_member) { g_batch_member = true; }
+BatchMemberScope::~BatchMemberScope() { g_batch_member = prev; }
 
 void build_aux(Op& op) {
   const int L = op.L;
   const int64_t N = 1ll << L;
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
   if (zb && L % 2) fail(TM_ERR_ARG, "diagonal BNNNI operators need an even width");
+  if (g_batch_member) return;
   // one in-place pass buffer of nlb * 2^NA * 2^L elements (FP64 size)
   const int64_t per = zb ? 16 * N : 4 * N;
   op.ws_a.alloc((size_t)per * 8);
   if (op.kind == K_XDM || op.kind == K_ZBM) op.xp.alloc((size_t)N * 8);  // full-space result before contraction
 }
 
-// y = T x (or T^T x for transposed views); scaled: FP32 result divided by the
-// returned factor.
-// T: arithmetic and pass-buffer type (float, double, or dfloat: FP64-accurate
-// products on the FP32 pipes); IO: element type of x and y.
-template <class T, class IO = T>
-double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cudaStream_t s) {
-  const int L = op.L;
-  const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
-  const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
-  AuxCoef c64 = coef_of(op);
-  const double gb = step_bound(op, c64, dir);
-  // FP32 and double-float steps are normalised (FP32 exponent range)
-  const bool norm = (sizeof(T) == 4) || std::is_same<T, dfloat>::value;
-  AuxCoefT<T> c;
-  for (int k = 0; k < 2; ++k) {
-    c.b1[k] = (T)c64.b1[k];
-    c.b2[k] = (T)c64.b2[k];
-    c.b3[k] = (T)c64.b3[k];
+// ------------------------------------------------------------------ autotuner inputs
+namespace {
+__global__ void tune_fill_kernel(double* v, int64_t n, uint64_t seed) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) {
+    uint64_t z = seed + 0x9e3779b97f4a7c15ull * (uint64_t)(i + 1);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    v[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
   }
-  c.g = norm ? (T)(1.0 / gb) : (T)1;
+}
+__global__ void tune_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += st) y[i] = (float)x[i];
+}
+}  // namespace
+
+void fill_uniform_dev(double* v, int64_t n, uint64_t seed, cudaStream_t s) {
+  tune_fill_kernel<<<grid_for(n), 256, 0, s>>>(v, n, seed);
+  TM_CKK("tune_fill");
+}
+void to_f32_dev(const double* x, float* y, int64_t n, cudaStream_t s) {
+  tune_f32_kernel<<<grid_for(n), 256, 0, s>>>(x, y, n);
+  TM_CKK("tune_f32");
+}
+
+// ------------------------------------------------------------------ pass plans and tuning
+// Tile bits and threads per block of the chain passes, per (element size,
+// carried bits, width).  Defaults: 2^13-element tiles for 4-byte elements and
+// 2^12 for 8-byte ones (32 KB either way), 256 threads; the autotuner
+// (tm_chain_autotune) overrides entries with measured choices.
+namespace {
+struct ChainTune {
+  int tile_bits = 0, threads = 0;
+};
+std::mutex g_tune_mu;
+ChainTune g_tune[2][2][33];  // [elem 4/8][zb][L]
+}  // namespace
+
+void chain_tuning(int L, size_t elem, bool zb, int& tile_bits, int& threads) {
+  tile_bits = (elem == 8) ? 12 : 13;
+  threads = 256;
+  if (L < 0 || L > 32) return;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const ChainTune& t = g_tune[elem == 8][zb ? 1 : 0][L];
+  if (t.tile_bits) tile_bits = t.tile_bits;
+  if (t.threads) threads = t.threads;
+}
+
+void chain_set_tuning(int L, size_t elem, bool zb, int tile_bits, int threads) {
+  if (L < 0 || L > 32) fail(TM_ERR_ARG, "width out of range");
+  if (tile_bits && (tile_bits < 10 || tile_bits > (elem == 8 ? 13 : 14))) fail(TM_ERR_ARG, "tile bits out of range");
+  if (threads && threads != 64 && threads != 128 && threads != 256) fail(TM_ERR_ARG, "threads must be 64, 128 or 256");
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune[elem == 8][zb ? 1 : 0][L] = ChainTune{tile_bits, threads};
+}
+
+// The passes of one product: the first holds up to cap0 steps (its sites
+// start at 0), the others up to cap1 (they carry a few contiguous low sites
+// for coalescing); the steps are spread evenly over the passes needed.
+std::vector<ChainPass> chain_plan(int L, bool zb, int nlb, int tile_bits) {
   const int NA = zb ? 2 : 1, KS = zb ? 2 : 1;
   const int nsteps = zb ? L / 2 : L;
-  const double gscale = norm ? std::pow(gb, (double)nsteps) : 1.0;
-  const double sf = scaled ? 1.0 : gscale;
-  const int bc = zb ? 0 : op.boundary;
-  const int nlb = zb ? 4 : (bc == 0 ? 2 : 1);
-  const int tile_bits = (sizeof(T) == 8) ? 12 : 13;  // 32 KB tiles
-  T* P = op.ws_a.as<T>();
-  const uint32_t* smap = reduced ? op.smap.as<uint32_t>() : nullptr;
-  IO* fold_out = reduced ? op.xp.as<IO>() : y;
-  const double postc = zb ? sf : (reduced ? sf : op.normfactor * sf);
-  const double* post = reduced ? nullptr : op.tvec.as<double>();
-  // passes: the first holds up to cap0 steps (its sites start at 0), the
-  // others up to cap1 (they carry a few contiguous low sites for
-  // coalescing); the steps are spread evenly over the passes needed
   const int cbn = zb ? 2 : 3;
   const int cap0 = std::max(1, (tile_bits - NA) / KS), cap1 = std::max(1, (tile_bits - NA - cbn) / KS);
   const int npass = (nsteps <= cap0) ? 1 : 1 + (nsteps - cap0 + cap1 - 1) / cap1;
+  std::vector<ChainPass> out;
   int t0 = 0, pass = 0;
   while (t0 < nsteps) {
     // tile state bits: contiguous low sites for coalescing (none when the
@@ -407,10 +518,55 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
     cp.first = (t0 == 0);
     cp.last = (t0 + T_ >= nsteps);
     cp.nlb = nlb;
-    const int64_t nblocks = (int64_t)(cp.last ? 1 : nlb) << cp.no;
-    const int tile = 1 << (NA + cp.nst);
-    const size_t shm = chain_acc_offset(tile, sizeof(T)) + (cp.last ? (size_t)(tile >> NA) * 8 : 0);
-    const int threads = 256;
+    out.push_back(cp);
+    t0 += T_;
+  }
+  return out;
+}
+
+// blocks of one pass and its dynamic shared memory
+int64_t chain_pass_blocks(const ChainPass& cp) { return (int64_t)(cp.last ? 1 : cp.nlb) << cp.no; }
+size_t chain_pass_smem(const ChainPass& cp, bool zb, size_t elem) {
+  const int NA = zb ? 2 : 1;
+  const int tile = 1 << (NA + cp.nst);
+  return chain_acc_offset(tile, elem) + (cp.last ? (size_t)(tile >> NA) * 8 : 0);
+}
+
+// y = T x (or T^T x for transposed views); scaled: FP32 result divided by the
+// returned factor.
+// T: arithmetic and pass-buffer type (float, double, or dfloat: FP64-accurate
+// products on the FP32 pipes); IO: element type of x and y.
+template <class T, class IO = T>
+double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cudaStream_t s) {
+  const int L = op.L;
+  const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
+  const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
+  AuxCoef c64 = coef_of(op);
+  const double gb = step_bound(op, c64, dir);
+  // FP32 and double-float steps are normalised (FP32 exponent range)
+  const bool norm = (sizeof(T) == 4) || std::is_same<T, dfloat>::value;
+  AuxCoefT<T> c;
+  for (int k = 0; k < 2; ++k) {
+    c.b1[k] = (T)c64.b1[k];
+    c.b2[k] = (T)c64.b2[k];
+    c.b3[k] = (T)c64.b3[k];
+  }
+  c.g = norm ? (T)(1.0 / gb) : (T)1;
+  const int nsteps = zb ? L / 2 : L;
+  const double gscale = norm ? std::pow(gb, (double)nsteps) : 1.0;
+  const double sf = scaled ? 1.0 : gscale;
+  const int bc = zb ? 0 : op.boundary;
+  const int nlb = zb ? 4 : (bc == 0 ? 2 : 1);
+  int tile_bits = 0, threads = 0;
+  chain_tuning(L, sizeof(T), zb, tile_bits, threads);
+  T* P = op.ws_a.as<T>();
+  const uint32_t* smap = reduced ? op.smap.as<uint32_t>() : nullptr;
+  IO* fold_out = reduced ? op.xp.as<IO>() : y;
+  const double postc = zb ? sf : (reduced ? sf : op.normfactor * sf);
+  const double* post = reduced ? nullptr : op.tvec.as<double>();
+  for (const ChainPass& cp : chain_plan(L, zb, nlb, tile_bits)) {
+    const int64_t nblocks = chain_pass_blocks(cp);
+    const size_t shm = chain_pass_smem(cp, zb, sizeof(T));
     if (zb) {
       raise_smem_limit((const void*)chain_kernel<T, 1, IO>, shm);
       chain_kernel<T, 1, IO><<<(unsigned)nblocks, threads, shm, s>>>(P, x, op.tvec.as<double>(), smap, fold_out, post,
@@ -421,7 +577,6 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
                                                                 postc, L, bc, dir, c, cp);
     }
     TM_CKK("aux_chain");
-    t0 += T_;
   }
   if (reduced) {
     red_contract<IO><<<grid_for(op.n), 256, 0, s>>>(fold_out, op.idx.as<uint32_t>(), op.dup.as<uint16_t>(),
@@ -429,6 +584,174 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
     TM_CKK("red_contract");
   }
   return scaled ? gscale : 1.0;
+}
+
+// ------------------------------------------------------------------ batch members
+void chain_inst_fill(const Op& op, int dir, ChainInst& rec) {
+  const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
+  const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
+  const int L = op.L;
+  rec.L = L;
+  rec.zb = zb;
+  rec.bc = zb ? 0 : op.boundary;
+  rec.dir = dir;
+  rec.nlb = zb ? 4 : (rec.bc == 0 ? 2 : 1);
+  rec.n = op.n;
+  // full DNNI applies the normfactor at the output; the BNNNI Tvec holds it
+  rec.nf = (reduced || zb) ? 1.0 : op.normfactor;
+  const AuxCoef c = coef_of(op);
+  const double gb = step_bound(op, c, dir);
+  const int nsteps = zb ? L / 2 : L;
+  for (int q = 0; q < 2; ++q) {
+    rec.c32.b1[q] = (float)c.b1[q];
+    rec.c32.b2[q] = (float)c.b2[q];
+    rec.c32.b3[q] = (float)c.b3[q];
+    rec.cdf.b1[q] = dfloat(c.b1[q]);
+    rec.cdf.b2[q] = dfloat(c.b2[q]);
+    rec.cdf.b3[q] = dfloat(c.b3[q]);
+    rec.c64.b1[q] = c.b1[q];
+    rec.c64.b2[q] = c.b2[q];
+    rec.c64.b3[q] = c.b3[q];
+  }
+  rec.c32.g = (float)(1.0 / gb);
+  rec.cdf.g = dfloat(1.0 / gb);
+  rec.c64.g = 1.0;
+  rec.gs32 = rec.gsdf = std::pow(gb, (double)nsteps);
+  rec.gs64 = 1.0;
+  int tb4 = 0, th4 = 0, tb8 = 0, th8 = 0;
+  chain_tuning(L, 4, zb, tb4, th4);
+  chain_tuning(L, 8, zb, tb8, th8);
+  const std::vector<ChainPass> p4 = chain_plan(L, zb, rec.nlb, tb4), p8 = chain_plan(L, zb, rec.nlb, tb8);
+  if ((int)p4.size() > kChainMaxPass || (int)p8.size() > kChainMaxPass) fail(TM_ERR_LIMIT, "too many chain passes");
+  rec.np4 = (int)p4.size();
+  rec.np8 = (int)p8.size();
+  for (int q = 0; q < rec.np4; ++q) rec.p4[q] = p4[q];
+  for (int q = 0; q < rec.np8; ++q) rec.p8[q] = p8[q];
+  rec.smap = reduced ? op.smap.as<uint32_t>() : nullptr;
+  rec.tvec = op.tvec.as<double>();
+  rec.idx = reduced ? op.idx.as<uint32_t>() : nullptr;
+  rec.dup = reduced ? op.dup.as<uint16_t>() : nullptr;
+}
+
+namespace {
+template <class T, int ZB, class IO, int MODE>
+void launch_batch_pass(const ChainInst* inst, const int2* km, int count, const int64_t* start, int pass, int64_t nblk,
+                       int j, int threads, size_t smem, cudaStream_t s) {
+  raise_smem_limit((const void*)chain_batch_kernel<T, ZB, IO, MODE>, smem);
+  chain_batch_kernel<T, ZB, IO, MODE><<<(unsigned)nblk, threads, smem, s>>>(inst, km, start, count, pass, j);
+  TM_CKK("chain_batch");
+}
+
+template <int ZB, int MODE>
+int batch_product_mode(const ChainInst* inst, const int2* km, int count, const int64_t* start, int np,
+                       const std::vector<int64_t>& nblk,
+                       const int64_t* rstart, int64_t nrblk, int j, int threads, size_t smem, cudaStream_t s) {
+  int launches = 0;
+  for (int p = 0; p < np; ++p) {
+    if (nblk[p] == 0) continue;
+    const int64_t* st = start + (size_t)p * (count + 1);
+    if constexpr (MODE == kModeF32)
+      launch_batch_pass<float, ZB, float, MODE>(inst, km, count, st, p, nblk[p], j, threads, smem, s);
+    else if constexpr (MODE == kModeDF)
+      launch_batch_pass<dfloat, ZB, double, MODE>(inst, km, count, st, p, nblk[p], j, threads, smem, s);
+    else
+      launch_batch_pass<double, ZB, double, MODE>(inst, km, count, st, p, nblk[p], j, threads, smem, s);
+    ++launches;
+  }
+  if constexpr (MODE == kModeF32)
+    contract_batch_kernel<float, MODE><<<(unsigned)nrblk, 256, 0, s>>>(inst, km, rstart, count, j);
+  else
+    contract_batch_kernel<double, MODE><<<(unsigned)nrblk, 256, 0, s>>>(inst, km, rstart, count, j);
+  TM_CKK("contract_batch");
+  return launches + 1;
+}
+}  // namespace
+
+int chain_batch_product(const ChainInst* inst, const int2* km, int count, const int64_t* start4, const int64_t* start8,
+                        int np4max,
+                        int np8max, const std::vector<int64_t>& nblk4, const std::vector<int64_t>& nblk8,
+                        const int64_t* rstart, int64_t nrblk, int zb, int mode, int j, int threads4, int threads8,
+                        size_t smem4, size_t smem8, cudaStream_t s) {
+  if (zb) {
+    if (mode == kModeF32)
+      return batch_product_mode<1, kModeF32>(inst, km, count, start4, np4max, nblk4, rstart, nrblk, j, threads4, smem4, s);
+    if (mode == kModeDF)
+      return batch_product_mode<1, kModeDF>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
+    return batch_product_mode<1, kModeF64>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
+  }
+  if (mode == kModeF32)
+    return batch_product_mode<0, kModeF32>(inst, km, count, start4, np4max, nblk4, rstart, nrblk, j, threads4, smem4, s);
+  if (mode == kModeDF)
+    return batch_product_mode<0, kModeDF>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
+  return batch_product_mode<0, kModeF64>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
+}
+
+// ------------------------------------------------------------------ autotuner
+// Time the operator's product (FP32, or the 8-byte double-float engine) over
+// the tile sizes and block sizes the chain kernels take, CUDA events on the
+// operator's stream, and keep the fastest for this (element size, carried
+// bits, width) in the tuning table.  Results do not depend on the choice
+// (same arithmetic per element, in the same order).
+void chain_autotune(const Op& op0, tm_dtype dt, int& best_tb, int& best_th, double& best_ms) {
+  const Op& op = op0.parent ? *op0.parent : op0;
+  if (op.kind != K_ZBT && op.kind != K_ZBM && op.kind != K_XDT && op.kind != K_XDM)
+    fail(TM_ERR_UNSUPPORTED, "the autotuner covers the aux-bit operators (models B and D)");
+  if (!op.ws_a.p) fail(TM_ERR_ARG, "operator has no product buffers (a sweep member)");
+  const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
+  const size_t elem = (dt == TM_F32) ? 4 : 8;
+  cudaStream_t s = op.stream;
+  AllocStream guard(s);
+  DBuf x, y, x32, y32;
+  x.alloc((size_t)op.n * 8);
+  y.alloc((size_t)op.n * 8);
+  x32.alloc((size_t)op.n * 4);
+  y32.alloc((size_t)op.n * 4);
+  fill_uniform_dev(x.as<double>(), op.n, 7, s);
+  to_f32_dev(x.as<double>(), x32.as<float>(), op.n, s);
+  int tb0 = 0, th0 = 0;
+  chain_tuning(op.L, elem, zb, tb0, th0);
+  const int tbs[4] = {11, 12, 13, 14};
+  const int ths[2] = {128, 256};
+  cudaEvent_t e0, e1;
+  TM_CK(cudaEventCreate(&e0));
+  TM_CK(cudaEventCreate(&e1));
+  best_ms = 1e30;
+  best_tb = tb0;
+  best_th = th0;
+  try {
+    for (int tb : tbs) {
+      if (tb > (elem == 8 ? 13 : 14)) continue;
+      for (int th : ths) {
+        chain_set_tuning(op.L, elem, zb, tb, th);
+        auto run = [&]() {
+          if (elem == 4)
+            matvec_aux_dir<float>(op, x32.as<float>(), y32.as<float>(), true, 0, s);
+          else
+            matvec_aux_dir<dfloat, double>(op, x.as<double>(), y.as<double>(), false, 0, s);
+        };
+        run();
+        TM_CK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; ++r) run();
+        TM_CK(cudaEventRecord(e1, s));
+        TM_CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        TM_CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms / 3.0 < best_ms) {
+          best_ms = ms / 3.0;
+          best_tb = tb;
+          best_th = th;
+        }
+      }
+    }
+  } catch (...) {
+    chain_set_tuning(op.L, elem, zb, tb0 == ((elem == 8) ? 12 : 13) ? 0 : tb0, th0 == 256 ? 0 : th0);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  chain_set_tuning(op.L, elem, zb, best_tb, best_th);
 }
 
 template <class T>

@@ -1,14 +1,16 @@
-// Parameter sweeps: many independent operators solved concurrently.
+// Parameter sweeps: many independent operators solved together.
 //
 // The reference runs one parameter point per tmat invocation (TMat/main.cpp,
 // TMat/pfunc.cpp:16-106): build the operator, solve, write the outputs.  A
-// sweep over (betaJ, kappa, h, L) points is that loop run many times.  Here
-// the points run on a pool of host threads, each building, solving and
+// sweep over (betaJ, kappa, h, L) points is that loop run many times.
+//
+// Aux-bit operators (models B and D) run as one device batch (tm_sweep.cu):
+// every chain pass is one launch over all points' tiles, and the points run
+// Arnoldi in lockstep, one CUDA graph per restart cycle.  The other operator
+// families run on a pool of host threads, each building, solving and
 // releasing one operator at a time on that operator's own CUDA stream, so the
-// kernels of different points overlap on the GPU (the small per-point
-// launches of L <= 24 operators do not fill 152 SMs on their own).  Device
-// memory is allocated stream-ordered, so one point's frees do not stall the
-// others.
+// kernels of different points overlap on the GPU.  Device memory is
+// allocated stream-ordered, so one point's frees do not stall the others.
 #include <algorithm>
 #include <atomic>
 #include <string>
@@ -27,6 +29,24 @@ extern "C" tm_status tm_eigs_batch(const tm_params* params, int count, char mode
     return TM_ERR_ARG;
   }
   if (count == 0) return TM_OK;
+  const bool aux = (model == 'B' && (axialdir == 3 || axialdir == 7)) ||
+                   (model == 'D' && dim == 2 &&
+                    (axialdir == 1 || axialdir == 2 || axialdir == 5 || axialdir == 6 || axialdir == 17 ||
+                     axialdir == 18));
+  if (aux) {
+    tm_sweep* sw = nullptr;
+    tm_status c = tm_sweep_create(params, count, model, dim, axialdir, extend_cond, &sw);
+    if (c != TM_OK) {
+      if (status)
+        for (int i = 0; i < count; ++i) status[i] = c;
+      return c;
+    }
+    c = tm_sweep_eigs(sw, nev, 0, tol, mode, vals_re, vals_im, infos, status);
+    const std::string err = tm_last_error();
+    tm_sweep_destroy(sw);
+    if (c != TM_OK) set_error(err);
+    return c;
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     set_error("tm_eigs_batch: no CUDA device");

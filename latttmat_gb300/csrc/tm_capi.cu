@@ -33,12 +33,19 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
 
 static std::atomic<int64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// kernels replayed inside a CUDA graph (or taken back when counted at capture)
+void note_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// The attribute belongs to the current device, so the cache is kept per
+// (device, kernel).
 void raise_smem_limit(const void* kernel, size_t bytes) {
   static std::mutex mu;
-  static std::unordered_map<const void*, size_t> cur;
+  static std::unordered_map<const void*, size_t> cur[64];
+  int dev = 0;
+  TM_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) fail(TM_ERR_LIMIT, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(mu);
-  size_t& c = cur[kernel];
+  size_t& c = cur[dev][kernel];
   if (bytes <= c) return;
   TM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   c = bytes;
@@ -65,9 +72,12 @@ static void pool_setup(int dev) {
   done[dev] = true;
 }
 
+static std::atomic<int64_t> g_allocs{0};
+
 void DBuf::alloc(size_t b) {
   release();
   if (b == 0) b = 16;
+  g_allocs.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e;
   if (g_alloc_stream) {
     int dev = 0;
@@ -350,7 +360,7 @@ static void build_op(Op& op) {
   if (!bfly_core(op.kind)) build_aux(op);
 }
 
-static Op* create_op(const tm_params* p, char model, int dim, int axialdir, int ec) {
+Op* create_op(const tm_params* p, char model, int dim, int axialdir, int ec) {
   if (!p) fail(TM_ERR_ARG, "null params");
   if (dim != 2 && dim != 3) fail(TM_ERR_ARG, "dim must be 2 or 3");
   if (model != 'A' && model != 'B' && model != 'D') fail(TM_ERR_ARG, "model must be A, B or D");
@@ -696,6 +706,8 @@ tm_status tm_phys_extend(const tm_op* op, const double* ql, const double* qr, do
 }
 
 int64_t tm_launch_count(void) { return g_launches.load(); }
+
+int64_t tm_alloc_count(void) { return ltm::g_allocs.load(); }
 
 void tm_debug_set_eo_tile_bits(int bits) { ltm::eo_set_tile_bits_cap(bits); }
 

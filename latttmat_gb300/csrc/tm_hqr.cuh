@@ -5,8 +5,9 @@
 //    Matrix Computations, Alg. 7.4.2, 7.5.1, 7.5.2) for all eigenvalues.
 //  geneig_vector: right eigenvector for one (complex) eigenvalue by inverse
 //    iteration on (A - lambda I) with complex LU and partial pivoting.
-// The device kernels in tm_arnoldi.cu call these on shared/local arrays; a CPU
-// test compiles the same header with the host compiler.
+// The Arnoldi solver (tm_arnoldi.cu) calls these on the host, where the
+// projected matrices are brought back anyway; a CPU test compiles the same
+// header with the host compiler.
 #pragma once
 #include <math.h>
 

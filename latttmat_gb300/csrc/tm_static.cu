@@ -34,11 +34,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// Device address of g_static_scratch for the current device (looked up once
-// per device, with that device current, and cached).
-double* scratch_for_current_device() {
-  int dev = 0;
-  TM_CK(cudaGetDevice(&dev));
+// Device address of g_static_scratch on device `dev`, which must be the
+// current device (looked up once per device, with that device current, and
+// cached).
+double* scratch_for_device(int dev) {
   if (dev < 0 || dev >= kMaxDevices) fail(TM_ERR_LIMIT, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_scratch_ptr[dev]) {
@@ -68,7 +67,16 @@ void perform_op_static(const Op& op, const double* x, double* y, cudaStream_t s)
              kStaticScratchDoubles);
     fail(TM_ERR_LIMIT, buf);
   }
-  double* base = scratch_for_current_device();
+  // the operator's tables live on b.device; the scratch and the launches must
+  // be on that device too
+  int dev = 0;
+  TM_CK(cudaGetDevice(&dev));
+  if (dev != b.device) {
+    char buf[160];
+    snprintf(buf, sizeof(buf), "the operator was created on device %d but device %d is current", b.device, dev);
+    fail(TM_ERR_ARG, buf);
+  }
+  double* base = scratch_for_device(dev);
   double* xp = base;
   double* yp = xp + R;
   double* u = yp + R;
@@ -95,6 +103,9 @@ extern "C" tm_status tm_perform_op_dev_noalloc(const tm_op* op, const double* x_
   } catch (const Failure& f) {
     set_error(f.msg);
     return f.code;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return TM_ERR_CUDA;
   }
   return TM_OK;
 }

@@ -1,0 +1,850 @@
+// Parameter sweeps of aux-bit operators (diagonal BNNNI, DNNI) solved as one
+// batch on the device.
+//
+// The reference runs one parameter point per tmat invocation (TMat/main.cpp,
+// TMat/pfunc.cpp:16-106): build the operator, solve with Spectra, write the
+// outputs.  A sweep over (betaJ, kappa, kappa2, h, L) points is that run
+// repeated.  Here every point of a sweep is a member of one batch:
+//   - an instance table in device memory (ChainInst, tm_chain.h) holds each
+//     member's pass geometry, Boltzmann factors and buffers, whatever its
+//     width;
+//   - each chain pass is ONE launch over the tiles of every member (a block
+//     finds its member by binary search over the pass's block prefix); so are
+//     the contraction and the Krylov vector kernels (row chunks of
+//     kSweepRows);
+//   - the members run Arnoldi in lockstep: at step j every member extends its
+//     basis by column j+1, and member i takes part when j >= k_i, its kept
+//     columns after the last restart (km[i] on the device);
+//   - the steps of one restart cycle are captured once in a CUDA graph and
+//     replayed each cycle;
+//   - between cycles the host solves each member's small projected problem
+//     (the Krylov-Schur restart of tm_arnoldi.cu, tm_krylov.h) and uploads the
+//     new kept bases; converged members go idle;
+//   - members are grouped into waves whose buffers fit a share of the free
+//     device memory; a wave holds members of any mix of widths.
+// Mixed precision as in tm_arnoldi.cu: FP32 products until the Ritz residuals
+// reach the FP32 floor, then FP64-accurate (double-float) products from the
+// combined wanted Ritz vectors until the tolerance is met.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "tm_blas.cuh"
+#include "tm_chain.h"
+#include "tm_internal.h"
+#include "tm_krylov.h"
+
+namespace ltm {
+
+void note_launches(int64_t n);
+
+namespace {
+
+constexpr int kSweepMaxM = 24;  // largest Krylov subspace of a sweep member
+// per-member small values (doubles): CGS coefficients, |w|^2, projected matrix
+constexpr int kScH1 = 0, kScH2 = 32, kScN = 64, kScH = 72;
+constexpr int kScStride = kScH + (kSweepMaxM + 1) * (kSweepMaxM + 1) + 7;  // 704
+
+__device__ __forceinline__ int find_member(const int64_t* __restrict__ start, int count, int64_t b) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// the member and row range of a row-chunk block
+struct RowBlock {
+  int i;
+  int64_t r0, r1;
+};
+
+__device__ __forceinline__ RowBlock row_block(const ChainInst* __restrict__ inst, const int64_t* __restrict__ rstart,
+                                              int count) {
+  __shared__ int s_i;
+  if (threadIdx.x == 0) s_i = find_member(rstart, count, blockIdx.x);
+  __syncthreads();
+  RowBlock rb;
+  rb.i = s_i;
+  rb.r0 = ((int64_t)blockIdx.x - rstart[s_i]) * kSweepRows;
+  rb.r1 = min(rb.r0 + (int64_t)kSweepRows, inst[s_i].n);
+  return rb;
+}
+
+__device__ __forceinline__ bool step_on(int2 km, int j) { return km.y != kModeIdle && j >= km.x; }
+
+// x32 = (float) V[:, j] for the members in the FP32 phase
+__global__ void __launch_bounds__(256) sw_to_f32(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                                                 const int64_t* __restrict__ rstart, int count, int j) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  const int2 k = km[rb.i];
+  if (k.y != kModeF32 || j < k.x) return;
+  const ChainInst& I = inst[rb.i];
+  const double* v = I.V + (int64_t)j * I.ldv;
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) I.x32[r] = (float)v[r];
+}
+
+// partial dots of w against columns 0..j: one warp per column, lanes over rows
+__global__ void __launch_bounds__(256) sw_mdot(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                                               const int64_t* __restrict__ rstart, int count, int j,
+                                               double* __restrict__ part) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  if (!step_on(km[rb.i], j)) return;
+  const ChainInst& I = inst[rb.i];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int c = warp; c <= j; c += nw) {
+    const double* __restrict__ v = I.V + (int64_t)c * I.ldv;
+    double acc = 0.0;
+    for (int64_t r = rb.r0 + lane; r < rb.r1; r += 32) acc = fma(v[r], I.w[r], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) part[(int64_t)blockIdx.x * kSweepMaxM + c] = acc;
+  }
+}
+
+// partial |w|^2 (slot 0)
+__global__ void __launch_bounds__(256) sw_nrm(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                                              const int64_t* __restrict__ rstart, int count, int j,
+                                              double* __restrict__ part) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  if (!step_on(km[rb.i], j)) return;
+  const ChainInst& I = inst[rb.i];
+  double acc = 0.0;
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) acc = fma(I.w[r], I.w[r], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
+    part[(int64_t)blockIdx.x * kSweepMaxM] = t;
+  }
+}
+
+// sum the row-chunk partials of each member into sc[off + c], c <= j (one
+// block per member, one thread per column; fixed order, so deterministic)
+__global__ void sw_reduce(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                          const int64_t* __restrict__ rstart, int j, const double* __restrict__ part, int off) {
+  const int i = blockIdx.x, c = threadIdx.x;
+  if (!step_on(km[i], j) || c > j) return;
+  double acc = 0.0;
+  for (int64_t b = rstart[i]; b < rstart[i + 1]; ++b) acc += part[b * kSweepMaxM + c];
+  inst[i].sc[off + c] = acc;
+}
+
+// w -= V[:, 0..j] h, h = sc[off .. off + j]
+__global__ void __launch_bounds__(256) sw_maxpy(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                                                const int64_t* __restrict__ rstart, int count, int j, int off) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  if (!step_on(km[rb.i], j)) return;
+  const ChainInst& I = inst[rb.i];
+  __shared__ double hs[kSweepMaxM];
+  if (threadIdx.x <= j) hs[threadIdx.x] = I.sc[off + threadIdx.x];
+  __syncthreads();
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) {
+    double acc = I.w[r];
+    for (int c = 0; c <= j; ++c) acc = fma(-I.V[(int64_t)c * I.ldv + r], hs[c], acc);
+    I.w[r] = acc;
+  }
+}
+
+// |w|^2 from the partials; column j of the projected matrix:
+// H[0..j, j] = h1 + h2, H[j+1, j] = |w|
+__global__ void sw_hcol(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                        const int64_t* __restrict__ rstart, int j, int m, const double* __restrict__ part) {
+  const int i = blockIdx.x, c = threadIdx.x;
+  if (!step_on(km[i], j)) return;
+  double* sc = inst[i].sc;
+  double* H = sc + kScH;
+  const int ld = m + 1;
+  if (c == 0) {
+    double acc = 0.0;
+    for (int64_t b = rstart[i]; b < rstart[i + 1]; ++b) acc += part[b * kSweepMaxM];
+    sc[kScN] = acc;
+    H[(j + 1) + j * ld] = sqrt(acc);
+  }
+  if (c <= j) H[c + j * ld] = sc[kScH1 + c] + sc[kScH2 + c];
+}
+
+// V[:, j+1] = w / |w| (zero column on a breakdown: the residual is then 0)
+__global__ void __launch_bounds__(256) sw_normalize(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
+                                                    const int64_t* __restrict__ rstart, int count, int j) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  if (!step_on(km[rb.i], j)) return;
+  const ChainInst& I = inst[rb.i];
+  const double nsq = I.sc[kScN];
+  const double f = nsq > 0.0 ? 1.0 / sqrt(nsq) : 0.0;
+  double* v = I.V + (int64_t)(j + 1) * I.ldv;
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) v[r] = I.w[r] * f;
+}
+
+// Restart / new start vector of the members with rot[i].x > 0:
+// V[:, 0..k) = V[:, 0..m) W_i (W_i m x k column-major at Wall + i*m*m) and,
+// when rot[i].y, V[:, k] = V[:, m].  Each thread holds one row's m values, so
+// the columns are rewritten in place.
+__global__ void __launch_bounds__(256) sw_rotate(const ChainInst* __restrict__ inst, const int64_t* __restrict__ rstart,
+                                                 int count, int m, const double* __restrict__ Wall,
+                                                 const int2* __restrict__ rot) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  const int2 rp = rot[rb.i];
+  if (rp.x <= 0) return;
+  const ChainInst& I = inst[rb.i];
+  __shared__ double Ws[kSweepMaxM * kSweepMaxM];
+  for (int q = threadIdx.x; q < m * rp.x; q += blockDim.x) Ws[q] = Wall[(int64_t)rb.i * m * m + q];
+  __syncthreads();
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) {
+    double v[kSweepMaxM];
+#pragma unroll
+    for (int q = 0; q < kSweepMaxM; ++q)
+      if (q < m) v[q] = I.V[(int64_t)q * I.ldv + r];
+    for (int c = 0; c < rp.x; ++c) {
+      double acc = 0.0;
+#pragma unroll
+      for (int q = 0; q < kSweepMaxM; ++q)
+        if (q < m) acc = fma(v[q], Ws[c * m + q], acc);
+      I.V[(int64_t)c * I.ldv + r] = acc;
+    }
+    if (rp.y) I.V[(int64_t)rp.x * I.ldv + r] = I.V[(int64_t)m * I.ldv + r];
+  }
+}
+
+// |V[:, 0]|^2 partials and scaling, for members with flag[i] set
+__global__ void __launch_bounds__(256) sw_col0_nrm(const ChainInst* __restrict__ inst, const int64_t* __restrict__ rstart,
+                                                   int count, const int* __restrict__ flag, double* __restrict__ part) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  if (!flag[rb.i]) return;
+  const ChainInst& I = inst[rb.i];
+  double acc = 0.0;
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) acc = fma(I.V[r], I.V[r], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
+    part[(int64_t)blockIdx.x * kSweepMaxM] = t;
+  }
+}
+
+__global__ void __launch_bounds__(256) sw_col0_scale(const ChainInst* __restrict__ inst,
+                                                     const int64_t* __restrict__ rstart, int count,
+                                                     const int* __restrict__ flag, const double* __restrict__ part) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  if (!flag[rb.i]) return;
+  const ChainInst& I = inst[rb.i];
+  __shared__ double f;
+  if (threadIdx.x == 0) {
+    double acc = 0.0;
+    for (int64_t b = rstart[rb.i]; b < rstart[rb.i + 1]; ++b) acc += part[b * kSweepMaxM];
+    f = acc > 0.0 ? 1.0 / sqrt(acc) : 0.0;
+  }
+  __syncthreads();
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) I.V[r] *= f;
+}
+
+// y_i = w_i (the product-only entry point), for members in `mode`
+__global__ void __launch_bounds__(256) sw_copy_out(const ChainInst* __restrict__ inst, const int64_t* __restrict__ rstart,
+                                                   int count, double* const* __restrict__ y) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  const ChainInst& I = inst[rb.i];
+  double* yi = y[rb.i];
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) yi[r] = I.w[r];
+}
+
+__global__ void __launch_bounds__(256) sw_copy_in(const ChainInst* __restrict__ inst, const int64_t* __restrict__ rstart,
+                                                  int count, const double* const* __restrict__ x) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  const ChainInst& I = inst[rb.i];
+  const double* xi = x[rb.i];
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) I.V[r] = xi[r];
+}
+
+// ------------------------------------------------------------------ host side
+struct OpDeleter {
+  void operator()(Op* o) const {
+    if (!o) return;
+    cudaStream_t st = o->stream;
+    delete o;
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+  }
+};
+
+// Solve state of one member.
+struct Member {
+  std::unique_ptr<Op, OpDeleter> op;
+  int phase = kModeIdle;  // product mode of the current cycles
+  int k = 0;              // kept columns
+  bool done = false;
+  tm_status status = TM_OK;
+  std::string msg;
+  double best = 1e300;
+  int stall = 0, cycles = 0;
+  tm_eigs_info info{};
+  std::vector<std::complex<double>> vals;
+};
+
+}  // namespace
+
+struct Sweep {
+  char model;
+  int dim, axialdir, ec;
+  std::vector<Member> mem;
+  cudaStream_t s = nullptr;
+  int zb = 0;
+  size_t budget_override = 0;  // bytes of member buffers per wave (0: from free memory)
+  int64_t graph_launches = 0;
+
+  ~Sweep() {
+    mem.clear();
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  }
+
+  // device memory one member needs in a wave (basis of m+1 columns)
+  size_t member_bytes(const Op& o, int m) const {
+    const int64_t N = 1ll << o.L;
+    const int64_t per = zb ? 16 * N : 4 * N;
+    return (size_t)per * 8 + (size_t)N * 8 + (size_t)(m + 1) * o.n * 8 + (size_t)o.n * 12 + kScStride * 8 + 4096;
+  }
+
+  std::vector<std::pair<int, int>> waves(int m) const {
+    size_t budget = budget_override;
+    if (!budget) {
+      size_t fr = 0, tot = 0;
+      TM_CK(cudaMemGetInfo(&fr, &tot));
+      budget = (size_t)(0.6 * (double)fr);
+    }
+    std::vector<std::pair<int, int>> w;
+    int a = 0;
+    size_t used = 0;
+    for (int i = 0; i < (int)mem.size(); ++i) {
+      const size_t b = member_bytes(*mem[i].op, m);
+      if (i > a && used + b > budget) {
+        w.push_back({a, i});
+        a = i;
+        used = 0;
+      }
+      used += b;
+    }
+    if (a < (int)mem.size()) w.push_back({a, (int)mem.size()});
+    return w;
+  }
+};
+
+namespace {
+
+// Buffers and device tables of one wave of members [a, b).
+struct Wave {
+  Sweep& sw;
+  int a, b, count, m;
+  std::vector<std::unique_ptr<DBuf>> bufs;
+  DBuf inst, kmd, start4, start8, rstart, part, sc, Wall, rot, flag, yptr;
+  std::vector<ChainInst> host;
+  std::vector<int64_t> nblk4, nblk8, rst;
+  int np4max = 0, np8max = 0, threads4 = 256, threads8 = 256;
+  size_t smem4 = 0, smem8 = 0;
+  int64_t nrblk = 0;
+  std::map<int, cudaGraphExec_t> graphs;  // by first step of the cycle
+  std::map<int, int64_t> graph_kernels;
+
+  Wave(Sweep& s_, int a_, int b_, int m_) : sw(s_), a(a_), b(b_), count(b_ - a_), m(m_) {
+    cudaStream_t s = sw.s;
+    host.resize(count);
+    int Lmax = 0;
+    for (int q = 0; q < count; ++q) {
+      const Op& o = *sw.mem[a + q].op;
+      ChainInst& I = host[q];
+      std::memset(&I, 0, sizeof(I));
+      chain_inst_fill(o, 0, I);
+      const int64_t N = 1ll << o.L;
+      auto mk = [&](size_t bytes) {
+        bufs.emplace_back(new DBuf());
+        bufs.back()->alloc(bytes);
+        return bufs.back()->p;
+      };
+      I.P = mk((size_t)(sw.zb ? 16 * N : 4 * N) * 8);
+      I.fold = mk((size_t)N * 8);
+      I.ldv = (o.n + 1) & ~(int64_t)1;
+      I.V = static_cast<double*>(mk((size_t)(m + 1) * I.ldv * 8));
+      I.w = static_cast<double*>(mk((size_t)o.n * 8));
+      I.x32 = static_cast<float*>(mk((size_t)o.n * 4));
+      np4max = std::max(np4max, I.np4);
+      np8max = std::max(np8max, I.np8);
+      for (int p = 0; p < I.np4; ++p) smem4 = std::max(smem4, chain_pass_smem(I.p4[p], sw.zb, 4));
+      for (int p = 0; p < I.np8; ++p) smem8 = std::max(smem8, chain_pass_smem(I.p8[p], sw.zb, 8));
+      Lmax = std::max(Lmax, o.L);
+    }
+    // threads per block: the tuned choice at the widest member (most of the work)
+    int tb = 0;
+    chain_tuning(Lmax, 4, sw.zb, tb, threads4);
+    chain_tuning(Lmax, 8, sw.zb, tb, threads8);
+    sc.alloc((size_t)count * kScStride * 8);
+    TM_CK(cudaMemsetAsync(sc.p, 0, sc.bytes, s));
+    for (int q = 0; q < count; ++q) host[q].sc = sc.as<double>() + (size_t)q * kScStride;
+    // block prefixes per pass
+    std::vector<int64_t> s4((size_t)std::max(np4max, 1) * (count + 1), 0), s8((size_t)std::max(np8max, 1) * (count + 1), 0);
+    nblk4.assign(std::max(np4max, 1), 0);
+    nblk8.assign(std::max(np8max, 1), 0);
+    for (int p = 0; p < np4max; ++p)
+      for (int q = 0; q < count; ++q)
+        s4[(size_t)p * (count + 1) + q + 1] =
+            s4[(size_t)p * (count + 1) + q] + (p < host[q].np4 ? chain_pass_blocks(host[q].p4[p]) : 0);
+    for (int p = 0; p < np8max; ++p)
+      for (int q = 0; q < count; ++q)
+        s8[(size_t)p * (count + 1) + q + 1] =
+            s8[(size_t)p * (count + 1) + q] + (p < host[q].np8 ? chain_pass_blocks(host[q].p8[p]) : 0);
+    for (int p = 0; p < np4max; ++p) nblk4[p] = s4[(size_t)p * (count + 1) + count];
+    for (int p = 0; p < np8max; ++p) nblk8[p] = s8[(size_t)p * (count + 1) + count];
+    for (int64_t v : nblk4)
+      if (v >= (1ll << 31)) fail(TM_ERR_LIMIT, "sweep wave too large for one launch");
+    for (int64_t v : nblk8)
+      if (v >= (1ll << 31)) fail(TM_ERR_LIMIT, "sweep wave too large for one launch");
+    rst.assign(count + 1, 0);
+    for (int q = 0; q < count; ++q) rst[q + 1] = rst[q] + (host[q].n + kSweepRows - 1) / kSweepRows;
+    nrblk = rst[count];
+    auto up = [&](DBuf& d, const void* src, size_t bytes) {
+      d.alloc(bytes);
+      TM_CK(cudaMemcpyAsync(d.p, src, bytes, cudaMemcpyHostToDevice, s));
+    };
+    up(inst, host.data(), sizeof(ChainInst) * count);
+    up(start4, s4.data(), s4.size() * 8);
+    up(start8, s8.data(), s8.size() * 8);
+    up(rstart, rst.data(), rst.size() * 8);
+    kmd.alloc((size_t)count * sizeof(int2));
+    part.alloc((size_t)nrblk * kSweepMaxM * 8);
+    Wall.alloc((size_t)count * m * m * 8);
+    rot.alloc((size_t)count * sizeof(int2));
+    flag.alloc((size_t)count * sizeof(int));
+    yptr.alloc((size_t)count * sizeof(void*));
+    // synchronise here: the host vectors above must outlive the copies
+    TM_CK(cudaStreamSynchronize(s));
+  }
+
+  ~Wave() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+  }
+
+  const ChainInst* I() const { return inst.as<ChainInst>(); }
+  const int2* km() const { return kmd.as<int2>(); }
+
+  int product(int mode, int j) {
+    int nl = 0;
+    if (mode == kModeF32) {
+      sw_to_f32<<<(unsigned)nrblk, 256, 0, sw.s>>>(I(), km(), rstart.as<int64_t>(), count, j);
+      TM_CKK("sw_to_f32");
+      ++nl;
+    }
+    nl += chain_batch_product(I(), km(), count, start4.as<int64_t>(), start8.as<int64_t>(), np4max, np8max, nblk4, nblk8,
+                              rstart.as<int64_t>(), nrblk, sw.zb, mode, j, threads4, threads8, smem4, smem8, sw.s);
+    return nl;
+  }
+
+  // one Arnoldi step at column j for every member taking part
+  void step(int j, bool f32_phase, bool df_phase, bool f64_phase) {
+    cudaStream_t s = sw.s;
+    const int64_t* rs = rstart.as<int64_t>();
+    double* pt = part.as<double>();
+    if (f32_phase) product(kModeF32, j);
+    if (df_phase) product(kModeDF, j);
+    if (f64_phase) product(kModeF64, j);
+    for (int pass = 0; pass < 2; ++pass) {
+      const int off = pass ? kScH2 : kScH1;
+      sw_mdot<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j, pt);
+      TM_CKK("sw_mdot");
+      sw_reduce<<<count, 32, 0, s>>>(I(), km(), rs, j, pt, off);
+      TM_CKK("sw_reduce");
+      sw_maxpy<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j, off);
+      TM_CKK("sw_maxpy");
+    }
+    sw_nrm<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j, pt);
+    TM_CKK("sw_nrm");
+    sw_hcol<<<count, 32, 0, s>>>(I(), km(), rs, j, m, pt);
+    TM_CKK("sw_hcol");
+    sw_normalize<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j);
+    TM_CKK("sw_normalize");
+  }
+
+  // the steps j = k0 .. m-1 of a cycle, as a CUDA graph captured on first use
+  void cycle(int k0, bool f32_phase, bool df_phase, bool f64_phase) {
+    const int key = k0 | (f32_phase << 8) | (df_phase << 9) | (f64_phase << 10);
+    auto it = graphs.find(key);
+    if (it == graphs.end()) {
+      const int64_t l0 = tm_launch_count();
+      cudaGraph_t g;
+      TM_CK(cudaStreamBeginCapture(sw.s, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int j = k0; j < m; ++j) step(j, f32_phase, df_phase, f64_phase);
+      } catch (...) {
+        cudaStreamEndCapture(sw.s, &g);
+        throw;
+      }
+      TM_CK(cudaStreamEndCapture(sw.s, &g));
+      cudaGraphExec_t ex;
+      TM_CK(cudaGraphInstantiate(&ex, g, 0));
+      TM_CK(cudaGraphDestroy(g));
+      graph_kernels[key] = tm_launch_count() - l0;
+      it = graphs.emplace(key, ex).first;
+      // the kernels were counted when captured; count them per replay instead
+      note_launches(-graph_kernels[key]);
+    }
+    TM_CK(cudaGraphLaunch(it->second, sw.s));
+    note_launches(graph_kernels[key]);
+  }
+
+  // normalise V[:, 0] of the flagged members
+  void normalize_starts(const std::vector<int>& fl) {
+    TM_CK(cudaMemcpyAsync(flag.p, fl.data(), fl.size() * sizeof(int), cudaMemcpyHostToDevice, sw.s));
+    sw_col0_nrm<<<(unsigned)nrblk, 256, 0, sw.s>>>(I(), rstart.as<int64_t>(), count, flag.as<int>(), part.as<double>());
+    TM_CKK("sw_col0_nrm");
+    sw_col0_scale<<<(unsigned)nrblk, 256, 0, sw.s>>>(I(), rstart.as<int64_t>(), count, flag.as<int>(),
+                                                      part.as<double>());
+    TM_CKK("sw_col0_scale");
+  }
+};
+
+}  // namespace
+
+// Solve every member: nev wanted eigenvalues to tol (relative), mode
+// TM_EIGS_F64 or TM_EIGS_MIXED.
+void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
+  if (nev < 1) fail(TM_ERR_ARG, "nev must be >= 1");
+  int64_t nmin = INT64_MAX;
+  for (auto& mb : sw.mem) nmin = std::min(nmin, mb.op->n);
+  int m = ncv > 0 ? ncv : ((nev > 4) ? 2 * nev + 1 : 2 * nev + 3);
+  m = std::max(m, 2 * nev + 2);
+  m = std::min<int64_t>(m, nmin - 1);
+  if (m > kSweepMaxM - 1) fail(TM_ERR_LIMIT, "sweep subspace larger than 23");
+  if (m < nev + 2) fail(TM_ERR_ARG, "operators too small for the requested eigenvalues");
+  if (tol <= 0) tol = 1e-10;
+  const double tol32 = std::max(tol, 3e-7);
+  const int first_phase = (mode == TM_EIGS_MIXED) ? kModeF32 : kModeF64;
+  const int final_phase = (mode == TM_EIGS_MIXED) ? kModeDF : kModeF64;
+  const int max_cycles = (mode == TM_EIGS_MIXED) ? 200 : 300;
+  for (auto& wv : sw.waves(m)) {
+    AllocStream guard(sw.s);
+    Wave W(sw, wv.first, wv.second, m);
+    const int count = W.count;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<int2> kmh(count);
+    std::vector<int> fl(count, 1);
+    for (int q = 0; q < count; ++q) {
+      Member& mb = sw.mem[W.a + q];
+      mb.phase = first_phase;
+      mb.k = 0;
+      mb.done = false;
+      mb.info = tm_eigs_info{};
+      mb.info.ncv = m;
+      fill_uniform(W.host[q].V, mb.op->n, 0, sw.s);  // start vector uniform(0,1), seed 0
+    }
+    W.normalize_starts(fl);
+    std::vector<double> sch((size_t)count * kScStride, 0.0), Wh((size_t)count * m * m, 0.0);
+    std::vector<int2> roth(count);
+    while (true) {
+      int kmin = m;
+      bool ph[4] = {false, false, false, false};
+      for (int q = 0; q < count; ++q) {
+        Member& mb = sw.mem[W.a + q];
+        const bool on = !mb.done && mb.status == TM_OK;
+        kmh[q] = make_int2(mb.k, on ? mb.phase : kModeIdle);
+        if (on) {
+          kmin = std::min(kmin, mb.k);
+          ph[mb.phase] = true;
+        }
+      }
+      if (kmin >= m) break;  // every member finished
+      TM_CK(cudaMemcpyAsync(W.kmd.p, kmh.data(), count * sizeof(int2), cudaMemcpyHostToDevice, sw.s));
+      W.cycle(kmin, ph[kModeF32], ph[kModeDF], ph[kModeF64]);
+      TM_CK(cudaMemcpyAsync(sch.data(), W.sc.p, sch.size() * 8, cudaMemcpyDeviceToHost, sw.s));
+      TM_CK(cudaStreamSynchronize(sw.s));
+      bool any_rot = false, any_start = false;
+      for (int q = 0; q < count; ++q) {
+        roth[q] = make_int2(0, 0);
+        fl[q] = 0;
+        Member& mb = sw.mem[W.a + q];
+        if (mb.done || mb.status != TM_OK) continue;
+        double* Hh = sch.data() + (size_t)q * kScStride + kScH;
+        const int steps = m - mb.k;
+        mb.info.matvecs += steps;
+        if (mb.phase != kModeF32) mb.info.matvecs_f64 += steps;
+        ++mb.cycles;
+        try {
+          const int kvec = krylov_kvec(m, nev);
+          Ritz R = krylov_project(Hh, m, kvec);
+          const double ref = std::abs(R.theta[0]);
+          const bool f32 = (mb.phase == kModeF32);
+          bool ok = true;
+          int nconv = 0;
+          double worst = 0.0;
+          for (int i = 0; i < nev; ++i) {
+            const double lim = f32 ? tol32 * ref : tol * std::max(std::abs(R.theta[i]), 1e-300);
+            worst = std::max(worst, R.resid[i] / std::max(ref, 1e-300));
+            if (R.resid[i] <= lim)
+              ++nconv;
+            else
+              ok = false;
+          }
+          bool to_final = false;
+          if (f32) {
+            if (ok) {
+              to_final = true;
+            } else if (worst < 0.7 * mb.best) {
+              mb.best = worst;
+              mb.stall = 0;
+            } else if (++mb.stall >= 3 && worst < 1e-4) {
+              to_final = true;
+            }
+          } else if (ok) {
+            mb.done = true;
+            mb.info.nconv = nev;
+            double mr = 0;
+            for (int i = 0; i < nev; ++i) mr = std::max(mr, R.resid[i] / std::max(std::abs(R.theta[i]), 1e-300));
+            mb.info.max_resid = mr;
+            mb.vals.assign(R.theta.begin(), R.theta.begin() + nev);
+            continue;
+          }
+          if (mb.cycles >= max_cycles) {
+            mb.status = TM_ERR_NOCONV;
+            mb.msg = "sweep member did not converge";
+            mb.vals.assign(R.theta.begin(), R.theta.begin() + nev);
+            continue;
+          }
+          double* Wq = Wh.data() + (size_t)q * m * m;
+          if (to_final) {
+            // restart from the sum of the wanted Ritz vectors' real parts with
+            // FP64-accurate products (the FP32 phase's projection is only FP32
+            // accurate, so it is rebuilt)
+            for (int i = 0; i < m; ++i) {
+              double acc = 0.0;
+              for (int c = 0; c < nev; ++c) acc += R.y[c][i].real();
+              Wq[i] = acc;
+            }
+            roth[q] = make_int2(1, 0);
+            fl[q] = 1;
+            std::fill(Hh, Hh + (m + 1) * (m + 1), 0.0);
+            mb.phase = final_phase;
+            mb.k = 0;
+            mb.cycles = 0;
+            any_start = true;
+          } else {
+            std::vector<double> Wm;
+            int knew = krylov_basis(R, m, krylov_keep(m, nev, nconv, kvec), Wm);
+            if (knew >= m - 1) knew = m - 2;
+            std::copy(Wm.begin(), Wm.begin() + (size_t)m * knew, Wq);
+            std::vector<double> Hn;
+            krylov_restart_h(Hh, m, Wm, knew, R.beta, Hn);
+            std::copy(Hn.begin(), Hn.end(), Hh);
+            roth[q] = make_int2(knew, 1);
+            mb.k = knew;
+            ++mb.info.restarts;
+          }
+          any_rot = true;
+        } catch (const Failure& f) {
+          mb.status = f.code;
+          mb.msg = f.msg;
+        }
+      }
+      if (any_rot) {
+        TM_CK(cudaMemcpyAsync(W.Wall.p, Wh.data(), Wh.size() * 8, cudaMemcpyHostToDevice, sw.s));
+        TM_CK(cudaMemcpyAsync(W.rot.p, roth.data(), count * sizeof(int2), cudaMemcpyHostToDevice, sw.s));
+        TM_CK(cudaMemcpyAsync(W.sc.p, sch.data(), sch.size() * 8, cudaMemcpyHostToDevice, sw.s));
+        sw_rotate<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count, m, W.Wall.as<double>(),
+                                                       W.rot.as<int2>());
+        TM_CKK("sw_rotate");
+        if (any_start) W.normalize_starts(fl);
+      }
+    }
+    TM_CK(cudaStreamSynchronize(sw.s));
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int q = 0; q < count; ++q) sw.mem[W.a + q].info.seconds = secs;
+  }
+}
+
+// y_i = T_i x_i for every member (device FP64 vectors; FP32 computed and
+// widened, or double-float / FP64), one launch per pass over all members.
+void sweep_product(Sweep& sw, const double* const* x, double* const* y, tm_dtype dt) {
+  const int mode = (dt == TM_F32) ? kModeF32 : (dt == TM_F64_DF ? kModeDF : kModeF64);
+  for (auto& wv : sw.waves(1)) {
+    AllocStream guard(sw.s);
+    Wave W(sw, wv.first, wv.second, 1);
+    const int count = W.count;
+    std::vector<int2> kmh(count, make_int2(0, mode));
+    TM_CK(cudaMemcpyAsync(W.kmd.p, kmh.data(), count * sizeof(int2), cudaMemcpyHostToDevice, sw.s));
+    TM_CK(cudaMemcpyAsync(W.yptr.p, x + W.a, count * sizeof(void*), cudaMemcpyHostToDevice, sw.s));
+    sw_copy_in<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count,
+                                                    W.yptr.as<const double* const>());
+    TM_CKK("sw_copy_in");
+    W.product(mode, 0);
+    TM_CK(cudaStreamSynchronize(sw.s));  // the pointer table is rewritten below
+    TM_CK(cudaMemcpyAsync(W.yptr.p, y + W.a, count * sizeof(void*), cudaMemcpyHostToDevice, sw.s));
+    sw_copy_out<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count, W.yptr.as<double* const>());
+    TM_CKK("sw_copy_out");
+    TM_CK(cudaStreamSynchronize(sw.s));
+    for (auto& mb : sw.mem) mb.op->matvecs++;
+  }
+}
+
+bool sweep_supported(const Op& o) { return o.kind == K_ZBM || o.kind == K_ZBT || o.kind == K_XDM || o.kind == K_XDT; }
+
+Sweep* sweep_create(const tm_params* params, int count, char model, int dim, int axialdir, int ec) {
+  if (!params || count < 1) fail(TM_ERR_ARG, "a sweep needs at least one parameter point");
+  std::unique_ptr<Sweep> sw(new Sweep());
+  sw->model = model;
+  sw->dim = dim;
+  sw->axialdir = axialdir;
+  sw->ec = ec;
+  TM_CK(cudaStreamCreateWithFlags(&sw->s, cudaStreamNonBlocking));
+  sw->mem.resize(count);
+  {
+    BatchMemberScope scope;
+    for (int i = 0; i < count; ++i) {
+      sw->mem[i].op.reset(create_op(&params[i], model, dim, axialdir, ec));
+      if (!sweep_supported(*sw->mem[i].op))
+        fail(TM_ERR_UNSUPPORTED, "sweeps cover the aux-bit operators (models B and D)");
+    }
+  }
+  sw->zb = (sw->mem[0].op->kind == K_ZBM || sw->mem[0].op->kind == K_ZBT);
+  TM_CK(cudaDeviceSynchronize());  // tables were built on the members' own streams
+  return sw.release();
+}
+
+}  // namespace ltm
+
+using namespace ltm;
+
+struct tm_sweep {
+  ltm::Sweep* impl;
+};
+
+#define SW_BEGIN try {
+#define SW_END                           \
+  }                                      \
+  catch (const Failure& f) {             \
+    set_error(f.msg);                    \
+    return f.code;                       \
+  }                                      \
+  catch (const std::exception& e) {      \
+    set_error(e.what());                 \
+    return TM_ERR_CUDA;                  \
+  }                                      \
+  return TM_OK;
+
+extern "C" {
+
+tm_status tm_sweep_create(const tm_params* params, int count, char model, int dim, int axialdir, int extend_cond,
+                          tm_sweep** out) {
+  SW_BEGIN
+  if (!out) fail(TM_ERR_ARG, "null output");
+  *out = nullptr;
+  Sweep* s = sweep_create(params, count, model, dim, axialdir, extend_cond);
+  *out = new tm_sweep{s};
+  SW_END
+}
+
+tm_status tm_sweep_destroy(tm_sweep* sw) {
+  SW_BEGIN
+  if (!sw) return TM_OK;
+  delete sw->impl;
+  delete sw;
+  SW_END
+}
+
+int tm_sweep_count(const tm_sweep* sw) { return sw ? (int)sw->impl->mem.size() : -1; }
+
+int64_t tm_sweep_rows(const tm_sweep* sw, int i) {
+  if (!sw || i < 0 || i >= (int)sw->impl->mem.size()) return -1;
+  return sw->impl->mem[i].op->n;
+}
+
+double tm_sweep_normfactor(const tm_sweep* sw, int i) {
+  if (!sw || i < 0 || i >= (int)sw->impl->mem.size()) return 0.0;
+  return sw->impl->mem[i].op->normfactor;
+}
+
+tm_status tm_sweep_set_wave_bytes(tm_sweep* sw, size_t bytes) {
+  SW_BEGIN
+  if (!sw) fail(TM_ERR_ARG, "null sweep");
+  sw->impl->budget_override = bytes;
+  SW_END
+}
+
+tm_status tm_sweep_perform_op_dev(tm_sweep* sw, const double* const* x_dev, double* const* y_dev, tm_dtype dtype) {
+  SW_BEGIN
+  if (!sw || !x_dev || !y_dev) fail(TM_ERR_ARG, "null argument");
+  if (dtype != TM_F32 && dtype != TM_F64 && dtype != TM_F64_DF) fail(TM_ERR_ARG, "bad dtype");
+  sweep_product(*sw->impl, x_dev, y_dev, dtype);
+  SW_END
+}
+
+tm_status tm_sweep_eigs(tm_sweep* sw, int nev, int ncv, double tol, int mode, double* vals_re, double* vals_im,
+                        tm_eigs_info* infos, tm_status* status) {
+  SW_BEGIN
+  if (!sw || !vals_re || !vals_im) fail(TM_ERR_ARG, "null argument");
+  if (mode != TM_EIGS_F64 && mode != TM_EIGS_MIXED) fail(TM_ERR_ARG, "bad mode");
+  Sweep& s = *sw->impl;
+  for (auto& mb : s.mem) {
+    mb.status = TM_OK;
+    mb.msg.clear();
+    mb.vals.clear();
+    mb.best = 1e300;
+    mb.stall = 0;
+    mb.cycles = 0;
+  }
+  sweep_solve(s, nev, ncv, tol, mode);
+  tm_status first = TM_OK;
+  for (int i = 0; i < (int)s.mem.size(); ++i) {
+    Member& mb = s.mem[i];
+    const double nf = mb.op->normfactor;
+    for (int c = 0; c < nev; ++c) {
+      const std::complex<double> z = c < (int)mb.vals.size() ? mb.vals[c] : std::complex<double>(0.0, 0.0);
+      vals_re[(size_t)i * nev + c] = z.real() / nf;
+      vals_im[(size_t)i * nev + c] = z.imag() / nf;
+    }
+    mb.op->matvecs += mb.info.matvecs;
+    if (infos) infos[i] = mb.info;
+    if (status) status[i] = mb.status;
+    if (mb.status != TM_OK && first == TM_OK) {
+      first = mb.status;
+      set_error("sweep member " + std::to_string(i) + ": " + mb.msg);
+    }
+  }
+  return first;
+  SW_END
+}
+
+tm_status tm_chain_autotune(const tm_op* op, tm_dtype dtype, int* tile_bits, int* threads, double* ms) {
+  SW_BEGIN
+  if (!op) fail(TM_ERR_ARG, "null operator");
+  if (dtype != TM_F32 && dtype != TM_F64_DF) fail(TM_ERR_ARG, "the autotuner times TM_F32 or TM_F64_DF products");
+  int tb = 0, th = 0;
+  double t = 0;
+  chain_autotune(*op->impl, dtype, tb, th, t);
+  if (tile_bits) *tile_bits = tb;
+  if (threads) *threads = th;
+  if (ms) *ms = t;
+  SW_END
+}
+
+tm_status tm_chain_set_tuning(char model, int L, tm_dtype dtype, int tile_bits, int threads) {
+  SW_BEGIN
+  if (model != 'B' && model != 'D') fail(TM_ERR_ARG, "model must be B or D");
+  chain_set_tuning(L, dtype == TM_F32 ? 4 : 8, model == 'B', tile_bits, threads);
+  SW_END
+}
+
+}  // extern "C"

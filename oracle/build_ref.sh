@@ -8,10 +8,12 @@
 # Spectra and Eigen, which are absent, so it is not built; the oracle's own
 # Lanczos drives the compiled perform_op instead.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# (default: $TMAT_REFERENCE_ROOT, else /root/reference, where the reference is
+# mounted in the build container; exits 3 when the sources are absent)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${TMAT_REFERENCE_ROOT:-/root/reference}}"
 SRC="$REF/TMat"
 if [ ! -f "$SRC/tmatreduce.cpp" ]; then
   echo "reference sources not found under $SRC; skipping oracle/_ref" >&2

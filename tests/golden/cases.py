@@ -54,6 +54,16 @@ CASES = [
     ("zbm_L12_noflip", "B", 2, 7, 2, 0.5, 0.6, 0.2, 0.0, 12, 2),
     ("zbm_L16_noflip", "B", 2, 7, 2, 0.6, 0.8, 0.0, 0.0, 16, 2),
     ("zbm_L14_h", "B", 2, 7, 0, 0.5, 0.45, 0.1, 0.05, 14, 2),
+    # instances of the 256-point B/7 parameter sweep (widths 16..24, betaJ grid
+    # on [0.2, 1.0], kappa1 uniform; bench.batch_points), numbered by position
+    ("zbm_sw000_L24", "B", 2, 7, 2, 0.2, 0.5118216247002567, 0.0, 0.0, 24, 2),
+    ("zbm_sw001_L22", "B", 2, 7, 2, 0.2031372549019608, 0.9504636963259353, 0.0, 0.0, 22, 2),
+    ("zbm_sw002_L20", "B", 2, 7, 2, 0.2062745098039216, 0.14415961271963373, 0.0, 0.0, 20, 2),
+    ("zbm_sw003_L18", "B", 2, 7, 2, 0.20941176470588235, 0.9486494471372439, 0.0, 0.0, 18, 2),
+    ("zbm_sw005_L16", "B", 2, 7, 2, 0.21568627450980393, 0.42332644897257565, 0.0, 0.0, 16, 2),
+    ("zbm_sw128_L24", "B", 2, 7, 2, 0.6015686274509804, 0.2838064889441311, 0.0, 0.0, 24, 2),
+    ("zbm_sw192_L18", "B", 2, 7, 2, 0.8023529411764707, 0.3626968570578484, 0.0, 0.0, 18, 2),
+    ("zbm_sw255_L18", "B", 2, 7, 2, 1.0, 0.3856578446575508, 0.0, 0.0, 18, 2),
     # two-layer parallel TMs: y-ANNNI full (YATMatVecProd2D and its _T, even L:
     # at odd L the reference's final permutation reads its own output buffer),
     # y2-ANNNI full (Y2ATMatVecProd2D), y-ANNNI and BNNNI reduced
@@ -78,7 +88,21 @@ CASES = [
     ("x3d_5x5_cfg5", "A", 3, 1, 0, 0.2, 0.4, 0.0, 0.0, (5, 5), 2),
 ]
 
-FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums only
+# The headline x-ANNNI reduced operator (A/5, betaJ=0.3, kappa=0.6, h=0) at the
+# widths where the even/odd product splits its tiles over CTA clusters (30, 32)
+# and below; flip off as the reference driver runs neigs > 1 (extend_cond 2),
+# and flip on at L=32.  nev = 0: tables and product only, no eigenvalues.
+# Outputs are stored as checksums plus values at SAMPLE_COUNT seeded indices.
+LARGE_CASES = [
+    ("xam_L26_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 26, 4),
+    ("xam_L28_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 28, 4),
+    ("xam_L30_noflip", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 30, 4),
+    ("xam_L32_flip", "A", 2, 5, 0, 0.3, 0.6, 0.0, 0.0, 32, 0),
+    ("xam_L32_cfg2", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 32, 4),
+]
+
+FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums and samples
+SAMPLE_COUNT = 4096
 
 
 def case_dict(c):
@@ -102,8 +126,14 @@ def checksum_weights(n: int) -> np.ndarray:
     return np.random.default_rng(12345).uniform(0.5, 1.5, n)
 
 
+def sample_indices(n: int) -> np.ndarray:
+    """Sorted distinct seeded positions at which long outputs are stored."""
+    idx = np.unique(np.random.default_rng(777).integers(0, n, SAMPLE_COUNT))
+    return idx.astype(np.int64)
+
+
 def by_name(name):
-    for c in CASES:
+    for c in CASES + LARGE_CASES:
         if c[0] == name:
             return case_dict(c)
     raise KeyError(name)

@@ -9,9 +9,16 @@ oracle/_ref/libtmat_ref.so, on the seeded inputs of cases.py:
     (Spectra, the reference's solver, is not vendored);
   * moments / phys_extend of the leading eigenvector through the reference's own
     functions.
-Long outputs are stored as checksums (sum w*y with fixed weights, ||y||).
+Long outputs are stored as checksums (sum w*y with fixed weights, ||y||) and
+as values at seeded sample positions (cases.sample_indices).
 
-Usage: python tests/golden/make_golden.py   (needs oracle/_ref built)
+The LARGE_CASES of cases.py (x-ANNNI reduced at L = 26..32) run only when named
+or with --large; their eigenvalues use the reference solver's Krylov size
+(ncv = 2*nev+3, TMat/tmat.hpp:88) at tol 1e-12, and the number of reference
+products each ARPACK solve took is stored beside them.  At L = 32 a product
+takes about two minutes on 8 cores and the eigenvalues about an hour and a half.
+
+Usage: python tests/golden/make_golden.py [--large] [names...]   (needs oracle/_ref built)
 """
 from __future__ import annotations
 
@@ -27,7 +34,10 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-from cases import CASES, FULL_VECTOR_MAX, case_dict, checksum_weights, general, seeded_input  # noqa: E402
+import time  # noqa: E402
+
+from cases import (CASES, FULL_VECTOR_MAX, LARGE_CASES, case_dict, checksum_weights, general,  # noqa: E402
+                   sample_indices, seeded_input)
 from oracle.refbind import RefOp, available  # noqa: E402
 
 
@@ -35,23 +45,41 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def gen(c):
+def log(msg):
+    print(f"[{time.strftime('%H:%M:%S')}] {msg}", flush=True)
+
+
+def gen(c, large=False):
     d = case_dict(c)
+    t0 = time.perf_counter()
     op = RefOp(d["model"], d["dim"], d["axialdir"], d["betaJ"], d["kappa"], d["h"], d["size"], d["kappa2"],
                d["extend_cond"])
     n = op.n
+    log(f"{d['name']}: n={n}, constructed in {time.perf_counter() - t0:.1f} s")
     out = dict(n=np.int64(n), normfactor=np.float64(op.normfactor))
+    samp = sample_indices(n) if n > FULL_VECTOR_MAX else None
+    if samp is not None:
+        out["samp_idx"] = samp
     x = seeded_input(n, 1)
+    t0 = time.perf_counter()
     y = op.perform_op(x)
+    log(f"{d['name']}: one product in {time.perf_counter() - t0:.1f} s")
     w = checksum_weights(n)
     out["y_chk"] = np.array([np.dot(w, y), np.linalg.norm(y)])
     if n <= FULL_VECTOR_MAX:
         out["y"] = y
+    else:
+        out["y_samp"] = y[samp]
+    del y
     if op.has_transpose():
         yt = op.perform_op_t(x)
         out["yt_chk"] = np.array([np.dot(w, yt), np.linalg.norm(yt)])
         if n <= FULL_VECTOR_MAX:
             out["yt"] = yt
+        else:
+            out["yt_samp"] = yt[samp]
+        del yt
+    del x, w
     idx, dup = op.orbit()
     if idx is not None:
         out["orbit_n"] = np.int64(len(idx))
@@ -61,15 +89,43 @@ def gen(c):
         if n <= FULL_VECTOR_MAX:
             out["idx"] = idx.astype(np.uint64)
             out["dup"] = dup.astype(np.uint16)
+        else:
+            out["idx_samp"] = idx[samp].astype(np.uint64)
+            out["dup_samp"] = dup[samp].astype(np.uint16)
+    del idx, dup
     # eigenvalues through ARPACK on the reference matvec
     nev = d["nev"]
-    lin = sla.LinearOperator((n, n), matvec=lambda v: op.perform_op(np.ravel(v)), dtype=np.float64)
+    if nev == 0:
+        return d["name"], out
+    count = [0]
+
+    def mv(v):
+        count[0] += 1
+        return op.perform_op(np.ravel(v))
+
+    lin = sla.LinearOperator((n, n), matvec=mv, dtype=np.float64)
     sym = not op.has_transpose() and not general(d)
     v0 = np.random.default_rng(0).uniform(0, 1, n)
-    if sym:
-        vals, vecs = sla.eigsh(lin, k=nev, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, max(2 * nev + 8, 20)))
+    if large:
+        # the reference solver's Krylov size (suggested_nev, TMat/tmat.hpp:88)
+        ncv, tol = 2 * nev + 3, 1e-12
+        if n <= (1 << 28):
+            # product count of the reference's settings (Spectra's default tol 1e-10)
+            sla.eigsh(lin, k=nev, which="LM", tol=1e-10, v0=v0, ncv=ncv)
+            out["arpack_matvecs_tol1e10"] = np.int64(count[0])
+            log(f"{d['name']}: ARPACK ncv={ncv} tol=1e-10 took {count[0]} products")
+            count[0] = 0
     else:
-        vals, vecs = sla.eigs(lin, k=nev, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, max(2 * nev + 8, 20)))
+        ncv, tol = min(n - 1, max(2 * nev + 8, 20)), 1e-13
+    t0 = time.perf_counter()
+    if sym:
+        vals, vecs = sla.eigsh(lin, k=nev, which="LM", tol=tol, v0=v0, ncv=ncv)
+    else:
+        vals, vecs = sla.eigs(lin, k=nev, which="LM", tol=tol, v0=v0, ncv=ncv)
+    if large:
+        out["arpack_matvecs"] = np.int64(count[0])
+        out["arpack_ncv_tol"] = np.array([ncv, tol])
+        log(f"{d['name']}: ARPACK ncv={ncv} tol={tol} took {count[0]} products, {time.perf_counter() - t0:.0f} s")
     order = np.argsort(-np.abs(vals), kind="stable")
     vals = vals[order]
     vecs = vecs[:, order]
@@ -93,6 +149,10 @@ def gen(c):
             out["ql"] = ql
     if n <= FULL_VECTOR_MAX:
         out["q0"] = q
+    else:
+        out["q0_samp"] = q[samp]
+        if not sym:
+            out["ql_samp"] = ql[samp]
     mom, mst = op.moments(ql, q)
     phys, pst = op.phys_extend(ql, q)
     out["moments"] = mom
@@ -102,16 +162,21 @@ def gen(c):
     return d["name"], out
 
 
-def main(names=None):
+def main(args):
     if not available():
         raise SystemExit("oracle/_ref/libtmat_ref.so missing: run oracle/build_ref.sh first")
-    for c in CASES:
+    large = "--large" in args
+    names = [a for a in args if not a.startswith("--")]
+    for c in CASES + LARGE_CASES:
+        is_large = c in LARGE_CASES
         if names and c[0] not in names:
             continue
-        name, out = gen(c)
+        if not names and is_large and not large:
+            continue
+        name, out = gen(c, large=is_large)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
-        print(f"{name}: n={int(out['n'])} evals={out['evals_re'][:2]}")
+        log(f"{name}: n={int(out['n'])} evals={out.get('evals_re', [])[:2]}")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or None)
+    main(sys.argv[1:])

@@ -61,6 +61,50 @@ def test_field_derivative_equals_magnetisation(pt):
     assert g[3] == pytest.approx(-bj * L * m[0], rel=1e-9, abs=1e-10)
 
 
+# The two adjoint points of the gradient workload: A/5 reduced perpendicular
+# TM at L=24 (betaJ=0.35, kappa=0.55, h=0.05; h != 0 keeps the flip reduction
+# off) and the 3D ANNNI perpendicular TM on a 5x5 periodic layer (betaJ=0.2,
+# kappa=0.4, h=0; R = 170,440).
+CFG5 = [
+    ("A", 2, 5, 0, 0.35, 0.55, 0.05, 24, 2),
+    ("A", 3, 1, 0, 0.2, 0.4, 0.0, (5, 5), 2),
+]
+
+
+@pytest.mark.parametrize("pt", CFG5)
+def test_grad_at_the_workload_points(pt):
+    """Adjoint gradient of ln(lambda0) and of xi at the workload's two points
+    against central finite differences (step 1e-5) of FP64 eigenvalues, and
+    d ln(lambda0)/dh against the magnetisation moment."""
+    model, dim, ax, ec, bj, k, h, size, nev = pt
+    op, vals, vecs = lam(model, dim, ax, ec, bj, k, h, size, nev)
+    nf = op.getnormfactor()
+    g0 = op.grad(vecs[0], vals[0] * nf)
+    g1 = op.grad(vecs[1], vals[1] * nf)
+    xi = 1.0 / np.log(vals[0] / abs(vals[1]))
+    dxi = -xi * xi * (g0 - g1)
+    params = [bj, k, 0.0, h]
+    for t in (0, 1, 3):
+        if t == 3 and h == 0.0:
+            continue  # the flip-reduced sector is only defined at h = 0
+        pp, pm = list(params), list(params)
+        pp[t] += STEP
+        pm[t] -= STEP
+        _, vp, _ = lam(model, dim, ax, ec, pp[0], pp[1], pp[3], size, nev)
+        _, vm, _ = lam(model, dim, ax, ec, pm[0], pm[1], pm[3], size, nev)
+        fd = (np.log(vp[0]) - np.log(vm[0])) / (2 * STEP)
+        assert abs(g0[t] - fd) < 2e-6 * max(1.0, abs(fd)), (t, g0[t], fd)
+        xp = 1.0 / np.log(vp[0] / abs(vp[1]))
+        xm = 1.0 / np.log(vm[0] / abs(vm[1]))
+        fdx = (xp - xm) / (2 * STEP)
+        assert abs(dxi[t] - fdx) < 1e-5 * max(1.0, abs(fdx)), (t, dxi[t], fdx)
+    if dim == 2 or h != 0.0:
+        q = vecs[0] / np.linalg.norm(vecs[0])
+        m, _ = op.moments(q)
+        L = op.getLayerSize()
+        assert g0[3] == pytest.approx(-bj * L * m[0], rel=1e-9, abs=1e-10)
+
+
 def test_grad_xi_from_lambda1():
     """d xi from lambda1's eigenpair: xi = 1/ln(lambda0/|lambda1|)."""
     args = ("A", 2, 5, 2, 0.4, 0.6, 0.0, 14, 3)
@@ -75,3 +119,22 @@ def test_grad_xi_from_lambda1():
     xp = 1.0 / np.log(vp[0] / abs(vp[1]))
     xm = 1.0 / np.log(vm[0] / abs(vm[1]))
     assert dxi == pytest.approx((xp - xm) / (2 * STEP), rel=1e-5)
+
+
+@pytest.mark.parametrize("args", [("A", 2, 5, 0, 0.35, 0.55, 0.05, 16), ("A", 2, 1, 0, 0.5, 0.3, 0.1, 10)])
+def test_cpp_eigen_function_forward_backward(tmp_path, args):
+    """The C++ forward/backward pair of include/latttmat.hpp (EigenFunction),
+    compiled here against the library, one forward and one backward on the GPU
+    checked against central differences of its own forward pass."""
+    import os
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    pkg = os.path.join(root, "latttmat_gb300")
+    exe = tmp_path / "eigen_function_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "cpp", "eigen_function_check.cpp"), "-o", str(exe), "-L", pkg,
+                    "-llatttmat_gb300", "-Wl,-rpath," + pkg], check=True)
+    r = subprocess.run([str(exe)] + [str(a) for a in args], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "MISMATCH" not in r.stdout

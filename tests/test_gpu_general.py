@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import latttmat_gb300 as lt
-from gpu_util import case_names, fixture, make_op, rel_err, seeded_input
+from gpu_util import case_names, checksum_weights, fixture, make_op, rel_err, seeded_input
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +28,12 @@ def test_transpose_product(name):
     t = op.get_t_instance()
     x = seeded_input(op.rows(), 1)
     yt = t.perform_op(x)
-    assert rel_err(yt, f["yt"]) < 1e-12
+    if "yt" in f:
+        assert rel_err(yt, f["yt"]) < 1e-12
+    else:
+        assert rel_err(yt[f["samp_idx"]], f["yt_samp"]) < 1e-12
+        w = checksum_weights(op.rows())
+        np.testing.assert_allclose([np.dot(w, yt), np.linalg.norm(yt)], f["yt_chk"], rtol=1e-12)
     # <y, T x> == <T^T y, x>
     z = seeded_input(op.rows(), 2)
     assert np.dot(z, op.perform_op(x)) == pytest.approx(np.dot(t.perform_op(z), x), rel=1e-11)
@@ -45,9 +50,13 @@ def test_general_eigenvalues_and_left_vector(name, mode):
     assert_eigs_match(vals, ref, 1e-10)
     q = np.real(vecs[0])
     q = q / np.linalg.norm(q) * np.sign(q.sum())
-    assert rel_err(q, f["q0"]) < 1e-6
     ql = vecl / np.linalg.norm(vecl) * np.sign(vecl.sum())
-    assert rel_err(ql, f["ql"]) < 1e-6
+    if "q0" in f:
+        assert rel_err(q, f["q0"]) < 1e-6
+        assert rel_err(ql, f["ql"]) < 1e-6
+    else:  # long vectors: the values at the sampled positions
+        assert rel_err(q[f["samp_idx"]], f["q0_samp"]) < 1e-6
+        assert rel_err(ql[f["samp_idx"]], f["ql_samp"]) < 1e-6
     m, st = op.moments(ql, q)
     np.testing.assert_allclose(m, f["moments"], rtol=1e-6, atol=1e-9)
     assert st == int(f["moments_status"])

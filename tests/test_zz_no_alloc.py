@@ -67,11 +67,16 @@ def test_noalloc_matches_regular_product(L, ec):
     for y, ref in zip(outs, refs):
         assert bool(torch.isfinite(y).all())
         assert _rel(y, ref) < 1e-12
-    # no allocation per call: free device memory is unchanged across calls
+    # no allocation per call: the library's allocation counter (every device
+    # buffer it makes goes through one allocator) does not move, and neither
+    # does the device's free memory (this assumes no other process allocates
+    # on the same GPU meanwhile)
+    allocs0 = lt.alloc_count()
     free0 = torch.cuda.mem_get_info()[0]
     for x, y in zip(xs, outs):
         _call(fn, op, x, y)
     torch.cuda.synchronize()
+    assert lt.alloc_count() == allocs0
     assert torch.cuda.mem_get_info()[0] == free0
     for y, ref in zip(outs, refs):
         assert _rel(y, ref) < 1e-12
