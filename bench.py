@@ -6,15 +6,21 @@ One step = one solve from operator construction (orbit tables, Boltzmann
 weights, even/odd plan, all on the GPU) to converged eigenvalues, in mixed
 precision (FP32 matvec bulk, FP64 Gram-Schmidt / Rayleigh-Ritz / refinement
 matvecs).  The CUDA path runs through the C ABI (liblatttmat_gb300.so).
+Beside the headline: the plain FP64 GPU solve of the same operator, the error
+of both against the reference's eigenvalues (tests/golden/xam_L32_cfg2.npz,
+ARPACK on the reference product), and the 256-point B/7 parameter sweep as a
+device batch in mixed precision and in FP64 against one plain FP64 solve per
+point.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--L 32] [--impl reference]
 
 N>1 (torchrun): independent replicas (the path does not shard), max over ranks.
 --impl reference: the reference algorithm on the host cores (the oracle port of
-TMat/tmatreduce.cpp, OpenMP, all cores): the L=32 orbit table is built once,
-each step times a bounded sample of leading-bit slices of the L=32 product,
-and the value is table + matvecs x (product time), matvecs as the GPU solver
-needed (34 by default, the ARPACK count at tol 1e-12).
+TMat/tmatreduce.cpp, OpenMP, all cores): the L=32 orbit table is built once;
+the K timed steps together run every leading-bit slice of one L=32 product
+exactly once, so their sum is one measured full product; the value is table +
+products x (product time), the product count from the reference's own ARPACK
+solve at L=28 with its solver's settings (ncv = 2 nev + 3, tol 1e-10).
 """
 from __future__ import annotations
 
@@ -141,6 +147,23 @@ def max_over_ranks(v, world):
 
 
 # ------------------------------------------------------------------ reference arm
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def reference_products():
+    """Products the reference's solver takes on this workload: the count of the
+    reference's own ARPACK solve at L=28 (ncv 11, tol 1e-10), recorded with its
+    fixture; 34 (the same solve's count at L=24) if the fixture is absent."""
+    path = os.path.join(GOLDEN, "xam_L28_noflip.npz")
+    try:
+        import numpy as np
+
+        f = np.load(path)
+        return int(f["arpack_matvecs_tol1e10"]), "reference ARPACK (ncv 11, tol 1e-10) at L=28"
+    except Exception:
+        return 34, "ARPACK count at L=24 (fixture absent)"
+
+
 def reference_arm(args, world, rank):
     if rank != 0:
         return
@@ -155,54 +178,67 @@ def reference_arm(args, world, rank):
     t_table = time.perf_counter() - t0
     nsl = op.xam_nslices()
     x = np.random.default_rng(0).uniform(-1, 1, op.n)
-    per_step = max(1, nsl // 32)
+    for w in range(args.warmup):  # untimed: one slice each
+        op.xam_slices(x, w % nsl, 1)
+    # the K timed steps partition the product's slices: together one full product
     times = []
-    for it in range(args.warmup + args.steps):
-        first = (it * per_step) % nsl
+    for i in range(args.steps):
+        a, b = i * nsl // args.steps, (i + 1) * nsl // args.steps
         t1 = time.perf_counter()
-        op.xam_slices(x, first, per_step)
-        dt = time.perf_counter() - t1
-        if it >= args.warmup:
-            times.append(dt)
-    t_mv = statistics.mean(times) * nsl / per_step
-    nmv = int(os.environ.get("BENCH_REF_MATVECS", "34"))
+        if b > a:
+            op.xam_slices(x, a, b - a)
+        times.append(time.perf_counter() - t1)
+    t_mv = sum(times)  # every slice ran exactly once over the K steps
+    nmv, nmv_src = reference_products()
     value = t_table + nmv * t_mv
+    cfg = {"workload": f"A/5 reduced perpendicular TM L={L}, betaJ={BETAJ}, kappa={KAPPA}, h={H}, neigs={NEV}, "
+                       f"flip off (driver semantics for neigs>1)",
+           "L": L, "R": op.n, "tol": 1e-10, "matvecs": nmv}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"A/5 reduced perpendicular TM L={L}, betaJ={BETAJ}, kappa={KAPPA}, h={H}, "
-                               f"neigs={NEV}, flip off (R={op.n})", "L": L, "R": op.n, "matvecs": nmv},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": cfg,
         "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port",
-                         "sample": f"orbit table at L={L} built once ({t_table:.1f} s, serial as the reference); "
-                                   f"{per_step} of {nsl} leading-bit slices of one L={L} product per step "
-                                   f"({statistics.mean(times):.2f} s), scaled to a full product ({t_mv:.1f} s) "
-                                   f"x {nmv} products"},
+                         "sample": f"orbit table at L={L} built once ({t_table:.1f} s, serial as the reference); the "
+                                   f"{args.steps} timed steps ran the {nsl} leading-bit slices of one L={L} product "
+                                   f"once each ({t_mv:.1f} s measured for the full product); value = table + "
+                                   f"{nmv} products ({nmv_src}); ms_per_step is the mean step (a slice share)"},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ CPU baseline sample for our line
-def cpu_baseline_sample(sample_L, nmv):
+def cpu_baseline_sample(sample_L, nmv, L=32, slices=8):
+    """About 10-30 s of host work: the orbit table at sample_L (extrapolated to
+    L by the 2^L * L work ratio) plus a measured share of one product two
+    sites below L (scaled by the same ratio)."""
     from oracle import oracle as orc
     import numpy as np
 
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
-    op = orc.OracleOp("A", 2, 5, BETAJ, KAPPA, H, sample_L, 0.0, 2)
+    orc.OracleOp("A", 2, 5, BETAJ, KAPPA, H, sample_L, 0.0, 2)
     t_table = time.perf_counter() - t0
+    f = (2.0 ** L * L) / (2.0 ** sample_L * sample_L)
+    # the product share: running slices needs the exact orbit table, which at
+    # L=32 alone takes ~45 s, so the share is timed at L-2 and scaled
+    Lp = L - 2
+    op = orc.OracleOp("A", 2, 5, BETAJ, KAPPA, H, Lp, 0.0, 2)
+    nsl = op.xam_nslices()
     x = np.random.default_rng(0).uniform(-1, 1, op.n)
+    k = min(slices, nsl)
     t1 = time.perf_counter()
-    op.perform_op(x)
-    t_mv = time.perf_counter() - t1
-    # scale to L=32 by the work of each phase: table O(2^L * L), product O(2^L * L)
-    f = (2.0 ** 32 * 32) / (2.0 ** sample_L * sample_L)
-    value = t_table * f + nmv * t_mv * f
+    op.xam_slices(x, 0, k)
+    t_share = time.perf_counter() - t1
+    fp = (2.0 ** L * L) / (2.0 ** Lp * Lp)
+    t_mv = t_share * nsl / k * fp
+    value = t_table * f + nmv * t_mv
     return {"value": value, "unit": "s", "cores": cores, "kind": "port",
-            "sample": f"oracle port of the reference (TMat/tmatreduce.cpp algorithm, OpenMP) at L={sample_L}: "
-                      f"table {t_table:.2f} s + one product {t_mv:.2f} s, extrapolated to L=32 by the 2^L*L work "
-                      f"ratio ({f:.1f}x) with {nmv} products"}
+            "sample": f"oracle port of the reference (TMat/tmatreduce.cpp algorithm, OpenMP): table at L={sample_L} "
+                      f"({t_table:.2f} s) x {f:.1f} + {nmv} products, each {k} of {nsl} leading-bit slices at L={Lp} "
+                      f"({t_share:.2f} s) scaled to a full L={L} product ({t_mv:.1f} s)"}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -297,6 +333,15 @@ def gpu_arm(args, world, rank, local):
     achieved = ach1 if dom == 1 else ach2
     traffic = EO_TRAFFIC.get(f"L{L}_pass{dom}")
     del op
+
+    # the plain FP64 GPU form of the same solve (every product in FP64), and
+    # both forms' errors against the reference's eigenvalues
+    plain = None
+    if rank == 0 and L == 32 and mode == lt.TM_EIGS_MIXED:
+        try:
+            plain = f64_plain_and_errors(lt, torch, L, vals)
+        except Exception as exc:  # reported beside the headline, never required
+            plain = {"failed": f"{exc}"}
     batch = None
     if args.batch > 0 and rank == 0:
         try:
@@ -310,7 +355,7 @@ def gpu_arm(args, world, rank, local):
         cpu = None
         if not args.no_cpu_baseline:
             try:
-                cpu = cpu_baseline_sample(args.cpu_sample_L, int(mean_info["matvecs"]))
+                cpu = cpu_baseline_sample(args.cpu_sample_L, reference_products()[0], L=L)
             except Exception as exc:  # baseline is reported, never required
                 cpu = {"value": None, "unit": "s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {exc}"}
         out = {
@@ -338,6 +383,7 @@ def gpu_arm(args, world, rank, local):
                          "alg_bytes": {"pass1": b1, "pass2": b2}},
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "f64_plain_and_errors": plain,
             "batch_sweep": batch,
         }
         print(json.dumps(out), flush=True)
@@ -355,29 +401,99 @@ def batch_points(count, seed_L=0, seed_k=1):
     return [(float(bj[i]), float(k1[i]), 0.0, 0.0, int(Ls[i])) for i in range(count)]
 
 
+def f64_plain_and_errors(lt, torch, L, vals_mixed):
+    """Seconds of the plain FP64 GPU solve at L (one warm-up, one timed) and
+    the relative error of lambda0, lambda1, f = ln(lambda0)/L and
+    xi = 1/ln(lambda0/|lambda1|) of both forms against the reference's
+    eigenvalues (ARPACK on the reference product, tol 1e-12, ncv 11)."""
+    import numpy as np
+
+    def solve():
+        op = lt.TMatOp("A", 2, 5, BETAJ, KAPPA, H, L, 0.0, 2)
+        vals, _, _, info = op.eigs(NEV, tol=1e-10, mode=lt.TM_EIGS_F64)
+        op.close()
+        return vals, info
+
+    solve()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    v64, info64 = solve()
+    t64 = time.perf_counter() - t0
+    out = {"seconds": t64, "matvecs": info64["matvecs"], "max_rel_resid": info64["max_resid"],
+           "eigenvalues": [float(v) for v in v64]}
+    path = os.path.join(GOLDEN, f"xam_L{L}_cfg2.npz")
+    if os.path.exists(path):
+        ref = np.load(path)["evals_re"]
+
+        def obs(v):
+            l0, l1 = abs(v[0]), abs(v[1])
+            return np.array([l0, l1, np.log(l0) / L, 1.0 / np.log(l0 / l1)])
+
+        names = ["lambda0", "lambda1", "f", "xi"]
+        for tag, v in (("mixed", vals_mixed), ("f64", v64)):
+            e = np.abs(obs(v) - obs(ref)) / np.abs(obs(ref))
+            out[f"rel_err_{tag}"] = {k: float(x) for k, x in zip(names, e)}
+            out[f"rel_err_{tag}"]["lambda0..3_max"] = float(np.max(np.abs(np.asarray(v)[:len(ref)] - ref) / np.abs(ref)))
+        out["reference"] = "tests/golden/xam_L32_cfg2.npz (reference product + ARPACK, tol 1e-12, ncv 11)"
+    return out
+
+
 def batch_sweep(count):
-    """Seconds for the sweep solved concurrently (tm_eigs_batch, mixed
-    precision) and one instance at a time in FP64, both to 1e-10, k=2."""
+    """The parameter sweep solved as one device batch (tm_sweep) in mixed
+    precision and in FP64 (equal concurrency: every point in the batch), and
+    one plain FP64 tm_eigs solve per point on an evenly spaced sample; all to
+    1e-10, k=2.  Seconds include operator construction."""
+    import numpy as np
+
     import latttmat_gb300 as lt
 
     pts = batch_points(count)
-    lt.eigs_batch("B", 2, 7, pts[:4], nev=2, tol=1e-10, mode=lt.TM_EIGS_MIXED, extend_cond=2)  # warm-up
+    warm = lt.Sweep("B", 2, 7, pts[:6], extend_cond=2)
+    warm.eigs(2, tol=1e-10, mode=lt.TM_EIGS_MIXED)
+    warm.eigs(2, tol=1e-10, mode=lt.TM_EIGS_F64)
+    warm.close()
+    res = {}
+    launches = {}
+    for tag, mode in (("mixed", lt.TM_EIGS_MIXED), ("f64", lt.TM_EIGS_F64)):
+        l0 = lt.launch_count()
+        t0 = time.perf_counter()
+        sw = lt.Sweep("B", 2, 7, pts, extend_cond=2)
+        t1 = time.perf_counter()
+        vals, info, st = sw.eigs(2, tol=1e-10, mode=mode)
+        t2 = time.perf_counter()
+        stats = sw.stats()
+        sw.close()
+        launches[tag] = lt.launch_count() - l0
+        res[tag] = dict(seconds=t2 - t0, create_s=t1 - t0, solve_s=t2 - t1, vals=vals, failed=int(np.sum(st != 0)),
+                        matvecs=int(sum(i["matvecs"] for i in info)),
+                        matvecs_f64=int(sum(i["matvecs_f64"] for i in info)), stats=stats)
+    dev = float(np.max(np.abs(res["mixed"]["vals"] - res["f64"]["vals"]) / np.abs(res["f64"]["vals"])))
+    # plain: one FP64 solve after another on every 8th point (all widths)
+    sample = pts[::8]
     t0 = time.perf_counter()
-    vals, info, st = lt.eigs_batch("B", 2, 7, pts, nev=2, tol=1e-10, mode=lt.TM_EIGS_MIXED, extend_cond=2)
-    t_batch = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    for (bj, k, k2, h, L) in pts:
+    for (bj, k, k2, h, L) in sample:
         op = lt.TMatOp("B", 2, 7, bj, k, h, L, k2, 2)
         op.eigs(2, tol=1e-10, mode=lt.TM_EIGS_F64)
         op.close()
     t_plain = time.perf_counter() - t0
+    plain_per_point = t_plain / len(sample)
     return {"workload": f"{count} x B/7 reduced diagonal BNNNI, L in {{16..24}} (seed 0), betaJ in [0.2,1.0], "
                         "kappa1 ~ U[0,1] (seed 1), neigs=2, tol 1e-10",
-            "batched_mixed_s": t_batch, "points_per_s": count / t_batch,
-            "plain_f64_sequential_s": t_plain, "speedup": t_plain / t_batch,
-            "failed": int(sum(1 for c in st if c != 0)),
-            "note": "batched: tm_eigs_batch, 16 host threads, one CUDA stream per instance; plain: one "
-                    "FP64 solve after another through the same library"}
+            "batched_mixed_s": res["mixed"]["seconds"], "batched_f64_s": res["f64"]["seconds"],
+            "batched_mixed_per_point_s": res["mixed"]["seconds"] / count,
+            "batched_f64_per_point_s": res["f64"]["seconds"] / count,
+            "plain_f64_per_point_s": plain_per_point,
+            "speedup_mixed_vs_batched_f64": res["f64"]["seconds"] / res["mixed"]["seconds"],
+            "speedup_mixed_vs_plain_f64": plain_per_point * count / res["mixed"]["seconds"],
+            "max_rel_dev_mixed_vs_f64": dev,
+            "matvecs": {k: {"all": res[k]["matvecs"], "fp64_accurate": res[k]["matvecs_f64"]} for k in res},
+            "create_s": {k: res[k]["create_s"] for k in res},
+            "sweep_stats": {k: res[k]["stats"] for k in res},
+            "gpu_launches": launches,
+            "failed": res["mixed"]["failed"] + res["f64"]["failed"],
+            "note": f"batched: tm_sweep (one launch per chain pass over all {count} points, one CUDA graph per "
+                    f"Arnoldi step of every point); plain: tm_eigs FP64 one point after another on {len(sample)} "
+                    "evenly spaced points (every 8th), per point"}
 
 
 def eo_plan_sizes(L):

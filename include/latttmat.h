@@ -200,8 +200,8 @@ tm_status tm_eigs_batch(const tm_params* params, int count, char model, int dim,
  * differ) solved as one batch on the device.  The reference builds one
  * operator per tmat run (TMat/pfunc.cpp:16-106).  Here each chain pass of the
  * product is one launch over every member's tiles (an instance table in
- * device memory), the members run Arnoldi in lockstep with each restart
- * cycle captured in a CUDA graph, and members are processed in waves that fit
+ * device memory), every member extends its Arnoldi basis by one column per
+ * step (one CUDA graph per step) and restarts on its own, and members are processed in waves that fit
  * the free device memory (tm_sweep_set_wave_bytes overrides the share). */
 typedef struct tm_sweep tm_sweep;
 tm_status tm_sweep_create(const tm_params* params, int count, char model, int dim, int axialdir,
@@ -211,6 +211,10 @@ int tm_sweep_count(const tm_sweep* sweep);
 int64_t tm_sweep_rows(const tm_sweep* sweep, int i);        /* rows of member i */
 double tm_sweep_normfactor(const tm_sweep* sweep, int i);   /* normfactor of member i */
 tm_status tm_sweep_set_wave_bytes(tm_sweep* sweep, size_t bytes);  /* 0: 60% of free memory */
+/* Diagnostics of the last tm_sweep_eigs: {waves, steps, seconds building the
+ * waves, seconds in steps (device work, host-timed), seconds in host
+ * restarts}; returns the count written (<= cap). */
+int tm_sweep_stats(const tm_sweep* sweep, double* out, int cap);
 
 /* y_i = T_i x_i for every member: host arrays of `count` device pointers to
  * FP64 vectors (length tm_sweep_rows(i)); dtype TM_F64, TM_F64_DF or TM_F32
@@ -234,6 +238,24 @@ tm_status tm_sweep_eigs(tm_sweep* sweep, int nev, int ncv, double tol, int mode,
 tm_status tm_chain_autotune(const tm_op* op, tm_dtype dtype, int* tile_bits, int* threads, double* ms);
 /* Sets one entry of the tuning table (tile_bits 0 / threads 0: the default). */
 tm_status tm_chain_set_tuning(char model, int L, tm_dtype dtype, int tile_bits, int threads);
+
+/* ---- configuration planting (replaces DumpConfig) ----------------------- */
+
+/* Plant `nconfig` layer sequences of `length` layers from the leading
+ * eigenvector of a periodic x-ANNNI perpendicular TM (model 'A', axialdir 1:
+ * XAT2DDumpConfig::dump, DumpConfig/dumpconfig.cpp:88-136; axialdir 5:
+ * XAM2DDumpConfig::dump, DumpConfig/dumpreduce.cpp:47-122).  vec_host: the
+ * eigenvector as tm_eigs returns it (length rows; its absolute values are
+ * used, as the reference reads X_vec.dat).  seed: the seed of the
+ * reference's generator (std::mt19937 + uniform_real_distribution, as
+ * MyUtility::setseed; its random stream is consumed in the reference's
+ * order, so the same seed plants the same configurations).  states_out:
+ * host, nconfig * length layer states (bit i = site i; the reference writes
+ * each as a line of L digits, bit 0 first, to <prefix>_config_<k>.dat).
+ * All chains advance together on the device: one launch per step computes
+ * every chain's transfer-matrix column, cumulative sums and draw. */
+tm_status tm_dump_configs(const tm_op* op, const double* vec_host, int nconfig, int length, uint32_t seed,
+                          uint64_t* states_out);
 
 /* ---- observables ------------------------------------------------------- */
 

@@ -45,8 +45,8 @@ EXPORTED_SYMBOLS = (
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
     "tm_profile_matvec", "tm_launch_count", "tm_alloc_count", "tm_perform_op_dev_noalloc", "tm_eigs_batch",
     "tm_debug_set_eo_tile_bits", "tm_sweep_create", "tm_sweep_destroy", "tm_sweep_count", "tm_sweep_rows",
-    "tm_sweep_normfactor", "tm_sweep_set_wave_bytes", "tm_sweep_perform_op_dev", "tm_sweep_eigs",
-    "tm_chain_autotune", "tm_chain_set_tuning",
+    "tm_sweep_normfactor", "tm_sweep_set_wave_bytes", "tm_sweep_stats", "tm_sweep_perform_op_dev", "tm_sweep_eigs",
+    "tm_chain_autotune", "tm_chain_set_tuning", "tm_dump_configs",
 )
 
 
@@ -120,6 +120,7 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.tm_sweep_normfactor.argtypes = [P, ctypes.c_int]
     lib.tm_sweep_normfactor.restype = ctypes.c_double
     lib.tm_sweep_set_wave_bytes.argtypes = [P, ctypes.c_size_t]
+    lib.tm_sweep_stats.argtypes = [P, P, ctypes.c_int]
     lib.tm_sweep_perform_op_dev.argtypes = [P, P, P, ctypes.c_int]
     lib.tm_sweep_eigs.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, P, P, P, P]
     lib.tm_chain_autotune.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
@@ -128,6 +129,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     for f in ("tm_sweep_create", "tm_sweep_destroy", "tm_sweep_set_wave_bytes", "tm_sweep_perform_op_dev",
               "tm_sweep_eigs", "tm_chain_autotune", "tm_chain_set_tuning"):
         getattr(lib, f).restype = ctypes.c_int
+    lib.tm_dump_configs.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, P]
+    lib.tm_dump_configs.restype = ctypes.c_int
     lib.tm_last_error.restype = ctypes.c_char_p
     lib.tm_version.restype = ctypes.c_char_p
     for f in ("tm_create", "tm_transpose", "tm_destroy", "tm_perform_op", "tm_perform_op_dev", "tm_orbit_table",
@@ -191,6 +194,13 @@ class Sweep:
     def normfactor(self, i: int) -> float:
         return float(self._lib.tm_sweep_normfactor(self._h, int(i)))
 
+    def stats(self) -> dict:
+        """Diagnostics of the last eigs(): waves, steps, seconds per phase."""
+        out = np.zeros(5)
+        n = self._lib.tm_sweep_stats(self._h, _ptr(out), 5)
+        keys = ("waves", "steps", "wave_build_s", "step_s", "restart_s")
+        return {k: float(out[i]) for i, k in enumerate(keys[:n])}
+
     def set_wave_bytes(self, nbytes: int) -> None:
         _check(self._lib.tm_sweep_set_wave_bytes(self._h, int(nbytes)))
 
@@ -238,6 +248,16 @@ def chain_autotune(op: "TMatOp", dtype: int = TM_F32):
     ms = ctypes.c_double()
     _check(load_library().tm_chain_autotune(op._h, int(dtype), ctypes.byref(tb), ctypes.byref(th), ctypes.byref(ms)))
     return tb.value, th.value, ms.value
+
+
+def write_configs(states: np.ndarray, L: int, prefix: str) -> None:
+    """Write planted configurations as the reference does: <prefix>_config_<k>.dat,
+    one line per layer, L digits, site 0 first (DumpConfig/dumpconfig.hpp:32-40)."""
+    for k, row in enumerate(np.asarray(states)):
+        with open(f"{prefix}_config_{k}.dat", "w") as fh:
+            for st in row:
+                st = int(st)
+                fh.write("".join("1" if (st >> i) & 1 else "0" for i in range(L)) + "\n")
 
 
 def chain_set_tuning(model: str, L: int, dtype: int, tile_bits: int, threads: int) -> None:
@@ -409,6 +429,16 @@ class TMatOp:
         g = np.zeros(4)
         _check(self._lib.tm_grad(self._h, _ptr(qr), qlp, float(lambda_internal), _ptr(g)))
         return g
+
+    def dump_configs(self, vec: np.ndarray, nconfig: int, length: int, seed: int) -> np.ndarray:
+        """Plant configurations from the leading eigenvector (the reference's
+        DumpConfig): uint64 layer states, shape (nconfig, length)."""
+        v = np.ascontiguousarray(vec, dtype=np.float64)
+        if v.shape != (self.rows(),):
+            raise ValueError(f"vec has shape {v.shape}, expected ({self.rows()},)")
+        out = np.zeros((int(nconfig), int(length)), dtype=np.uint64)
+        _check(self._lib.tm_dump_configs(self._h, _ptr(v), int(nconfig), int(length), int(seed), _ptr(out)))
+        return out
 
     def profile_matvec(self, dtype: int = TM_F32, iters: int = 10):
         """Per-stage average ms of the internal-order product (CUDA events)."""

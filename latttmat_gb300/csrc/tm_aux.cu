@@ -111,34 +111,51 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
   // FP64 fold accumulators after the padded tile, at a 16-byte boundary
   // (the FP32 tile's padded size is not a multiple of 8 bytes)
   double* acc = reinterpret_cast<double*>(smraw + chain_acc_offset(tile, sizeof(T)));
-  // Step coefficients, functions of the control bits only, multiplied out
-  // once per launch.  BNNNI: out(aux, s) = vt[f][aux][s] * sum_q wt[s][q]
-  // in(q, aux) with f = (fl, fr) (the reference's v and d factors, the step
-  // normalisation folded into vt).  DNNI: out(a, s) = sum_q cf[nb][a][s][q]
-  // in(q, a).
-  __shared__ T vt[64];
-  __shared__ T wt[16];
+  // Step coefficients, functions of the control bits only.  The step's
+  // matrix factorises as out(a', s') = z_f[s'] u[a'][s'] sum_q w[s'][q]
+  // in(q, a'): w and u (the step normalisation folded into u) are the same
+  // for every group and sit in shared memory, read as broadcast rows; only
+  // z depends on the group's control bits f and is formed in registers.
+  //   BNNNI dir 0: w = b1[sr^al] b2[sr^ar] b2[sl^al], u = b1[sr^pl] b3[sr^pr] b3[sl^pl],
+  //                z = b2[sr^fr] b2[sl^fl];
+  //   BNNNI dir 1: w = b2[sr^ar] b2[sl^al], u = b1[sl^pr] b3[sr^pr] b3[sl^pl],
+  //                z = b1[sl^fr] b2[sr^fr] b2[sl^fl];
+  //   DNNI:        w = b2[s^q], u = b1[s^a], z = b2[nb^s].
+  // (TMat/tmat.cpp:344-376 and 521-588 form the same products per element.)
+  constexpr int NS = 1 << KS;
+  __shared__ __align__(16) T wrow[16];  // [s'][q]
+  __shared__ __align__(16) T urow[16];  // [s'][a']
   if (ZB) {
-    for (int k = threadIdx.x; k < 64; k += blockDim.x) {
-      const int f = k >> 4, aux = (k >> 2) & 3, sv = k & 3;
-      const int fl = f >> 1, fr = f & 1, pl = aux >> 1, pr = aux & 1, sl = sv >> 1, sr = sv & 1;
-      T v;
-      if (!dir)
-        v = c.b1[sr ^ pl] * c.b2[sr ^ fr] * c.b2[sl ^ fl] * c.b3[sr ^ pr] * c.b3[sl ^ pl];
-      else
-        v = c.b1[sl ^ fr] * c.b1[sl ^ pr] * c.b2[sr ^ fr] * c.b2[sl ^ fl] * c.b3[sr ^ pr] * c.b3[sl ^ pl];
-      vt[k] = v * c.g;
-    }
     for (int k = threadIdx.x; k < 16; k += blockDim.x) {
       const int sv = k >> 2, q = k & 3, sl = sv >> 1, sr = sv & 1, al = q >> 1, ar = q & 1;
-      wt[k] = !dir ? c.b1[sr ^ al] * c.b2[sr ^ ar] * c.b2[sl ^ al] : c.b2[sr ^ ar] * c.b2[sl ^ al];
+      wrow[k] = !dir ? c.b1[sr ^ al] * c.b2[sr ^ ar] * c.b2[sl ^ al] : c.b2[sr ^ ar] * c.b2[sl ^ al];
+      const int pl = q >> 1, pr = q & 1;  // here q is a' = (pl, pr)
+      urow[k] = (!dir ? c.b1[sr ^ pl] * c.b3[sr ^ pr] * c.b3[sl ^ pl] : c.b1[sl ^ pr] * c.b3[sr ^ pr] * c.b3[sl ^ pl]) *
+                c.g;
     }
   } else {
-    for (int k = threadIdx.x; k < 16; k += blockDim.x) {
-      const int nb = k >> 3, a = (k >> 2) & 1, sv = (k >> 1) & 1, q = k & 1;
-      wt[k] = c.b1[sv ^ a] * c.b2[nb ^ sv] * c.b2[sv ^ q] * c.g;
+    for (int k = threadIdx.x; k < 4; k += blockDim.x) {
+      const int sv = k >> 1, q = k & 1;
+      wrow[k] = c.b2[sv ^ q];
+      urow[k] = c.b1[sv ^ q] * c.g;  // q is a here
     }
   }
+  // native FP64 (bound by the FP64 pipe): z_f[s'] u[a'][s'] for all four f
+  // from a table, one multiply per output fewer
+  constexpr bool kZuTable = ZB && std::is_same<T, double>::value;
+  __shared__ __align__(16) T zutab[kZuTable ? 64 : 1];
+  if constexpr (kZuTable) {
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) {
+      const int f = k >> 4, sv = (k >> 2) & 3, aux = k & 3;
+      const int fl = f >> 1, fr = f & 1, sl = sv >> 1, sr = sv & 1, pl = aux >> 1, pr = aux & 1;
+      T z = c.b2[sr ^ fr] * c.b2[sl ^ fl];
+      if (dir) z = z * c.b1[sl ^ fr];
+      const T u = (!dir ? c.b1[sr ^ pl] * c.b3[sr ^ pr] * c.b3[sl ^ pl] : c.b1[sl ^ pr] * c.b3[sr ^ pr] * c.b3[sl ^ pl]) * c.g;
+      zutab[k] = z * u;
+    }
+  }
+  // the factors z selects from, in registers (no indexed access)
+  const T b1_0 = c.b1[0], b1_1 = c.b1[1], b2_0 = c.b2[0], b2_1 = c.b2[1];
   // outer index: state bits, then (unless last) the lastbit pass
   const uint64_t ob = blk & ((1ull << cp.no) - 1);
   const int lb_outer = (int)(blk >> cp.no);
@@ -147,18 +164,35 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
   const int nloop = cp.last ? cp.nlb : 1;
   if (cp.last)
     for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) acc[e] = 0.0;
+  // The aux bits and the cb low sites are contiguous in HBM, so a pass with
+  // 2^(NA + cb) >= VEC elements per run moves whole 16-byte chunks (VEC
+  // consecutive tile elements sit in consecutive padded slots: VEC divides 32).
+  constexpr int VEC = 16 / (int)sizeof(T);
+  const bool vec_io = (1 << (NA + cp.jbit0)) >= VEC;
   for (int li = 0; li < nloop; ++li) {
     const int lb = cp.last ? li : lb_outer;
     // load / build the tile
-    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-      const int aux = e & ((1 << NA) - 1);
-      const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, site0);
-      T v;
-      if (cp.first)
-        v = chain_init<T, ZB, IO>(x, pre, smap, L, bc, r, aux, lb, c);
-      else
-        v = P[(((uint64_t)lb << L | r) << NA) | (uint64_t)aux];
-      sm[spad(e)] = v;
+    if (!cp.first && vec_io) {
+      for (int e = threadIdx.x * VEC; e < tile; e += blockDim.x * VEC) {
+        const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, site0);
+        const uint64_t at = (((uint64_t)lb << L | r) << NA) | (uint64_t)(e & ((1 << NA) - 1));
+        const uint4 raw = __ldcs(reinterpret_cast<const uint4*>(P + at));
+        const T* v = reinterpret_cast<const T*>(&raw);
+        T* dst = sm + spad(e);
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) dst[k] = v[k];
+      }
+    } else {
+      for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        const int aux = e & ((1 << NA) - 1);
+        const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, site0);
+        T v;
+        if (cp.first)
+          v = chain_init<T, ZB, IO>(x, pre, smap, L, bc, r, aux, lb, c);
+        else
+          v = P[(((uint64_t)lb << L | r) << NA) | (uint64_t)aux];
+        sm[spad(e)] = v;
+      }
     }
     __syncthreads();
     for (int j = 0; j < cp.T; ++j) {
@@ -166,69 +200,86 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
       const int sb = NA + cp.jbit0 + KS * j;  // tile bit of the step's lowest site
       const bool lastst = (t == nsteps - 1);
       const int groups = tile >> GB;
+      // Slot of (group base, aux q, step sites sp): spad(ebase) + q +
+      // spad(sp << sb), since spad(a | b) = spad(a) + spad(b) for disjoint
+      // a, b and q < 4 never reaches bit 5 of an aux-aligned base.
+      const int o1 = spad(1 << sb), o2 = ZB ? spad(2 << sb) : 0, o3 = ZB ? spad(3 << sb) : 0;
+      // The control sites (the next step's sites) are tile bits [sb + KS,
+      // sb + 2 KS) unless this is the pass's last step; then they are outer
+      // bits of the block, or the lastbit pass at the product's last step.
+      const bool ctl_in_tile = (j + 1 < cp.T);
+      const int ctl_outer = lastst ? (ZB ? lb : (bc == 0 ? lb : 0))
+                                   : (int)((rbase >> (KS * t + KS)) & (uint64_t)((1 << KS) - 1));
       for (int gi = threadIdx.x; gi < groups; gi += blockDim.x) {
         // tile index of the group base: insert zeros at [0, NA) and [sb, sb+KS)
-        int rest = gi;
-        const int lo = rest & ((1 << (sb - NA)) - 1);
-        const int hi = rest >> (sb - NA);
+        const int lo = gi & ((1 << (sb - NA)) - 1);
+        const int hi = gi >> (sb - NA);
         const int ebase = (hi << (sb + KS)) | (lo << NA);
-        const uint64_t r = rbase | tile_state((uint64_t)(ebase >> NA), cp.jbit0, site0);
+        const int ctl = ctl_in_tile ? ((ebase >> (sb + KS)) & ((1 << KS) - 1)) : ctl_outer;
+        T* b0 = sm + spad(ebase);
+        // an offset the compiler cannot see through: the coefficient rows are
+        // re-read (broadcast) per group instead of held in registers across
+        // the loop, which would leave too few for the group's values
+        int z0 = 0;
+        asm volatile("" : "+r"(z0));
+        const T* wr = wrow + z0;
+        const T* ur = urow + z0;
         if (!ZB) {
           // DNNI: out(a, s) = b1[s^a] b2[nb^s] (b2[s] in(0, a) + b2[s^1] in(1, a)),
           // in(q, s') = value with aux q and site t = s'
-          const int nb = lastst ? (bc == 0 ? lb : 0) : (int)((r >> (t + 1)) & 1);
-          const T* cfn = wt + nb * 8;
+          const int nb = ctl;
+          T* b1p = b0 + o1;
           T in[2][2];
 #pragma unroll
-          for (int q = 0; q < 2; ++q)
+          for (int q = 0; q < 2; ++q) {
+            in[q][0] = b0[q];
+            in[q][1] = b1p[q];
+          }
 #pragma unroll
-            for (int sp = 0; sp < 2; ++sp) in[q][sp] = sm[spad(ebase | q | (sp << sb))];
+          for (int sv = 0; sv < 2; ++sv) {
+            const T z = (nb ^ sv) ? b2_1 : b2_0;
+            const T w0 = wr[sv * 2], w1 = wr[sv * 2 + 1];
+            T* bo = sv ? b1p : b0;
 #pragma unroll
-          for (int a = 0; a < 2; ++a)
-#pragma unroll
-            for (int sv = 0; sv < 2; ++sv)
-              sm[spad(ebase | a | (sv << sb))] = cfn[a * 4 + sv * 2] * in[0][a] + cfn[a * 4 + sv * 2 + 1] * in[1][a];
+            for (int a = 0; a < 2; ++a) bo[a] = (ur[sv * 2 + a] * z) * (w0 * in[0][a] + w1 * in[1][a]);
+          }
         } else {
-          // BNNNI: out((pl,pr), (sl,sr)) = v * sum_q w(q) in(q, (pl,pr))
-          const int fl = lastst ? (lb >> 1) : (int)((r >> (2 * t + 3)) & 1);
-          const int fr = lastst ? (lb & 1) : (int)((r >> (2 * t + 2)) & 1);
-          const T* vf = vt + ((fl << 1) | fr) * 16;
+          // BNNNI: out((pl,pr), (sl,sr)) = z_f[s'] u[a'][s'] sum_q w[s'][q] in(q, a')
+          const int fl = ctl >> 1, fr = ctl & 1;
+          T* const bp[4] = {b0, b0 + o1, b0 + o2, b0 + o3};
           T in[4][4];
 #pragma unroll
           for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int sp = 0; sp < 4; ++sp) in[q][sp] = sm[spad(ebase | q | (sp << sb))];
-          if constexpr (sizeof(T) == 4) {
-            // every input is read before any output is written, so each
-            // output is stored as soon as it is formed (fewer live registers)
+            for (int sp = 0; sp < 4; ++sp) in[q][sp] = bp[sp][q];
+          // every input is read before any output is written, so each output
+          // is stored as soon as it is formed (fewer live registers)
 #pragma unroll
-            for (int aux = 0; aux < 4; ++aux)
-#pragma unroll
-              for (int sv = 0; sv < 4; ++sv) {
-                T d = in[0][aux] * wt[sv * 4];
-                d += in[1][aux] * wt[sv * 4 + 1];
-                d += in[2][aux] * wt[sv * 4 + 2];
-                d += in[3][aux] * wt[sv * 4 + 3];
-                sm[spad(ebase | aux | (sv << sb))] = vf[aux * 4 + sv] * d;
-              }
-          } else {
-            T out[4][4];
-#pragma unroll
-            for (int sv = 0; sv < 4; ++sv) {
-              const T w0 = wt[sv * 4], w1 = wt[sv * 4 + 1], w2 = wt[sv * 4 + 2], w3 = wt[sv * 4 + 3];
+          for (int sv = 0; sv < NS; ++sv) {
+            const int sl = sv >> 1, sr = sv & 1;
+            const T w0 = wr[sv * 4], w1 = wr[sv * 4 + 1], w2 = wr[sv * 4 + 2], w3 = wr[sv * 4 + 3];
+            if constexpr (kZuTable) {
+              const T* zu = zutab + ctl * 16 + sv * 4 + z0;
 #pragma unroll
               for (int aux = 0; aux < 4; ++aux) {
                 T d = in[0][aux] * w0;
                 d += in[1][aux] * w1;
                 d += in[2][aux] * w2;
                 d += in[3][aux] * w3;
-                out[aux][sv] = vf[aux * 4 + sv] * d;
+                bp[sv][aux] = zu[aux] * d;
+              }
+            } else {
+              T z = ((sr ^ fr) ? b2_1 : b2_0) * ((sl ^ fl) ? b2_1 : b2_0);
+              if (dir) z = z * ((sl ^ fr) ? b1_1 : b1_0);
+#pragma unroll
+              for (int aux = 0; aux < 4; ++aux) {
+                T d = in[0][aux] * w0;
+                d += in[1][aux] * w1;
+                d += in[2][aux] * w2;
+                d += in[3][aux] * w3;
+                bp[sv][aux] = (ur[sv * 4 + aux] * z) * d;
               }
             }
-#pragma unroll
-            for (int aux = 0; aux < 4; ++aux)
-#pragma unroll
-              for (int sv = 0; sv < 4; ++sv) sm[spad(ebase | aux | (sv << sb))] = out[aux][sv];
           }
         }
       }
@@ -240,6 +291,17 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
 #pragma unroll
         for (int aux = 0; aux < (1 << NA); ++aux) a += (double)sm[spad((e << NA) | aux)];
         acc[e] = a;
+      }
+    } else if (vec_io) {
+      for (int e = threadIdx.x * VEC; e < tile; e += blockDim.x * VEC) {
+        const uint64_t r = rbase | tile_state((uint64_t)(e >> NA), cp.jbit0, site0);
+        uint4 raw;
+        T* v = reinterpret_cast<T*>(&raw);
+        const T* src = sm + spad(e);
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) v[k] = src[k];
+        const uint64_t at = (((uint64_t)lb << L | r) << NA) | (uint64_t)(e & ((1 << NA) - 1));
+        __stcs(reinterpret_cast<uint4*>(P + at), raw);
       }
     } else {
       for (int e = threadIdx.x; e < tile; e += blockDim.x) {
@@ -276,41 +338,34 @@ __global__ void red_contract(const T* __restrict__ z, const uint32_t* __restrict
   for (; i < n; i += st) y[i] = (T)((double)z[idx[i]] * post * (double)dup[i] * tv[i]);
 }
 
+__device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp) {
+  return (int64_t)(cp.last ? 1 : cp.nlb) << cp.no;
+}
+
 // ------------------------------------------------------------------ batched product
-// One pass over every batch member's tiles: the block finds its instance by
-// binary search over the pass's block prefix, then runs the same tile body
-// as chain_kernel on that instance's geometry (copied to shared memory).
+// One pass over every batch member's tiles: a block takes its member from the
+// per-block member map, then runs the same tile body as chain_kernel on
+// kBatchTiles consecutive tiles of that member's geometry (copied to shared
+// memory).  km[i] = (Krylov column the member extends, product mode).
 template <class T, int ZB, class IO, int MODE>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3))
     chain_batch_kernel(const ChainInst* __restrict__ inst, const int2* __restrict__ km, const int64_t* __restrict__ start,
-                       int count, int pass, int j) {
+                       const int* __restrict__ bmem, int pass) {
   __shared__ ChainPass cps;
-  __shared__ int s_i;
-  if (threadIdx.x == 0) {
-    const int64_t b = blockIdx.x;
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (start[mid] <= b)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    s_i = lo;
-  }
-  __syncthreads();
+  const int s_i = bmem[blockIdx.x];  // the member of this block
   const ChainInst& I = inst[s_i];
   const int64_t blk = (int64_t)blockIdx.x - start[s_i];
   const int np = (sizeof(T) == 4) ? I.np4 : I.np8;
   const int2 kmi = km[s_i];
-  if (kmi.y != MODE || j < kmi.x || pass >= np) return;  // uniform over the block
+  if (kmi.y != MODE || pass >= np) return;  // uniform over the block
+  const int j = kmi.x;
   {
     const int* src = reinterpret_cast<const int*>((sizeof(T) == 4) ? &I.p4[pass] : &I.p8[pass]);
     int* dst = reinterpret_cast<int*>(&cps);
     for (int q = threadIdx.x; q < (int)(sizeof(ChainPass) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
   }
   __syncthreads();
-  if (blk >= chain_pass_blocks_dev(cps)) return;
+  const int64_t ntiles = chain_pass_blocks_dev(cps);
   const IO* x = (MODE == kModeF32) ? reinterpret_cast<const IO*>(I.x32)
                                    : reinterpret_cast<const IO*>(I.V + (int64_t)j * I.ldv);
   const AuxCoefT<T>* c;
@@ -320,33 +375,26 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3))
     c = reinterpret_cast<const AuxCoefT<T>*>(&I.cdf);
   else
     c = reinterpret_cast<const AuxCoefT<T>*>(&I.c64);
-  chain_block<T, ZB, IO>(reinterpret_cast<T*>(I.P), x, I.tvec, I.smap, reinterpret_cast<IO*>(I.fold), nullptr, 1.0,
-                         I.L, I.bc, I.dir, *c, cps, (uint64_t)blk);
+  for (int q = 0; q < kBatchTiles; ++q) {
+    const int64_t tile = blk * kBatchTiles + q;
+    if (tile >= ntiles) break;  // uniform over the block
+    if (q) __syncthreads();     // the previous tile's last reads of shared memory
+    chain_block<T, ZB, IO>(reinterpret_cast<T*>(I.P), x, I.tvec, I.smap, reinterpret_cast<IO*>(I.fold), nullptr, 1.0,
+                           I.L, I.bc, I.dir, *c, cps, (uint64_t)tile);
+  }
 }
 
 // w[k] = fold[idx[k]] * gs * dup[k] * tvec[k] (reduced) or fold[k] * gs * nf *
-// tvec[k] (full), per instance; kSweepRows rows per block
+// tvec[k] (full), per member; kSweepRows rows per block
 template <class IO, int MODE>
 __global__ void __launch_bounds__(256) contract_batch_kernel(const ChainInst* __restrict__ inst,
                                                              const int2* __restrict__ km,
-                                                             const int64_t* __restrict__ rstart, int count, int j) {
-  __shared__ int s_i;
-  if (threadIdx.x == 0) {
-    const int64_t b = blockIdx.x;
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (rstart[mid] <= b)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    s_i = lo;
-  }
-  __syncthreads();
+                                                             const int64_t* __restrict__ rstart,
+                                                             const int* __restrict__ rmem) {
+  const int s_i = rmem[blockIdx.x];  // the member of this row block
   const ChainInst& I = inst[s_i];
   const int2 kmi = km[s_i];
-  if (kmi.y != MODE || j < kmi.x) return;
+  if (kmi.y != MODE) return;
   const int64_t r0 = ((int64_t)blockIdx.x - rstart[s_i]) * kSweepRows;
   const int64_t r1 = min(r0 + (int64_t)kSweepRows, I.n);
   const double gs = (MODE == kModeF32) ? I.gs32 : (MODE == kModeDF ? I.gsdf : I.gs64);
@@ -355,10 +403,6 @@ __global__ void __launch_bounds__(256) contract_batch_kernel(const ChainInst* __
     const double f = I.idx ? (double)z[I.idx[r]] * (double)I.dup[r] : (double)z[r] * I.nf;
     I.w[r] = f * gs * I.tvec[r];
   }
-}
-
-__device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp) {
-  return (int64_t)(cp.last ? 1 : cp.nlb) << cp.no;
 }
 
 }  // namespace
@@ -454,8 +498,9 @@ void to_f32_dev(const double* x, float* y, int64_t n, cudaStream_t s) {
 // ------------------------------------------------------------------ pass plans and tuning
 // Tile bits and threads per block of the chain passes, per (element size,
 // carried bits, width).  Defaults: 2^13-element tiles for 4-byte elements and
-// 2^12 for 8-byte ones (32 KB either way), 256 threads; the autotuner
-// (tm_chain_autotune) overrides entries with measured choices.
+// 2^12 for 8-byte ones (32 KB either way), 256 threads, except where the
+// built-in table of measured choices has an entry; tm_chain_autotune and
+// tm_chain_set_tuning override entries at run time.
 namespace {
 struct ChainTune {
   int tile_bits = 0, threads = 0;
@@ -464,10 +509,27 @@ std::mutex g_tune_mu;
 ChainTune g_tune[2][2][33];  // [elem 4/8][zb][L]
 }  // namespace
 
+// Choices of the autotuner (python -m latttmat_gb300.autotune) measured on a
+// GB300 for the diagonal BNNNI widths of the 256-point parameter sweep:
+// {L, tile bits, threads} for 4-byte and for 8-byte elements.
+struct TunedEntry {
+  int L, tb4, th4, tb8, th8;
+};
+constexpr TunedEntry kTunedBNNNI[] = {
+    {16, 11, 128, 11, 128}, {18, 13, 256, 13, 256}, {20, 11, 128, 11, 128},
+    {22, 13, 128, 13, 128}, {24, 12, 128, 12, 128},
+};
+
 void chain_tuning(int L, size_t elem, bool zb, int& tile_bits, int& threads) {
   tile_bits = (elem == 8) ? 12 : 13;
   threads = 256;
   if (L < 0 || L > 32) return;
+  if (zb)
+    for (const TunedEntry& t : kTunedBNNNI)
+      if (t.L == L) {
+        tile_bits = (elem == 8) ? t.tb8 : t.tb4;
+        threads = (elem == 8) ? t.th8 : t.th4;
+      }
   std::lock_guard<std::mutex> lock(g_tune_mu);
   const ChainTune& t = g_tune[elem == 8][zb ? 1 : 0][L];
   if (t.tile_bits) tile_bits = t.tile_bits;
@@ -587,7 +649,7 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
 }
 
 // ------------------------------------------------------------------ batch members
-void chain_inst_fill(const Op& op, int dir, ChainInst& rec) {
+void chain_inst_fill(const Op& op, int dir, ChainInst& rec, int tb4, int tb8) {
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
   const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
   const int L = op.L;
@@ -618,9 +680,9 @@ void chain_inst_fill(const Op& op, int dir, ChainInst& rec) {
   rec.c64.g = 1.0;
   rec.gs32 = rec.gsdf = std::pow(gb, (double)nsteps);
   rec.gs64 = 1.0;
-  int tb4 = 0, th4 = 0, tb8 = 0, th8 = 0;
-  chain_tuning(L, 4, zb, tb4, th4);
-  chain_tuning(L, 8, zb, tb8, th8);
+  int th = 0;
+  if (tb4 <= 0) chain_tuning(L, 4, zb, tb4, th);
+  if (tb8 <= 0) chain_tuning(L, 8, zb, tb8, th);
   const std::vector<ChainPass> p4 = chain_plan(L, zb, rec.nlb, tb4), p8 = chain_plan(L, zb, rec.nlb, tb8);
   if ((int)p4.size() > kChainMaxPass || (int)p8.size() > kChainMaxPass) fail(TM_ERR_LIMIT, "too many chain passes");
   rec.np4 = (int)p4.size();
@@ -635,55 +697,46 @@ void chain_inst_fill(const Op& op, int dir, ChainInst& rec) {
 
 namespace {
 template <class T, int ZB, class IO, int MODE>
-void launch_batch_pass(const ChainInst* inst, const int2* km, int count, const int64_t* start, int pass, int64_t nblk,
-                       int j, int threads, size_t smem, cudaStream_t s) {
+void launch_batch_pass(const ChainInst* inst, const int2* km, const int64_t* start, const int* bmem, int pass,
+                       int64_t nblk, int threads, size_t smem, cudaStream_t s) {
   raise_smem_limit((const void*)chain_batch_kernel<T, ZB, IO, MODE>, smem);
-  chain_batch_kernel<T, ZB, IO, MODE><<<(unsigned)nblk, threads, smem, s>>>(inst, km, start, count, pass, j);
+  chain_batch_kernel<T, ZB, IO, MODE><<<(unsigned)nblk, threads, smem, s>>>(inst, km, start, bmem, pass);
   TM_CKK("chain_batch");
 }
 
 template <int ZB, int MODE>
-int batch_product_mode(const ChainInst* inst, const int2* km, int count, const int64_t* start, int np,
-                       const std::vector<int64_t>& nblk,
-                       const int64_t* rstart, int64_t nrblk, int j, int threads, size_t smem, cudaStream_t s) {
+int batch_product_mode(const ChainBatch& B, const int2* km, const ChainBatch::Plan& P, cudaStream_t s) {
   int launches = 0;
-  for (int p = 0; p < np; ++p) {
-    if (nblk[p] == 0) continue;
-    const int64_t* st = start + (size_t)p * (count + 1);
+  for (int p = 0; p < P.np; ++p) {
+    if (P.nblk[p] == 0) continue;
+    const int64_t* st = P.start + (size_t)p * (B.count + 1);
+    const int* bm = P.bmem + P.boff[p];
     if constexpr (MODE == kModeF32)
-      launch_batch_pass<float, ZB, float, MODE>(inst, km, count, st, p, nblk[p], j, threads, smem, s);
+      launch_batch_pass<float, ZB, float, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s);
     else if constexpr (MODE == kModeDF)
-      launch_batch_pass<dfloat, ZB, double, MODE>(inst, km, count, st, p, nblk[p], j, threads, smem, s);
+      launch_batch_pass<dfloat, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s);
     else
-      launch_batch_pass<double, ZB, double, MODE>(inst, km, count, st, p, nblk[p], j, threads, smem, s);
+      launch_batch_pass<double, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s);
     ++launches;
   }
   if constexpr (MODE == kModeF32)
-    contract_batch_kernel<float, MODE><<<(unsigned)nrblk, 256, 0, s>>>(inst, km, rstart, count, j);
+    contract_batch_kernel<float, MODE><<<(unsigned)B.nrblk, 256, 0, s>>>(B.inst, km, B.rstart, B.rmem);
   else
-    contract_batch_kernel<double, MODE><<<(unsigned)nrblk, 256, 0, s>>>(inst, km, rstart, count, j);
+    contract_batch_kernel<double, MODE><<<(unsigned)B.nrblk, 256, 0, s>>>(B.inst, km, B.rstart, B.rmem);
   TM_CKK("contract_batch");
   return launches + 1;
 }
 }  // namespace
 
-int chain_batch_product(const ChainInst* inst, const int2* km, int count, const int64_t* start4, const int64_t* start8,
-                        int np4max,
-                        int np8max, const std::vector<int64_t>& nblk4, const std::vector<int64_t>& nblk8,
-                        const int64_t* rstart, int64_t nrblk, int zb, int mode, int j, int threads4, int threads8,
-                        size_t smem4, size_t smem8, cudaStream_t s) {
-  if (zb) {
-    if (mode == kModeF32)
-      return batch_product_mode<1, kModeF32>(inst, km, count, start4, np4max, nblk4, rstart, nrblk, j, threads4, smem4, s);
-    if (mode == kModeDF)
-      return batch_product_mode<1, kModeDF>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
-    return batch_product_mode<1, kModeF64>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
+int chain_batch_product(const ChainBatch& B, const int2* km, int mode, cudaStream_t s) {
+  if (B.zb) {
+    if (mode == kModeF32) return batch_product_mode<1, kModeF32>(B, km, B.p4, s);
+    if (mode == kModeDF) return batch_product_mode<1, kModeDF>(B, km, B.p8, s);
+    return batch_product_mode<1, kModeF64>(B, km, B.p8, s);
   }
-  if (mode == kModeF32)
-    return batch_product_mode<0, kModeF32>(inst, km, count, start4, np4max, nblk4, rstart, nrblk, j, threads4, smem4, s);
-  if (mode == kModeDF)
-    return batch_product_mode<0, kModeDF>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
-  return batch_product_mode<0, kModeF64>(inst, km, count, start8, np8max, nblk8, rstart, nrblk, j, threads8, smem8, s);
+  if (mode == kModeF32) return batch_product_mode<0, kModeF32>(B, km, B.p4, s);
+  if (mode == kModeDF) return batch_product_mode<0, kModeDF>(B, km, B.p8, s);
+  return batch_product_mode<0, kModeF64>(B, km, B.p8, s);
 }
 
 // ------------------------------------------------------------------ autotuner

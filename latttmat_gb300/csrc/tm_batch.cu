@@ -5,8 +5,9 @@
 // sweep over (betaJ, kappa, h, L) points is that loop run many times.
 //
 // Aux-bit operators (models B and D) run as one device batch (tm_sweep.cu):
-// every chain pass is one launch over all points' tiles, and the points run
-// Arnoldi in lockstep, one CUDA graph per restart cycle.  The other operator
+// every chain pass is one launch over all points' tiles, and every point
+// extends its Arnoldi basis by one column per step (one CUDA graph per step),
+// restarting on its own.  The other operator
 // families run on a pool of host threads, each building, solving and
 // releasing one operator at a time on that operator's own CUDA stream, so the
 // kernels of different points overlap on the GPU.  Device memory is

@@ -35,14 +35,15 @@ struct ChainPass {
 };
 
 constexpr int kChainMaxPass = 8;
+constexpr int kBatchTiles = 4;  // tiles of one member per block of a batched pass
 
 // Product modes of a batch member in one step.
 enum { kModeIdle = 0, kModeF32 = 1, kModeDF = 2, kModeF64 = 3 };
 
 // One operator of a batched product, in device memory.  The batch kernels
-// find their instance from the block index (prefix tables per pass) and skip
-// instances whose mode (km[i].y, set per restart cycle) differs from the
-// launch's or whose kept Krylov columns reach past the step (j < km[i].x).
+// find their member from a per-block member map and skip members whose
+// product mode (km[i].y, set per step) differs from the launch's; km[i].x is
+// the Krylov column the member extends this step.
 struct ChainInst {
   ChainPass p4[kChainMaxPass];  // passes of the 4-byte (FP32) plan
   ChainPass p8[kChainMaxPass];  // passes of the 8-byte (FP64, double-float) plan
@@ -77,18 +78,33 @@ int64_t chain_pass_blocks(const ChainPass& cp);
 size_t chain_pass_smem(const ChainPass& cp, bool zb, size_t elem);
 
 // Fill the geometry and coefficients of `rec` for operator `op` (an aux-bit
-// operator; dir 1 for its transpose).
-void chain_inst_fill(const Op& op, int dir, ChainInst& rec);
+// operator; dir 1 for its transpose), with tiles of 2^tb4 (4-byte) and 2^tb8
+// (8-byte) elements (0: the tuning table's choice for the width).
+void chain_inst_fill(const Op& op, int dir, ChainInst& rec, int tb4 = 0, int tb8 = 0);
 
-// Batched product step j for every instance in `mode`: one launch per pass
-// over all instances' tiles, then one contraction launch into each w.
-//   inst/count: device table; start4/start8: block prefixes per pass
-//   ([pass][count+1]) of the 4- and 8-byte plans; rstart: row-chunk prefix
-//   ([count+1], kSweepRows rows per block).  Returns the launches issued.
-int chain_batch_product(const ChainInst* inst, const int2* km, int count, const int64_t* start4, const int64_t* start8,
-                        int np4max, int np8max, const std::vector<int64_t>& nblk4, const std::vector<int64_t>& nblk8,
-                        const int64_t* rstart, int64_t nrblk, int zb, int mode, int j, int threads4, int threads8,
-                        size_t smem4, size_t smem8, cudaStream_t s);
+// Device tables of a batched product over `count` members.
+struct ChainBatch {
+  const ChainInst* inst = nullptr;
+  int count = 0, zb = 0;
+  // per plan (4-byte, 8-byte): passes, block prefix [pass][count+1] (blocks of
+  // kBatchTiles tiles), the member of every block (per pass, from boff[p]),
+  // blocks per pass, threads per block and dynamic shared memory
+  struct Plan {
+    int np = 0, threads = 256;
+    size_t smem = 0;
+    const int64_t* start = nullptr;
+    const int* bmem = nullptr;
+    std::vector<int64_t> nblk, boff;
+  } p4, p8;
+  const int64_t* rstart = nullptr;  // row-chunk prefix [count+1] (kSweepRows rows per block)
+  const int* rmem = nullptr;        // the member of every row block
+  int64_t nrblk = 0;
+};
+
+// Batched product of every member in `mode` (input: column km[i].x of its
+// basis, or its x32 in FP32): one launch per pass over all members' tiles,
+// then one contraction launch into each w.  Returns the launches issued.
+int chain_batch_product(const ChainBatch& B, const int2* km, int mode, cudaStream_t s);
 
 constexpr int kSweepRows = 4096;  // rows per block of the batched row kernels
 

@@ -9,19 +9,19 @@
 //     member's pass geometry, Boltzmann factors and buffers, whatever its
 //     width;
 //   - each chain pass is ONE launch over the tiles of every member (a block
-//     finds its member by binary search over the pass's block prefix); so are
-//     the contraction and the Krylov vector kernels (row chunks of
-//     kSweepRows);
-//   - the members run Arnoldi in lockstep: at step j every member extends its
-//     basis by column j+1, and member i takes part when j >= k_i, its kept
-//     columns after the last restart (km[i] on the device);
-//   - the steps of one restart cycle are captured once in a CUDA graph and
-//     replayed each cycle;
-//   - between cycles the host solves each member's small projected problem
-//     (the Krylov-Schur restart of tm_arnoldi.cu, tm_krylov.h) and uploads the
-//     new kept bases; converged members go idle;
+//     takes its member from a per-block member map); so are the contraction
+//     and the Krylov vector kernels (row chunks of kSweepRows);
+//   - every step, each active member extends its Arnoldi basis by one column
+//     (member i at its own column j_i, km[i] on the device), so members
+//     restart independently and none waits for another's cycle;
+//   - one step of all members is captured once in a CUDA graph and replayed;
+//   - after each step the host takes the projected matrices back; a member
+//     whose basis is full gets its small projected problem solved (the
+//     Krylov-Schur restart of tm_arnoldi.cu, tm_krylov.h) and its kept basis
+//     rotated in before the next step; converged members go idle;
 //   - members are grouped into waves whose buffers fit a share of the free
-//     device memory; a wave holds members of any mix of widths.
+//     device memory; a wave holds members of any mix of widths, all with the
+//     tile size tuned for its widest member.
 // Mixed precision as in tm_arnoldi.cu: FP32 products until the Ritz residuals
 // reach the FP32 floor, then FP64-accurate (double-float) products from the
 // combined wanted Ritz vectors until the tolerance is met.
@@ -51,55 +51,45 @@ constexpr int kSweepMaxM = 24;  // largest Krylov subspace of a sweep member
 constexpr int kScH1 = 0, kScH2 = 32, kScN = 64, kScH = 72;
 constexpr int kScStride = kScH + (kSweepMaxM + 1) * (kSweepMaxM + 1) + 7;  // 704
 
-__device__ __forceinline__ int find_member(const int64_t* __restrict__ start, int count, int64_t b) {
-  int lo = 0, hi = count - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (start[mid] <= b)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
 // the member and row range of a row-chunk block
 struct RowBlock {
   int i;
   int64_t r0, r1;
 };
 
+// (rmem: the member of every row block, stored after the prefix rstart[count + 1])
 __device__ __forceinline__ RowBlock row_block(const ChainInst* __restrict__ inst, const int64_t* __restrict__ rstart,
                                               int count) {
-  __shared__ int s_i;
-  if (threadIdx.x == 0) s_i = find_member(rstart, count, blockIdx.x);
-  __syncthreads();
+  const int* rmem = reinterpret_cast<const int*>(rstart + count + 1);
   RowBlock rb;
-  rb.i = s_i;
-  rb.r0 = ((int64_t)blockIdx.x - rstart[s_i]) * kSweepRows;
-  rb.r1 = min(rb.r0 + (int64_t)kSweepRows, inst[s_i].n);
+  rb.i = rmem[blockIdx.x];
+  rb.r0 = ((int64_t)blockIdx.x - rstart[rb.i]) * kSweepRows;
+  rb.r1 = min(rb.r0 + (int64_t)kSweepRows, inst[rb.i].n);
   return rb;
 }
 
-__device__ __forceinline__ bool step_on(int2 km, int j) { return km.y != kModeIdle && j >= km.x; }
+// km[i] = (column j the member extends this step, product mode or idle)
+__device__ __forceinline__ bool step_on(int2 km) { return km.y != kModeIdle; }
 
 // x32 = (float) V[:, j] for the members in the FP32 phase
 __global__ void __launch_bounds__(256) sw_to_f32(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                                                 const int64_t* __restrict__ rstart, int count, int j) {
+                                                 const int64_t* __restrict__ rstart, int count) {
   const RowBlock rb = row_block(inst, rstart, count);
   const int2 k = km[rb.i];
-  if (k.y != kModeF32 || j < k.x) return;
+  if (k.y != kModeF32) return;
   const ChainInst& I = inst[rb.i];
-  const double* v = I.V + (int64_t)j * I.ldv;
+  const double* v = I.V + (int64_t)k.x * I.ldv;
   for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) I.x32[r] = (float)v[r];
 }
 
 // partial dots of w against columns 0..j: one warp per column, lanes over rows
 __global__ void __launch_bounds__(256) sw_mdot(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                                               const int64_t* __restrict__ rstart, int count, int j,
+                                               const int64_t* __restrict__ rstart, int count,
                                                double* __restrict__ part) {
   const RowBlock rb = row_block(inst, rstart, count);
-  if (!step_on(km[rb.i], j)) return;
+  const int2 k = km[rb.i];
+  if (!step_on(k)) return;
+  const int j = k.x;
   const ChainInst& I = inst[rb.i];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int c = warp; c <= j; c += nw) {
@@ -113,10 +103,10 @@ __global__ void __launch_bounds__(256) sw_mdot(const ChainInst* __restrict__ ins
 
 // partial |w|^2 (slot 0)
 __global__ void __launch_bounds__(256) sw_nrm(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                                              const int64_t* __restrict__ rstart, int count, int j,
+                                              const int64_t* __restrict__ rstart, int count,
                                               double* __restrict__ part) {
   const RowBlock rb = row_block(inst, rstart, count);
-  if (!step_on(km[rb.i], j)) return;
+  if (!step_on(km[rb.i])) return;
   const ChainInst& I = inst[rb.i];
   double acc = 0.0;
   for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) acc = fma(I.w[r], I.w[r], acc);
@@ -134,9 +124,10 @@ __global__ void __launch_bounds__(256) sw_nrm(const ChainInst* __restrict__ inst
 // sum the row-chunk partials of each member into sc[off + c], c <= j (one
 // block per member, one thread per column; fixed order, so deterministic)
 __global__ void sw_reduce(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                          const int64_t* __restrict__ rstart, int j, const double* __restrict__ part, int off) {
+                          const int64_t* __restrict__ rstart, const double* __restrict__ part, int off) {
   const int i = blockIdx.x, c = threadIdx.x;
-  if (!step_on(km[i], j) || c > j) return;
+  const int2 k = km[i];
+  if (!step_on(k) || c > k.x) return;
   double acc = 0.0;
   for (int64_t b = rstart[i]; b < rstart[i + 1]; ++b) acc += part[b * kSweepMaxM + c];
   inst[i].sc[off + c] = acc;
@@ -144,9 +135,11 @@ __global__ void sw_reduce(const ChainInst* __restrict__ inst, const int2* __rest
 
 // w -= V[:, 0..j] h, h = sc[off .. off + j]
 __global__ void __launch_bounds__(256) sw_maxpy(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                                                const int64_t* __restrict__ rstart, int count, int j, int off) {
+                                                const int64_t* __restrict__ rstart, int count, int off) {
   const RowBlock rb = row_block(inst, rstart, count);
-  if (!step_on(km[rb.i], j)) return;
+  const int2 k = km[rb.i];
+  if (!step_on(k)) return;
+  const int j = k.x;
   const ChainInst& I = inst[rb.i];
   __shared__ double hs[kSweepMaxM];
   if (threadIdx.x <= j) hs[threadIdx.x] = I.sc[off + threadIdx.x];
@@ -161,9 +154,11 @@ __global__ void __launch_bounds__(256) sw_maxpy(const ChainInst* __restrict__ in
 // |w|^2 from the partials; column j of the projected matrix:
 // H[0..j, j] = h1 + h2, H[j+1, j] = |w|
 __global__ void sw_hcol(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                        const int64_t* __restrict__ rstart, int j, int m, const double* __restrict__ part) {
+                        const int64_t* __restrict__ rstart, int m, const double* __restrict__ part) {
   const int i = blockIdx.x, c = threadIdx.x;
-  if (!step_on(km[i], j)) return;
+  const int2 k = km[i];
+  if (!step_on(k)) return;
+  const int j = k.x;
   double* sc = inst[i].sc;
   double* H = sc + kScH;
   const int ld = m + 1;
@@ -178,9 +173,11 @@ __global__ void sw_hcol(const ChainInst* __restrict__ inst, const int2* __restri
 
 // V[:, j+1] = w / |w| (zero column on a breakdown: the residual is then 0)
 __global__ void __launch_bounds__(256) sw_normalize(const ChainInst* __restrict__ inst, const int2* __restrict__ km,
-                                                    const int64_t* __restrict__ rstart, int count, int j) {
+                                                    const int64_t* __restrict__ rstart, int count) {
   const RowBlock rb = row_block(inst, rstart, count);
-  if (!step_on(km[rb.i], j)) return;
+  const int2 k = km[rb.i];
+  if (!step_on(k)) return;
+  const int j = k.x;
   const ChainInst& I = inst[rb.i];
   const double nsq = I.sc[kScN];
   const double f = nsq > 0.0 ? 1.0 / sqrt(nsq) : 0.0;
@@ -286,8 +283,8 @@ struct OpDeleter {
 // Solve state of one member.
 struct Member {
   std::unique_ptr<Op, OpDeleter> op;
-  int phase = kModeIdle;  // product mode of the current cycles
-  int k = 0;              // kept columns
+  int phase = kModeIdle;  // product mode of the current steps
+  int j = 0;              // column extended by the next step (kept columns after a restart)
   bool done = false;
   tm_status status = TM_OK;
   std::string msg;
@@ -306,7 +303,9 @@ struct Sweep {
   cudaStream_t s = nullptr;
   int zb = 0;
   size_t budget_override = 0;  // bytes of member buffers per wave (0: from free memory)
-  int64_t graph_launches = 0;
+  // diagnostics of the last solve: waves, steps, seconds building waves, in
+  // steps (device work, host-timed), in host restarts
+  double stats[5] = {0, 0, 0, 0, 0};
 
   ~Sweep() {
     mem.clear();
@@ -354,24 +353,31 @@ struct Wave {
   Sweep& sw;
   int a, b, count, m;
   std::vector<std::unique_ptr<DBuf>> bufs;
-  DBuf inst, kmd, start4, start8, rstart, part, sc, Wall, rot, flag, yptr;
+  DBuf inst, kmd, start4, start8, bmem4, bmem8, rstart, part, sc, Wall, rot, flag, yptr;
   std::vector<ChainInst> host;
-  std::vector<int64_t> nblk4, nblk8, rst;
+  ChainBatch B;
   int np4max = 0, np8max = 0, threads4 = 256, threads8 = 256;
   size_t smem4 = 0, smem8 = 0;
   int64_t nrblk = 0;
-  std::map<int, cudaGraphExec_t> graphs;  // by first step of the cycle
+  std::map<int, cudaGraphExec_t> graphs;  // one step, by the product modes present
   std::map<int, int64_t> graph_kernels;
 
   Wave(Sweep& s_, int a_, int b_, int m_) : sw(s_), a(a_), b(b_), count(b_ - a_), m(m_) {
     cudaStream_t s = sw.s;
     host.resize(count);
+    // one tile size and block size per element size for the whole wave: the
+    // tuned choice at the widest member (most of the work), so every block
+    // of a launch gets the shared memory it uses
     int Lmax = 0;
+    for (int q = 0; q < count; ++q) Lmax = std::max(Lmax, sw.mem[a + q].op->L);
+    int tb4 = 0, tb8 = 0;
+    chain_tuning(Lmax, 4, sw.zb, tb4, threads4);
+    chain_tuning(Lmax, 8, sw.zb, tb8, threads8);
     for (int q = 0; q < count; ++q) {
       const Op& o = *sw.mem[a + q].op;
       ChainInst& I = host[q];
       std::memset(&I, 0, sizeof(I));
-      chain_inst_fill(o, 0, I);
+      chain_inst_fill(o, 0, I, tb4, tb8);
       const int64_t N = 1ll << o.L;
       auto mk = [&](size_t bytes) {
         bufs.emplace_back(new DBuf());
@@ -388,36 +394,44 @@ struct Wave {
       np8max = std::max(np8max, I.np8);
       for (int p = 0; p < I.np4; ++p) smem4 = std::max(smem4, chain_pass_smem(I.p4[p], sw.zb, 4));
       for (int p = 0; p < I.np8; ++p) smem8 = std::max(smem8, chain_pass_smem(I.p8[p], sw.zb, 8));
-      Lmax = std::max(Lmax, o.L);
     }
-    // threads per block: the tuned choice at the widest member (most of the work)
-    int tb = 0;
-    chain_tuning(Lmax, 4, sw.zb, tb, threads4);
-    chain_tuning(Lmax, 8, sw.zb, tb, threads8);
     sc.alloc((size_t)count * kScStride * 8);
     TM_CK(cudaMemsetAsync(sc.p, 0, sc.bytes, s));
     for (int q = 0; q < count; ++q) host[q].sc = sc.as<double>() + (size_t)q * kScStride;
-    // block prefixes per pass
-    std::vector<int64_t> s4((size_t)std::max(np4max, 1) * (count + 1), 0), s8((size_t)std::max(np8max, 1) * (count + 1), 0);
-    nblk4.assign(std::max(np4max, 1), 0);
-    nblk8.assign(std::max(np8max, 1), 0);
-    for (int p = 0; p < np4max; ++p)
-      for (int q = 0; q < count; ++q)
-        s4[(size_t)p * (count + 1) + q + 1] =
-            s4[(size_t)p * (count + 1) + q] + (p < host[q].np4 ? chain_pass_blocks(host[q].p4[p]) : 0);
-    for (int p = 0; p < np8max; ++p)
-      for (int q = 0; q < count; ++q)
-        s8[(size_t)p * (count + 1) + q + 1] =
-            s8[(size_t)p * (count + 1) + q] + (p < host[q].np8 ? chain_pass_blocks(host[q].p8[p]) : 0);
-    for (int p = 0; p < np4max; ++p) nblk4[p] = s4[(size_t)p * (count + 1) + count];
-    for (int p = 0; p < np8max; ++p) nblk8[p] = s8[(size_t)p * (count + 1) + count];
-    for (int64_t v : nblk4)
-      if (v >= (1ll << 31)) fail(TM_ERR_LIMIT, "sweep wave too large for one launch");
-    for (int64_t v : nblk8)
-      if (v >= (1ll << 31)) fail(TM_ERR_LIMIT, "sweep wave too large for one launch");
-    rst.assign(count + 1, 0);
+    // block prefixes per pass (kBatchTiles tiles per block) and the member of
+    // every block
+    auto plan_tables = [&](bool four, int npmax, std::vector<int64_t>& st, std::vector<int>& bm,
+                           std::vector<int64_t>& nblk, std::vector<int64_t>& boff) {
+      st.assign((size_t)std::max(npmax, 1) * (count + 1), 0);
+      nblk.assign(std::max(npmax, 1), 0);
+      boff.assign(std::max(npmax, 1), 0);
+      bm.clear();
+      for (int p = 0; p < npmax; ++p) {
+        boff[p] = (int64_t)bm.size();
+        for (int q = 0; q < count; ++q) {
+          const int np = four ? host[q].np4 : host[q].np8;
+          const int64_t nb =
+              p < np ? (chain_pass_blocks(four ? host[q].p4[p] : host[q].p8[p]) + kBatchTiles - 1) / kBatchTiles : 0;
+          st[(size_t)p * (count + 1) + q + 1] = st[(size_t)p * (count + 1) + q] + nb;
+          bm.insert(bm.end(), (size_t)nb, q);
+        }
+        nblk[p] = st[(size_t)p * (count + 1) + count];
+        if (nblk[p] >= (1ll << 31)) fail(TM_ERR_LIMIT, "sweep wave too large for one launch");
+      }
+    };
+    std::vector<int64_t> s4, s8;
+    std::vector<int> bm4, bm8;
+    plan_tables(true, np4max, s4, bm4, B.p4.nblk, B.p4.boff);
+    plan_tables(false, np8max, s8, bm8, B.p8.nblk, B.p8.boff);
+    std::vector<int64_t> rst(count + 1, 0);
     for (int q = 0; q < count; ++q) rst[q + 1] = rst[q] + (host[q].n + kSweepRows - 1) / kSweepRows;
     nrblk = rst[count];
+    // row prefix followed by the member of every row block (one buffer)
+    std::vector<int64_t> rtab(rst);
+    std::vector<int> rm;
+    for (int q = 0; q < count; ++q) rm.insert(rm.end(), (size_t)(rst[q + 1] - rst[q]), q);
+    rtab.resize(rst.size() + (rm.size() * 4 + 7) / 8, 0);
+    std::memcpy(rtab.data() + rst.size(), rm.data(), rm.size() * 4);
     auto up = [&](DBuf& d, const void* src, size_t bytes) {
       d.alloc(bytes);
       TM_CK(cudaMemcpyAsync(d.p, src, bytes, cudaMemcpyHostToDevice, s));
@@ -425,7 +439,25 @@ struct Wave {
     up(inst, host.data(), sizeof(ChainInst) * count);
     up(start4, s4.data(), s4.size() * 8);
     up(start8, s8.data(), s8.size() * 8);
-    up(rstart, rst.data(), rst.size() * 8);
+    up(bmem4, bm4.data(), std::max<size_t>(bm4.size(), 1) * 4);
+    up(bmem8, bm8.data(), std::max<size_t>(bm8.size(), 1) * 4);
+    up(rstart, rtab.data(), rtab.size() * 8);
+    B.inst = inst.as<ChainInst>();
+    B.count = count;
+    B.zb = sw.zb;
+    B.p4.np = np4max;
+    B.p4.threads = threads4;
+    B.p4.smem = smem4;
+    B.p4.start = start4.as<int64_t>();
+    B.p4.bmem = bmem4.as<int>();
+    B.p8.np = np8max;
+    B.p8.threads = threads8;
+    B.p8.smem = smem8;
+    B.p8.start = start8.as<int64_t>();
+    B.p8.bmem = bmem8.as<int>();
+    B.rstart = rstart.as<int64_t>();
+    B.rmem = reinterpret_cast<const int*>(rstart.as<int64_t>() + count + 1);
+    B.nrblk = nrblk;
     kmd.alloc((size_t)count * sizeof(int2));
     part.alloc((size_t)nrblk * kSweepMaxM * 8);
     Wall.alloc((size_t)count * m * m * 8);
@@ -443,53 +475,53 @@ struct Wave {
   const ChainInst* I() const { return inst.as<ChainInst>(); }
   const int2* km() const { return kmd.as<int2>(); }
 
-  int product(int mode, int j) {
+  int product(int mode) {
     int nl = 0;
     if (mode == kModeF32) {
-      sw_to_f32<<<(unsigned)nrblk, 256, 0, sw.s>>>(I(), km(), rstart.as<int64_t>(), count, j);
+      sw_to_f32<<<(unsigned)nrblk, 256, 0, sw.s>>>(I(), km(), rstart.as<int64_t>(), count);
       TM_CKK("sw_to_f32");
       ++nl;
     }
-    nl += chain_batch_product(I(), km(), count, start4.as<int64_t>(), start8.as<int64_t>(), np4max, np8max, nblk4, nblk8,
-                              rstart.as<int64_t>(), nrblk, sw.zb, mode, j, threads4, threads8, smem4, smem8, sw.s);
+    nl += chain_batch_product(B, km(), mode, sw.s);
     return nl;
   }
 
-  // one Arnoldi step at column j for every member taking part
-  void step(int j, bool f32_phase, bool df_phase, bool f64_phase) {
+  // one Arnoldi step of every member taking part (each at its own column)
+  void step(bool f32_phase, bool df_phase, bool f64_phase) {
     cudaStream_t s = sw.s;
     const int64_t* rs = rstart.as<int64_t>();
     double* pt = part.as<double>();
-    if (f32_phase) product(kModeF32, j);
-    if (df_phase) product(kModeDF, j);
-    if (f64_phase) product(kModeF64, j);
+    if (f32_phase) product(kModeF32);
+    if (df_phase) product(kModeDF);
+    if (f64_phase) product(kModeF64);
     for (int pass = 0; pass < 2; ++pass) {
       const int off = pass ? kScH2 : kScH1;
-      sw_mdot<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j, pt);
+      sw_mdot<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, pt);
       TM_CKK("sw_mdot");
-      sw_reduce<<<count, 32, 0, s>>>(I(), km(), rs, j, pt, off);
+      sw_reduce<<<count, 32, 0, s>>>(I(), km(), rs, pt, off);
       TM_CKK("sw_reduce");
-      sw_maxpy<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j, off);
+      sw_maxpy<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, off);
       TM_CKK("sw_maxpy");
     }
-    sw_nrm<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j, pt);
+    sw_nrm<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, pt);
     TM_CKK("sw_nrm");
-    sw_hcol<<<count, 32, 0, s>>>(I(), km(), rs, j, m, pt);
+    sw_hcol<<<count, 32, 0, s>>>(I(), km(), rs, m, pt);
     TM_CKK("sw_hcol");
-    sw_normalize<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count, j);
+    sw_normalize<<<(unsigned)nrblk, 256, 0, s>>>(I(), km(), rs, count);
     TM_CKK("sw_normalize");
   }
 
-  // the steps j = k0 .. m-1 of a cycle, as a CUDA graph captured on first use
-  void cycle(int k0, bool f32_phase, bool df_phase, bool f64_phase) {
-    const int key = k0 | (f32_phase << 8) | (df_phase << 9) | (f64_phase << 10);
+  // one step of every member, as a CUDA graph captured on first use per set
+  // of product modes present
+  void run_step(bool f32_phase, bool df_phase, bool f64_phase) {
+    const int key = (f32_phase << 0) | (df_phase << 1) | (f64_phase << 2);
     auto it = graphs.find(key);
     if (it == graphs.end()) {
       const int64_t l0 = tm_launch_count();
       cudaGraph_t g;
       TM_CK(cudaStreamBeginCapture(sw.s, cudaStreamCaptureModeThreadLocal));
       try {
-        for (int j = k0; j < m; ++j) step(j, f32_phase, df_phase, f64_phase);
+        step(f32_phase, df_phase, f64_phase);
       } catch (...) {
         cudaStreamEndCapture(sw.s, &g);
         throw;
@@ -536,17 +568,23 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
   const int first_phase = (mode == TM_EIGS_MIXED) ? kModeF32 : kModeF64;
   const int final_phase = (mode == TM_EIGS_MIXED) ? kModeDF : kModeF64;
   const int max_cycles = (mode == TM_EIGS_MIXED) ? 200 : 300;
+  for (double& v : sw.stats) v = 0.0;
+  using clk = std::chrono::steady_clock;
+  auto since = [](clk::time_point t) { return std::chrono::duration<double>(clk::now() - t).count(); };
   for (auto& wv : sw.waves(m)) {
     AllocStream guard(sw.s);
+    const auto tw = clk::now();
     Wave W(sw, wv.first, wv.second, m);
+    sw.stats[0] += 1;
+    sw.stats[2] += since(tw);
     const int count = W.count;
-    auto t0 = std::chrono::steady_clock::now();
+    const auto t0 = clk::now();
     std::vector<int2> kmh(count);
     std::vector<int> fl(count, 1);
     for (int q = 0; q < count; ++q) {
       Member& mb = sw.mem[W.a + q];
       mb.phase = first_phase;
-      mb.k = 0;
+      mb.j = 0;
       mb.done = false;
       mb.info = tm_eigs_info{};
       mb.info.ncv = m;
@@ -556,32 +594,37 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
     std::vector<double> sch((size_t)count * kScStride, 0.0), Wh((size_t)count * m * m, 0.0);
     std::vector<int2> roth(count);
     while (true) {
-      int kmin = m;
       bool ph[4] = {false, false, false, false};
+      bool any = false;
       for (int q = 0; q < count; ++q) {
         Member& mb = sw.mem[W.a + q];
         const bool on = !mb.done && mb.status == TM_OK;
-        kmh[q] = make_int2(mb.k, on ? mb.phase : kModeIdle);
+        kmh[q] = make_int2(mb.j, on ? mb.phase : kModeIdle);
         if (on) {
-          kmin = std::min(kmin, mb.k);
+          any = true;
           ph[mb.phase] = true;
         }
       }
-      if (kmin >= m) break;  // every member finished
+      if (!any) break;  // every member finished
+      const auto ts = clk::now();
       TM_CK(cudaMemcpyAsync(W.kmd.p, kmh.data(), count * sizeof(int2), cudaMemcpyHostToDevice, sw.s));
-      W.cycle(kmin, ph[kModeF32], ph[kModeDF], ph[kModeF64]);
+      W.run_step(ph[kModeF32], ph[kModeDF], ph[kModeF64]);
       TM_CK(cudaMemcpyAsync(sch.data(), W.sc.p, sch.size() * 8, cudaMemcpyDeviceToHost, sw.s));
       TM_CK(cudaStreamSynchronize(sw.s));
+      sw.stats[1] += 1;
+      sw.stats[3] += since(ts);
+      const auto th = clk::now();
       bool any_rot = false, any_start = false;
       for (int q = 0; q < count; ++q) {
         roth[q] = make_int2(0, 0);
         fl[q] = 0;
         Member& mb = sw.mem[W.a + q];
-        if (mb.done || mb.status != TM_OK) continue;
+        if (kmh[q].y == kModeIdle) continue;
+        mb.info.matvecs += 1;
+        if (mb.phase != kModeF32) mb.info.matvecs_f64 += 1;
+        if (++mb.j < m) continue;  // basis not full yet
+        // end of this member's cycle: project, test, restart
         double* Hh = sch.data() + (size_t)q * kScStride + kScH;
-        const int steps = m - mb.k;
-        mb.info.matvecs += steps;
-        if (mb.phase != kModeF32) mb.info.matvecs_f64 += steps;
         ++mb.cycles;
         try {
           const int kvec = krylov_kvec(m, nev);
@@ -638,7 +681,7 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
             fl[q] = 1;
             std::fill(Hh, Hh + (m + 1) * (m + 1), 0.0);
             mb.phase = final_phase;
-            mb.k = 0;
+            mb.j = 0;
             mb.cycles = 0;
             any_start = true;
           } else {
@@ -650,7 +693,7 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
             krylov_restart_h(Hh, m, Wm, knew, R.beta, Hn);
             std::copy(Hn.begin(), Hn.end(), Hh);
             roth[q] = make_int2(knew, 1);
-            mb.k = knew;
+            mb.j = knew;
             ++mb.info.restarts;
           }
           any_rot = true;
@@ -668,9 +711,10 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
         TM_CKK("sw_rotate");
         if (any_start) W.normalize_starts(fl);
       }
+      sw.stats[4] += since(th);
     }
     TM_CK(cudaStreamSynchronize(sw.s));
-    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const double secs = since(t0);
     for (int q = 0; q < count; ++q) sw.mem[W.a + q].info.seconds = secs;
   }
 }
@@ -689,13 +733,13 @@ void sweep_product(Sweep& sw, const double* const* x, double* const* y, tm_dtype
     sw_copy_in<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count,
                                                     W.yptr.as<const double* const>());
     TM_CKK("sw_copy_in");
-    W.product(mode, 0);
+    W.product(mode);
     TM_CK(cudaStreamSynchronize(sw.s));  // the pointer table is rewritten below
     TM_CK(cudaMemcpyAsync(W.yptr.p, y + W.a, count * sizeof(void*), cudaMemcpyHostToDevice, sw.s));
     sw_copy_out<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count, W.yptr.as<double* const>());
     TM_CKK("sw_copy_out");
     TM_CK(cudaStreamSynchronize(sw.s));
-    for (auto& mb : sw.mem) mb.op->matvecs++;
+    for (int q = 0; q < count; ++q) sw.mem[W.a + q].op->matvecs++;
   }
 }
 
@@ -781,6 +825,13 @@ tm_status tm_sweep_set_wave_bytes(tm_sweep* sw, size_t bytes) {
   if (!sw) fail(TM_ERR_ARG, "null sweep");
   sw->impl->budget_override = bytes;
   SW_END
+}
+
+int tm_sweep_stats(const tm_sweep* sw, double* out, int cap) {
+  if (!sw || !out) return 0;
+  int n = 0;
+  for (; n < cap && n < 5; ++n) out[n] = sw->impl->stats[n];
+  return n;
 }
 
 tm_status tm_sweep_perform_op_dev(tm_sweep* sw, const double* const* x_dev, double* const* y_dev, tm_dtype dtype) {

@@ -35,6 +35,16 @@ for f in utility tmat tmatreduce tmat3d tmatphys; do
 done
 "$CXX" "${FLAGS[@]}" -c "$HERE/refshim/ref_shim.cpp" -o "$OUT/ref_shim.o" &
 PIDS+=($!)
+# configuration planting (DumpConfig), for its golden fixtures
+DSRC="$REF/DumpConfig"
+for f in dumpconfig dumpreduce utilityb; do
+  "$CXX" "${FLAGS[@]}" -I"$DSRC" -c "$DSRC/$f.cpp" -o "$OUT/dump_$f.o" &
+  PIDS+=($!)
+  OBJS+=("$OUT/dump_$f.o")
+done
+"$CXX" "${FLAGS[@]}" -I"$DSRC" -c "$HERE/refshim/dump_shim.cpp" -o "$OUT/dump_shim.o" &
+PIDS+=($!)
+OBJS+=("$OUT/dump_shim.o")
 for p in "${PIDS[@]}"; do wait "$p"; done
 "$CXX" -shared -fopenmp -o "$OUT/libtmat_ref.so" "${OBJS[@]}" "$OUT/ref_shim.o"
 echo "built $OUT/libtmat_ref.so"

@@ -41,8 +41,30 @@ def lib():
         L.ref_orbit.argtypes = [P, P, P, ctypes.c_int64]
         L.ref_moments.argtypes = [P, P, P, P]
         L.ref_phys_extend.argtypes = [P, P, P, P, ctypes.c_int]
+        L.ref_dump.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_char_p]
         _lib = L
     return _lib
+
+
+def ref_dump(model, axialdir, extend_cond, betaJ, kappa, kappa2, h, size, vecfile, veclfile, nconfig, length,
+             seed, prefix):
+    """Run the reference's DumpConfig dump() (fixed seed); returns its status."""
+    return lib().ref_dump(model.encode(), int(axialdir), int(extend_cond), float(betaJ), float(kappa),
+                          float(kappa2), float(h), int(size), vecfile.encode(), (veclfile or "").encode(),
+                          int(nconfig), int(length), int(seed), prefix.encode())
+
+
+def read_configs(prefix, nconfig, L):
+    """Layer states of <prefix>_config_<k>.dat files (L digits per line, site 0 first)."""
+    out = []
+    for k in range(nconfig):
+        rows = []
+        for line in open(f"{prefix}_config_{k}.dat").read().split():
+            rows.append(sum(1 << i for i, ch in enumerate(line[:L]) if ch == "1"))
+        out.append(rows)
+    return np.array(out, dtype=np.uint64)
 
 
 class RefOp:

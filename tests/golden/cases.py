@@ -101,6 +101,18 @@ LARGE_CASES = [
     ("xam_L32_cfg2", "A", 2, 5, 2, 0.3, 0.6, 0.0, 0.0, 32, 4),
 ]
 
+# Configuration planting (the reference's DumpConfig) from the leading
+# eigenvector: (name, model, axialdir, extend_cond, betaJ, kappa, kappa2, h,
+# size, nconfig, length, seed).  Fixtures hold the eigenvector used and the
+# layer states the reference's own dump() planted with that seed.
+DUMP_CASES = [
+    ("dump_xat_L10", "A", 1, 0, 0.4, 0.3, 0.0, 0.05, 10, 4, 64, 12345),
+    ("dump_xat_L12", "A", 1, 0, 0.6, 0.5, 0.0, 0.0, 12, 3, 40, 7),
+    ("dump_xam_L12", "A", 5, 2, 0.35, 0.5, 0.0, 0.0, 12, 4, 64, 777),
+    ("dump_xam_L14_flip", "A", 5, 0, 0.45, 0.4, 0.0, 0.0, 14, 3, 48, 99),
+    ("dump_xam_L16_h", "A", 5, 0, 0.3, 0.6, 0.0, 0.05, 16, 2, 40, 2024),
+]
+
 FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums and samples
 SAMPLE_COUNT = 4096
 

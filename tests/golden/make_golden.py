@@ -18,7 +18,9 @@ or with --large; their eigenvalues use the reference solver's Krylov size
 products each ARPACK solve took is stored beside them.  At L = 32 a product
 takes about two minutes on 8 cores and the eigenvalues about an hour and a half.
 
-Usage: python tests/golden/make_golden.py [--large] [names...]   (needs oracle/_ref built)
+The DUMP_CASES (configuration planting) run when named or with --dump.
+
+Usage: python tests/golden/make_golden.py [--large] [--dump] [names...]   (needs oracle/_ref built)
 """
 from __future__ import annotations
 
@@ -36,9 +38,9 @@ sys.path.insert(0, HERE)
 
 import time  # noqa: E402
 
-from cases import (CASES, FULL_VECTOR_MAX, LARGE_CASES, case_dict, checksum_weights, general,  # noqa: E402
-                   sample_indices, seeded_input)
-from oracle.refbind import RefOp, available  # noqa: E402
+from cases import (CASES, DUMP_CASES, FULL_VECTOR_MAX, LARGE_CASES, case_dict, checksum_weights,  # noqa: E402
+                   general, sample_indices, seeded_input)
+from oracle.refbind import RefOp, available, read_configs, ref_dump  # noqa: E402
 
 
 def sha(a: np.ndarray) -> str:
@@ -162,11 +164,44 @@ def gen(c, large=False):
     return d["name"], out
 
 
+def gen_dump(c):
+    """Leading eigenvector of the reference operator (ARPACK on its product),
+    written as the reference's X_vec.dat, and the configurations the
+    reference's dump() plants from it with the case's seed."""
+    import tempfile
+
+    name, model, ax, ec, bj, k, k2, h, size, nconf, length, seed = c
+    op = RefOp(model, 2, ax, bj, k, h, size, k2, ec)
+    n = op.n
+    lin = sla.LinearOperator((n, n), matvec=lambda v: op.perform_op(np.ravel(v)), dtype=np.float64)
+    v0 = np.random.default_rng(0).uniform(0, 1, n)
+    vals, vecs = sla.eigsh(lin, k=2, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, 20))
+    q = np.real(vecs[:, int(np.argmax(np.abs(vals)))])
+    q = q / np.linalg.norm(q)
+    q = q * np.sign(q.sum())
+    with tempfile.TemporaryDirectory() as td:
+        vf = os.path.join(td, "RUN_vec.dat")
+        q.astype(np.float64).tofile(vf)
+        st = ref_dump(model, ax, ec, bj, k, k2, h, size, vf, None, nconf, length, seed, os.path.join(td, "RUN"))
+        if st != 0:
+            raise RuntimeError(f"reference dump failed ({st})")
+        configs = read_configs(os.path.join(td, "RUN"), nconf, size)
+    out = dict(vec=q, configs=configs, n=np.int64(n))
+    log(f"{name}: n={n} configs {configs.shape}")
+    return name, out
+
+
 def main(args):
     if not available():
         raise SystemExit("oracle/_ref/libtmat_ref.so missing: run oracle/build_ref.sh first")
     large = "--large" in args
     names = [a for a in args if not a.startswith("--")]
+    for c in DUMP_CASES:
+        if (names and c[0] in names) or (not names and "--dump" in args):
+            name, out = gen_dump(c)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    if "--dump" in args and not names:
+        return
     for c in CASES + LARGE_CASES:
         is_large = c in LARGE_CASES
         if names and c[0] not in names:

@@ -71,3 +71,18 @@ def test_published_probe_values():
     np.testing.assert_allclose(nf, [84970.93472621, 45042.94793585], rtol=1e-11)
     fl = oracle.OracleOp("A", 2, 5, 0.5, 0.5, 0.0, 12, 0.0, 0).eigs(2)
     np.testing.assert_allclose(fl, [84970.93472621, 36870.69770993], rtol=1e-11)
+
+
+def test_dump_fixtures_are_well_formed():
+    """The planted-configuration fixtures (made by the reference's own dump())
+    hold one unit eigenvector of the operator's size and nconfig x length
+    layer states of L bits each."""
+    from cases import DUMP_CASES
+
+    for name, model, ax, ec, bj, k, k2, h, size, nconf, length, seed in DUMP_CASES:
+        f = fixture(name)
+        o = _op(dict(model=model, dim=2, axialdir=ax, betaJ=bj, kappa=k, h=h, size=size, kappa2=k2,
+                     extend_cond=ec))
+        assert f["vec"].shape == (o.n,) and abs(np.linalg.norm(f["vec"]) - 1.0) < 1e-12
+        assert f["configs"].shape == (nconf, length)
+        assert int(f["configs"].max()) < (1 << size)
