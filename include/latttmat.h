@@ -223,12 +223,35 @@ tm_status tm_sweep_perform_op_dev(tm_sweep* sweep, const double* const* x_dev, d
                                   tm_dtype dtype);
 
 /* Largest-magnitude eigenvalues of every member (Arnoldi; ncv 0 = the
- * reference's suggested_nev rule; start vector uniform(0,1), seed 0).
+ * reference's suggested_nev rule with at least 12 columns; start vector
+ * uniform(0,1), seed 0).
  * vals_re/vals_im: host, count*nev, eigenvalues / normfactor in descending
  * magnitude; infos, status: host arrays of count or NULL.  Returns TM_OK or
  * the first failing member's code. */
 tm_status tm_sweep_eigs(tm_sweep* sweep, int nev, int ncv, double tol, int mode, double* vals_re,
                         double* vals_im, tm_eigs_info* infos, tm_status* status);
+
+/* As tm_sweep_eigs, and each member's leading eigenvector (real, unit norm)
+ * into vec0_host[i] (host, tm_sweep_rows(i) doubles; NULL entries skip a
+ * member), taken from the member's converged Ritz vector on the device. */
+tm_status tm_sweep_eigs_vec(tm_sweep* sweep, int nev, int ncv, double tol, int mode, double* vals_re,
+                            double* vals_im, double* const* vec0_host, tm_eigs_info* infos, tm_status* status);
+
+/* transpose 1: the sweep's solves and products use the members' transposes
+ * T^T (their eigenvectors are the left eigenvectors of T, as the reference's
+ * getlefteigvec takes them from get_t_instance, TMat/pfunc.hpp:47-68). */
+tm_status tm_sweep_set_transpose(tm_sweep* sweep, int transpose);
+
+/* Batched adjoint (no reference counterpart): grad4[4 i + t] = d ln(lambda_i)
+ * / d(betaJ, kappa, kappa2, h)_t of every member's reported eigenvalue, from
+ * its right and left eigenvectors (host arrays of device-independent host
+ * pointers, tm_sweep_rows(i) doubles each; ql_host NULL for symmetric
+ * operators) and its internal eigenvalue (reported eigenvalue times
+ * normfactor).  The Boltzmann-weight term is one batched reduction over all
+ * members; the chain term is one batched tangent product per parameter (one
+ * launch per pass over every member), as tm_grad computes for one operator. */
+tm_status tm_sweep_grad(tm_sweep* sweep, const double* const* qr_host, const double* const* ql_host,
+                        const double* lambda_internal, double* grad4);
 
 /* Autotuner of the aux-bit chain kernels (no reference counterpart): times
  * the operator's product (TM_F32 or TM_F64_DF) over 2^11..2^14-element tiles
@@ -278,6 +301,9 @@ tm_status tm_phys_extend(const tm_op* op, const double* ql_host, const double* q
 
 /* d ln(lambda)/d(betaJ, kappa, kappa2, h) of the eigenvalue whose right
  * eigenvector is qr (and left eigenvector ql, NULL for symmetric operators),
+ * for the x-ANNNI (model A, 2D and 3D), DNNI (model D) and diagonal BNNNI
+ * (model B, axialdir 3 and 7) operators; the two-layer operators return
+ * TM_ERR_UNSUPPORTED.
  * host FP64 vectors of length rows.  lambda_internal is the operator's own
  * eigenvalue (reported eigenvalue times normfactor).  The result includes the
  * -d ln(normfactor) term, so it is the derivative of the reported eigenvalue. */

@@ -45,7 +45,8 @@ EXPORTED_SYMBOLS = (
     "tm_orbit_table", "tm_eigs", "tm_moments", "tm_phys_extend", "tm_grad", "tm_last_error", "tm_version",
     "tm_profile_matvec", "tm_launch_count", "tm_alloc_count", "tm_perform_op_dev_noalloc", "tm_eigs_batch",
     "tm_debug_set_eo_tile_bits", "tm_sweep_create", "tm_sweep_destroy", "tm_sweep_count", "tm_sweep_rows",
-    "tm_sweep_normfactor", "tm_sweep_set_wave_bytes", "tm_sweep_stats", "tm_sweep_perform_op_dev", "tm_sweep_eigs",
+    "tm_sweep_normfactor", "tm_sweep_set_wave_bytes", "tm_sweep_stats", "tm_sweep_eigs_vec",
+    "tm_sweep_set_transpose", "tm_sweep_grad", "tm_sweep_perform_op_dev", "tm_sweep_eigs",
     "tm_chain_autotune", "tm_chain_set_tuning", "tm_dump_configs",
 )
 
@@ -121,6 +122,11 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.tm_sweep_normfactor.restype = ctypes.c_double
     lib.tm_sweep_set_wave_bytes.argtypes = [P, ctypes.c_size_t]
     lib.tm_sweep_stats.argtypes = [P, P, ctypes.c_int]
+    lib.tm_sweep_eigs_vec.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, P, P, P, P, P]
+    lib.tm_sweep_set_transpose.argtypes = [P, ctypes.c_int]
+    lib.tm_sweep_grad.argtypes = [P, P, P, P, P]
+    for f in ("tm_sweep_eigs_vec", "tm_sweep_set_transpose", "tm_sweep_grad"):
+        getattr(lib, f).restype = ctypes.c_int
     lib.tm_sweep_perform_op_dev.argtypes = [P, P, P, ctypes.c_int]
     lib.tm_sweep_eigs.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, P, P, P, P]
     lib.tm_chain_autotune.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
@@ -212,20 +218,51 @@ class Sweep:
         _check(self._lib.tm_sweep_perform_op_dev(self._h, ctypes.cast(xa, ctypes.c_void_p),
                                                  ctypes.cast(ya, ctypes.c_void_p), int(dtype)))
 
-    def eigs(self, nev: int = 2, tol: float = 1e-10, mode: int = TM_EIGS_MIXED, ncv: int = 0):
-        """(vals complex [count, nev] / normfactor, info dicts, status codes)."""
+    def eigs(self, nev: int = 2, tol: float = 1e-10, mode: int = TM_EIGS_MIXED, ncv: int = 0,
+             vectors: bool = False):
+        """(vals complex [count, nev] / normfactor, info dicts, status codes),
+        and with vectors=True a fourth item: each member's leading eigenvector."""
         n = self.count()
         vr = np.zeros(n * nev)
         vi = np.zeros(n * nev)
         infos = (tm_eigs_info * n)()
         st = np.zeros(n, dtype=np.int32)
-        code = self._lib.tm_sweep_eigs(self._h, int(nev), int(ncv), float(tol), int(mode), _ptr(vr), _ptr(vi),
-                                       ctypes.byref(infos), _ptr(st))
+        if vectors:
+            vecs = [np.zeros(self.rows(i)) for i in range(n)]
+            ptrs = (ctypes.c_void_p * n)(*[ctypes.c_void_p(v.ctypes.data) for v in vecs])
+            code = self._lib.tm_sweep_eigs_vec(self._h, int(nev), int(ncv), float(tol), int(mode), _ptr(vr),
+                                               _ptr(vi), ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(infos),
+                                               _ptr(st))
+        else:
+            code = self._lib.tm_sweep_eigs(self._h, int(nev), int(ncv), float(tol), int(mode), _ptr(vr), _ptr(vi),
+                                           ctypes.byref(infos), _ptr(st))
         if code != TM_OK and not np.any(st == TM_OK):
             _check(code)
         vals = (vr + 1j * vi).reshape(n, nev)
         info = [{k: getattr(infos[i], k) for k, _ in tm_eigs_info._fields_} for i in range(n)]
+        if vectors:
+            return vals, info, st.copy(), vecs
         return vals, info, st.copy()
+
+    def set_transpose(self, transpose: bool = True) -> None:
+        """Solve the members' transposes (left eigenvectors)."""
+        _check(self._lib.tm_sweep_set_transpose(self._h, int(bool(transpose))))
+
+    def grad(self, qr, ql, lambda_internal) -> np.ndarray:
+        """Batched adjoint: d ln(lambda_i)/d(betaJ, kappa, kappa2, h), shape (count, 4)."""
+        n = self.count()
+        qr = [np.ascontiguousarray(v, dtype=np.float64) for v in qr]
+        pr = (ctypes.c_void_p * n)(*[ctypes.c_void_p(v.ctypes.data) for v in qr])
+        pl = None
+        if ql is not None:
+            ql = [np.ascontiguousarray(v, dtype=np.float64) for v in ql]
+            pl = (ctypes.c_void_p * n)(*[ctypes.c_void_p(v.ctypes.data) for v in ql])
+        lam = np.ascontiguousarray(lambda_internal, dtype=np.float64)
+        g = np.zeros(n * 4)
+        _check(self._lib.tm_sweep_grad(self._h, ctypes.cast(pr, ctypes.c_void_p),
+                                       ctypes.cast(pl, ctypes.c_void_p) if pl is not None else None, _ptr(lam),
+                                       _ptr(g)))
+        return g.reshape(n, 4)
 
     def close(self):
         if getattr(self, "_h", None):

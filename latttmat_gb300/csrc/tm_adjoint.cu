@@ -18,6 +18,7 @@
 #include <cmath>
 #include <vector>
 
+#include "tm_chain.h"
 #include "tm_group.cuh"
 #include "tm_internal.h"
 
@@ -82,6 +83,8 @@ __device__ void gvec(const GradParams& p, uint64_t s, double g[4]) {
     g[0] = -0.5 * (2 * n1 - L) + 0.5 * p.k * (2 * n2 - L) - 0.5 * p.h * (2 * n0 - L);
     g[1] = 0.5 * p.bj * (2 * n2 - L);
     g[3] = -0.5 * p.bj * (2 * n0 - L);
+  } else if (p.kind == K_ZBT || p.kind == K_ZBM || p.kind == K_XDT || p.kind == K_XDM) {
+    aux_tvec_grad(p.kind, L, p.boundary, p.bj, p.k2, p.h, s, g);
   } else if (p.kind == K_XAM3) {
     int n1a = popc64(s ^ rshift3d(s, p.s1, p.s2, 1));
     int n1b = popc64(s ^ dshift3d(s, p.s1, p.s2, 1));
@@ -206,12 +209,42 @@ int nblocks(int64_t n) {
 
 void ensure_state_map(Op& op);
 
-void adjoint_grad(const Op& op, const double* qr_h, const double* ql_h, double lam, double grad[4]) {
-  if (op.kind != K_XAT && op.kind != K_XAM && op.kind != K_XAM3)
-    fail(TM_ERR_UNSUPPORTED, "adjoint provided for the Kronecker-core (model A) operators");
+void matvec_aux_tangent(const Op& op, const double* x, double* y, const AuxCoef& db, int dir, cudaStream_t s);
+
+// Aux-bit operators (DNNI, diagonal BNNNI): T = D_out C D_in with the
+// diagonal Boltzmann weights D (Tvec, times dup in the reduced output) and
+// the chain C of local step gates built from b1 = e^{+-bJ}, b2 = e^{-+bJ k},
+// b3 = e^{-+bJ k2}.  d ln(lambda) = 2 <g>_{lr} + <l, D_out (dC) D_in r> /
+// (lambda <l, r>); the second term is a tangent product of the chain
+// (matvec_aux_tangent) per parameter the gates depend on.
+static void adjoint_grad_aux(const Op& op, const double* dqr, const double* qlp, double lam, double wsum,
+                             double grad[4]) {
   cudaStream_t s = op.stream;
   const int64_t n = op.n;
-  const bool reduced = (op.kind != K_XAT);
+  const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
+  DBuf y;
+  y.alloc((size_t)n * 8);
+  std::vector<double> yh(n), lh(n);
+  TM_CK(cudaMemcpyAsync(lh.data(), qlp ? qlp : dqr, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+  for (int t = 0; t < 3; ++t) {
+    if (t == 2 && !zb) break;  // DNNI gates do not depend on kappa2
+    const AuxCoef db = aux_coef_derivative(op.mp.betaJ, op.mp.kappa, op.mp.kappa2, t);
+    matvec_aux_tangent(op, dqr, y.as<double>(), db, 0, s);
+    TM_CK(cudaMemcpyAsync(yh.data(), y.p, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+    double quad = 0.0;
+    for (int64_t i = 0; i < n; ++i) quad += lh[i] * yh[i];
+    grad[t] += quad / (lam * wsum);
+  }
+}
+
+void adjoint_grad(const Op& op, const double* qr_h, const double* ql_h, double lam, double grad[4]) {
+  const bool aux = (op.kind == K_ZBT || op.kind == K_ZBM || op.kind == K_XDT || op.kind == K_XDM);
+  if (op.kind != K_XAT && op.kind != K_XAM && op.kind != K_XAM3 && !aux)
+    fail(TM_ERR_UNSUPPORTED, "adjoint provided for the x-ANNNI, DNNI and diagonal BNNNI operators");
+  cudaStream_t s = op.stream;
+  const int64_t n = op.n;
+  const bool reduced = (op.kind == K_XAM || op.kind == K_XAM3 || op.kind == K_ZBM || op.kind == K_XDM);
   DBuf dqr, dql, part;
   dqr.alloc((size_t)n * 8);
   TM_CK(cudaMemcpyAsync(dqr.p, qr_h, (size_t)n * 8, cudaMemcpyHostToDevice, s));
@@ -235,6 +268,10 @@ void adjoint_grad(const Op& op, const double* qr_h, const double* ql_h, double l
     for (int k = 0; k < 5; ++k) sums[k] += hp[(size_t)b * 5 + k];
   const double wsum = sums[4];
   for (int k = 0; k < 4; ++k) grad[k] = 2.0 * sums[k] / wsum;
+  if (aux) {
+    adjoint_grad_aux(op, dqr.as<double>(), qlp, lam, wsum, grad);
+    return;
+  }
 
   // tangent term for betaJ through the full space
   if (reduced) ensure_state_map(const_cast<Op&>(op));

@@ -47,6 +47,13 @@ __device__ __forceinline__ int spad(int e) { return e + (e >> 5); }
 
 __device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp);
 
+// the part of a tile value the fold sums: the value, or for a tangent pair
+// its derivative (the tangent product's output)
+__device__ __forceinline__ double fold_part(float x) { return (double)x; }
+__device__ __forceinline__ double fold_part(double x) { return x; }
+__device__ __forceinline__ double fold_part(dfloat x) { return (double)x; }
+__device__ __forceinline__ double fold_part(tangent x) { return x.d; }
+
 // byte offset of the fold accumulators in chain_kernel's shared memory
 __host__ __device__ __forceinline__ size_t chain_acc_offset(int tile, size_t elem) {
   return (((size_t)(tile + tile / 32 + 1) * elem) + 15) & ~(size_t)15;
@@ -289,7 +296,7 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
       for (int e = threadIdx.x; e < (tile >> NA); e += blockDim.x) {
         double a = acc[e];
 #pragma unroll
-        for (int aux = 0; aux < (1 << NA); ++aux) a += (double)sm[spad((e << NA) | aux)];
+        for (int aux = 0; aux < (1 << NA); ++aux) a += fold_part(sm[spad((e << NA) | aux)]);
         acc[e] = a;
       }
     } else if (vec_io) {
@@ -322,7 +329,7 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
 }
 
 template <class T, int ZB, class IO>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3)) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : (sizeof(T) == 8 ? 3 : 2))) chain_kernel(T* __restrict__ P, const IO* __restrict__ x,
                                                     const double* __restrict__ pre, const uint32_t* __restrict__ smap,
                                                     IO* __restrict__ y, const double* __restrict__ post, double postc,
                                                     int L, int bc, int dir, AuxCoefT<T> c, ChainPass cp) {
@@ -348,19 +355,20 @@ __device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp) {
 // kBatchTiles consecutive tiles of that member's geometry (copied to shared
 // memory).  km[i] = (Krylov column the member extends, product mode).
 template <class T, int ZB, class IO, int MODE>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3))
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : (sizeof(T) == 8 ? 3 : 2)))
     chain_batch_kernel(const ChainInst* __restrict__ inst, const int2* __restrict__ km, const int64_t* __restrict__ start,
-                       const int* __restrict__ bmem, int pass) {
+                       const int* __restrict__ bmem, int pass, int theta) {
   __shared__ ChainPass cps;
   const int s_i = bmem[blockIdx.x];  // the member of this block
   const ChainInst& I = inst[s_i];
   const int64_t blk = (int64_t)blockIdx.x - start[s_i];
-  const int np = (sizeof(T) == 4) ? I.np4 : I.np8;
+  const int np = (sizeof(T) == 4) ? I.np4 : (sizeof(T) == 8 ? I.np8 : I.np16);
   const int2 kmi = km[s_i];
   if (kmi.y != MODE || pass >= np) return;  // uniform over the block
   const int j = kmi.x;
   {
-    const int* src = reinterpret_cast<const int*>((sizeof(T) == 4) ? &I.p4[pass] : &I.p8[pass]);
+    const int* src = reinterpret_cast<const int*>((sizeof(T) == 4) ? &I.p4[pass]
+                                                  : (sizeof(T) == 8 ? &I.p8[pass] : &I.p16[pass]));
     int* dst = reinterpret_cast<int*>(&cps);
     for (int q = threadIdx.x; q < (int)(sizeof(ChainPass) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
   }
@@ -373,6 +381,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 3))
     c = reinterpret_cast<const AuxCoefT<T>*>(&I.c32);
   else if constexpr (MODE == kModeDF)
     c = reinterpret_cast<const AuxCoefT<T>*>(&I.cdf);
+  else if constexpr (MODE == kModeTangent)
+    c = reinterpret_cast<const AuxCoefT<T>*>(&I.ctan[theta]);
   else
     c = reinterpret_cast<const AuxCoefT<T>*>(&I.c64);
   for (int q = 0; q < kBatchTiles; ++q) {
@@ -397,7 +407,7 @@ __global__ void __launch_bounds__(256) contract_batch_kernel(const ChainInst* __
   if (kmi.y != MODE) return;
   const int64_t r0 = ((int64_t)blockIdx.x - rstart[s_i]) * kSweepRows;
   const int64_t r1 = min(r0 + (int64_t)kSweepRows, I.n);
-  const double gs = (MODE == kModeF32) ? I.gs32 : (MODE == kModeDF ? I.gsdf : I.gs64);
+  const double gs = (MODE == kModeF32) ? I.gs32 : (MODE == kModeDF ? I.gsdf : (MODE == kModeF64 ? I.gs64 : 1.0));
   const IO* z = reinterpret_cast<const IO*>(I.fold);
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const double f = I.idx ? (double)z[I.idx[r]] * (double)I.dup[r] : (double)z[r] * I.nf;
@@ -521,6 +531,11 @@ constexpr TunedEntry kTunedBNNNI[] = {
 };
 
 void chain_tuning(int L, size_t elem, bool zb, int& tile_bits, int& threads) {
+  if (elem >= 16) {  // tangent pairs (adjoint): 32 KB tiles, fewer threads
+    tile_bits = 11;
+    threads = 128;
+    return;
+  }
   tile_bits = (elem == 8) ? 12 : 13;
   threads = 256;
   if (L < 0 || L > 32) return;
@@ -598,8 +613,17 @@ size_t chain_pass_smem(const ChainPass& cp, bool zb, size_t elem) {
 // returned factor.
 // T: arithmetic and pass-buffer type (float, double, or dfloat: FP64-accurate
 // products on the FP32 pipes); IO: element type of x and y.
+template <class T>
+T coef_with_derivative(double v, double d) {
+  if constexpr (std::is_same<T, tangent>::value)
+    return tangent(v, d);
+  else
+    return (T)v;
+}
+
 template <class T, class IO = T>
-double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cudaStream_t s) {
+double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cudaStream_t s,
+                      const AuxCoef* dcoef = nullptr, void* pass_buf = nullptr) {
   const int L = op.L;
   const bool reduced = (op.kind == K_XDM || op.kind == K_ZBM);
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
@@ -609,9 +633,9 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
   const bool norm = (sizeof(T) == 4) || std::is_same<T, dfloat>::value;
   AuxCoefT<T> c;
   for (int k = 0; k < 2; ++k) {
-    c.b1[k] = (T)c64.b1[k];
-    c.b2[k] = (T)c64.b2[k];
-    c.b3[k] = (T)c64.b3[k];
+    c.b1[k] = coef_with_derivative<T>(c64.b1[k], dcoef ? dcoef->b1[k] : 0.0);
+    c.b2[k] = coef_with_derivative<T>(c64.b2[k], dcoef ? dcoef->b2[k] : 0.0);
+    c.b3[k] = coef_with_derivative<T>(c64.b3[k], dcoef ? dcoef->b3[k] : 0.0);
   }
   c.g = norm ? (T)(1.0 / gb) : (T)1;
   const int nsteps = zb ? L / 2 : L;
@@ -621,7 +645,7 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
   const int nlb = zb ? 4 : (bc == 0 ? 2 : 1);
   int tile_bits = 0, threads = 0;
   chain_tuning(L, sizeof(T), zb, tile_bits, threads);
-  T* P = op.ws_a.as<T>();
+  T* P = pass_buf ? static_cast<T*>(pass_buf) : op.ws_a.as<T>();
   const uint32_t* smap = reduced ? op.smap.as<uint32_t>() : nullptr;
   IO* fold_out = reduced ? op.xp.as<IO>() : y;
   const double postc = zb ? sf : (reduced ? sf : op.normfactor * sf);
@@ -683,6 +707,26 @@ void chain_inst_fill(const Op& op, int dir, ChainInst& rec, int tb4, int tb8) {
   int th = 0;
   if (tb4 <= 0) chain_tuning(L, 4, zb, tb4, th);
   if (tb8 <= 0) chain_tuning(L, 8, zb, tb8, th);
+  int tb16 = 0;
+  chain_tuning(L, 16, zb, tb16, th);
+  const std::vector<ChainPass> p16 = chain_plan(L, zb, rec.nlb, tb16);
+  if ((int)p16.size() > kChainMaxPass) fail(TM_ERR_LIMIT, "too many chain passes");
+  rec.np16 = (int)p16.size();
+  for (int q = 0; q < rec.np16; ++q) rec.p16[q] = p16[q];
+  for (int t = 0; t < 3; ++t) {
+    const AuxCoef db = aux_coef_derivative(op.mp.betaJ, op.mp.kappa, op.mp.kappa2, t);
+    for (int q = 0; q < 2; ++q) {
+      rec.ctan[t].b1[q] = tangent(c.b1[q], db.b1[q]);
+      rec.ctan[t].b2[q] = tangent(c.b2[q], db.b2[q]);
+      rec.ctan[t].b3[q] = tangent(c.b3[q], db.b3[q]);
+    }
+    rec.ctan[t].g = tangent(1.0);
+  }
+  rec.kind = op.kind;
+  rec.bj = op.mp.betaJ;
+  rec.kap = op.mp.kappa;
+  rec.kap2 = op.mp.kappa2;
+  rec.h = op.mp.h;
   const std::vector<ChainPass> p4 = chain_plan(L, zb, rec.nlb, tb4), p8 = chain_plan(L, zb, rec.nlb, tb8);
   if ((int)p4.size() > kChainMaxPass || (int)p8.size() > kChainMaxPass) fail(TM_ERR_LIMIT, "too many chain passes");
   rec.np4 = (int)p4.size();
@@ -698,25 +742,27 @@ void chain_inst_fill(const Op& op, int dir, ChainInst& rec, int tb4, int tb8) {
 namespace {
 template <class T, int ZB, class IO, int MODE>
 void launch_batch_pass(const ChainInst* inst, const int2* km, const int64_t* start, const int* bmem, int pass,
-                       int64_t nblk, int threads, size_t smem, cudaStream_t s) {
+                       int64_t nblk, int threads, size_t smem, cudaStream_t s, int theta) {
   raise_smem_limit((const void*)chain_batch_kernel<T, ZB, IO, MODE>, smem);
-  chain_batch_kernel<T, ZB, IO, MODE><<<(unsigned)nblk, threads, smem, s>>>(inst, km, start, bmem, pass);
+  chain_batch_kernel<T, ZB, IO, MODE><<<(unsigned)nblk, threads, smem, s>>>(inst, km, start, bmem, pass, theta);
   TM_CKK("chain_batch");
 }
 
 template <int ZB, int MODE>
-int batch_product_mode(const ChainBatch& B, const int2* km, const ChainBatch::Plan& P, cudaStream_t s) {
+int batch_product_mode(const ChainBatch& B, const int2* km, const ChainBatch::Plan& P, cudaStream_t s, int theta) {
   int launches = 0;
   for (int p = 0; p < P.np; ++p) {
     if (P.nblk[p] == 0) continue;
     const int64_t* st = P.start + (size_t)p * (B.count + 1);
     const int* bm = P.bmem + P.boff[p];
     if constexpr (MODE == kModeF32)
-      launch_batch_pass<float, ZB, float, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s);
+      launch_batch_pass<float, ZB, float, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s, theta);
     else if constexpr (MODE == kModeDF)
-      launch_batch_pass<dfloat, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s);
+      launch_batch_pass<dfloat, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s, theta);
+    else if constexpr (MODE == kModeTangent)
+      launch_batch_pass<tangent, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s, theta);
     else
-      launch_batch_pass<double, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s);
+      launch_batch_pass<double, ZB, double, MODE>(B.inst, km, st, bm, p, P.nblk[p], P.threads, P.smem, s, theta);
     ++launches;
   }
   if constexpr (MODE == kModeF32)
@@ -728,15 +774,17 @@ int batch_product_mode(const ChainBatch& B, const int2* km, const ChainBatch::Pl
 }
 }  // namespace
 
-int chain_batch_product(const ChainBatch& B, const int2* km, int mode, cudaStream_t s) {
+int chain_batch_product(const ChainBatch& B, const int2* km, int mode, cudaStream_t s, int theta) {
   if (B.zb) {
-    if (mode == kModeF32) return batch_product_mode<1, kModeF32>(B, km, B.p4, s);
-    if (mode == kModeDF) return batch_product_mode<1, kModeDF>(B, km, B.p8, s);
-    return batch_product_mode<1, kModeF64>(B, km, B.p8, s);
+    if (mode == kModeF32) return batch_product_mode<1, kModeF32>(B, km, B.p4, s, theta);
+    if (mode == kModeDF) return batch_product_mode<1, kModeDF>(B, km, B.p8, s, theta);
+    if (mode == kModeTangent) return batch_product_mode<1, kModeTangent>(B, km, B.p16, s, theta);
+    return batch_product_mode<1, kModeF64>(B, km, B.p8, s, theta);
   }
-  if (mode == kModeF32) return batch_product_mode<0, kModeF32>(B, km, B.p4, s);
-  if (mode == kModeDF) return batch_product_mode<0, kModeDF>(B, km, B.p8, s);
-  return batch_product_mode<0, kModeF64>(B, km, B.p8, s);
+  if (mode == kModeF32) return batch_product_mode<0, kModeF32>(B, km, B.p4, s, theta);
+  if (mode == kModeDF) return batch_product_mode<0, kModeDF>(B, km, B.p8, s, theta);
+  if (mode == kModeTangent) return batch_product_mode<0, kModeTangent>(B, km, B.p16, s, theta);
+  return batch_product_mode<0, kModeF64>(B, km, B.p8, s, theta);
 }
 
 // ------------------------------------------------------------------ autotuner
@@ -815,6 +863,19 @@ double matvec_aux(const Op& op, const T* x, T* y, bool scaled, cudaStream_t s) {
 
 template double matvec_aux<float>(const Op&, const float*, float*, bool, cudaStream_t);
 template double matvec_aux<double>(const Op&, const double*, double*, bool, cudaStream_t);
+
+// Tangent product of the adjoint: y = D_out (dC/dtheta) D_in x, the chain
+// steps differentiated with respect to one parameter whose effect on the step
+// factors b1, b2, b3 is `db` (the Boltzmann weights Tvec held fixed), FP64.
+void matvec_aux_tangent(const Op& op, const double* x, double* y, const AuxCoef& db, int dir, cudaStream_t s) {
+  // the pass buffer at 16 bytes per element (the operator's holds 8)
+  const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
+  const int64_t per = (zb ? 16ll : 4ll) << op.L;
+  AllocStream guard(s);
+  DBuf P;
+  P.alloc((size_t)per * sizeof(tangent));
+  matvec_aux_dir<tangent, double>(op, x, y, false, dir, s, &db, P.p);
+}
 
 // FP64-accurate product in double-float arithmetic (the solver's refinement
 // products for the aux-bit operators)

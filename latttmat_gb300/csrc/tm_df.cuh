@@ -86,4 +86,27 @@ __device__ __forceinline__ dfloat& operator*=(dfloat& a, dfloat b) {
   return a;
 }
 
+// Forward-mode tangent pair (value, derivative with respect to one
+// parameter): the adjoint's tangent products of the aux-bit chains run the
+// chain steps in this type, d(a b) = da b + a db, d(a + b) = da + db.
+struct __align__(16) tangent {
+  double v, d;
+  __host__ __device__ tangent() {}
+  __host__ __device__ tangent(double x) : v(x), d(0.0) {}
+  __host__ __device__ tangent(double x, double dx) : v(x), d(dx) {}
+};
+
+__host__ __device__ __forceinline__ tangent operator+(tangent a, tangent b) { return tangent(a.v + b.v, a.d + b.d); }
+__host__ __device__ __forceinline__ tangent operator*(tangent a, tangent b) {
+  return tangent(a.v * b.v, a.d * b.v + a.v * b.d);
+}
+__host__ __device__ __forceinline__ tangent& operator+=(tangent& a, tangent b) {
+  a = a + b;
+  return a;
+}
+__host__ __device__ __forceinline__ tangent& operator*=(tangent& a, tangent b) {
+  a = a * b;
+  return a;
+}
+
 }  // namespace ltm

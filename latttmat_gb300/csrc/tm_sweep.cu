@@ -267,6 +267,65 @@ __global__ void __launch_bounds__(256) sw_copy_in(const ChainInst* __restrict__ 
   for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) I.V[r] = xi[r];
 }
 
+// V[:, col] = x_i (the gradient's right and left vectors)
+__global__ void __launch_bounds__(256) sw_copy_col(const ChainInst* __restrict__ inst,
+                                                  const int64_t* __restrict__ rstart, int count, int col,
+                                                  const double* const* __restrict__ x) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  const ChainInst& I = inst[rb.i];
+  const double* xi = x[rb.i];
+  double* v = I.V + (int64_t)col * I.ldv;
+  for (int64_t r = rb.r0 + threadIdx.x; r < rb.r1; r += blockDim.x) v[r] = xi[r];
+}
+
+// Partial sums of the adjoint's weight term over each member's rows, with
+// r = V[:, 0] and l = V[:, 1]: slots 0..3 sum l r g_t (g = d ln Tvec/d theta),
+// slot 4 sums l r; slot 5 sums l w (w = the last tangent product) when dot_w.
+__global__ void __launch_bounds__(256) sw_grad_sums(const ChainInst* __restrict__ inst,
+                                                   const int64_t* __restrict__ rstart, int count, int dot_w,
+                                                   double* __restrict__ part) {
+  const RowBlock rb = row_block(inst, rstart, count);
+  const ChainInst& I = inst[rb.i];
+  const double* r = I.V;
+  const double* l = I.V + I.ldv;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t i = rb.r0 + threadIdx.x; i < rb.r1; i += blockDim.x) {
+    if (dot_w) {
+      acc[5] += l[i] * I.w[i];
+      continue;
+    }
+    const uint64_t st = I.idx ? (uint64_t)I.idx[i] : (uint64_t)i;
+    double g[4];
+    aux_tvec_grad(I.kind, I.L, I.bc, I.bj, I.kap2, I.h, st, g);
+    const double lr = l[i] * r[i];
+    for (int t = 0; t < 4; ++t) acc[t] += lr * g[t];
+    acc[4] += lr;
+  }
+  __shared__ double sh[6][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = 0; k < 6; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[k][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[threadIdx.x][q];
+    part[(int64_t)blockIdx.x * kSweepMaxM + threadIdx.x] = t;
+  }
+}
+
+// out[i * 8 + c] = sum of member i's row-block partials in slot c (c < 6)
+__global__ void sw_sum_slots(const int64_t* __restrict__ rstart, const double* __restrict__ part,
+                             double* __restrict__ out) {
+  const int i = blockIdx.x, c = threadIdx.x;
+  if (c >= 6) return;
+  double acc = 0.0;
+  for (int64_t b = rstart[i]; b < rstart[i + 1]; ++b) acc += part[b * kSweepMaxM + c];
+  out[(int64_t)i * 8 + c] = acc;
+}
+
 // ------------------------------------------------------------------ host side
 struct OpDeleter {
   void operator()(Op* o) const {
@@ -303,6 +362,7 @@ struct Sweep {
   cudaStream_t s = nullptr;
   int zb = 0;
   size_t budget_override = 0;  // bytes of member buffers per wave (0: from free memory)
+  int dir = 0;                 // 1: the members' transposes (left eigenvectors)
   // diagnostics of the last solve: waves, steps, seconds building waves, in
   // steps (device work, host-timed), in host restarts
   double stats[5] = {0, 0, 0, 0, 0};
@@ -316,13 +376,13 @@ struct Sweep {
   }
 
   // device memory one member needs in a wave (basis of m+1 columns)
-  size_t member_bytes(const Op& o, int m) const {
+  size_t member_bytes(const Op& o, int m, size_t elem = 8) const {
     const int64_t N = 1ll << o.L;
     const int64_t per = zb ? 16 * N : 4 * N;
-    return (size_t)per * 8 + (size_t)N * 8 + (size_t)(m + 1) * o.n * 8 + (size_t)o.n * 12 + kScStride * 8 + 4096;
+    return (size_t)per * elem + (size_t)N * 8 + (size_t)(m + 1) * o.n * 8 + (size_t)o.n * 12 + kScStride * 8 + 4096;
   }
 
-  std::vector<std::pair<int, int>> waves(int m) const {
+  std::vector<std::pair<int, int>> waves(int m, size_t elem = 8) const {
     size_t budget = budget_override;
     if (!budget) {
       size_t fr = 0, tot = 0;
@@ -333,7 +393,7 @@ struct Sweep {
     int a = 0;
     size_t used = 0;
     for (int i = 0; i < (int)mem.size(); ++i) {
-      const size_t b = member_bytes(*mem[i].op, m);
+      const size_t b = member_bytes(*mem[i].op, m, elem);
       if (i > a && used + b > budget) {
         w.push_back({a, i});
         a = i;
@@ -353,16 +413,18 @@ struct Wave {
   Sweep& sw;
   int a, b, count, m;
   std::vector<std::unique_ptr<DBuf>> bufs;
-  DBuf inst, kmd, start4, start8, bmem4, bmem8, rstart, part, sc, Wall, rot, flag, yptr;
+  DBuf inst, kmd, start4, start8, start16, bmem4, bmem8, bmem16, rstart, part, sc, Wall, rot, flag, yptr;
   std::vector<ChainInst> host;
   ChainBatch B;
-  int np4max = 0, np8max = 0, threads4 = 256, threads8 = 256;
-  size_t smem4 = 0, smem8 = 0;
+  DBuf slots;  // per-member sums of the adjoint (8 doubles each)
+  int np4max = 0, np8max = 0, np16max = 0, threads4 = 256, threads8 = 256;
+  size_t smem4 = 0, smem8 = 0, smem16 = 0;
   int64_t nrblk = 0;
   std::map<int, cudaGraphExec_t> graphs;  // one step, by the product modes present
   std::map<int, int64_t> graph_kernels;
 
-  Wave(Sweep& s_, int a_, int b_, int m_) : sw(s_), a(a_), b(b_), count(b_ - a_), m(m_) {
+  Wave(Sweep& s_, int a_, int b_, int m_, bool tangent_bufs = false)
+      : sw(s_), a(a_), b(b_), count(b_ - a_), m(m_) {
     cudaStream_t s = sw.s;
     host.resize(count);
     // one tile size and block size per element size for the whole wave: the
@@ -377,14 +439,14 @@ struct Wave {
       const Op& o = *sw.mem[a + q].op;
       ChainInst& I = host[q];
       std::memset(&I, 0, sizeof(I));
-      chain_inst_fill(o, 0, I, tb4, tb8);
+      chain_inst_fill(o, sw.dir, I, tb4, tb8);
       const int64_t N = 1ll << o.L;
       auto mk = [&](size_t bytes) {
         bufs.emplace_back(new DBuf());
         bufs.back()->alloc(bytes);
         return bufs.back()->p;
       };
-      I.P = mk((size_t)(sw.zb ? 16 * N : 4 * N) * 8);
+      I.P = mk((size_t)(sw.zb ? 16 * N : 4 * N) * (tangent_bufs ? 16 : 8));
       I.fold = mk((size_t)N * 8);
       I.ldv = (o.n + 1) & ~(int64_t)1;
       I.V = static_cast<double*>(mk((size_t)(m + 1) * I.ldv * 8));
@@ -394,13 +456,15 @@ struct Wave {
       np8max = std::max(np8max, I.np8);
       for (int p = 0; p < I.np4; ++p) smem4 = std::max(smem4, chain_pass_smem(I.p4[p], sw.zb, 4));
       for (int p = 0; p < I.np8; ++p) smem8 = std::max(smem8, chain_pass_smem(I.p8[p], sw.zb, 8));
+      np16max = std::max(np16max, I.np16);
+      for (int p = 0; p < I.np16; ++p) smem16 = std::max(smem16, chain_pass_smem(I.p16[p], sw.zb, 16));
     }
     sc.alloc((size_t)count * kScStride * 8);
     TM_CK(cudaMemsetAsync(sc.p, 0, sc.bytes, s));
     for (int q = 0; q < count; ++q) host[q].sc = sc.as<double>() + (size_t)q * kScStride;
     // block prefixes per pass (kBatchTiles tiles per block) and the member of
     // every block
-    auto plan_tables = [&](bool four, int npmax, std::vector<int64_t>& st, std::vector<int>& bm,
+    auto plan_tables = [&](int four, int npmax, std::vector<int64_t>& st, std::vector<int>& bm,
                            std::vector<int64_t>& nblk, std::vector<int64_t>& boff) {
       st.assign((size_t)std::max(npmax, 1) * (count + 1), 0);
       nblk.assign(std::max(npmax, 1), 0);
@@ -409,9 +473,9 @@ struct Wave {
       for (int p = 0; p < npmax; ++p) {
         boff[p] = (int64_t)bm.size();
         for (int q = 0; q < count; ++q) {
-          const int np = four ? host[q].np4 : host[q].np8;
-          const int64_t nb =
-              p < np ? (chain_pass_blocks(four ? host[q].p4[p] : host[q].p8[p]) + kBatchTiles - 1) / kBatchTiles : 0;
+          const int np = four == 4 ? host[q].np4 : (four == 8 ? host[q].np8 : host[q].np16);
+          const ChainPass* pp = four == 4 ? host[q].p4 : (four == 8 ? host[q].p8 : host[q].p16);
+          const int64_t nb = p < np ? (chain_pass_blocks(pp[p]) + kBatchTiles - 1) / kBatchTiles : 0;
           st[(size_t)p * (count + 1) + q + 1] = st[(size_t)p * (count + 1) + q] + nb;
           bm.insert(bm.end(), (size_t)nb, q);
         }
@@ -419,10 +483,11 @@ struct Wave {
         if (nblk[p] >= (1ll << 31)) fail(TM_ERR_LIMIT, "sweep wave too large for one launch");
       }
     };
-    std::vector<int64_t> s4, s8;
-    std::vector<int> bm4, bm8;
-    plan_tables(true, np4max, s4, bm4, B.p4.nblk, B.p4.boff);
-    plan_tables(false, np8max, s8, bm8, B.p8.nblk, B.p8.boff);
+    std::vector<int64_t> s4, s8, s16;
+    std::vector<int> bm4, bm8, bm16;
+    plan_tables(4, np4max, s4, bm4, B.p4.nblk, B.p4.boff);
+    plan_tables(8, np8max, s8, bm8, B.p8.nblk, B.p8.boff);
+    if (tangent_bufs) plan_tables(16, np16max, s16, bm16, B.p16.nblk, B.p16.boff);
     std::vector<int64_t> rst(count + 1, 0);
     for (int q = 0; q < count; ++q) rst[q + 1] = rst[q] + (host[q].n + kSweepRows - 1) / kSweepRows;
     nrblk = rst[count];
@@ -441,6 +506,16 @@ struct Wave {
     up(start8, s8.data(), s8.size() * 8);
     up(bmem4, bm4.data(), std::max<size_t>(bm4.size(), 1) * 4);
     up(bmem8, bm8.data(), std::max<size_t>(bm8.size(), 1) * 4);
+    if (tangent_bufs) {
+      up(start16, s16.data(), s16.size() * 8);
+      up(bmem16, bm16.data(), std::max<size_t>(bm16.size(), 1) * 4);
+      int tb16 = 0;
+      chain_tuning(Lmax, 16, sw.zb, tb16, B.p16.threads);
+      B.p16.np = np16max;
+      B.p16.smem = smem16;
+      B.p16.start = start16.as<int64_t>();
+      B.p16.bmem = bmem16.as<int>();
+    }
     up(rstart, rtab.data(), rtab.size() * 8);
     B.inst = inst.as<ChainInst>();
     B.count = count;
@@ -459,11 +534,12 @@ struct Wave {
     B.rmem = reinterpret_cast<const int*>(rstart.as<int64_t>() + count + 1);
     B.nrblk = nrblk;
     kmd.alloc((size_t)count * sizeof(int2));
-    part.alloc((size_t)nrblk * kSweepMaxM * 8);
+    part.alloc((size_t)nrblk * kSweepMaxM * 8 + 64);
     Wall.alloc((size_t)count * m * m * 8);
     rot.alloc((size_t)count * sizeof(int2));
     flag.alloc((size_t)count * sizeof(int));
     yptr.alloc((size_t)count * sizeof(void*));
+    slots.alloc((size_t)count * 8 * 8);
     // synchronise here: the host vectors above must outlive the copies
     TM_CK(cudaStreamSynchronize(s));
   }
@@ -475,14 +551,14 @@ struct Wave {
   const ChainInst* I() const { return inst.as<ChainInst>(); }
   const int2* km() const { return kmd.as<int2>(); }
 
-  int product(int mode) {
+  int product(int mode, int theta = 0) {
     int nl = 0;
     if (mode == kModeF32) {
       sw_to_f32<<<(unsigned)nrblk, 256, 0, sw.s>>>(I(), km(), rstart.as<int64_t>(), count);
       TM_CKK("sw_to_f32");
       ++nl;
     }
-    nl += chain_batch_product(B, km(), mode, sw.s);
+    nl += chain_batch_product(B, km(), mode, sw.s, theta);
     return nl;
   }
 
@@ -554,11 +630,16 @@ struct Wave {
 
 // Solve every member: nev wanted eigenvalues to tol (relative), mode
 // TM_EIGS_F64 or TM_EIGS_MIXED.
-void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
+// vec_out (host pointers per member, or null): each member's leading
+// eigenvector (real, unit norm), taken when the member converges.
+void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode, double* const* vec_out = nullptr) {
   if (nev < 1) fail(TM_ERR_ARG, "nev must be >= 1");
   int64_t nmin = INT64_MAX;
   for (auto& mb : sw.mem) nmin = std::min(nmin, mb.op->n);
-  int m = ncv > 0 ? ncv : ((nev > 4) ? 2 * nev + 1 : 2 * nev + 3);
+  // ncv 0: the reference's suggested_nev rule, but at least 12 columns --
+  // members restart less often, and over the 256-point B/7 sweep a 12-column
+  // subspace took 15% fewer products than the 7 columns the rule gives at nev=2
+  int m = ncv > 0 ? ncv : std::max((nev > 4) ? 2 * nev + 1 : 2 * nev + 3, 12);
   m = std::max(m, 2 * nev + 2);
   m = std::min<int64_t>(m, nmin - 1);
   if (m > kSweepMaxM - 1) fail(TM_ERR_LIMIT, "sweep subspace larger than 23");
@@ -615,6 +696,7 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
       sw.stats[3] += since(ts);
       const auto th = clk::now();
       bool any_rot = false, any_start = false;
+      std::vector<int> extract;
       for (int q = 0; q < count; ++q) {
         roth[q] = make_int2(0, 0);
         fl[q] = 0;
@@ -659,6 +741,21 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
             for (int i = 0; i < nev; ++i) mr = std::max(mr, R.resid[i] / std::max(std::abs(R.theta[i]), 1e-300));
             mb.info.max_resid = mr;
             mb.vals.assign(R.theta.begin(), R.theta.begin() + nev);
+            if (vec_out && vec_out[W.a + q]) {
+              // the leading Ritz vector V y0 into column 0, y0 turned so its
+              // largest component is real positive (the vector is real)
+              const std::vector<std::complex<double>>& y0 = R.y[0];
+              int kmax = 0;
+              for (int i = 1; i < m; ++i)
+                if (std::abs(y0[i]) > std::abs(y0[kmax])) kmax = i;
+              const std::complex<double> ph = std::conj(y0[kmax]) / std::max(std::abs(y0[kmax]), 1e-300);
+              double* Wq = Wh.data() + (size_t)q * m * m;
+              for (int i = 0; i < m; ++i) Wq[i] = (y0[i] * ph).real();
+              roth[q] = make_int2(1, 0);
+              fl[q] = 1;
+              any_rot = any_start = true;
+              extract.push_back(q);
+            }
             continue;
           }
           if (mb.cycles >= max_cycles) {
@@ -710,6 +807,9 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode) {
                                                        W.rot.as<int2>());
         TM_CKK("sw_rotate");
         if (any_start) W.normalize_starts(fl);
+        for (int q : extract)
+          TM_CK(cudaMemcpyAsync(vec_out[W.a + q], W.host[q].V, (size_t)W.host[q].n * 8, cudaMemcpyDeviceToHost,
+                                sw.s));
       }
       sw.stats[4] += since(th);
     }
@@ -740,6 +840,54 @@ void sweep_product(Sweep& sw, const double* const* x, double* const* y, tm_dtype
     TM_CKK("sw_copy_out");
     TM_CK(cudaStreamSynchronize(sw.s));
     for (int q = 0; q < count; ++q) sw.mem[W.a + q].op->matvecs++;
+  }
+}
+
+// d ln(lambda_i)/d(betaJ, kappa, kappa2, h) of every member, from its right
+// and left leading eigenvectors (host) and its internal eigenvalue: the
+// Boltzmann-weight term 2 <g>_{lr} from one batched reduction, and the chain
+// term <l, D_out (dC) D_in r> / (lambda <l, r>) from batched tangent
+// products, one per parameter the step factors depend on (the same formula
+// as tm_grad for one operator).
+void sweep_grad(Sweep& sw, const double* const* qr, const double* const* ql, const double* lam, double* grad) {
+  for (auto& wv : sw.waves(1, 16)) {
+    AllocStream guard(sw.s);
+    Wave W(sw, wv.first, wv.second, 1, true);
+    const int count = W.count;
+    auto copy_col = [&](int col, const double* const* src) {
+      TM_CK(cudaMemcpyAsync(W.yptr.p, src + W.a, count * sizeof(void*), cudaMemcpyHostToDevice, sw.s));
+      sw_copy_col<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count, col,
+                                                       W.yptr.as<const double* const>());
+      TM_CKK("sw_copy_col");
+      TM_CK(cudaStreamSynchronize(sw.s));  // the pointer table is rewritten next
+    };
+    copy_col(0, qr);
+    copy_col(1, ql ? ql : qr);
+    std::vector<double> sums((size_t)count * 8);
+    auto slot_sums = [&](int dot_w) {
+      sw_grad_sums<<<(unsigned)W.nrblk, 256, 0, sw.s>>>(W.I(), W.rstart.as<int64_t>(), count, dot_w,
+                                                        W.part.as<double>());
+      TM_CKK("sw_grad_sums");
+      sw_sum_slots<<<count, 32, 0, sw.s>>>(W.rstart.as<int64_t>(), W.part.as<double>(), W.slots.as<double>());
+      TM_CKK("sw_sum_slots");
+      TM_CK(cudaMemcpyAsync(sums.data(), W.slots.p, sums.size() * 8, cudaMemcpyDeviceToHost, sw.s));
+      TM_CK(cudaStreamSynchronize(sw.s));
+    };
+    slot_sums(0);
+    std::vector<double> wsum(count);
+    for (int q = 0; q < count; ++q) {
+      wsum[q] = sums[(size_t)q * 8 + 4];
+      for (int t = 0; t < 4; ++t) grad[(size_t)(W.a + q) * 4 + t] = 2.0 * sums[(size_t)q * 8 + t] / wsum[q];
+    }
+    for (int t = 0; t < 3; ++t) {
+      if (t == 2 && !sw.zb) break;  // DNNI steps do not depend on kappa2
+      std::vector<int2> kmh(count, make_int2(0, kModeTangent));
+      TM_CK(cudaMemcpyAsync(W.kmd.p, kmh.data(), count * sizeof(int2), cudaMemcpyHostToDevice, sw.s));
+      W.product(kModeTangent, t);
+      slot_sums(1);
+      for (int q = 0; q < count; ++q)
+        grad[(size_t)(W.a + q) * 4 + t] += sums[(size_t)q * 8 + 5] / (lam[W.a + q] * wsum[q]);
+    }
   }
 }
 
@@ -827,6 +975,27 @@ tm_status tm_sweep_set_wave_bytes(tm_sweep* sw, size_t bytes) {
   SW_END
 }
 
+tm_status tm_sweep_set_transpose(tm_sweep* sw, int transpose) {
+  SW_BEGIN
+  if (!sw) fail(TM_ERR_ARG, "null sweep");
+  sw->impl->dir = transpose ? 1 : 0;
+  SW_END
+}
+
+tm_status tm_sweep_grad(tm_sweep* sw, const double* const* qr_host, const double* const* ql_host,
+                        const double* lambda_internal, double* grad4) {
+  SW_BEGIN
+  if (!sw || !qr_host || !lambda_internal || !grad4) fail(TM_ERR_ARG, "null argument");
+  if (sw->impl->dir) fail(TM_ERR_ARG, "gradients are taken on the sweep of the operators, not of their transposes");
+  for (auto& mb : sw->impl->mem)
+    if (!mb.op->symmetric && !ql_host) fail(TM_ERR_ARG, "general operators need the left eigenvectors");
+  for (int i = 0; i < (int)sw->impl->mem.size(); ++i)
+    if (!(lambda_internal[i] != 0.0) || !std::isfinite(lambda_internal[i]))
+      fail(TM_ERR_ARG, "eigenvalues must be finite and nonzero");
+  sweep_grad(*sw->impl, qr_host, ql_host, lambda_internal, grad4);
+  SW_END
+}
+
 int tm_sweep_stats(const tm_sweep* sw, double* out, int cap) {
   if (!sw || !out) return 0;
   int n = 0;
@@ -842,8 +1011,21 @@ tm_status tm_sweep_perform_op_dev(tm_sweep* sw, const double* const* x_dev, doub
   SW_END
 }
 
+static tm_status sweep_eigs_impl(tm_sweep* sw, int nev, int ncv, double tol, int mode, double* vals_re,
+                                 double* vals_im, double* const* vec0, tm_eigs_info* infos, tm_status* status);
+
 tm_status tm_sweep_eigs(tm_sweep* sw, int nev, int ncv, double tol, int mode, double* vals_re, double* vals_im,
                         tm_eigs_info* infos, tm_status* status) {
+  return sweep_eigs_impl(sw, nev, ncv, tol, mode, vals_re, vals_im, nullptr, infos, status);
+}
+
+tm_status tm_sweep_eigs_vec(tm_sweep* sw, int nev, int ncv, double tol, int mode, double* vals_re, double* vals_im,
+                            double* const* vec0_host, tm_eigs_info* infos, tm_status* status) {
+  return sweep_eigs_impl(sw, nev, ncv, tol, mode, vals_re, vals_im, vec0_host, infos, status);
+}
+
+static tm_status sweep_eigs_impl(tm_sweep* sw, int nev, int ncv, double tol, int mode, double* vals_re,
+                                 double* vals_im, double* const* vec0, tm_eigs_info* infos, tm_status* status) {
   SW_BEGIN
   if (!sw || !vals_re || !vals_im) fail(TM_ERR_ARG, "null argument");
   if (mode != TM_EIGS_F64 && mode != TM_EIGS_MIXED) fail(TM_ERR_ARG, "bad mode");
@@ -856,7 +1038,7 @@ tm_status tm_sweep_eigs(tm_sweep* sw, int nev, int ncv, double tol, int mode, do
     mb.stall = 0;
     mb.cycles = 0;
   }
-  sweep_solve(s, nev, ncv, tol, mode);
+  sweep_solve(s, nev, ncv, tol, mode, vec0);
   tm_status first = TM_OK;
   for (int i = 0; i < (int)s.mem.size(); ++i) {
     Member& mb = s.mem[i];

@@ -174,3 +174,42 @@ def test_chain_autotune_choices_give_the_same_product(model, ax, L):
     finally:
         for dt in (lt.TM_F32, lt.TM_F64_DF):
             lt.chain_set_tuning(model, L, dt, 0, 0)
+
+
+@pytest.mark.parametrize("model,ax,ec,points", [
+    ("B", 7, 2, MIXED_B7[:4] + [(0.55, 0.35, 0.1, 0.0, 14)]),
+    ("B", 7, 0, [(0.5, 0.35, 0.1, 0.05, 10), (0.4, 0.6, 0.2, 0.02, 12)]),
+    ("D", 5, 2, [(0.4, 0.3, 0.0, 0.1, 13), (0.5, 0.7, 0.0, 0.0, 16), (0.45, 0.5, 0.0, 0.05, 12)]),
+])
+def test_sweep_adjoint_matches_single_operators(model, ax, ec, points):
+    """Batched adjoint: leading right eigenvectors from the sweep, left ones
+    from the sweep of the transposes, gradients from one batched reduction
+    and batched tangent products -- against tm_grad on each operator with its
+    own tm_eigs eigenvectors (1e-8 relative to max(|grad|, 1))."""
+    right = lt.Sweep(model, 2, ax, points, extend_cond=ec)
+    vals, _, st, vr = right.eigs(2, tol=1e-12, mode=lt.TM_EIGS_MIXED, vectors=True)
+    assert list(st) == [lt.TM_OK] * len(points)
+    sym = model == "D"
+    vl = None
+    if not sym:
+        left = lt.Sweep(model, 2, ax, points, extend_cond=ec)
+        left.set_transpose(True)
+        vals_l, _, st_l, vl = left.eigs(2, tol=1e-12, mode=lt.TM_EIGS_MIXED, vectors=True)
+        assert list(st_l) == [lt.TM_OK] * len(points)
+        np.testing.assert_allclose(np.abs(vals_l[:, 0]), np.abs(vals[:, 0]), rtol=1e-10)
+        left.close()
+    lam = np.array([np.real(vals[i, 0]) * right.normfactor(i) for i in range(len(points))])
+    g = right.grad(vr, vl, lam)
+    for i, (bj, k, k2, h, L) in enumerate(points):
+        op = lt.TMatOp(model, 2, ax, bj, k, h, L, k2, ec)
+        v1, vecs, vecl, _ = op.eigs(2, tol=1e-13, mode=lt.TM_EIGS_F64, vectors=True, left=not sym)
+        qr = np.real(vecs[0])
+        g1 = op.grad(qr, float(np.real(v1[0])) * op.getnormfactor(), None if sym else np.asarray(vecl))
+        assert np.max(np.abs(g[i] - g1)) < 1e-8 * max(1.0, np.max(np.abs(g1))), (i, g[i], g1)
+        # the sweep's eigenvector is the operator's (up to sign)
+        q = vr[i] * np.sign(vr[i].sum())
+        qq = qr / np.linalg.norm(qr)
+        qq = qq * np.sign(qq.sum())
+        assert rel_err(q, qq) < 1e-7
+        op.close()
+    right.close()
