@@ -442,7 +442,10 @@ def batch_sweep(count):
     """The parameter sweep solved as one device batch (tm_sweep) in mixed
     precision and in FP64 (equal concurrency: every point in the batch), and
     one plain FP64 tm_eigs solve per point on an evenly spaced sample; all to
-    1e-10, k=2.  Seconds include operator construction."""
+    1e-10, k=2.  Then the same with the adjoint: the batch adds the sweep of
+    the transposes (left eigenvectors) and the batched gradient; the plain
+    form solves for both eigenvectors and calls tm_grad per point.  Seconds
+    include operator construction."""
     import numpy as np
 
     import latttmat_gb300 as lt
@@ -454,29 +457,61 @@ def batch_sweep(count):
     warm.close()
     res = {}
     launches = {}
+    right = None
     for tag, mode in (("mixed", lt.TM_EIGS_MIXED), ("f64", lt.TM_EIGS_F64)):
         l0 = lt.launch_count()
         t0 = time.perf_counter()
         sw = lt.Sweep("B", 2, 7, pts, extend_cond=2)
         t1 = time.perf_counter()
-        vals, info, st = sw.eigs(2, tol=1e-10, mode=mode)
+        if tag == "mixed":
+            vals, info, st, vecs = sw.eigs(2, tol=1e-10, mode=mode, vectors=True)
+            right = (sw, vals, vecs)
+        else:
+            vals, info, st = sw.eigs(2, tol=1e-10, mode=mode)
         t2 = time.perf_counter()
         stats = sw.stats()
-        sw.close()
+        if tag != "mixed":
+            sw.close()
         launches[tag] = lt.launch_count() - l0
         res[tag] = dict(seconds=t2 - t0, create_s=t1 - t0, solve_s=t2 - t1, vals=vals, failed=int(np.sum(st != 0)),
                         matvecs=int(sum(i["matvecs"] for i in info)),
                         matvecs_f64=int(sum(i["matvecs_f64"] for i in info)), stats=stats)
     dev = float(np.max(np.abs(res["mixed"]["vals"] - res["f64"]["vals"]) / np.abs(res["f64"]["vals"])))
-    # plain: one FP64 solve after another on every 8th point (all widths)
-    sample = pts[::8]
+    # batched adjoint: left eigenvectors from the sweep of the transposes, then
+    # the batched gradient (its time adds to the mixed sweep's)
+    sw, vals_r, vec_r = right
     t0 = time.perf_counter()
-    for (bj, k, k2, h, L) in sample:
+    left = lt.Sweep("B", 2, 7, pts, extend_cond=2)
+    left.set_transpose(True)
+    _, _, st_l, vec_l = left.eigs(2, tol=1e-10, mode=lt.TM_EIGS_MIXED, vectors=True)
+    lam = np.array([np.real(vals_r[i, 0]) * sw.normfactor(i) for i in range(count)])
+    grads = sw.grad(vec_r, vec_l, lam)
+    t_adj = time.perf_counter() - t0
+    left.close()
+    sw.close()
+    # plain: one FP64 solve after another on every 8th point (all widths),
+    # without and with the adjoint
+    sample = list(range(0, count, 8))
+    t_plain = t_plain_adj = 0.0
+    gdevs = []
+    for i in sample:
+        bj, k, k2, h, L = pts[i]
+        t0 = time.perf_counter()
         op = lt.TMatOp("B", 2, 7, bj, k, h, L, k2, 2)
         op.eigs(2, tol=1e-10, mode=lt.TM_EIGS_F64)
         op.close()
-    t_plain = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        op = lt.TMatOp("B", 2, 7, bj, k, h, L, k2, 2)
+        v1, vecs1, vecl1, _ = op.eigs(2, tol=1e-10, mode=lt.TM_EIGS_F64, vectors=True, left=True)
+        g1 = op.grad(np.real(vecs1[0]), float(np.real(v1[0])) * op.getnormfactor(), np.asarray(vecl1))
+        op.close()
+        t2 = time.perf_counter()
+        t_plain += t1 - t0
+        t_plain_adj += t2 - t1
+        gdevs.append(float(np.max(np.abs(grads[i] - g1)) / max(1.0, float(np.max(np.abs(g1))))))
     plain_per_point = t_plain / len(sample)
+    plain_adj_per_point = t_plain_adj / len(sample)
+    batched_adj_s = res["mixed"]["seconds"] + t_adj
     return {"workload": f"{count} x B/7 reduced diagonal BNNNI, L in {{16..24}} (seed 0), betaJ in [0.2,1.0], "
                         "kappa1 ~ U[0,1] (seed 1), neigs=2, tol 1e-10",
             "batched_mixed_s": res["mixed"]["seconds"], "batched_f64_s": res["f64"]["seconds"],
@@ -486,14 +521,25 @@ def batch_sweep(count):
             "speedup_mixed_vs_batched_f64": res["f64"]["seconds"] / res["mixed"]["seconds"],
             "speedup_mixed_vs_plain_f64": plain_per_point * count / res["mixed"]["seconds"],
             "max_rel_dev_mixed_vs_f64": dev,
+            "batched_adjoint_s": batched_adj_s,
+            "batched_adjoint_per_point_s": batched_adj_s / count,
+            "plain_f64_adjoint_per_point_s": plain_adj_per_point,
+            "speedup_batched_adjoint_vs_plain": plain_adj_per_point * count / batched_adj_s,
+            "grad_dev_batched_vs_plain": {"median": float(np.median(gdevs)), "max": float(np.max(gdevs)),
+                                          "points_above_1e-6": int(np.sum(np.array(gdevs) > 1e-6)),
+                                          "note": "relative to max(|grad|, 1); both forms solve to 1e-10, so the "
+                                                  "eigenvectors differ by ~tol / gap where lambda1/lambda0 is "
+                                                  "close to 1 (ordered phase)"},
             "matvecs": {k: {"all": res[k]["matvecs"], "fp64_accurate": res[k]["matvecs_f64"]} for k in res},
             "create_s": {k: res[k]["create_s"] for k in res},
             "sweep_stats": {k: res[k]["stats"] for k in res},
             "gpu_launches": launches,
-            "failed": res["mixed"]["failed"] + res["f64"]["failed"],
+            "failed": res["mixed"]["failed"] + res["f64"]["failed"] + int(np.sum(st_l != 0)),
             "note": f"batched: tm_sweep (one launch per chain pass over all {count} points, one CUDA graph per "
-                    f"Arnoldi step of every point); plain: tm_eigs FP64 one point after another on {len(sample)} "
-                    "evenly spaced points (every 8th), per point"}
+                    "Arnoldi step of every point); batched adjoint: the sweep of the transposes for the left "
+                    "vectors and tm_sweep_grad (one batched reduction and one batched tangent product per "
+                    f"parameter); plain: tm_eigs FP64 (with both eigenvectors and tm_grad for the adjoint) one "
+                    f"point after another on {len(sample)} evenly spaced points (every 8th), per point"}
 
 
 def eo_plan_sizes(L):
