@@ -82,6 +82,10 @@ typedef struct {
                            verification, 3 not accepted (FP64 Lanczos continued) */
   double refine_est;    /* last estimated max relative residual */
   double refine_true;   /* last verified max relative residual (0 if none) */
+  /* mixed mode only: split of the solve (host clock, stream synchronised) */
+  int matvecs_phase1;     /* FP32 products of the FP32 Lanczos phase */
+  double seconds_phase1;  /* FP32 Lanczos phase */
+  double seconds_refine;  /* refinement, including its FP64-accurate products */
 } tm_eigs_info;
 
 /* ---- operator lifetime ------------------------------------------------- */

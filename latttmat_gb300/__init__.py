@@ -67,7 +67,8 @@ class tm_eigs_info(ctypes.Structure):
                 ("restarts", ctypes.c_int), ("ncv", ctypes.c_int), ("max_resid", ctypes.c_double),
                 ("seconds", ctypes.c_double), ("refine_rounds", ctypes.c_int), ("refine_checks", ctypes.c_int),
                 ("refine_outcome", ctypes.c_int), ("refine_est", ctypes.c_double),
-                ("refine_true", ctypes.c_double)]
+                ("refine_true", ctypes.c_double), ("matvecs_phase1", ctypes.c_int),
+                ("seconds_phase1", ctypes.c_double), ("seconds_refine", ctypes.c_double)]
 
 
 _lib = None

@@ -117,6 +117,11 @@ void combine_f32_dd(const float* V, int64_t ldv, int m, const double* Y, int k, 
 // H[k + j*ldh] = V[k] . W[j]: V double-float columns, up to 4 FP32 vectors W
 void mdot_dd_block(const dfloat* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H, int64_t ldh,
                    double* part, cudaStream_t s);
+// G[i + j*nx] = V[i] . V[j] for i < nx <= 4, j < ny <= 8 (the first nx of
+// ny contiguous double-float columns against all of them) in one sweep
+void mdot_dd_gram(const dfloat* V, int64_t ldv, int nx, int ny, int64_t n, double* G, double* part, cudaStream_t s);
+// V[:, c] = sum_j V[:, j] Y[c*k + j], c < k <= 4, in place (Y FP64 on the device)
+void combine_dd_inplace(dfloat* V, int64_t ldv, int k, const double* Y, int64_t n, cudaStream_t s);
 // conversions: out = fl32(x); out = x * scale (FP64); out = x * scale (double-float)
 void df_to_f32(const dfloat* x, float* out, int64_t n, cudaStream_t s);
 void df_to_f64(const dfloat* x, double scale, double* out, int64_t n, cudaStream_t s);

@@ -280,6 +280,97 @@ __global__ void __launch_bounds__(BT) mdot_dd_block_kernel(const dfloat* __restr
   }
 }
 
+// part[b][i * NY + j] partial sums of V[i] . V[j], i < nx, j < ny (all
+// double-float columns of one block)
+template <int NX, int NY>
+__global__ void __launch_bounds__(BT) mdot_dd_gram_kernel(const dfloat* __restrict__ V, int64_t ldv, int nx,
+                                                          int ny, int64_t n, double* __restrict__ part) {
+  dfloat acc[NX][NY];
+#pragma unroll
+  for (int i = 0; i < NX; ++i)
+#pragma unroll
+    for (int j = 0; j < NY; ++j) acc[i][j] = dfloat(0.f, 0.f);
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t t = (int64_t)blockIdx.x * BT + threadIdx.x; t < n2; t += st) {
+    df2 row[NY];
+#pragma unroll
+    for (int j = 0; j < NY; ++j)
+      row[j] = (j < ny) ? ld2(V + (int64_t)j * ldv, t) : df2{dfloat(0.f, 0.f), dfloat(0.f, 0.f)};
+#pragma unroll
+    for (int i = 0; i < NX; ++i)
+#pragma unroll
+      for (int j = 0; j < NY; ++j)
+        if (i < nx && j < ny) {
+          acc[i][j] = df_fma(row[i].a, row[j].a, acc[i][j]);
+          acc[i][j] = df_fma(row[i].b, row[j].b, acc[i][j]);
+        }
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int64_t t = n - 1;
+    for (int i = 0; i < nx; ++i)
+      for (int j = 0; j < ny; ++j) acc[i][j] = df_fma(V[(int64_t)i * ldv + t], V[(int64_t)j * ldv + t], acc[i][j]);
+  }
+  __shared__ double sh[BT / 32][NX * NY];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NX; ++i)
+#pragma unroll
+    for (int j = 0; j < NY; ++j) {
+      const double v = warp_sum_d((double)acc[i][j].hi + (double)acc[i][j].lo);
+      if (lane == 0) sh[wid][i * NY + j] = v;
+    }
+  __syncthreads();
+  for (int q = threadIdx.x; q < NX * NY; q += BT) {
+    double a = 0.0;
+    for (int w = 0; w < BT / 32; ++w) a += sh[w][q];
+    part[(int64_t)blockIdx.x * (NX * NY) + q] = a;
+  }
+}
+
+// V[:, c] = sum_j V[:, j] Y[c * k + j], c < k <= KK, in place (each thread
+// reads its rows of all k columns before writing any)
+template <int KK>
+__global__ void __launch_bounds__(BT) combine_dd_inplace_kernel(dfloat* __restrict__ V, int64_t ldv, int k,
+                                                                const double* __restrict__ Y, int64_t n) {
+  __shared__ double ys[KK * KK];
+  for (int q = threadIdx.x; q < k * k; q += BT) ys[q] = Y[q];
+  __syncthreads();
+  dfloat yd[KK * KK];
+#pragma unroll
+  for (int q = 0; q < KK * KK; ++q) yd[q] = (q < k * k) ? dfloat(ys[q]) : dfloat(0.f, 0.f);
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * BT;
+  for (int64_t t = (int64_t)blockIdx.x * BT + threadIdx.x; t < n2; t += st) {
+    df2 row[KK];
+#pragma unroll
+    for (int j = 0; j < KK; ++j)
+      if (j < k) row[j] = ld2(V + (int64_t)j * ldv, t);
+#pragma unroll
+    for (int c = 0; c < KK; ++c)
+      if (c < k) {
+        df2 o{dfloat(0.f, 0.f), dfloat(0.f, 0.f)};
+#pragma unroll
+        for (int j = 0; j < KK; ++j)
+          if (j < k) {
+            o.a = df_fma(yd[c * k + j], row[j].a, o.a);
+            o.b = df_fma(yd[c * k + j], row[j].b, o.b);
+          }
+        st2(V + (int64_t)c * ldv, t, o);
+      }
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int64_t t = n - 1;
+    dfloat r[KK];
+    for (int j = 0; j < k; ++j) r[j] = V[(int64_t)j * ldv + t];
+    for (int c = 0; c < k; ++c) {
+      dfloat o(0.f, 0.f);
+      for (int j = 0; j < k; ++j) o = df_fma(yd[c * k + j], r[j], o);
+      V[(int64_t)c * ldv + t] = o;
+    }
+  }
+}
+
 __global__ void block_final_df_kernel(const double* __restrict__ part, int nb, int kv, int nw, int stride, int nws,
                                       double* H, int64_t ldh, int k0) {
   const int t = blockIdx.x;
@@ -388,6 +479,23 @@ void mdot_dd_block(const dfloat* V, int64_t ldv, int nv, const F32Cols& W, int n
     block_final_df_kernel<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * NW, NW, H, ldh, k0);
     TM_CKK("mdot_dd_block_final");
   }
+}
+
+void mdot_dd_gram(const dfloat* V, int64_t ldv, int nx, int ny, int64_t n, double* G, double* part, cudaStream_t s) {
+  if (nx < 1 || nx > 4 || ny < nx || ny > 8) fail(TM_ERR_LIMIT, "mdot_dd_gram: 1..4 of up to 8 columns");
+  constexpr int NX = 4, NY = 8;
+  const int nb = blocks_df(n);
+  mdot_dd_gram_kernel<NX, NY><<<nb, BT, 0, s>>>(V, ldv, nx, ny, n, part);
+  TM_CKK("mdot_dd_gram");
+  // column-major G (ld nx): entry (i, j) from the partials' slot i * NY + j
+  block_final_df_kernel<<<nx * ny, 256, 0, s>>>(part, nb, nx, ny, NX * NY, NY, G, nx, 0);
+  TM_CKK("mdot_dd_gram_final");
+}
+
+void combine_dd_inplace(dfloat* V, int64_t ldv, int k, const double* Y, int64_t n, cudaStream_t s) {
+  if (k < 1 || k > 4) fail(TM_ERR_LIMIT, "combine_dd_inplace: 1..4 columns");
+  combine_dd_inplace_kernel<4><<<blocks_df(n), BT, 0, s>>>(V, ldv, k, Y, n);
+  TM_CKK("combine_dd_inplace");
 }
 
 void df_to_f32(const dfloat* x, float* out, int64_t n, cudaStream_t s) {

@@ -140,37 +140,73 @@ __device__ __forceinline__ float fma_t(float r, float x, float y) { return fmaf(
 __device__ __forceinline__ double fma_t(double r, double x, double y) { return fma(r, x, y); }
 __device__ __forceinline__ dfloat fma_t(dfloat r, dfloat x, dfloat y) { return df_fma_unnorm(r, x, y); }
 
-// in-register butterflies over the 2^NB elements held by one thread
+// In-register butterflies on all NB levels of the 2^NB elements held by one
+// thread.  Output pair of level lv: (x0 + r x1, x1 + r x0), or exchanged
+// (swap).
 template <class T, int NB>
-__device__ __forceinline__ void reg_bfly(T (&v)[1 << NB], int nb, T r, int swap) {
+__device__ __forceinline__ void reg_bfly(T (&v)[1 << NB], T r, int swap) {
   if (!swap) {
 #pragma unroll
-    for (int lv = 0; lv < NB; ++lv) {
-      if (lv < nb) {
+    for (int lv = 0; lv < NB; ++lv)
 #pragma unroll
-        for (int i = 0; i < (1 << NB); ++i) {
-          if (!(i & (1 << lv))) {
-            const T x0 = v[i], x1 = v[i | (1 << lv)];
-            v[i] = fma_t(r, x1, x0);
-            v[i | (1 << lv)] = fma_t(r, x0, x1);
-          }
+      for (int i = 0; i < (1 << NB); ++i)
+        if (!(i & (1 << lv))) {
+          const T x0 = v[i], x1 = v[i | (1 << lv)];
+          v[i] = fma_t(r, x1, x0);
+          v[i | (1 << lv)] = fma_t(r, x0, x1);
         }
-      }
-    }
   } else {
 #pragma unroll
-    for (int lv = 0; lv < NB; ++lv) {
-      if (lv < nb) {
+    for (int lv = 0; lv < NB; ++lv)
 #pragma unroll
-        for (int i = 0; i < (1 << NB); ++i) {
-          if (!(i & (1 << lv))) {
-            const T x0 = v[i], x1 = v[i | (1 << lv)];
-            v[i] = fma_t(r, x0, x1);
-            v[i | (1 << lv)] = fma_t(r, x1, x0);
-          }
+      for (int i = 0; i < (1 << NB); ++i)
+        if (!(i & (1 << lv))) {
+          const T x0 = v[i], x1 = v[i | (1 << lv)];
+          v[i] = fma_t(r, x0, x1);
+          v[i | (1 << lv)] = fma_t(r, x1, x0);
         }
-      }
+  }
+}
+
+// The FP32 butterflies with the elements held in pairs (v[k] = elements 2k,
+// 2k + 1): level 0 pairs the two halves of one register pair (two scalar
+// FMAs per pair); every higher level pairs whole register pairs, two
+// butterflies per packed FMA (sm_100+ FFMA2).
+template <int NB>
+__device__ __forceinline__ void reg_bfly_f2(float2 (&v)[1 << (NB - 1)], float r, int swap) {
+  const float2 r2 = make_float2(r, r);
+  if (!swap) {
+#pragma unroll
+    for (int k = 0; k < (1 << (NB - 1)); ++k) {
+      const float x0 = v[k].x, x1 = v[k].y;
+      v[k].x = fmaf(r, x1, x0);
+      v[k].y = fmaf(r, x0, x1);
     }
+#pragma unroll
+    for (int lv = 1; lv < NB; ++lv)
+#pragma unroll
+      for (int k = 0; k < (1 << (NB - 1)); ++k)
+        if (!(k & (1 << (lv - 1)))) {
+          const float2 a = v[k], b = v[k | (1 << (lv - 1))];
+          v[k] = __ffma2_rn(r2, b, a);
+          v[k | (1 << (lv - 1))] = __ffma2_rn(r2, a, b);
+        }
+  } else {
+#pragma unroll
+    for (int k = 0; k < (1 << (NB - 1)); ++k) {
+      const float x0 = v[k].x, x1 = v[k].y;
+      v[k].x = fmaf(r, x0, x1);
+      v[k].y = fmaf(r, x1, x0);
+    }
+#pragma unroll
+    for (int lv = 1; lv < NB; ++lv)
+#pragma unroll
+      for (int k = 0; k < (1 << (NB - 1)); ++k)
+        if (!(k & (1 << (lv - 1)))) {
+          const float2 a = v[k], b = v[k | (1 << (lv - 1))];
+          v[k] = __ffma2_rn(r2, a, b);
+          v[k | (1 << (lv - 1))] = __ffma2_rn(r2, b, a);
+        }
   }
 }
 
@@ -194,29 +230,54 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // 2^15 elements in FP32 and 2^14 in 8-byte types).
 constexpr int kMaxTileBits = 16;
 
-// One butterfly round on local bits [G0, G0 + gs) of the shared-memory tile.
-// G0 is a compile-time constant, so each of a thread's 2^KB slots is the
-// thread's base slot plus a constant: j0 and i << G0 have disjoint bits, and
-// spad(a | b) = spad(a) + spad(b) for disjoint a, b (no carry reaches bit 5).
-template <class T, int KB, int G0>
-__device__ __forceinline__ void smem_round(T* sm, int n, int gs, T r, int swap) {
-  const int nfree = 1 << (n - gs);
+// One butterfly round on local bits [G0, G0 + GS) of the shared-memory tile.
+// G0 and GS are compile-time constants, so each of a thread's 2^GS slots is
+// the thread's base slot plus a constant: j0 and i << G0 have disjoint bits,
+// and spad(a | b) = spad(a) + spad(b) for disjoint a, b (no carry reaches
+// bit 5).
+template <class T, int G0, int GS>
+__device__ __forceinline__ void smem_round(T* sm, int n, T r, int swap) {
+  const int nfree = 1 << (n - GS);
   for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
-    const int j0 = (f & ((1 << G0) - 1)) | ((f >> G0) << (G0 + gs));
+    const int j0 = (f & ((1 << G0) - 1)) | ((f >> G0) << (G0 + GS));
     T* b = sm + spad(j0);
-    T v[1 << KB];
+    if constexpr (std::is_same<T, float>::value && GS >= 2) {
+      float2 v[1 << (GS - 1)];
 #pragma unroll
-    for (int i = 0; i < (1 << KB); ++i)
-      if (i < (1 << gs)) v[i] = b[spad(i << G0)];
-    reg_bfly<T, KB>(v, gs, r, swap);
-    if constexpr (std::is_same<T, dfloat>::value) {
-      // the double-float levels skip renormalisation; once per round here
+      for (int k = 0; k < (1 << (GS - 1)); ++k) {
+        v[k].x = b[spad((2 * k) << G0)];
+        v[k].y = b[spad((2 * k + 1) << G0)];
+      }
+      reg_bfly_f2<GS>(v, r, swap);
 #pragma unroll
-      for (int i = 0; i < (1 << KB); ++i) v[i] = df_norm(v[i]);
+      for (int k = 0; k < (1 << (GS - 1)); ++k) {
+        b[spad((2 * k) << G0)] = v[k].x;
+        b[spad((2 * k + 1) << G0)] = v[k].y;
+      }
+    } else {
+      T v[1 << GS];
+#pragma unroll
+      for (int i = 0; i < (1 << GS); ++i) v[i] = b[spad(i << G0)];
+      reg_bfly<T, GS>(v, r, swap);
+      if constexpr (std::is_same<T, dfloat>::value) {
+        // the double-float levels skip renormalisation; once per round here
+#pragma unroll
+        for (int i = 0; i < (1 << GS); ++i) v[i] = df_norm(v[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < (1 << GS); ++i) b[spad(i << G0)] = v[i];
     }
-#pragma unroll
-    for (int i = 0; i < (1 << KB); ++i)
-      if (i < (1 << gs)) b[spad(i << G0)] = v[i];
+  }
+}
+
+// the last round when it covers fewer than KB bits (gs = 1 .. KB - 1)
+template <class T, int KB, int G0, int GS = 1>
+__device__ __forceinline__ void smem_round_tail(T* sm, int n, int gs, T r, int swap) {
+  if constexpr (GS < KB) {
+    if (gs == GS)
+      smem_round<T, G0, GS>(sm, n, r, swap);
+    else
+      smem_round_tail<T, KB, G0, GS + 1>(sm, n, gs, r, swap);
   }
 }
 
@@ -226,7 +287,10 @@ template <class T, int KB, int R = 0>
 __device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A, int nbits) {
   constexpr int G0 = R * KB;
   if (G0 >= nbits) return;
-  smem_round<T, KB, G0>(sm, A.n, min(KB, nbits - G0), coef_r<T>(A), A.swap);
+  if (G0 + KB <= nbits)
+    smem_round<T, G0, KB>(sm, A.n, coef_r<T>(A), A.swap);
+  else
+    smem_round_tail<T, KB, G0>(sm, A.n, nbits - G0, coef_r<T>(A), A.swap);
   __syncthreads();
   if constexpr ((R + 1) * KB < kMaxTileBits) smem_rounds<T, KB, R + 1>(sm, A, nbits);
 }
@@ -438,22 +502,17 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
   if constexpr (CL) cluster_reduce<T, KB>(cl, sm, rank, A, xchg);
   // Output.  w1 is class-major: the block of e-class C holds, for each tile,
   // the |C| values of C's members, so a warp writes a few contiguous runs.
-  for (int k0 = 0; k0 < (1 << kb); k0 += kOutBatch) {
-    uint32_t wb[kOutBatch], ws[kOutBatch];
-    uint16_t ev[kOutBatch];
+  // (the table entries of a whole batch are loaded before any is used, so
+  // their loads are in flight together)
+  constexpr int kOB = (1 << KB) < 12 ? (1 << KB) : 12;
+  for (int k0 = 0; k0 < (1 << kb); k0 += kOB) {
+    uint2 w[kOB];  // (w1 offset, it_e | class size << 16)
 #pragma unroll
-    for (int q = 0; q < kOutBatch; ++q) {
-      if (k0 + q < (1 << kb)) {
-        const uint32_t P = base + threadIdx.x + ((k0 + q) << p);
-        const uint2 w = __ldg(wout + P);  // (w1 offset, it_e | class size << 16)
-        wb[q] = w.x;
-        ev[q] = (uint16_t)(w.y & 0xffffu);
-        ws[q] = w.y >> 16;
-      }
-    }
+    for (int q = 0; q < kOB; ++q)
+      if (k0 + q < (1 << kb)) w[q] = __ldg(wout + base + threadIdx.x + ((k0 + q) << p));
 #pragma unroll
-    for (int q = 0; q < kOutBatch; ++q)
-      if (k0 + q < (1 << kb)) w1[(int64_t)wb[q] + tile * ws[q]] = sm[spad(ev[q] & lmask)];
+    for (int q = 0; q < kOB; ++q)
+      if (k0 + q < (1 << kb)) w1[(int64_t)w[q].x + tile * (w[q].y >> 16)] = sm[spad(w[q].y & lmask)];
   }
 }
 

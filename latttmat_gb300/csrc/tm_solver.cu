@@ -356,11 +356,23 @@ __global__ void hcol32_kernel(double* H, int ld, int j, const double* h1, const 
   }
 }
 
+// h1[i] = H(i, j) / S for i < j: the couplings of v(j) to the earlier basis
+// vectors that the recurrence already knows (beta(j-1), or after a thick
+// restart the couplings to the kept Ritz vectors; zero otherwise).
+__global__ void hprev32_kernel(const double* H, int ld, int j, double S, double* h1) {
+  const int i = threadIdx.x;
+  if (i < j) h1[i] = H[i + (int64_t)j * ld] / S;
+}
+
 // FP32-basis thick-restart Lanczos for the FP32 phase of mixed precision
-// (ncv <= 16).  The matvec returns y = T v / S; CGS2 runs on y with FP32
-// data and FP64 reductions, and S is folded into H, so no large factor ever
-// enters FP32 storage.  Sweeps over the basis per step: dots, fused
-// update+dots, fused update+norm (3 instead of 4).
+// (ncv <= 16).  The matvec returns y = T v / S; the Gram-Schmidt runs on y
+// with FP32 data and FP64 reductions, and S is folded into H, so no large
+// factor ever enters FP32 storage.  Per step: alpha = v(j) . y (one dot over
+// two vectors), then y - alpha v(j) - H(0:j, j) v(0:j) with the known
+// couplings and the full re-orthogonalisation dots in one sweep over the
+// basis, and the correction with the norm in a second sweep (Lanczos with
+// full re-orthogonalisation; the first Gram-Schmidt pass of CGS2 is the
+// three-term recurrence itself).
 struct Lanczos32 {
   const Op& op;
   cudaStream_t s;
@@ -397,7 +409,9 @@ struct Lanczos32 {
   void step(int j) {
     S = apply_internal(op, nullptr, nullptr, v(j), Y.as<float>(), true, s);
     ++matvecs;
-    mdot_f32(v(0), ld, j + 1, Y.as<float>(), n, h1.as<double>(), part.as<double>(), s);
+    hprev32_kernel<<<1, 64, 0, s>>>(Hd.as<double>(), m + 1, j, S, h1.as<double>());
+    TM_CKK("hprev32");
+    mdot_f32(v(j), ld, 1, Y.as<float>(), n, h1.as<double>() + j, part.as<double>(), s);
     axpy_dot_f32(v(0), ld, j + 1, h1.as<double>(), Y.as<float>(), W.as<float>(), n, h2.as<double>(),
                  part.as<double>(), s);
     axpy_nrm_f32(v(0), ld, j + 1, h2.as<double>(), W.as<float>(), n, nsq.as<double>(), part.as<double>(), s);
@@ -663,6 +677,36 @@ __global__ void f64_to_f32_scaled_kernel(const double* __restrict__ in, double s
     out[i] = (float)(in[i] * scale);
 }
 
+// Y = R^-1 for the Cholesky factor G = R^T R of a k x k Gram matrix
+// (column-major, symmetrised): X R^-1 has orthonormal columns when G = X^T X.
+// Y column-major (Y[c*k + j] = (R^-1)(j, c)).  False when G is not
+// numerically positive definite.
+bool chol_qr_inverse(const std::vector<double>& Gin, int k, std::vector<double>& Y) {
+  std::vector<double> R((size_t)k * k, 0.0);  // R[c*k + r], r <= c
+  for (int c = 0; c < k; ++c) {
+    for (int r = 0; r <= c; ++r) {
+      double v = 0.5 * (Gin[(size_t)r + (size_t)c * k] + Gin[(size_t)c + (size_t)r * k]);
+      for (int t = 0; t < r; ++t) v -= R[(size_t)r * k + t] * R[(size_t)c * k + t];
+      if (r < c) {
+        R[(size_t)c * k + r] = v / R[(size_t)r * k + r];
+      } else {
+        if (!(v > 1e-8)) return false;
+        R[(size_t)c * k + c] = std::sqrt(v);
+      }
+    }
+  }
+  Y.assign((size_t)k * k, 0.0);
+  for (int c = 0; c < k; ++c) {
+    Y[(size_t)c * k + c] = 1.0 / R[(size_t)c * k + c];
+    for (int r = c - 1; r >= 0; --r) {
+      double v = 0.0;
+      for (int t = r + 1; t <= c; ++t) v += R[(size_t)t * k + r] * Y[(size_t)c * k + t];
+      Y[(size_t)c * k + r] = -v / R[(size_t)r * k + r];
+    }
+  }
+  return true;
+}
+
 // FP64-accurate refinement of the FP32 phase's Ritz pairs.
 //
 // On GB300 FP64 arithmetic runs at a small fraction of the FP32 rate, so the
@@ -792,7 +836,19 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   // X0 block (FP64-accurate products and dots) and its rows against every C
   // column
   auto set_x0 = [&](int nb) {
-    for (int j = 0; j < nev; ++j) {
+    if (nev <= 4) {
+      // X0^T [X0 | A X0 / S] in one sweep over XA
+      mdot_dd_gram(x0(0), ld, nev, 2 * nev, n, hd.as<double>(), dpart.as<double>(), s);
+      std::vector<double> gg((size_t)2 * nev * nev);
+      TM_CK(cudaMemcpyAsync(gg.data(), hd.p, gg.size() * 8, cudaMemcpyDeviceToHost, s));
+      host_sync();
+      for (int j = 0; j < nev; ++j)
+        for (int i = 0; i < nev; ++i) {
+          mm(i, j) = gg[(size_t)i + (size_t)j * nev];
+          g(i, j) = S * gg[(size_t)i + (size_t)(nev + j) * nev];
+        }
+    } else {
+      for (int j = 0; j < nev; ++j) {
       std::vector<double> h(nev), q(nev);
       mdot_dd(x0(0), ld, nev, ax0(j), n, hd.as<double>(), dpart.as<double>(), s);
       TM_CK(cudaMemcpyAsync(h.data(), hd.p, nev * 8, cudaMemcpyDeviceToHost, s));
@@ -803,6 +859,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       for (int i = 0; i < nev; ++i) {
         g(i, j) = S * h[i];
         mm(i, j) = q[i];
+      }
       }
     }
     for (int j = 0; j < nev; ++j)
@@ -977,53 +1034,89 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
       for (int k = 0; k < nk; ++k)
         TM_CK(cudaMemcpyAsync(f32col(B32, nb + k), R32.as<float>() + (size_t)keep[k] * ld, (size_t)n * 4,
                               cudaMemcpyDeviceToDevice, s));
-      std::vector<double> q0(nk, 0.0);
-      for (int k = 0; k < nk; ++k) {
-        nrm2sq_f32(f32col(B32, nb + k), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&q0[k], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-      }
+      std::vector<double> q0(nk, 0.0);  // squared norms before the projection
       F32Cols wc{};
       F32ColsMut wm{};
       for (int k = 0; k < nk; ++k) {
         wc.c[k] = f32col(B32, nb + k);
         wm.c[k] = f32col(B32, nb + k);
       }
-      // second pass only when the first removed a large part of a column
-      // ("twice is enough": a norm ratio below 1/sqrt(2))
-      for (int pass = 0; pass < 2; ++pass) {
-        mdot_block_f32(B32.as<float>(), ld, nb, wc, nk, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+      // Block Gram-Schmidt against the subspace, then Cholesky QR within the
+      // block.  One sweep gives [B | W]^T W: the couplings H = B^T W and the
+      // block's own Gram matrix; W -= B H is the second sweep.  The Gram
+      // matrix of the updated block follows as W^T W - H^T H (B orthonormal
+      // to FP32 accuracy), and a third sweep maps W to W R^-1.  A column whose
+      // norm the projection more than halves gets a second projection first
+      // ("twice is enough"), with the Gram matrix taken afresh.
+      const int nv = nb + nk;
+      auto block_dots = [&](std::vector<double>& g) {
+        mdot_block_f32(B32.as<float>(), ld, nv, wc, nk, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+        g.resize((size_t)48 * nk);
+        TM_CK(cudaMemcpyAsync(g.data(), Hd.p, g.size() * 8, cudaMemcpyDeviceToHost, s));
+        host_sync();
+      };
+      std::vector<double> gq;
+      block_dots(gq);
+      auto gram_after = [&](const std::vector<double>& g, std::vector<double>& gp) {
+        gp.assign((size_t)nk * nk, 0.0);
+        for (int a = 0; a < nk; ++a)
+          for (int b = 0; b < nk; ++b) {
+            double v = g[(size_t)48 * b + nb + a];
+            for (int i = 0; i < nb; ++i) v -= g[(size_t)48 * a + i] * g[(size_t)48 * b + i];
+            gp[(size_t)b * nk + a] = v;
+          }
+      };
+      std::vector<double> gp;
+      gram_after(gq, gp);
+      for (int k = 0; k < nk; ++k) q0[k] = gq[(size_t)48 * k + nb + k];
+      bool again = false;
+      for (int k = 0; k < nk; ++k)
+        if (!(gp[(size_t)k * nk + k] >= 0.5 * q0[k])) again = true;
+      maxpy_block_f32(B32.as<float>(), ld, nb, Hd.as<double>(), 48, wm, nk, n, s);
+      if (again) {
+        block_dots(gq);
+        gram_after(gq, gp);
         maxpy_block_f32(B32.as<float>(), ld, nb, Hd.as<double>(), 48, wm, nk, n, s);
-        if (pass == 1) break;
-        std::vector<double> q1(nk, 0.0);
-        for (int k = 0; k < nk; ++k) {
-          nrm2sq_f32(f32col(B32, nb + k), n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-          TM_CK(cudaMemcpyAsync(&q1[k], lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-        }
-        host_sync();
-        bool again = false;
-        for (int k = 0; k < nk; ++k)
-          if (!(q1[k] >= 0.5 * q0[k])) again = true;
-        if (!again) break;
       }
-      host_sync();
-      int pos = nb;
+      // Cholesky of the block's Gram matrix, dropping a column whose remaining
+      // norm is below 1e-10 of its norm before the projection (it adds no
+      // direction); Rk: the kept columns' triangular factor
+      std::vector<int> kept;
+      std::vector<double> Rk((size_t)nk * nk, 0.0);  // Rk[c * nk + r], r <= c, over kept indices
       for (int k = 0; k < nk; ++k) {
-        float* w = f32col(B32, nb + k);
-        if (pos < nb + k) {
-          TM_CK(cudaMemcpyAsync(f32col(B32, pos), w, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-          w = f32col(B32, pos);
+        const int c = (int)kept.size();
+        std::vector<double> col(c + 1, 0.0);
+        for (int r = 0; r < c; ++r) {
+          double v = gp[(size_t)k * nk + kept[r]];
+          for (int t = 0; t < r; ++t) v -= Rk[(size_t)r * nk + t] * col[t];
+          col[r] = v / Rk[(size_t)r * nk + r];
         }
-        for (int pass = 0; pass < 2 && pos > nb; ++pass) {
-          mdot_f32(f32col(B32, nb), ld, pos - nb, w, n, lz.h1.as<double>(), lz.part.as<double>(), s);
-          maxpy_f32(f32col(B32, nb), ld, pos - nb, lz.h1.as<double>(), w, n, s);
+        double d = gp[(size_t)k * nk + k];
+        for (int t = 0; t < c; ++t) d -= col[t] * col[t];
+        if (!(q0[k] > 0.0) || !(d > 1e-10 * q0[k])) continue;
+        col[c] = std::sqrt(d);
+        for (int r = 0; r <= c; ++r) Rk[(size_t)c * nk + r] = col[r];
+        kept.push_back(k);
+      }
+      const int nkept = (int)kept.size();
+      int pos = nb;
+      if (nkept > 0) {
+        // Y = R^-1 over the kept columns (back substitution), rows indexed by
+        // the block's columns: new column c = sum_k W_k Y[c * nk + k]
+        std::vector<double> Rinv((size_t)nkept * nkept, 0.0), Y((size_t)nk * nkept, 0.0);
+        for (int c = 0; c < nkept; ++c) {
+          Rinv[(size_t)c * nkept + c] = 1.0 / Rk[(size_t)c * nk + c];
+          for (int r = c - 1; r >= 0; --r) {
+            double v = 0.0;
+            for (int t = r + 1; t <= c; ++t) v += Rk[(size_t)t * nk + r] * Rinv[(size_t)c * nkept + t];
+            Rinv[(size_t)c * nkept + r] = -v / Rk[(size_t)r * nk + r];
+          }
         }
-        double q = 0.0;
-        nrm2sq_f32(w, n, lz.nsq.as<double>(), lz.part.as<double>(), s);
-        TM_CK(cudaMemcpyAsync(&q, lz.nsq.p, 8, cudaMemcpyDeviceToHost, s));
-        host_sync();
-        if (!(q0[k] > 0.0) || !(q > 1e-10 * q0[k])) continue;
-        normalize_f32(w, lz.nsq.as<double>(), w, n, s);
-        ++pos;
+        for (int c = 0; c < nkept; ++c)
+          for (int r = 0; r <= c; ++r) Y[(size_t)c * nk + kept[r]] = Rinv[(size_t)c * nkept + r];
+        TM_CK(cudaMemcpyAsync(hd.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
+        rotate_f32(f32col(B32, nb), ld, nk, hd.as<double>(), nkept, n, s);
+        pos = nb + nkept;
       }
       for (int j = nb; j < pos; ++j) prod32(f32col(B32, j), f32col(AB32, j));
       if (pos > nb) add_gcols(nb, pos - nb);
@@ -1087,6 +1180,23 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         fill_x0 = [lp, lzp, &r, nev](dfloat* X) {
           const int64_t ld = lzp->ld, nn = lzp->n;
           lp->ritz_dd(r, nev, X, ld);
+          if (nev <= 4) {
+            // Cholesky QR: one sweep for the Gram matrix G = X^T X (close to
+            // the identity), X <- X R^-1 in a second
+            DBuf gpart;
+            gpart.alloc(dd_part_bytes(32));
+            mdot_dd_gram(X, ld, nev, nev, nn, lzp->h1.as<double>(), gpart.as<double>(), lzp->s);
+            std::vector<double> G((size_t)nev * nev);
+            TM_CK(cudaMemcpyAsync(G.data(), lzp->h1.p, G.size() * 8, cudaMemcpyDeviceToHost, lzp->s));
+            TM_CK(cudaStreamSynchronize(lzp->s));
+            std::vector<double> Y;
+            if (chol_qr_inverse(G, nev, Y)) {
+              TM_CK(cudaMemcpyAsync(lzp->h2.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, lzp->s));
+              combine_dd_inplace(X, ld, nev, lzp->h2.as<double>(), nn, lzp->s);
+              TM_CK(cudaStreamSynchronize(lzp->s));
+              return;
+            }
+          }
           for (int i = 0; i < nev; ++i) {
             dfloat* xi = X + (int64_t)i * ld;
             for (int pass = 0; pass < 2 && i > 0; ++pass) {
@@ -1120,17 +1230,22 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         };
         lz.matvecs += l32->matvecs;
         lz.restarts += l32->restarts;
+        info.matvecs_phase1 = l32->matvecs;
       } else {
         lz.conv_tol = tol32;
         lz.stagnation_stop = true;
         r = lz.run(nev, true, 200, conv32, &ok);
         lz.stagnation_stop = false;
+        info.matvecs_phase1 = lz.matvecs;
         lz.rotate(r, nb0);
         Lanczos* lzp = &lz;
         fill_x0 = [lzp, nev](dfloat* X) {
           for (int i = 0; i < nev; ++i) f64_to_df(lzp->v(i), 1.0, X + (int64_t)i * lzp->ld, lzp->n, lzp->s);
         };
       }
+      TM_CK(cudaStreamSynchronize(s));
+      const auto t1 = std::chrono::steady_clock::now();
+      info.seconds_phase1 = std::chrono::duration<double>(t1 - t0).count();
       // FP64-accurate refinement (refine_mixed); leaves the best Ritz
       // vectors in V's leading columns either way
       std::vector<double> thv(nev);
@@ -1141,6 +1256,8 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
       const bool refined = run_refine && refine_mixed(op, lz, nev, nb0, tol, thv, max_resid, fill_x0, extras, info);
       if (!run_refine && x0_f64) x0_f64();
       if (!refined && info.refine_outcome == 0) info.refine_outcome = 3;
+      TM_CK(cudaStreamSynchronize(s));
+      info.seconds_refine = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
       if (refined) {
         theta = thv;
         done = true;
