@@ -167,7 +167,8 @@ tm_status tm_orbit_table(const tm_op* op, uint64_t* idx_host, uint16_t* dup_host
  * operators, Krylov-Schur Arnoldi for general ones.  FP64 Gram-Schmidt and
  * Rayleigh-Ritz on the device.
  *   nev       wanted eigenvalues (reference `neigs`)
- *   ncv       subspace size (0 = tm_suggested_ncv)
+ *   ncv       subspace size (0 = tm_suggested_ncv; in TM_EIGS_MIXED mode on a
+ *             symmetric operator at least 16, which costs fewer products)
  *   tol       relative residual tolerance
  *   seed      start vector uniform(0,1) from splitmix64(seed)
  *   mode      TM_EIGS_F64 or TM_EIGS_MIXED

@@ -470,7 +470,9 @@ void combine_f32_dd(const float* V, int64_t ldv, int m, const double* Y, int k, 
 void mdot_dd_block(const dfloat* V, int64_t ldv, int nv, const F32Cols& W, int nw, int64_t n, double* H, int64_t ldh,
                    double* part, cudaStream_t s) {
   if (nw < 1 || nw > 4) fail(TM_ERR_LIMIT, "mdot_dd_block: 1..4 vectors");
-  constexpr int KV = 8, NW = 4;
+  // four double-float columns per launch: 16 accumulators keep the kernel
+  // near 64 registers, so an SM holds enough warps to cover the loads
+  constexpr int KV = 4, NW = 4;
   const int nb = blocks_df(n);
   for (int k0 = 0; k0 < nv; k0 += KV) {
     const int kv = std::min(KV, nv - k0);

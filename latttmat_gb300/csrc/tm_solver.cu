@@ -378,11 +378,12 @@ struct Lanczos32 {
   cudaStream_t s;
   int64_t n, ld;  // vector length, basis leading dimension
   int m;
+  int mp;  // size of the current projection (m, or fewer after a mid-cycle stop)
   DBuf V, W, Y, h1, h2, part, nsq, Hd, wd, Zd, Ysel;
   int matvecs = 0, restarts = 0;
   bool stagnation_stop = true;
 
-  Lanczos32(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), ld(col_ld(o.n)), m(ncv) {
+  Lanczos32(const Op& o, int ncv, cudaStream_t st) : op(o), s(st), n(o.n), ld(col_ld(o.n)), m(ncv), mp(ncv) {
     V.alloc((size_t)(m + 1) * ld * 4);
     W.alloc((size_t)n * 4);
     Y.alloc((size_t)n * 4);
@@ -420,42 +421,43 @@ struct Lanczos32 {
     normalize_f32(W.as<float>(), nsq.as<double>(), v(j + 1), n, s);
   }
 
+  // Rayleigh-Ritz on the first mp basis vectors
   Lanczos::CycleResult project() {
     Lanczos::CycleResult r;
-    std::vector<double> th(m), H((size_t)(m + 1) * (m + 1));
-    r.Z.resize((size_t)m * m);
+    std::vector<double> th(mp), H((size_t)(m + 1) * (m + 1));
+    r.Z.resize((size_t)mp * mp);
     TM_CK(cudaMemcpyAsync(H.data(), Hd.p, H.size() * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaStreamSynchronize(s));
-    sym_eig_host(H.data(), m, m + 1, th.data(), r.Z.data());
-    r.beta = H[m + (size_t)(m - 1) * (m + 1)];
-    r.order.resize(m);
+    sym_eig_host(H.data(), mp, m + 1, th.data(), r.Z.data());
+    r.beta = H[mp + (size_t)(mp - 1) * (m + 1)];
+    r.order.resize(mp);
     std::iota(r.order.begin(), r.order.end(), 0);
     std::stable_sort(r.order.begin(), r.order.end(),
                      [&](int a, int b) { return std::fabs(th[a]) > std::fabs(th[b]); });
-    for (int i = 0; i < m; ++i) {
+    for (int i = 0; i < mp; ++i) {
       int c = r.order[i];
       r.theta.push_back(th[c]);
-      r.resid.push_back(std::fabs(r.beta * r.Z[(size_t)c * m + (m - 1)]));
+      r.resid.push_back(std::fabs(r.beta * r.Z[(size_t)c * mp + (mp - 1)]));
     }
     return r;
   }
 
   std::vector<double> ysel(const Lanczos::CycleResult& r, int k) const {
-    std::vector<double> Y((size_t)m * k);
+    std::vector<double> Y((size_t)mp * k);
     for (int c = 0; c < k; ++c)
-      for (int j = 0; j < m; ++j) Y[(size_t)c * m + j] = r.Z[(size_t)r.order[c] * m + j];
+      for (int j = 0; j < mp; ++j) Y[(size_t)c * mp + j] = r.Z[(size_t)r.order[c] * mp + j];
     return Y;
   }
 
   void restart(const Lanczos::CycleResult& r, int k) {
     std::vector<double> Yh = ysel(r, k);
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    rotate_f32(V.as<float>(), ld, m, Ysel.as<double>(), k, n, s);
-    TM_CK(cudaMemcpyAsync(v(k), v(m), (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    rotate_f32(V.as<float>(), ld, mp, Ysel.as<double>(), k, n, s);
+    TM_CK(cudaMemcpyAsync(v(k), v(mp), (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0);
     for (int i = 0; i < k; ++i) {
       H[i + (size_t)i * (m + 1)] = r.theta[i];
-      double cpl = r.beta * r.Z[(size_t)r.order[i] * m + (m - 1)];
+      double cpl = r.beta * r.Z[(size_t)r.order[i] * mp + (mp - 1)];
       H[k + (size_t)i * (m + 1)] = cpl;
       H[i + (size_t)k * (m + 1)] = cpl;
     }
@@ -465,11 +467,11 @@ struct Lanczos32 {
 
   // Ritz vectors first .. first+k-1 as FP32 columns (leading dimension ld)
   void ritz_f32(const Lanczos::CycleResult& r, int first, int k, float* out) {
-    std::vector<double> Yh((size_t)m * k);
+    std::vector<double> Yh((size_t)mp * k);
     for (int c = 0; c < k; ++c)
-      for (int j = 0; j < m; ++j) Yh[(size_t)c * m + j] = r.Z[(size_t)r.order[first + c] * m + j];
+      for (int j = 0; j < mp; ++j) Yh[(size_t)c * mp + j] = r.Z[(size_t)r.order[first + c] * mp + j];
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    combine_f32(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ld, n, s);
+    combine_f32(V.as<float>(), ld, mp, Ysel.as<double>(), k, out, ld, n, s);
   }
 
   // Products of Ritz vectors first .. first+k-1 from the Lanczos relation
@@ -477,13 +479,13 @@ struct Lanczos32 {
   // A x / S = V_{m+1} [theta y; beta y_m] / S with no product of the
   // operator (FP32 columns, leading dimension ld).
   void ritz_f32_prod(const Lanczos::CycleResult& r, int first, int k, float* out) {
-    const int m1 = m + 1;
+    const int m1 = mp + 1;
     std::vector<double> Yh((size_t)m1 * k);
     for (int c = 0; c < k; ++c) {
       const int col = r.order[first + c];
       const double th = r.theta[first + c];
-      for (int j = 0; j < m; ++j) Yh[(size_t)c * m1 + j] = th * r.Z[(size_t)col * m + j] / S;
-      Yh[(size_t)c * m1 + m] = r.beta * r.Z[(size_t)col * m + (m - 1)] / S;
+      for (int j = 0; j < mp; ++j) Yh[(size_t)c * m1 + j] = th * r.Z[(size_t)col * mp + j] / S;
+      Yh[(size_t)c * m1 + mp] = r.beta * r.Z[(size_t)col * mp + (mp - 1)] / S;
     }
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
     combine_f32(V.as<float>(), ld, m1, Ysel.as<double>(), k, out, ld, n, s);
@@ -493,14 +495,14 @@ struct Lanczos32 {
   void ritz_dd(const Lanczos::CycleResult& r, int k, dfloat* out, int64_t ldo) {
     std::vector<double> Yh = ysel(r, k);
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    combine_f32_dd(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ldo, n, s);
+    combine_f32_dd(V.as<float>(), ld, mp, Ysel.as<double>(), k, out, ldo, n, s);
   }
 
   // FP64 Ritz vectors: out[:, c] = V32 * Z[:, order[c]], c < k (leading dimension ldo)
   void ritz_f64(const Lanczos::CycleResult& r, int k, double* out, int64_t ldo) {
     std::vector<double> Yh = ysel(r, k);
     TM_CK(cudaMemcpyAsync(Ysel.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    combine_f32_f64(V.as<float>(), ld, m, Ysel.as<double>(), k, out, ldo, n, s);
+    combine_f32_f64(V.as<float>(), ld, mp, Ysel.as<double>(), k, out, ldo, n, s);
   }
 
   template <class Conv>
@@ -510,7 +512,19 @@ struct Lanczos32 {
     double best = 1e300;
     int stall = 0;
     for (int cyc = 0; cyc < max_cycles; ++cyc) {
-      for (int j = k; j < m; ++j) step(j);
+      // once the previous cycle came within reach of the FP32 floor, test
+      // after every step (a Rayleigh-Ritz of the first j + 1 vectors), so the
+      // phase stops at the first product that gets there
+      const bool each = cyc > 0 && best <= 5e-5;
+      for (int j = k; j < m; ++j) {
+        step(j);
+        if (each && j + 1 < m && j + 1 > nev + 1) {
+          mp = j + 1;
+          r = project();
+          if (conv(r)) return r;
+        }
+      }
+      mp = m;
       r = project();
       if (conv(r)) return r;
       double worst = 0.0;
@@ -808,27 +822,25 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     }
   };
   // C columns j0 .. j0+cnt-1 (cnt <= 4) against columns 0 .. j0+cnt-1: one
-  // sweep over B32 gives b . A w and b . w for the whole block.  The C-C
-  // block enters the wanted pairs at second order, so one side of the
-  // symmetric product suffices.
+  // sweep over B32 gives b . A w for the whole block.  The C-C blocks enter
+  // the wanted pairs at second order: one side of the symmetric product
+  // suffices, and the C-C Gram block is the identity (C is orthonormal to
+  // FP32 accuracy, ~1e-6, which moves the wanted pairs by ~1e-6 of the
+  // squared C weights, ~1e-14).
   auto add_gcols = [&](int j0, int cnt) {
     const int nv = j0 + cnt;
     F32Cols w1{};
-    for (int c = 0; c < cnt; ++c) {
-      w1.c[c] = f32col(AB32, j0 + c);
-      w1.c[cnt + c] = f32col(B32, j0 + c);
-    }
-    mdot_block_f32(B32.as<float>(), ld, nv, w1, 2 * cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
-    std::vector<double> h((size_t)48 * 2 * cnt);
+    for (int c = 0; c < cnt; ++c) w1.c[c] = f32col(AB32, j0 + c);
+    mdot_block_f32(B32.as<float>(), ld, nv, w1, cnt, n, Hd.as<double>(), 48, bpart.as<double>(), s);
+    std::vector<double> h((size_t)48 * cnt);
     TM_CK(cudaMemcpyAsync(h.data(), Hd.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
     for (int c = 0; c < cnt; ++c) {
       const int j = j0 + c;
-      const double* gl = &h[(size_t)48 * c];          // b_i . A b_j / S
-      const double* mc = &h[(size_t)48 * (cnt + c)];  // b_i . b_j
+      const double* gl = &h[(size_t)48 * c];  // b_i . A b_j / S
       for (int i = nev; i <= j; ++i) {
         g(i, j) = g(j, i) = S * gl[i];
-        mm(i, j) = mm(j, i) = mc[i];
+        mm(i, j) = mm(j, i) = (i == j) ? 1.0 : 0.0;
       }
     }
     x0_rows(j0, cnt);
@@ -1020,14 +1032,14 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     force_grow = false;
     if (verified >= 3 || round + 1 >= 3 * kRefineRounds || nb + nev > cap) break;
     // grow: the residuals of the wanted pairs not yet well converged (all of
-    // them if none is left), block FP32 Gram-Schmidt (two passes) against the
-    // subspace, then within the block; FP32 products; a column that vanishes
-    // is dropped.  A residual already below 5% of the tolerance adds little,
-    // and its product costs as much as any other.
+    // them if none is left), orthonormalised against the subspace and within
+    // the block; FP32 products; a column that vanishes is dropped.  A residual
+    // already below a quarter of the tolerance (half of it is accepted) adds
+    // little, and its product costs as much as any other.
     {
       std::vector<int> keep;
       for (int c = 0; c < nev; ++c)
-        if (!(rn[c] <= 0.05 * tol * std::fabs(thv[c]))) keep.push_back(c);
+        if (!(rn[c] <= 0.25 * tol * std::fabs(thv[c]))) keep.push_back(c);
       if (keep.empty())
         for (int c = 0; c < nev; ++c) keep.push_back(c);
       const int nk = (int)keep.size();
@@ -1134,7 +1146,14 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
   cudaStream_t s = op.stream;
   const int64_t n = op.n;
   if (nev < 1 || nev >= n) fail(TM_ERR_ARG, "nev must satisfy 1 <= nev < rows");
-  if (ncv <= 0) ncv = (nev > 4) ? 2 * nev + 1 : 2 * nev + 3;
+  // The reference's rule (suggested_nev); the mixed mode takes at least 16
+  // columns: its FP32 phase keeps more Ritz vectors next to the wanted ones,
+  // and the refinement resolves the wanted ones against them in fewer rounds
+  // (L = 32 headline: 41 products against 45 with 11 columns).
+  if (ncv <= 0) {
+    ncv = (nev > 4) ? 2 * nev + 1 : 2 * nev + 3;
+    if (mode == TM_EIGS_MIXED) ncv = std::max(ncv, std::min(NV32, 2 * nev + 8));
+  }
   if (ncv >= n) ncv = (int)n - 1;
   if (ncv > 46) ncv = 46;
   if (ncv <= nev) fail(TM_ERR_ARG, "ncv must exceed nev");
@@ -1154,13 +1173,16 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
     bool ok = false;
     Lanczos::CycleResult r;
     if (mixed) {
-      // FP32 phase: Ritz residuals down to the FP32 floor (relative to the
-      // dominant Ritz value), stopping early if they stagnate
+      // FP32 phase: Ritz residuals down to the FP32 floor, relative to each
+      // wanted Ritz value (but no further than 1e-8 of the dominant one),
+      // stopping early if they stagnate.  A wanted pair that stops short of
+      // the floor costs the refinement more than the Lanczos steps that
+      // would have taken it there.
       const double tol32 = std::max(tol, 2e-7);
-      const int nb0 = std::max(nev, ncv - 1);
+      int nb0 = std::max(nev, ncv - 1);
       auto conv32 = [&](const Lanczos::CycleResult& rr) {
         for (int i = 0; i < nev; ++i)
-          if (rr.resid[i] > tol32 * std::fabs(rr.theta[0])) return false;
+          if (rr.resid[i] > tol32 * std::max(std::fabs(rr.theta[i]), 0.05 * std::fabs(rr.theta[0]))) return false;
         return true;
       };
       std::unique_ptr<Lanczos32> l32;
@@ -1172,6 +1194,7 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
         l32.reset(new Lanczos32(op, ncv, s));
         l32->start(seed);
         r = l32->run(nev, 200, conv32);
+        nb0 = std::min(nb0, l32->mp);  // a mid-cycle stop leaves fewer Ritz vectors
         // the wanted Ritz vectors in double-float for the refinement,
         // re-orthonormalised (CGS2): the FP32 basis is orthonormal to FP32
         // accuracy only
