@@ -210,6 +210,84 @@ __device__ __forceinline__ void reg_bfly_f2(float2 (&v)[1 << (NB - 1)], float r,
   }
 }
 
+// Double-float values two to a lane pair: hi words in one float2, lo words in
+// another.  df2_fma_unnorm is df_fma_unnorm (tm_df.cuh) on both lanes with the
+// same operation sequence (so the same results), on the packed FP32 pipes;
+// differences are taken as fma(b, -1, a), and -p comes from -r.hi, so no
+// operand needs a separate negation.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ void df2_fma_unnorm(float2 rh, float2 rl, float2 rhn, float2 xh, float2 xl, float2 yh,
+                                               float2 yl, float2& oh, float2& ol) {
+  const float2 np = __fmul2_rn(rhn, xh);  // -p, p = r.hi x.hi
+  float2 pe = __ffma2_rn(rh, xh, np);     // r.hi x.hi - p (exact)
+  pe = __ffma2_rn(rh, xl, pe);
+  pe = __ffma2_rn(rl, xh, pe);
+  const float2 sm = sub2(yh, np);            // p + y.hi
+  const float2 bb = __fadd2_rn(sm, np);      // s - p
+  const float2 t = sub2(sm, bb);             // s - bb
+  const float2 e2 = sub2(yh, bb);            // y.hi - bb
+  const float2 se = sub2(e2, __fadd2_rn(np, t));  // (p - (s - bb)) + (y.hi - bb)
+  oh = sm;
+  ol = __fadd2_rn(se, __fadd2_rn(pe, yl));
+}
+
+// reg_bfly for double-float values held as (hi pair, lo pair) per two
+// elements: level 0 within a pair (scalar), every higher level on whole
+// pairs, then one renormalisation per element
+template <int NB>
+__device__ __forceinline__ void reg_bfly_df2(float2 (&h)[1 << (NB - 1)], float2 (&l)[1 << (NB - 1)], dfloat r,
+                                             int swap) {
+  const float2 rh = make_float2(r.hi, r.hi), rl = make_float2(r.lo, r.lo), rhn = make_float2(-r.hi, -r.hi);
+  if (!swap) {
+#pragma unroll
+    for (int k = 0; k < (1 << (NB - 1)); ++k) {
+      const dfloat x0(h[k].x, l[k].x), x1(h[k].y, l[k].y);
+      const dfloat o0 = df_fma_unnorm(r, x1, x0), o1 = df_fma_unnorm(r, x0, x1);
+      h[k] = make_float2(o0.hi, o1.hi);
+      l[k] = make_float2(o0.lo, o1.lo);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < (1 << (NB - 1)); ++k) {
+      const dfloat x0(h[k].x, l[k].x), x1(h[k].y, l[k].y);
+      const dfloat o0 = df_fma_unnorm(r, x0, x1), o1 = df_fma_unnorm(r, x1, x0);
+      h[k] = make_float2(o0.hi, o1.hi);
+      l[k] = make_float2(o0.lo, o1.lo);
+    }
+  }
+  // no swap: (a + r b, b + r a); swap: (b + r a, a + r b)
+  if (!swap) {
+#pragma unroll
+    for (int lv = 1; lv < NB; ++lv)
+#pragma unroll
+      for (int k = 0; k < (1 << (NB - 1)); ++k)
+        if (!(k & (1 << (lv - 1)))) {
+          const int k1 = k | (1 << (lv - 1));
+          const float2 ah = h[k], al = l[k], bh = h[k1], bl = l[k1];
+          df2_fma_unnorm(rh, rl, rhn, bh, bl, ah, al, h[k], l[k]);
+          df2_fma_unnorm(rh, rl, rhn, ah, al, bh, bl, h[k1], l[k1]);
+        }
+  } else {
+#pragma unroll
+    for (int lv = 1; lv < NB; ++lv)
+#pragma unroll
+      for (int k = 0; k < (1 << (NB - 1)); ++k)
+        if (!(k & (1 << (lv - 1)))) {
+          const int k1 = k | (1 << (lv - 1));
+          const float2 ah = h[k], al = l[k], bh = h[k1], bl = l[k1];
+          df2_fma_unnorm(rh, rl, rhn, ah, al, bh, bl, h[k], l[k]);
+          df2_fma_unnorm(rh, rl, rhn, bh, bl, ah, al, h[k1], l[k1]);
+        }
+  }
+  // renormalise: hi' = hi + lo, lo' = lo - (hi' - hi)
+#pragma unroll
+  for (int k = 0; k < (1 << (NB - 1)); ++k) {
+    const float2 s2 = __fadd2_rn(h[k], l[k]);
+    l[k] = sub2(l[k], sub2(s2, h[k]));
+    h[k] = s2;
+  }
+}
+
 // asynchronous global->shared copy of one element (cp.async, sm_80+): the
 // gathers of a tile are all in flight at once without holding registers
 template <int SZ>
@@ -253,6 +331,20 @@ __device__ __forceinline__ void smem_round(T* sm, int n, T r, int swap) {
       for (int k = 0; k < (1 << (GS - 1)); ++k) {
         b[spad((2 * k) << G0)] = v[k].x;
         b[spad((2 * k + 1) << G0)] = v[k].y;
+      }
+    } else if constexpr (std::is_same<T, dfloat>::value && GS >= 2) {
+      float2 h[1 << (GS - 1)], l[1 << (GS - 1)];
+#pragma unroll
+      for (int k = 0; k < (1 << (GS - 1)); ++k) {
+        const dfloat a = b[spad((2 * k) << G0)], c = b[spad((2 * k + 1) << G0)];
+        h[k] = make_float2(a.hi, c.hi);
+        l[k] = make_float2(a.lo, c.lo);
+      }
+      reg_bfly_df2<GS>(h, l, r, swap);
+#pragma unroll
+      for (int k = 0; k < (1 << (GS - 1)); ++k) {
+        b[spad((2 * k) << G0)] = dfloat(h[k].x, l[k].x);
+        b[spad((2 * k + 1) << G0)] = dfloat(h[k].y, l[k].y);
       }
     } else {
       T v[1 << GS];
