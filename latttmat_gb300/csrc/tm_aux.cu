@@ -52,7 +52,7 @@ __device__ __forceinline__ int64_t chain_pass_blocks_dev(const ChainPass& cp);
 __device__ __forceinline__ double fold_part(float x) { return (double)x; }
 __device__ __forceinline__ double fold_part(double x) { return x; }
 __device__ __forceinline__ double fold_part(dfloat x) { return (double)x; }
-__device__ __forceinline__ double fold_part(tangent x) { return x.d; }
+__device__ __forceinline__ double fold_part(tangent x) { return (double)x.d; }
 
 // byte offset of the fold accumulators in chain_kernel's shared memory
 __host__ __device__ __forceinline__ size_t chain_acc_offset(int tile, size_t elem) {
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(256) contract_batch_kernel(const ChainInst* __
   if (kmi.y != MODE) return;
   const int64_t r0 = ((int64_t)blockIdx.x - rstart[s_i]) * kSweepRows;
   const int64_t r1 = min(r0 + (int64_t)kSweepRows, I.n);
-  const double gs = (MODE == kModeF32) ? I.gs32 : (MODE == kModeDF ? I.gsdf : (MODE == kModeF64 ? I.gs64 : 1.0));
+  const double gs = (MODE == kModeF32) ? I.gs32 : (MODE == kModeF64 ? I.gs64 : I.gsdf);  // tangent steps as DF
   const IO* z = reinterpret_cast<const IO*>(I.fold);
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const double f = I.idx ? (double)z[I.idx[r]] * (double)I.dup[r] : (double)z[r] * I.nf;
@@ -629,8 +629,9 @@ double matvec_aux_dir(const Op& op, const IO* x, IO* y, bool scaled, int dir, cu
   const bool zb = (op.kind == K_ZBT || op.kind == K_ZBM);
   AuxCoef c64 = coef_of(op);
   const double gb = step_bound(op, c64, dir);
-  // FP32 and double-float steps are normalised (FP32 exponent range)
-  const bool norm = (sizeof(T) == 4) || std::is_same<T, dfloat>::value;
+  // FP32 and double-float steps (tangent pairs included) are normalised
+  // (FP32 exponent range)
+  const bool norm = (sizeof(T) == 4) || std::is_same<T, dfloat>::value || std::is_same<T, tangent>::value;
   AuxCoefT<T> c;
   for (int k = 0; k < 2; ++k) {
     c.b1[k] = coef_with_derivative<T>(c64.b1[k], dcoef ? dcoef->b1[k] : 0.0);
@@ -720,7 +721,7 @@ void chain_inst_fill(const Op& op, int dir, ChainInst& rec, int tb4, int tb8) {
       rec.ctan[t].b2[q] = tangent(c.b2[q], db.b2[q]);
       rec.ctan[t].b3[q] = tangent(c.b3[q], db.b3[q]);
     }
-    rec.ctan[t].g = tangent(1.0);
+    rec.ctan[t].g = tangent(1.0 / gb);  // a constant: no derivative
   }
   rec.kind = op.kind;
   rec.bj = op.mp.betaJ;

@@ -88,23 +88,27 @@ __device__ __forceinline__ dfloat& operator*=(dfloat& a, dfloat b) {
 
 // Forward-mode tangent pair (value, derivative with respect to one
 // parameter): the adjoint's tangent products of the aux-bit chains run the
-// chain steps in this type, d(a b) = da b + a db, d(a + b) = da + db.
+// chain steps in this type, d(a b) = da b + a db, d(a + b) = da + db.  Both
+// parts are double-float, so the products run on the FP32 pipes at
+// FP64-level accuracy (~1e-14), in the FP32 exponent range (the chains
+// normalise their steps as the other double-float products do).
 struct __align__(16) tangent {
-  double v, d;
+  dfloat v, d;
   __host__ __device__ tangent() {}
   __host__ __device__ tangent(double x) : v(x), d(0.0) {}
   __host__ __device__ tangent(double x, double dx) : v(x), d(dx) {}
+  __host__ __device__ tangent(dfloat x, dfloat dx) : v(x), d(dx) {}
 };
 
-__host__ __device__ __forceinline__ tangent operator+(tangent a, tangent b) { return tangent(a.v + b.v, a.d + b.d); }
-__host__ __device__ __forceinline__ tangent operator*(tangent a, tangent b) {
-  return tangent(a.v * b.v, a.d * b.v + a.v * b.d);
+__device__ __forceinline__ tangent operator+(tangent a, tangent b) { return tangent(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ tangent operator*(tangent a, tangent b) {
+  return tangent(a.v * b.v, df_fma(a.d, b.v, a.v * b.d));
 }
-__host__ __device__ __forceinline__ tangent& operator+=(tangent& a, tangent b) {
+__device__ __forceinline__ tangent& operator+=(tangent& a, tangent b) {
   a = a + b;
   return a;
 }
-__host__ __device__ __forceinline__ tangent& operator*=(tangent& a, tangent b) {
+__device__ __forceinline__ tangent& operator*=(tangent& a, tangent b) {
   a = a * b;
   return a;
 }
