@@ -206,9 +206,11 @@ __global__ void __launch_bounds__(256) sw_rotate(const ChainInst* __restrict__ i
       if (q < m) v[q] = I.V[(int64_t)q * I.ldv + r];
     for (int c = 0; c < rp.x; ++c) {
       double acc = 0.0;
+      // zero coefficients are skipped: after a mid-cycle stop the columns
+      // past the member's last step may never have been written
 #pragma unroll
       for (int q = 0; q < kSweepMaxM; ++q)
-        if (q < m) acc = fma(v[q], Ws[c * m + q], acc);
+        if (q < m && Ws[c * m + q] != 0.0) acc = fma(v[q], Ws[c * m + q], acc);
       I.V[(int64_t)c * I.ldv + r] = acc;
     }
     if (rp.y) I.V[(int64_t)rp.x * I.ldv + r] = I.V[(int64_t)m * I.ldv + r];
@@ -704,9 +706,51 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode, double* cons
         if (kmh[q].y == kModeIdle) continue;
         mb.info.matvecs += 1;
         if (mb.phase != kModeF32) mb.info.matvecs_f64 += 1;
-        if (++mb.j < m) continue;  // basis not full yet
-        // end of this member's cycle: project, test, restart
         double* Hh = sch.data() + (size_t)q * kScStride + kScH;
+        if (++mb.j < m) {
+          // In the final phase, test the pairs after every step once the
+          // basis holds a few vectors (a Rayleigh-Ritz of the first j
+          // columns), so a member whose start vector was already accurate
+          // stops at the first step that converges it.
+          const int jc = mb.j;
+          if (mb.phase != final_phase || jc < std::min(m - 1, nev + 4)) continue;
+          try {
+            std::vector<double> Hj((size_t)(jc + 1) * jc);
+            for (int c = 0; c < jc; ++c)
+              for (int i = 0; i <= jc; ++i) Hj[i + (size_t)c * (jc + 1)] = Hh[i + (size_t)c * (m + 1)];
+            const Ritz R = krylov_project(Hj.data(), jc, nev);
+            bool ok = true;
+            double mr = 0.0;
+            for (int i = 0; i < nev; ++i) {
+              const double ai = std::max(std::abs(R.theta[i]), 1e-300);
+              if (!(R.resid[i] <= tol * ai)) ok = false;
+              mr = std::max(mr, R.resid[i] / ai);
+            }
+            if (!ok) continue;
+            mb.done = true;
+            mb.info.nconv = nev;
+            mb.info.max_resid = mr;
+            mb.vals.assign(R.theta.begin(), R.theta.begin() + nev);
+            if (vec_out && vec_out[W.a + q]) {
+              const std::vector<std::complex<double>>& y0 = R.y[0];
+              int kmax = 0;
+              for (int i = 1; i < jc; ++i)
+                if (std::abs(y0[i]) > std::abs(y0[kmax])) kmax = i;
+              const std::complex<double> ph = std::conj(y0[kmax]) / std::max(std::abs(y0[kmax]), 1e-300);
+              double* Wq = Wh.data() + (size_t)q * m * m;
+              for (int i = 0; i < m; ++i) Wq[i] = (i < jc) ? (y0[i] * ph).real() : 0.0;
+              roth[q] = make_int2(1, 0);
+              fl[q] = 1;
+              any_rot = any_start = true;
+              extract.push_back(q);
+            }
+          } catch (const Failure& f) {
+            mb.status = f.code;
+            mb.msg = f.msg;
+          }
+          continue;
+        }
+        // end of this member's cycle: project, test, restart
         ++mb.cycles;
         try {
           const int kvec = krylov_kvec(m, nev);
