@@ -708,25 +708,48 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode, double* cons
         if (mb.phase != kModeF32) mb.info.matvecs_f64 += 1;
         double* Hh = sch.data() + (size_t)q * kScStride + kScH;
         if (++mb.j < m) {
-          // In the final phase, test the pairs after every step once the
-          // basis holds a few vectors (a Rayleigh-Ritz of the first j
-          // columns), so a member whose start vector was already accurate
-          // stops at the first step that converges it.
+          // Once the basis holds a few vectors, test the pairs after every
+          // step (a Rayleigh-Ritz of the first j columns): a member in its
+          // final phase stops at the first step that converges it, and one in
+          // the FP32 phase moves on to the final phase as soon as it reaches
+          // the FP32 floor.
           const int jc = mb.j;
-          if (mb.phase != final_phase || jc < std::min(m - 1, nev + 4)) continue;
+          if (mb.cycles == 0 && mb.phase != final_phase) continue;  // the FP32 phase's first cycle runs whole
+          if (jc < std::min(m - 1, nev + 4)) continue;
           try {
             std::vector<double> Hj((size_t)(jc + 1) * jc);
             for (int c = 0; c < jc; ++c)
               for (int i = 0; i <= jc; ++i) Hj[i + (size_t)c * (jc + 1)] = Hh[i + (size_t)c * (m + 1)];
             const Ritz R = krylov_project(Hj.data(), jc, nev);
+            const bool f32 = (mb.phase != final_phase);
+            const double ref = std::max(std::abs(R.theta[0]), 1e-300);
             bool ok = true;
             double mr = 0.0;
             for (int i = 0; i < nev; ++i) {
               const double ai = std::max(std::abs(R.theta[i]), 1e-300);
-              if (!(R.resid[i] <= tol * ai)) ok = false;
+              if (!(R.resid[i] <= (f32 ? tol32 * ref : tol * ai))) ok = false;
               mr = std::max(mr, R.resid[i] / ai);
             }
             if (!ok) continue;
+            double* Wq = Wh.data() + (size_t)q * m * m;
+            if (f32) {
+              // restart the final phase from the wanted Ritz vectors' real
+              // parts (as at the end of a cycle)
+              for (int i = 0; i < m; ++i) {
+                double acc = 0.0;
+                if (i < jc)
+                  for (int c = 0; c < nev; ++c) acc += R.y[c][i].real();
+                Wq[i] = acc;
+              }
+              roth[q] = make_int2(1, 0);
+              fl[q] = 1;
+              std::fill(Hh, Hh + (m + 1) * (m + 1), 0.0);
+              mb.phase = final_phase;
+              mb.j = 0;
+              mb.cycles = 0;
+              any_rot = any_start = true;
+              continue;
+            }
             mb.done = true;
             mb.info.nconv = nev;
             mb.info.max_resid = mr;
@@ -737,7 +760,6 @@ void sweep_solve(Sweep& sw, int nev, int ncv, double tol, int mode, double* cons
               for (int i = 1; i < jc; ++i)
                 if (std::abs(y0[i]) > std::abs(y0[kmax])) kmax = i;
               const std::complex<double> ph = std::conj(y0[kmax]) / std::max(std::abs(y0[kmax]), 1e-300);
-              double* Wq = Wh.data() + (size_t)q * m * m;
               for (int i = 0; i < m; ++i) Wq[i] = (i < jc) ? (y0[i] * ph).real() : 0.0;
               roth[q] = make_int2(1, 0);
               fl[q] = 1;
