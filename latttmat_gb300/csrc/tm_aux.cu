@@ -54,6 +54,13 @@ __device__ __forceinline__ double fold_part(double x) { return x; }
 __device__ __forceinline__ double fold_part(dfloat x) { return (double)x; }
 __device__ __forceinline__ double fold_part(tangent x) { return (double)x.d; }
 
+// acc + a b in the chain's arithmetic: one renormalisation for double-float
+// (df_fma) instead of one per multiply and add
+__device__ __forceinline__ float mad_t(float a, float b, float acc) { return fmaf(a, b, acc); }
+__device__ __forceinline__ double mad_t(double a, double b, double acc) { return fma(a, b, acc); }
+__device__ __forceinline__ dfloat mad_t(dfloat a, dfloat b, dfloat acc) { return df_fma(a, b, acc); }
+__device__ __forceinline__ tangent mad_t(tangent a, tangent b, tangent acc) { return acc + a * b; }
+
 // byte offset of the fold accumulators in chain_kernel's shared memory
 __host__ __device__ __forceinline__ size_t chain_acc_offset(int tile, size_t elem) {
   return (((size_t)(tile + tile / 32 + 1) * elem) + 15) & ~(size_t)15;
@@ -248,7 +255,7 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
             const T w0 = wr[sv * 2], w1 = wr[sv * 2 + 1];
             T* bo = sv ? b1p : b0;
 #pragma unroll
-            for (int a = 0; a < 2; ++a) bo[a] = (ur[sv * 2 + a] * z) * (w0 * in[0][a] + w1 * in[1][a]);
+            for (int a = 0; a < 2; ++a) bo[a] = (ur[sv * 2 + a] * z) * mad_t(w1, in[1][a], w0 * in[0][a]);
           }
         } else {
           // BNNNI: out((pl,pr), (sl,sr)) = z_f[s'] u[a'][s'] sum_q w[s'][q] in(q, a')
@@ -270,9 +277,9 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
 #pragma unroll
               for (int aux = 0; aux < 4; ++aux) {
                 T d = in[0][aux] * w0;
-                d += in[1][aux] * w1;
-                d += in[2][aux] * w2;
-                d += in[3][aux] * w3;
+                d = mad_t(in[1][aux], w1, d);
+                d = mad_t(in[2][aux], w2, d);
+                d = mad_t(in[3][aux], w3, d);
                 bp[sv][aux] = zu[aux] * d;
               }
             } else {
@@ -281,9 +288,9 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
 #pragma unroll
               for (int aux = 0; aux < 4; ++aux) {
                 T d = in[0][aux] * w0;
-                d += in[1][aux] * w1;
-                d += in[2][aux] * w2;
-                d += in[3][aux] * w3;
+                d = mad_t(in[1][aux], w1, d);
+                d = mad_t(in[2][aux], w2, d);
+                d = mad_t(in[3][aux], w3, d);
                 bp[sv][aux] = (ur[sv * 4 + aux] * z) * d;
               }
             }
