@@ -61,6 +61,38 @@ __device__ __forceinline__ double mad_t(double a, double b, double acc) { return
 __device__ __forceinline__ dfloat mad_t(dfloat a, dfloat b, dfloat acc) { return df_fma(a, b, acc); }
 __device__ __forceinline__ tangent mad_t(tangent a, tangent b, tangent acc) { return acc + a * b; }
 
+// Double-float values two to a lane pair (hi words in one float2, lo words
+// in another), for the double-float BNNNI steps on the packed FP32 pipes.
+// Each is the scalar double-float operation of tm_df.cuh lane by lane, in
+// the same operation order; differences are fma(b, -1, a), and -p comes from
+// the weight's negated hi word, so no operand needs a separate negation.
+__device__ __forceinline__ float2 dsub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// x * w (operator*): w = (wh, wl) with wn = -wh
+__device__ __forceinline__ void df2_mul(float2 xh, float2 xl, float2 wh, float2 wl, float2 wn, float2& oh,
+                                       float2& ol) {
+  const float2 np = __fmul2_rn(xh, wn);  // -p
+  float2 e = __ffma2_rn(xh, wh, np);
+  e = __ffma2_rn(xh, wl, e);
+  e = __ffma2_rn(xl, wh, e);
+  oh = dsub2(e, np);                        // p + e
+  ol = dsub2(e, __fadd2_rn(oh, np));        // e - (h - p)
+}
+// x * w + y (df_fma)
+__device__ __forceinline__ void df2_fma(float2 xh, float2 xl, float2 wh, float2 wl, float2 wn, float2 yh, float2 yl,
+                                       float2& oh, float2& ol) {
+  const float2 np = __fmul2_rn(xh, wn);  // -p
+  float2 pe = __ffma2_rn(xh, wh, np);
+  pe = __ffma2_rn(xh, wl, pe);
+  pe = __ffma2_rn(xl, wh, pe);
+  const float2 sm = dsub2(yh, np);                     // p + y.hi
+  const float2 bb = __fadd2_rn(sm, np);                // s - p
+  const float2 e2 = dsub2(yh, bb);                     // y.hi - bb
+  float2 se = dsub2(e2, __fadd2_rn(np, dsub2(sm, bb)));  // (p - (s - bb)) + (y.hi - bb)
+  se = __fadd2_rn(se, __fadd2_rn(pe, yl));
+  oh = __fadd2_rn(sm, se);
+  ol = dsub2(se, dsub2(oh, sm));
+}
+
 // byte offset of the fold accumulators in chain_kernel's shared memory
 __host__ __device__ __forceinline__ size_t chain_acc_offset(int tile, size_t elem) {
   return (((size_t)(tile + tile / 32 + 1) * elem) + 15) & ~(size_t)15;
@@ -168,6 +200,34 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
       zutab[k] = z * u;
     }
   }
+  // double-float BNNNI: the steps run on packed lanes (aux pairs); z_f u
+  // for all four f and the weights, split into hi / lo planes (the weights
+  // duplicated across the two lanes, with the negated hi word)
+  constexpr bool kPacked = ZB && std::is_same<T, dfloat>::value;
+  __shared__ __align__(16) float zuh[kPacked ? 64 : 1], zul[kPacked ? 64 : 1];
+  __shared__ __align__(16) float2 wph[kPacked ? 16 : 1], wpl[kPacked ? 16 : 1], wpn[kPacked ? 16 : 1];
+  if constexpr (kPacked) {
+    // (from the coefficients, as urow and wrow are formed: those rows are
+    // written by other threads and read only after the tile barrier)
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) {
+      const int f = k >> 4, sv = (k >> 2) & 3, aux = k & 3;
+      const int fl = f >> 1, fr = f & 1, sl = sv >> 1, sr = sv & 1, pl = aux >> 1, pr = aux & 1;
+      const T u = (!dir ? c.b1[sr ^ pl] * c.b3[sr ^ pr] * c.b3[sl ^ pl] : c.b1[sl ^ pr] * c.b3[sr ^ pr] * c.b3[sl ^ pl]) *
+                  c.g;
+      T z = c.b2[sr ^ fr] * c.b2[sl ^ fl];
+      if (dir) z = z * c.b1[sl ^ fr];
+      const T zu = u * z;
+      zuh[k] = zu.hi;
+      zul[k] = zu.lo;
+    }
+    for (int k = threadIdx.x; k < 16; k += blockDim.x) {
+      const int sv = k >> 2, q = k & 3, sl = sv >> 1, sr = sv & 1, al = q >> 1, ar = q & 1;
+      const T w = !dir ? c.b1[sr ^ al] * c.b2[sr ^ ar] * c.b2[sl ^ al] : c.b2[sr ^ ar] * c.b2[sl ^ al];
+      wph[k] = make_float2(w.hi, w.hi);
+      wpl[k] = make_float2(w.lo, w.lo);
+      wpn[k] = make_float2(-w.hi, -w.hi);
+    }
+  }
   // the factors z selects from, in registers (no indexed access)
   const T b1_0 = c.b1[0], b1_1 = c.b1[1], b2_0 = c.b2[0], b2_1 = c.b2[1];
   // outer index: state bits, then (unless last) the lastbit pass
@@ -261,6 +321,43 @@ __device__ __forceinline__ void chain_block(T* __restrict__ P, const IO* __restr
           // BNNNI: out((pl,pr), (sl,sr)) = z_f[s'] u[a'][s'] sum_q w[s'][q] in(q, a')
           const int fl = ctl >> 1, fr = ctl & 1;
           T* const bp[4] = {b0, b0 + o1, b0 + o2, b0 + o3};
+          if constexpr (kPacked) {
+            // lanes: a' = 2 pp and 2 pp + 1
+            float2 ih[4][2], il[4][2];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+              for (int pp = 0; pp < 2; ++pp) {
+                const float* e0 = reinterpret_cast<const float*>(bp[2 * pp] + q);
+                const float* e1 = reinterpret_cast<const float*>(bp[2 * pp + 1] + q);
+                ih[q][pp] = make_float2(e0[0], e1[0]);
+                il[q][pp] = make_float2(e0[1], e1[1]);
+              }
+#pragma unroll
+            for (int sv = 0; sv < NS; ++sv) {
+              const int kw = sv * 4 + z0;
+#pragma unroll
+              for (int pp = 0; pp < 2; ++pp) {
+                float2 dh, dl;
+                df2_mul(ih[0][pp], il[0][pp], wph[kw], wpl[kw], wpn[kw], dh, dl);
+#pragma unroll
+                for (int q = 1; q < 4; ++q)
+                  df2_fma(ih[q][pp], il[q][pp], wph[kw + q], wpl[kw + q], wpn[kw + q], dh, dl, dh, dl);
+                const int kz = ctl * 16 + sv * 4 + 2 * pp + z0;
+                const float2 zh = *reinterpret_cast<const float2*>(zuh + kz);
+                const float2 zl = *reinterpret_cast<const float2*>(zul + kz);
+                // zu * d (operator* with zu first): the d operand is the one negated
+                float2 oh, ol;
+                df2_mul(zh, zl, dh, dl, make_float2(-dh.x, -dh.y), oh, ol);
+                float* o0 = reinterpret_cast<float*>(bp[sv] + 2 * pp);
+                o0[0] = oh.x;
+                o0[1] = ol.x;
+                o0[2] = oh.y;
+                o0[3] = ol.y;
+              }
+            }
+            continue;
+          }
           T in[4][4];
 #pragma unroll
           for (int q = 0; q < 4; ++q)
