@@ -272,7 +272,9 @@ tm_status tm_chain_set_tuning(char model, int L, tm_dtype dtype, int tile_bits, 
 /* Plant `nconfig` layer sequences of `length` layers from the leading
  * eigenvector of a periodic x-ANNNI perpendicular TM (model 'A', axialdir 1:
  * XAT2DDumpConfig::dump, DumpConfig/dumpconfig.cpp:88-136; axialdir 5:
- * XAM2DDumpConfig::dump, DumpConfig/dumpreduce.cpp:47-122).  vec_host: the
+ * XAM2DDumpConfig::dump, DumpConfig/dumpreduce.cpp:47-122) or of the reduced
+ * DNNI one (model 'D', axialdir 5: XDM2DDumpConfig::dump,
+ * DumpConfig/dumpreduce.cpp:516-591).  vec_host: the
  * eigenvector as tm_eigs returns it (length rows; its absolute values are
  * used, as the reference reads X_vec.dat).  seed: the seed of the
  * reference's generator (std::mt19937 + uniform_real_distribution, as

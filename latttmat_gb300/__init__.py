@@ -470,7 +470,8 @@ class TMatOp:
 
     def dump_configs(self, vec: np.ndarray, nconfig: int, length: int, seed: int) -> np.ndarray:
         """Plant configurations from the leading eigenvector (the reference's
-        DumpConfig): uint64 layer states, shape (nconfig, length)."""
+        DumpConfig, operators A/1, A/5 and D/5): uint64 layer states, shape
+        (nconfig, length)."""
         v = np.ascontiguousarray(vec, dtype=np.float64)
         if v.shape != (self.rows(),):
             raise ValueError(f"vec has shape {v.shape}, expected ({self.rows()},)")

@@ -2,7 +2,8 @@
 //
 // The reference samples equilibrium layer sequences from the leading
 // eigenvector q of a transfer matrix (DumpConfig/dumpconfig.cpp:88-136 for
-// the full x-ANNNI TM, DumpConfig/dumpreduce.cpp:47-122 for the reduced one):
+// the full x-ANNNI TM, DumpConfig/dumpreduce.cpp:47-122 for the reduced one,
+// DumpConfig/dumpreduce.cpp:516-591 for the reduced DNNI one):
 //   start:  a state with probability q_a^2 (cumulative sums, upper_bound on
 //           rand * total);
 //   step:   the next state with probability  T(a', a) q_a'  (the column of
@@ -19,10 +20,12 @@
 //     MyUtility::setseed, std::uniform_real_distribution<double>);
 //   - one kernel launch per step computes every chain's column (one block per
 //     chain), its cumulative sums and the upper_bound of its draw; the full
-//     TM column is analytic, the reduced column comes straight from its
-//     definition T_red[b, a] = dup_b Tvec_b Tvec_a sum_{s in orbit(a)}
+//     TM column is analytic, the reduced x-ANNNI column comes straight from
+//     its definition T_red[b, a] = dup_b Tvec_b Tvec_a sum_{s in orbit(a)}
 //     Th(idx_b, s), with Th(s', s) = e^{K (L - 2 popcount(s' ^ s))} from a
 //     table of L + 1 values (no cache is needed: a column costs one pass);
+//     the reduced DNNI column is the operator's own FP64 product of the unit
+//     vector, as the reference forms it (one product per chain and step);
 //   - for the full TM the chains run all their steps in one launch; for the
 //     reduced TM the host draws the state inside the chosen orbit, with the
 //     orbit enumerated in the reference's order (getEqvStates inserts into a
@@ -59,6 +62,7 @@ struct DumpArgs {
   const uint32_t* orb;      // reduced: orbit members of each chain's current rep [nchain][orb_cap]
   const int* orb_n;
   int orb_cap;
+  const double* ycol;       // reduced DNNI: [nchain][n] the chains' current columns T e_a
   double* pref;             // [nchain][n] cumulative sums (scratch)
   int64_t* cur;             // [nchain] current state (full) or rep index (reduced)
   uint64_t* states;         // full: [nchain][length] states
@@ -86,6 +90,7 @@ __device__ __forceinline__ double column(const DumpArgs& A, int c, uint64_t a, i
     // exp(selfintr(a) + crossintr(a, i)) q_i  (crossintr = betaJ (L - 2 popcount(a ^ i)))
     return exp(intr1 + A.bj * (A.L - 2.0 * popc64(a ^ (uint64_t)i))) * A.vec[i];
   }
+  if (A.ycol) return A.ycol[(int64_t)c * A.n + i] * A.vec[i];  // (T e_a)_i q_i
   // T_red[i, a] q_i
   const uint32_t si = A.idx[i];
   const uint32_t* orb = A.orb + (int64_t)c * A.orb_cap;
@@ -193,16 +198,25 @@ std::vector<uint64_t> eqv_states(uint64_t s, int L, bool flip) {
   return std::vector<uint64_t>(res.begin(), res.end());
 }
 
+__global__ void unit_vector_kernel(double* __restrict__ x, int64_t n, int64_t at) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = (i == at) ? 1.0 : 0.0;
+}
+
 }  // namespace
+
+// y = T x in the reference's vector order (tm_capi.cu)
+void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStream_t s);
 
 void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, uint32_t seed, uint64_t* out) {
   const Op& op = op0.parent ? *op0.parent : op0;
   const bool full = (op.kind == K_XAT && op.boundary == 0);
   const bool red = (op.kind == K_XAM && op.grp.periodic);
-  if (!full && !red)
+  const bool red_dnni = (op.kind == K_XDM && op.grp.periodic);
+  if (!full && !red && !red_dnni)
     fail(TM_ERR_UNSUPPORTED,
-         "configuration planting covers the periodic x-ANNNI perpendicular TMs (A/1 and A/5; the reference's "
-         "DumpConfig/main.cpp dispatch)");
+         "configuration planting covers the periodic x-ANNNI perpendicular TMs (A/1, A/5) and the reduced "
+         "DNNI one (D/5), the reference's finished DumpConfig dumpers of perpendicular TMs");
   if (nchain < 1 || length < 1) fail(TM_ERR_ARG, "nconfig and length must be >= 1");
   const int L = op.L;
   const int64_t n = op.n;
@@ -285,6 +299,12 @@ void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, ui
   A.idx = op.idx.as<uint32_t>();
   A.dup = op.dup.as<uint16_t>();
   A.tvec = op.tvec.as<double>();
+  DBuf dycol, dunit;
+  if (red_dnni) {
+    dycol.alloc((size_t)nchain * n * 8);
+    dunit.alloc((size_t)n * 8);
+    A.ycol = dycol.as<double>();
+  }
   A.orb = dorb.as<uint32_t>();
   A.orb_n = dorbn.as<int>();
   A.orb_cap = cap;
@@ -302,18 +322,39 @@ void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, ui
     }
     TM_CK(cudaMemcpyAsync(dorb.p, orb.data(), orb.size() * 4, cudaMemcpyHostToDevice, s));
     TM_CK(cudaMemcpyAsync(dorbn.p, orbn.data(), orbn.size() * 4, cudaMemcpyHostToDevice, s));
+    if (red_dnni) {
+      // the current columns T e_a, one FP64 product per chain
+      const int g = (int)std::min<int64_t>((n + 255) / 256, 1024);
+      for (int c = 0; c < nchain; ++c) {
+        unit_vector_kernel<<<g, 256, 0, s>>>(dunit.as<double>(), n, cur[c]);
+        TM_CKK("unit_vector");
+        matvec_ref_order(op, dunit.p, dycol.as<double>() + (int64_t)c * n, TM_F64, s);
+      }
+    }
     dump_reduced_kernel<<<nchain, kDumpThreads, 0, s>>>(A, rq);
     TM_CKK("dump_reduced");
     TM_CK(cudaMemcpyAsync(cur.data(), dcur.p, cur.size() * 8, cudaMemcpyDeviceToHost, s));
     TM_CK(cudaStreamSynchronize(s));
     // the layer state inside the chosen orbit, weights exp(crossintr(ra, e))
-    // in the reference's member order (DumpConfig/dumpreduce.cpp:97-111)
+    // in the reference's member order (DumpConfig/dumpreduce.cpp:97-111;
+    // the DNNI cross interaction adds the two diagonals,
+    // DumpConfig/dumpreduce.cpp:509-514)
+    const uint64_t lmask = (1ull << L) - 1;
+    auto rotr1 = [&](uint64_t x) { return (x >> 1) | ((x & 1ull) << (L - 1)); };
+    auto rotl1 = [&](uint64_t x) { return ((x << 1) & lmask) | (x >> (L - 1)); };
+    auto cross = [&](uint64_t a, uint64_t b) {
+      double v = bj * (L - 2.0 * __builtin_popcountll(a ^ b));
+      if (red_dnni)
+        v += A.kap * (L - 2.0 * __builtin_popcountll(a ^ rotr1(b))) +
+             A.kap * (L - 2.0 * __builtin_popcountll(a ^ rotl1(b)));
+      return v;
+    };
     for (int c = 0; c < nchain; ++c) {
       const std::vector<uint64_t> eq = eqv_states(idx_h[cur[c]], L, flip);
       std::vector<double> qcond(eq.size());
       double t = 0.0;
       for (size_t k = 0; k < eq.size(); ++k) {
-        t += std::exp(bj * (L - 2.0 * __builtin_popcountll(ra[c] ^ eq[k])));
+        t += std::exp(cross(ra[c], eq[k]));
         qcond[k] = t;
       }
       const double target = draws[(size_t)c * per + 1 + (rq - 1) * stride + 1] * qcond.back();

@@ -26,6 +26,8 @@ extern "C" int ref_dump(char model, int axialdir, int extend_cond, double betaJ,
       bs.reset(new DumpMat::XAT2DDumpConfig(mpara, vecfile));
     else if (model == 'A' && axialdir == 5)
       bs.reset(new DumpMat::XAM2DDumpConfig(mpara, vecfile, extend_cond));
+    else if (model == 'D' && axialdir == 5)
+      bs.reset(new DumpMat::XDM2DDumpConfig(mpara, vecfile, extend_cond));
     else
       return 2;
     MyUtility::setseed(seed);

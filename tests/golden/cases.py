@@ -111,6 +111,9 @@ DUMP_CASES = [
     ("dump_xam_L12", "A", 5, 2, 0.35, 0.5, 0.0, 0.0, 12, 4, 64, 777),
     ("dump_xam_L14_flip", "A", 5, 0, 0.45, 0.4, 0.0, 0.0, 14, 3, 48, 99),
     ("dump_xam_L16_h", "A", 5, 0, 0.3, 0.6, 0.0, 0.05, 16, 2, 40, 2024),
+    ("dump_xdm_L12", "D", 5, 2, 0.4, 0.3, 0.0, 0.0, 12, 4, 48, 4242),
+    ("dump_xdm_L13_h", "D", 5, 0, 0.5, 0.4, 0.0, 0.05, 13, 3, 40, 31),
+    ("dump_xdm_L14_flip", "D", 5, 0, 0.35, 0.6, 0.0, 0.0, 14, 3, 36, 8),
 ]
 
 FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums and samples
