@@ -387,6 +387,24 @@ __device__ __forceinline__ void smem_rounds(T* sm, const EOArgs& A, int nbits) {
   if constexpr ((R + 1) * KB < kMaxTileBits) smem_rounds<T, KB, R + 1>(sm, A, nbits);
 }
 
+// streaming (evict-first) loads and stores of data read or written once
+template <class V>
+__device__ __forceinline__ V ld_stream(const V* p) {
+  if constexpr (std::is_same<V, dfloat>::value) {
+    const float2 v = __ldcs(reinterpret_cast<const float2*>(p));
+    return dfloat(v.x, v.y);
+  } else {
+    return __ldcs(p);
+  }
+}
+template <class V>
+__device__ __forceinline__ void st_stream(V* p, V v) {
+  if constexpr (std::is_same<V, dfloat>::value)
+    __stcs(reinterpret_cast<float2*>(p), make_float2(v.hi, v.lo));
+  else
+    __stcs(p, v);
+}
+
 // acc += c * v over the 16 / sizeof(T) elements of a 16-byte chunk
 template <class T>
 __device__ __forceinline__ void axpy16(float4& acc, const float4& v, T c);
@@ -569,7 +587,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
       for (int i = 0; i < kGatherChunk; ++i) {
         if (c0 + i < (1 << kb)) {
           const uint32_t P = base + threadIdx.x + ((c0 + i) << p);
-          idx[i] = __ldg(mrow + P);
+          idx[i] = __ldcs(mrow + P);  // read once: evict first, keep u in L2
           ev[i] = __ldg(it_e + P);
         }
       }
@@ -604,7 +622,7 @@ __global__ void __launch_bounds__(1024, 1) eo_pass1(EOArgs A, const InT* __restr
       if (k0 + q < (1 << kb)) w[q] = __ldg(wout + base + threadIdx.x + ((k0 + q) << p));
 #pragma unroll
     for (int q = 0; q < kOB; ++q)
-      if (k0 + q < (1 << kb)) w1[(int64_t)w[q].x + tile * (w[q].y >> 16)] = sm[spad(w[q].y & lmask)];
+      if (k0 + q < (1 << kb)) st_stream(w1 + (int64_t)w[q].x + tile * (w[q].y >> 16), sm[spad(w[q].y & lmask)]);
   }
 }
 
@@ -692,8 +710,8 @@ __global__ void __launch_bounds__(1024, 1) eo_pass2(EOArgs A, const T* __restric
     for (int q = 0; q < kOutBatch; ++q) {
       const uint32_t k = kk + q * blockDim.x;
       if (k < k1) {
-        ov[q] = out_o[k];
-        sc[q] = scale[k];
+        ov[q] = ld_stream(out_o + k);
+        sc[q] = ld_stream(scale + k);
       }
     }
 #pragma unroll

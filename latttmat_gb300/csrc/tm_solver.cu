@@ -1169,7 +1169,9 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
     Lz.reset(new Lanczos(op, ncv, s, mixed_nv32 ? nev + 1 : 0));
     Lanczos& lz = *Lz;
     const bool mixed = (mode == TM_EIGS_MIXED);
-    lz.start(nullptr, seed);
+    // the FP64 basis starts here unless the FP32 basis runs the first phase
+    // (it then holds the refined vectors, and restarts from them if needed)
+    if (!mixed_nv32) lz.start(nullptr, seed);
     bool ok = false;
     Lanczos::CycleResult r;
     if (mixed) {
