@@ -47,7 +47,7 @@ EXPORTED_SYMBOLS = (
     "tm_debug_set_eo_tile_bits", "tm_sweep_create", "tm_sweep_destroy", "tm_sweep_count", "tm_sweep_rows",
     "tm_sweep_normfactor", "tm_sweep_set_wave_bytes", "tm_sweep_stats", "tm_sweep_eigs_vec",
     "tm_sweep_set_transpose", "tm_sweep_grad", "tm_sweep_perform_op_dev", "tm_sweep_eigs",
-    "tm_chain_autotune", "tm_chain_set_tuning", "tm_dump_configs",
+    "tm_chain_autotune", "tm_chain_set_tuning", "tm_dump_configs", "tm_dump_configs_lr",
 )
 
 
@@ -138,6 +138,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
         getattr(lib, f).restype = ctypes.c_int
     lib.tm_dump_configs.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, P]
     lib.tm_dump_configs.restype = ctypes.c_int
+    lib.tm_dump_configs_lr.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, P]
+    lib.tm_dump_configs_lr.restype = ctypes.c_int
     lib.tm_last_error.restype = ctypes.c_char_p
     lib.tm_version.restype = ctypes.c_char_p
     for f in ("tm_create", "tm_transpose", "tm_destroy", "tm_perform_op", "tm_perform_op_dev", "tm_orbit_table",
@@ -468,15 +470,26 @@ class TMatOp:
         _check(self._lib.tm_grad(self._h, _ptr(qr), qlp, float(lambda_internal), _ptr(g)))
         return g
 
-    def dump_configs(self, vec: np.ndarray, nconfig: int, length: int, seed: int) -> np.ndarray:
+    def dump_configs(self, vec: np.ndarray, nconfig: int, length: int, seed: int,
+                     vecl: Optional[np.ndarray] = None) -> np.ndarray:
         """Plant configurations from the leading eigenvector (the reference's
         DumpConfig, operators A/1, A/5 and D/5): uint64 layer states, shape
-        (nconfig, length)."""
+        (nconfig, length).  The two-layer parallel TM (A/2) plants from its
+        right and left eigenvectors (vecl) and gives length + 1 layers per
+        chain, as the reference writes them."""
         v = np.ascontiguousarray(vec, dtype=np.float64)
         if v.shape != (self.rows(),):
             raise ValueError(f"vec has shape {v.shape}, expected ({self.rows()},)")
-        out = np.zeros((int(nconfig), int(length)), dtype=np.uint64)
-        _check(self._lib.tm_dump_configs(self._h, _ptr(v), int(nconfig), int(length), int(seed), _ptr(out)))
+        if vecl is None:
+            out = np.zeros((int(nconfig), int(length)), dtype=np.uint64)
+            _check(self._lib.tm_dump_configs(self._h, _ptr(v), int(nconfig), int(length), int(seed), _ptr(out)))
+            return out
+        vl = np.ascontiguousarray(vecl, dtype=np.float64)
+        if vl.shape != (self.rows(),):
+            raise ValueError(f"vecl has shape {vl.shape}, expected ({self.rows()},)")
+        out = np.zeros((int(nconfig), int(length) + 1), dtype=np.uint64)
+        _check(self._lib.tm_dump_configs_lr(self._h, _ptr(v), _ptr(vl), int(nconfig), int(length), int(seed),
+                                            _ptr(out)))
         return out
 
     def profile_matvec(self, dtype: int = TM_F32, iters: int = 10):

@@ -26,6 +26,10 @@
 //     table of L + 1 values (no cache is needed: a column costs one pass);
 //     the reduced DNNI column is the operator's own FP64 product of the unit
 //     vector, as the reference forms it (one product per chain and step);
+//   - the two-layer parallel TM (YAT2DDumpConfig::dump,
+//     DumpConfig/dumpconfig.cpp:171-219) walks pairs of layers (ra, rb) ->
+//     (rb, rc): its column over rc is analytic, weighted by the right
+//     eigenvector at (rc, rb), and its start is drawn from |r| |l|;
 //   - for the full TM the chains run all their steps in one launch; for the
 //     reduced TM the host draws the state inside the chosen orbit, with the
 //     orbit enumerated in the reference's order (getEqvStates inserts into a
@@ -165,6 +169,80 @@ __global__ void __launch_bounds__(kDumpThreads) dump_full_kernel(DumpArgs A) {
   if (threadIdx.x == 0) A.cur[c] = a;
 }
 
+// Two-layer parallel TM (YAT): every step of chain blockIdx.x in one launch.
+// State = rb << L | ra; the column over rc is exp(selfintr(ra, rb) +
+// crossintr(ra, rc)) r[rc << L | rb], with selfintr = field + NN in the layer
+// + NN to the partner layer and crossintr = -kappa betaJ (L - 2 popcount(ra ^
+// rc)) (DumpConfig/dumpconfig.cpp:146-168).  Records ra0, the rb of every
+// step and the last rc: length + 1 layers.
+__device__ __forceinline__ double yat_column(const DumpArgs& A, uint64_t ra, uint64_t rb, int64_t rc, double intr1) {
+  return exp(intr1 + A.kap * (A.L - 2.0 * popc64(ra ^ (uint64_t)rc))) * A.vec[((uint64_t)rc << A.L) | rb];
+}
+
+__global__ void __launch_bounds__(kDumpThreads) dump_yat_kernel(DumpArgs A) {
+  __shared__ double warp_sums[kDumpThreads / 32];
+  __shared__ double carry;
+  __shared__ int64_t found;
+  const int c = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint64_t mask = (1ull << A.L) - 1;
+  const int64_t ncol = (int64_t)1 << A.L;
+  double* pref = A.pref + (int64_t)c * ncol;
+  uint64_t cur = (uint64_t)A.cur[c];
+  const double* d = A.draws + (int64_t)c * A.draws_per_chain;
+  if (tid == 0) A.states[(int64_t)c * (A.length + 1)] = cur & mask;
+  for (int rq = 1; rq < A.length; ++rq) {
+    const uint64_t ra = cur & mask, rb = cur >> A.L;
+    if (tid == 0) A.states[(int64_t)c * (A.length + 1) + rq] = rb;
+    const int L = A.L;
+    double intr1 = A.hj * (L - 2.0 * popc64(ra));
+    intr1 += A.bj * (L - 2.0 * popc64(ra ^ rot_r(ra, L, 1)));
+    intr1 += A.bj * (L - 2.0 * popc64(ra ^ rb));
+    if (tid == 0) carry = 0.0;
+    __syncthreads();
+    for (int64_t base = 0; base < ncol; base += blockDim.x) {
+      const int64_t i = base + tid;
+      double v = (i < ncol) ? yat_column(A, ra, rb, i, intr1) : 0.0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+      }
+      if (lane == 31) warp_sums[wid] = v;
+      __syncthreads();
+      if (wid == 0) {
+        double w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0.0;
+        for (int o = 1; o < 32; o <<= 1) {
+          const double t = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += t;
+        }
+        if (lane < (int)(blockDim.x >> 5)) warp_sums[lane] = w;
+      }
+      __syncthreads();
+      const double before = carry + (wid > 0 ? warp_sums[wid - 1] : 0.0);
+      if (i < ncol) pref[i] = before + v;
+      __syncthreads();
+      if (tid == blockDim.x - 1) carry = before + v;
+      __syncthreads();
+    }
+    if (tid == 0) {
+      const double target = d[1 + (rq - 1) * A.draw_stride] * pref[ncol - 1];
+      int64_t lo = 0, hi = ncol;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (pref[mid] <= target)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      found = lo < ncol ? lo : ncol - 1;
+    }
+    __syncthreads();
+    cur = ((uint64_t)found << A.L) | rb;
+    __syncthreads();
+  }
+  if (tid == 0) A.states[(int64_t)c * (A.length + 1) + A.length] = cur >> A.L;
+}
+
 // Reduced TM: step rq of every chain (the rep index of the next orbit).
 __global__ void __launch_bounds__(kDumpThreads) dump_reduced_kernel(DumpArgs A, int rq) {
   const int c = blockIdx.x;
@@ -208,15 +286,20 @@ __global__ void unit_vector_kernel(double* __restrict__ x, int64_t n, int64_t at
 // y = T x in the reference's vector order (tm_capi.cu)
 void matvec_ref_order(const Op& op, const void* x, void* y, tm_dtype dt, cudaStream_t s);
 
-void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, uint32_t seed, uint64_t* out) {
+void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int nchain, int length, uint32_t seed,
+                  uint64_t* out) {
   const Op& op = op0.parent ? *op0.parent : op0;
   const bool full = (op.kind == K_XAT && op.boundary == 0);
   const bool red = (op.kind == K_XAM && op.grp.periodic);
   const bool red_dnni = (op.kind == K_XDM && op.grp.periodic);
-  if (!full && !red && !red_dnni)
+  const bool yat = (op.kind == K_YAT && op.boundary == 0);
+  if (!full && !red && !red_dnni && !yat)
     fail(TM_ERR_UNSUPPORTED,
-         "configuration planting covers the periodic x-ANNNI perpendicular TMs (A/1, A/5) and the reduced "
-         "DNNI one (D/5), the reference's finished DumpConfig dumpers of perpendicular TMs");
+         "configuration planting covers the periodic x-ANNNI perpendicular TMs (A/1, A/5), the reduced DNNI "
+         "one (D/5) and the full two-layer parallel TM (A/2): the reference's finished DumpConfig dumpers of "
+         "those operators");
+  if (yat && !vecl_h) fail(TM_ERR_ARG, "the two-layer TM plants from its right and left eigenvectors");
+  if (!yat && vecl_h) fail(TM_ERR_UNSUPPORTED, "left/right planting is for the two-layer parallel TM (A/2)");
   if (nchain < 1 || length < 1) fail(TM_ERR_ARG, "nconfig and length must be >= 1");
   const int L = op.L;
   const int64_t n = op.n;
@@ -225,17 +308,18 @@ void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, ui
   AllocStream guard(s);
   // sampling weights: |q| as the reference reads its vector file
   // (DumpConfig/dumpconfig.hpp:56-77), start weights q^2 summed in order
+  // (|r| |l| for the two-layer TM, DumpConfig/dumpconfig.cpp:45-56)
   std::vector<double> vabs(n), qmargin(n);
   double acc = 0.0;
   for (int64_t i = 0; i < n; ++i) {
     vabs[i] = std::fabs(vec_h[i]);
-    acc += vabs[i] * vabs[i];
+    acc += vabs[i] * (yat ? std::fabs(vecl_h[i]) : vabs[i]);
     qmargin[i] = acc;
   }
   // the random stream, in the reference's order
   std::mt19937 rg(seed);
   std::uniform_real_distribution<> rrand;
-  const int stride = full ? 1 : 2;
+  const int stride = (full || yat) ? 1 : 2;
   const int per = 1 + stride * (length - 1);
   std::vector<double> draws((size_t)nchain * per);
   for (double& d : draws) d = rrand(rg);
@@ -258,7 +342,7 @@ void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, ui
   up(ddraw, draws.data(), draws.size() * 8);
   up(dth, th.data(), th.size() * 8);
   up(dcur, cur.data(), cur.size() * 8);
-  dpref.alloc((size_t)nchain * n * 8);
+  dpref.alloc((size_t)nchain * (yat ? ((int64_t)1 << L) : n) * 8);
   DumpArgs A{};
   A.L = L;
   A.n_is_full = full;
@@ -275,6 +359,15 @@ void dump_configs(const Op& op0, const double* vec_h, int nchain, int length, ui
   A.thtab = dth.as<double>();
   A.pref = dpref.as<double>();
   A.cur = dcur.as<int64_t>();
+  if (yat) {
+    dstates.alloc((size_t)nchain * (length + 1) * 8);
+    A.states = dstates.as<uint64_t>();
+    dump_yat_kernel<<<nchain, kDumpThreads, 0, s>>>(A);
+    TM_CKK("dump_yat");
+    TM_CK(cudaMemcpyAsync(out, dstates.p, (size_t)nchain * (length + 1) * 8, cudaMemcpyDeviceToHost, s));
+    TM_CK(cudaStreamSynchronize(s));
+    return;
+  }
   if (full) {
     std::vector<uint64_t> st0((size_t)nchain * length, 0);
     for (int c = 0; c < nchain; ++c) st0[(size_t)c * length] = (uint64_t)cur[c];
@@ -374,7 +467,22 @@ extern "C" tm_status tm_dump_configs(const tm_op* op, const double* vec_host, in
                                      uint64_t* states_out) {
   try {
     if (!op || !vec_host || !states_out) fail(TM_ERR_ARG, "null argument");
-    dump_configs(*op->impl, vec_host, nconfig, length, seed, states_out);
+    dump_configs(*op->impl, vec_host, nullptr, nconfig, length, seed, states_out);
+  } catch (const Failure& f) {
+    set_error(f.msg);
+    return f.code;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return TM_ERR_CUDA;
+  }
+  return TM_OK;
+}
+
+extern "C" tm_status tm_dump_configs_lr(const tm_op* op, const double* vecr_host, const double* vecl_host, int nconfig,
+                                        int length, uint32_t seed, uint64_t* states_out) {
+  try {
+    if (!op || !vecr_host || !vecl_host || !states_out) fail(TM_ERR_ARG, "null argument");
+    dump_configs(*op->impl, vecr_host, vecl_host, nconfig, length, seed, states_out);
   } catch (const Failure& f) {
     set_error(f.msg);
     return f.code;

@@ -24,6 +24,8 @@ extern "C" int ref_dump(char model, int axialdir, int extend_cond, double betaJ,
   try {
     if (model == 'A' && axialdir == 1)
       bs.reset(new DumpMat::XAT2DDumpConfig(mpara, vecfile));
+    else if (model == 'A' && axialdir == 2)
+      bs.reset(new DumpMat::YAT2DDumpConfig(mpara, vecfile, veclfile ? veclfile : ""));
     else if (model == 'A' && axialdir == 5)
       bs.reset(new DumpMat::XAM2DDumpConfig(mpara, vecfile, extend_cond));
     else if (model == 'D' && axialdir == 5)

@@ -114,6 +114,8 @@ DUMP_CASES = [
     ("dump_xdm_L12", "D", 5, 2, 0.4, 0.3, 0.0, 0.0, 12, 4, 48, 4242),
     ("dump_xdm_L13_h", "D", 5, 0, 0.5, 0.4, 0.0, 0.05, 13, 3, 40, 31),
     ("dump_xdm_L14_flip", "D", 5, 0, 0.35, 0.6, 0.0, 0.0, 14, 3, 36, 8),
+    ("dump_yat_L6", "A", 2, 0, 0.4, 0.3, 0.0, 0.0, 6, 4, 40, 17),
+    ("dump_yat_L8_h", "A", 2, 0, 0.6, 0.5, 0.0, 0.05, 8, 3, 32, 321),
 ]
 
 FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums and samples

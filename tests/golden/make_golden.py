@@ -173,20 +173,35 @@ def gen_dump(c):
     name, model, ax, ec, bj, k, k2, h, size, nconf, length, seed = c
     op = RefOp(model, 2, ax, bj, k, h, size, k2, ec)
     n = op.n
-    lin = sla.LinearOperator((n, n), matvec=lambda v: op.perform_op(np.ravel(v)), dtype=np.float64)
     v0 = np.random.default_rng(0).uniform(0, 1, n)
-    vals, vecs = sla.eigsh(lin, k=2, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, 20))
-    q = np.real(vecs[:, int(np.argmax(np.abs(vals)))])
-    q = q / np.linalg.norm(q)
-    q = q * np.sign(q.sum())
+
+    def leading(matvec, symmetric):
+        lin = sla.LinearOperator((n, n), matvec=lambda v: matvec(np.ravel(v)), dtype=np.float64)
+        if symmetric:
+            vals, vecs = sla.eigsh(lin, k=2, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, 20))
+        else:
+            vals, vecs = sla.eigs(lin, k=2, which="LM", tol=1e-13, v0=v0, ncv=min(n - 1, 20))
+        q = np.real(vecs[:, int(np.argmax(np.abs(vals)))])
+        q = q / np.linalg.norm(q)
+        return q * np.sign(q.sum())
+
+    two_layer = (model, ax) == ("A", 2)  # YAT2DDumpConfig: right and left vectors
+    q = leading(op.perform_op, not two_layer)
+    ql = leading(op.perform_op_t, False) if two_layer else None
     with tempfile.TemporaryDirectory() as td:
         vf = os.path.join(td, "RUN_vec.dat")
         q.astype(np.float64).tofile(vf)
-        st = ref_dump(model, ax, ec, bj, k, k2, h, size, vf, None, nconf, length, seed, os.path.join(td, "RUN"))
+        vlf = None
+        if ql is not None:
+            vlf = os.path.join(td, "RUN_vecl.dat")
+            ql.astype(np.float64).tofile(vlf)
+        st = ref_dump(model, ax, ec, bj, k, k2, h, size, vf, vlf, nconf, length, seed, os.path.join(td, "RUN"))
         if st != 0:
             raise RuntimeError(f"reference dump failed ({st})")
         configs = read_configs(os.path.join(td, "RUN"), nconf, size)
     out = dict(vec=q, configs=configs, n=np.int64(n))
+    if ql is not None:
+        out["vecl"] = ql
     log(f"{name}: n={n} configs {configs.shape}")
     return name, out
 

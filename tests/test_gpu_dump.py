@@ -18,10 +18,11 @@ def test_planted_configurations_match_the_reference(case):
     f = fixture(name)
     op = lt.TMatOp(model, 2, ax, bj, k, h, size, k2, ec)
     assert op.rows() == int(f["n"])
-    states = op.dump_configs(f["vec"], nconf, length, seed)
+    vecl = f["vecl"] if "vecl" in f else None  # the two-layer TM plants from both vectors
+    states = op.dump_configs(f["vec"], nconf, length, seed, vecl=vecl)
     np.testing.assert_array_equal(states, f["configs"])
     # a second call with the same seed plants the same configurations
-    np.testing.assert_array_equal(op.dump_configs(f["vec"], nconf, length, seed), states)
+    np.testing.assert_array_equal(op.dump_configs(f["vec"], nconf, length, seed, vecl=vecl), states)
 
 
 def test_planting_writes_the_reference_file_format(tmp_path):
@@ -43,3 +44,12 @@ def test_planting_refuses_other_operators():
     with pytest.raises(lt.TMError) as e:
         op.dump_configs(np.ones(op.rows()), 1, 4, 0)
     assert e.value.code == lt.TM_ERR_UNSUPPORTED
+    # left/right planting is the two-layer TM's; the two-layer TM needs both vectors
+    sym = lt.TMatOp("A", 2, 5, 0.4, 0.3, 0.0, 10, 0.0, 2)
+    with pytest.raises(lt.TMError) as e:
+        sym.dump_configs(np.ones(sym.rows()), 1, 4, 0, vecl=np.ones(sym.rows()))
+    assert e.value.code == lt.TM_ERR_UNSUPPORTED
+    yat = lt.TMatOp("A", 2, 2, 0.4, 0.3, 0.0, 6, 0.0, 0)
+    with pytest.raises(lt.TMError) as e:
+        yat.dump_configs(np.ones(yat.rows()), 1, 4, 0)
+    assert e.value.code == lt.TM_ERR_ARG
