@@ -286,14 +286,16 @@ tm_status tm_chain_set_tuning(char model, int L, tm_dtype dtype, int tile_bits, 
  * every chain's transfer-matrix column, cumulative sums and draw. */
 tm_status tm_dump_configs(const tm_op* op, const double* vec_host, int nconfig, int length, uint32_t seed,
                           uint64_t* states_out);
-/* The same for the full two-layer parallel TM (model 'A', axialdir 2:
- * YAT2DDumpConfig::dump, DumpConfig/dumpconfig.cpp:171-219), which plants from
- * its right and left leading eigenvectors (start weights |r| |l|, steps
- * weighted by |r|; the reference reads both files, GenDumpConfig::initq).
- * states_out: nconfig * (length + 1) layer states per chain, as the reference
- * writes them: the first layer, the partner layer of every step, the last
- * layer.  Other operators return TM_ERR_UNSUPPORTED here (tm_dump_configs
- * plants from their one vector). */
+/* The same for the two-layer parallel TMs, which plant from their right and
+ * left leading eigenvectors (start weights |r| |l|, steps weighted by |r|; the
+ * reference reads both files, GenDumpConfig::initq): the full one (model 'A',
+ * axialdir 2: YAT2DDumpConfig::dump, DumpConfig/dumpconfig.cpp:171-219;
+ * states_out holds nconfig * (length + 1) layers, as the reference writes
+ * them: the first layer, the partner layer of every step, the last layer) and
+ * the reduced ones (model 'A' axialdir 6 and model 'B' axialdir 6:
+ * YAM2DDumpConfig / YBM2DDumpConfig::dump, DumpConfig/dumpreduce.cpp:156-256;
+ * nconfig * length layers).  Other operators return TM_ERR_UNSUPPORTED here
+ * (tm_dump_configs plants from their one vector). */
 tm_status tm_dump_configs_lr(const tm_op* op, const double* vecr_host, const double* vecl_host, int nconfig,
                              int length, uint32_t seed, uint64_t* states_out);
 

@@ -474,9 +474,9 @@ class TMatOp:
                      vecl: Optional[np.ndarray] = None) -> np.ndarray:
         """Plant configurations from the leading eigenvector (the reference's
         DumpConfig, operators A/1, A/5 and D/5): uint64 layer states, shape
-        (nconfig, length).  The two-layer parallel TM (A/2) plants from its
-        right and left eigenvectors (vecl) and gives length + 1 layers per
-        chain, as the reference writes them."""
+        (nconfig, length).  The two-layer parallel TMs (A/2, A/6, B/6) plant
+        from their right and left eigenvectors (vecl); the full one (A/2)
+        gives length + 1 layers per chain, as the reference writes them."""
         v = np.ascontiguousarray(vec, dtype=np.float64)
         if v.shape != (self.rows(),):
             raise ValueError(f"vec has shape {v.shape}, expected ({self.rows()},)")
@@ -487,7 +487,8 @@ class TMatOp:
         vl = np.ascontiguousarray(vecl, dtype=np.float64)
         if vl.shape != (self.rows(),):
             raise ValueError(f"vecl has shape {vl.shape}, expected ({self.rows()},)")
-        out = np.zeros((int(nconfig), int(length) + 1), dtype=np.uint64)
+        layers = int(length) + 1 if (self.model, self.axialdir) == ("A", 2) else int(length)
+        out = np.zeros((int(nconfig), layers), dtype=np.uint64)
         _check(self._lib.tm_dump_configs_lr(self._h, _ptr(v), _ptr(vl), int(nconfig), int(length), int(seed),
                                             _ptr(out)))
         return out

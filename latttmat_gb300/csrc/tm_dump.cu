@@ -29,7 +29,11 @@
 //   - the two-layer parallel TM (YAT2DDumpConfig::dump,
 //     DumpConfig/dumpconfig.cpp:171-219) walks pairs of layers (ra, rb) ->
 //     (rb, rc): its column over rc is analytic, weighted by the right
-//     eigenvector at (rc, rb), and its start is drawn from |r| |l|;
+//     eigenvector at (rc, rb), and its start is drawn from |r| |l|; the
+//     reduced two-layer TMs (YAM2DDumpConfig / YBM2DDumpConfig::dump,
+//     DumpConfig/dumpreduce.cpp:156-256) take their columns from the
+//     operator's products and draw the layer pair inside the chosen orbit
+//     among the members that continue the chain (low layer = rb);
 //   - for the full TM the chains run all their steps in one launch; for the
 //     reduced TM the host draws the state inside the chosen orbit, with the
 //     orbit enumerated in the reference's order (getEqvStates inserts into a
@@ -281,6 +285,39 @@ __global__ void unit_vector_kernel(double* __restrict__ x, int64_t n, int64_t at
     x[i] = (i == at) ? 1.0 : 0.0;
 }
 
+// The orbit of a two-layer state in the order the reference lists it:
+// YAMMatVecProd2D::getEqvStates, TMat/tmatreduce.cpp:911-943 -- the joint
+// rotations of both layers, then those of the bit-reversed pair, then (with
+// the spin flip) the same for the flipped pair, inserted into a
+// std::unordered_set and read back in its order.
+std::vector<uint64_t> eqv_states_2layer(uint64_t s, int L, bool flip) {
+  std::unordered_set<uint64_t> res;
+  const uint64_t lm = (1ull << L) - 1, mask = (1ull << (2 * L)) - 1;
+  auto rot1 = [&](uint64_t x) { return (x >> 1) | ((x & 1ull) << (L - 1)); };
+  auto brev = [&](uint64_t x) {
+    uint64_t r = 0;
+    for (int i = 0; i < L; ++i) r |= ((x >> i) & 1ull) << (L - 1 - i);
+    return r;
+  };
+  auto scan = [&](uint64_t st) {
+    uint64_t hi = st >> L, lo = st & lm;
+    for (uint64_t nx = st; res.find(nx) == res.end();) {
+      res.insert(nx);
+      hi = rot1(hi);
+      lo = rot1(lo);
+      nx = hi << L | lo;
+    }
+  };
+  scan(s);
+  scan(brev(s >> L) << L | brev(s & lm));
+  if (flip) {
+    const uint64_t f = ~s & mask;
+    scan(f);
+    scan(brev(f >> L) << L | brev(f & lm));
+  }
+  return std::vector<uint64_t>(res.begin(), res.end());
+}
+
 }  // namespace
 
 // y = T x in the reference's vector order (tm_capi.cu)
@@ -293,13 +330,14 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
   const bool red = (op.kind == K_XAM && op.grp.periodic);
   const bool red_dnni = (op.kind == K_XDM && op.grp.periodic);
   const bool yat = (op.kind == K_YAT && op.boundary == 0);
-  if (!full && !red && !red_dnni && !yat)
+  const bool red2 = (op.kind == K_YAM);  // YAM (A/6) and YBM (B/6): periodic only
+  const bool two_layer = yat || red2;
+  if (!full && !red && !red_dnni && !two_layer)
     fail(TM_ERR_UNSUPPORTED,
          "configuration planting covers the periodic x-ANNNI perpendicular TMs (A/1, A/5), the reduced DNNI "
-         "one (D/5) and the full two-layer parallel TM (A/2): the reference's finished DumpConfig dumpers of "
-         "those operators");
-  if (yat && !vecl_h) fail(TM_ERR_ARG, "the two-layer TM plants from its right and left eigenvectors");
-  if (!yat && vecl_h) fail(TM_ERR_UNSUPPORTED, "left/right planting is for the two-layer parallel TM (A/2)");
+         "one (D/5) and the two-layer parallel TMs (A/2, A/6, B/6): the reference's finished DumpConfig dumpers");
+  if (two_layer && !vecl_h) fail(TM_ERR_ARG, "the two-layer TMs plant from their right and left eigenvectors");
+  if (!two_layer && vecl_h) fail(TM_ERR_UNSUPPORTED, "left/right planting is for the two-layer parallel TMs");
   if (nchain < 1 || length < 1) fail(TM_ERR_ARG, "nconfig and length must be >= 1");
   const int L = op.L;
   const int64_t n = op.n;
@@ -313,7 +351,7 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
   double acc = 0.0;
   for (int64_t i = 0; i < n; ++i) {
     vabs[i] = std::fabs(vec_h[i]);
-    acc += vabs[i] * (yat ? std::fabs(vecl_h[i]) : vabs[i]);
+    acc += vabs[i] * (two_layer ? std::fabs(vecl_h[i]) : vabs[i]);
     qmargin[i] = acc;
   }
   // the random stream, in the reference's order
@@ -383,7 +421,8 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
   std::vector<uint32_t> idx_h(n);
   TM_CK(cudaMemcpyAsync(idx_h.data(), op.idx.p, n * 4, cudaMemcpyDeviceToHost, s));
   TM_CK(cudaStreamSynchronize(s));
-  const bool flip = op.grp.flip;
+  const bool flip = red2 ? (op.censym != 0) : (op.grp.flip != 0);
+  const bool by_product = red_dnni || red2;  // columns from the operator's own products
   const int cap = 4 * L;
   std::vector<uint32_t> orb((size_t)nchain * cap);
   std::vector<int> orbn(nchain);
@@ -393,7 +432,7 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
   A.dup = op.dup.as<uint16_t>();
   A.tvec = op.tvec.as<double>();
   DBuf dycol, dunit;
-  if (red_dnni) {
+  if (by_product) {
     dycol.alloc((size_t)nchain * n * 8);
     dunit.alloc((size_t)n * 8);
     A.ycol = dycol.as<double>();
@@ -401,21 +440,29 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
   A.orb = dorb.as<uint32_t>();
   A.orb_n = dorbn.as<int>();
   A.orb_cap = cap;
+  // ra: the chain's current layer state (a layer pair for the two-layer
+  // TMs, whose dumpers record its low layer at the start of every step and
+  // once more at the end)
+  const uint64_t lmask = (1ull << L) - 1;
   std::vector<uint64_t> ra(nchain);
   for (int c = 0; c < nchain; ++c) {
     ra[c] = idx_h[cur[c]];
-    out[(size_t)c * length] = ra[c];
+    if (!red2) out[(size_t)c * length] = ra[c];
   }
   for (int rq = 1; rq < length; ++rq) {
-    // the current orbits (for the column sums)
-    for (int c = 0; c < nchain; ++c) {
-      const std::vector<uint64_t> m = eqv_states(idx_h[cur[c]], L, flip);
-      orbn[c] = (int)m.size();
-      for (size_t k = 0; k < m.size(); ++k) orb[(size_t)c * cap + k] = (uint32_t)m[k];
+    if (red2)
+      for (int c = 0; c < nchain; ++c) out[(size_t)c * length + rq - 1] = ra[c] & lmask;
+    if (!by_product) {
+      // the current orbits (for the analytic column sums)
+      for (int c = 0; c < nchain; ++c) {
+        const std::vector<uint64_t> m = eqv_states(idx_h[cur[c]], L, flip);
+        orbn[c] = (int)m.size();
+        for (size_t k = 0; k < m.size(); ++k) orb[(size_t)c * cap + k] = (uint32_t)m[k];
+      }
+      TM_CK(cudaMemcpyAsync(dorb.p, orb.data(), orb.size() * 4, cudaMemcpyHostToDevice, s));
+      TM_CK(cudaMemcpyAsync(dorbn.p, orbn.data(), orbn.size() * 4, cudaMemcpyHostToDevice, s));
     }
-    TM_CK(cudaMemcpyAsync(dorb.p, orb.data(), orb.size() * 4, cudaMemcpyHostToDevice, s));
-    TM_CK(cudaMemcpyAsync(dorbn.p, orbn.data(), orbn.size() * 4, cudaMemcpyHostToDevice, s));
-    if (red_dnni) {
+    if (by_product) {
       // the current columns T e_a, one FP64 product per chain
       const int g = (int)std::min<int64_t>((n + 255) / 256, 1024);
       for (int c = 0; c < nchain; ++c) {
@@ -432,7 +479,6 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
     // in the reference's member order (DumpConfig/dumpreduce.cpp:97-111;
     // the DNNI cross interaction adds the two diagonals,
     // DumpConfig/dumpreduce.cpp:509-514)
-    const uint64_t lmask = (1ull << L) - 1;
     auto rotr1 = [&](uint64_t x) { return (x >> 1) | ((x & 1ull) << (L - 1)); };
     auto rotl1 = [&](uint64_t x) { return ((x << 1) & lmask) | (x >> (L - 1)); };
     auto cross = [&](uint64_t a, uint64_t b) {
@@ -443,20 +489,30 @@ void dump_configs(const Op& op0, const double* vec_h, const double* vecl_h, int 
       return v;
     };
     for (int c = 0; c < nchain; ++c) {
-      const std::vector<uint64_t> eq = eqv_states(idx_h[cur[c]], L, flip);
+      const std::vector<uint64_t> eq =
+          red2 ? eqv_states_2layer(idx_h[cur[c]], L, flip) : eqv_states(idx_h[cur[c]], L, flip);
       std::vector<double> qcond(eq.size());
       double t = 0.0;
       for (size_t k = 0; k < eq.size(); ++k) {
-        t += std::exp(cross(ra[c], eq[k]));
+        if (!red2) {
+          t += std::exp(cross(ra[c], eq[k]));
+        } else if ((eq[k] & lmask) == (ra[c] >> L)) {
+          // members whose low layer continues the chain (rb), weight
+          // exp(crossintr(ra, rc)), crossintr = -kappa betaJ (L - 2 popcount)
+          // (DumpConfig/dumpreduce.cpp:152-155, 236-244)
+          t += std::exp(A.kap * (L - 2.0 * __builtin_popcountll((ra[c] & lmask) ^ (eq[k] >> L))));
+        }
         qcond[k] = t;
       }
       const double target = draws[(size_t)c * per + 1 + (rq - 1) * stride + 1] * qcond.back();
       size_t k = std::upper_bound(qcond.begin(), qcond.end(), target) - qcond.begin();
       if (k >= eq.size()) k = eq.size() - 1;
       ra[c] = eq[k];
-      out[(size_t)c * length + rq] = ra[c];
+      if (!red2) out[(size_t)c * length + rq] = ra[c];
     }
   }
+  if (red2)
+    for (int c = 0; c < nchain; ++c) out[(size_t)c * length + length - 1] = ra[c] & lmask;
 }
 
 }  // namespace ltm

@@ -28,6 +28,10 @@ extern "C" int ref_dump(char model, int axialdir, int extend_cond, double betaJ,
       bs.reset(new DumpMat::YAT2DDumpConfig(mpara, vecfile, veclfile ? veclfile : ""));
     else if (model == 'A' && axialdir == 5)
       bs.reset(new DumpMat::XAM2DDumpConfig(mpara, vecfile, extend_cond));
+    else if (model == 'A' && axialdir == 6)
+      bs.reset(new DumpMat::YAM2DDumpConfig(mpara, vecfile, veclfile ? veclfile : "", extend_cond));
+    else if (model == 'B' && axialdir == 6)
+      bs.reset(new DumpMat::YBM2DDumpConfig(mpara, vecfile, veclfile ? veclfile : "", extend_cond));
     else if (model == 'D' && axialdir == 5)
       bs.reset(new DumpMat::XDM2DDumpConfig(mpara, vecfile, extend_cond));
     else

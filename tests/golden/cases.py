@@ -116,7 +116,11 @@ DUMP_CASES = [
     ("dump_xdm_L14_flip", "D", 5, 0, 0.35, 0.6, 0.0, 0.0, 14, 3, 36, 8),
     ("dump_yat_L6", "A", 2, 0, 0.4, 0.3, 0.0, 0.0, 6, 4, 40, 17),
     ("dump_yat_L8_h", "A", 2, 0, 0.6, 0.5, 0.0, 0.05, 8, 3, 32, 321),
+    ("dump_yam_L8", "A", 6, 2, 0.5, 0.4, 0.0, 0.0, 8, 4, 40, 55),
+    ("dump_yam_L9_flip", "A", 6, 0, 0.4, 0.6, 0.0, 0.0, 9, 3, 32, 6),
+    ("dump_ybm_L8_flip", "B", 6, 0, 0.45, 0.3, 0.2, 0.0, 8, 3, 32, 1234),
 ]
+TWO_LAYER_DUMP = (("A", 2), ("A", 6), ("B", 6))   # planted from right and left eigenvectors
 
 FULL_VECTOR_MAX = 70000   # store full matvec outputs up to this length, else checksums and samples
 SAMPLE_COUNT = 4096

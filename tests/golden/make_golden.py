@@ -185,7 +185,7 @@ def gen_dump(c):
         q = q / np.linalg.norm(q)
         return q * np.sign(q.sum())
 
-    two_layer = (model, ax) == ("A", 2)  # YAT2DDumpConfig: right and left vectors
+    two_layer = (model, ax) in (("A", 2), ("A", 6), ("B", 6))  # GenDumpConfig: right and left vectors
     q = leading(op.perform_op, not two_layer)
     ql = leading(op.perform_op_t, False) if two_layer else None
     with tempfile.TemporaryDirectory() as td:

@@ -76,11 +76,11 @@ def test_published_probe_values():
 def test_dump_fixtures_are_well_formed():
     """The planted-configuration fixtures (made by the reference's own dump())
     hold one unit eigenvector of the operator's size (two, right and left,
-    for the two-layer parallel TM) and nconfig x length layer states of L
-    bits each (length + 1 for the two-layer TM, whose dumper writes the first
-    layer, the partner layer of every step and the last layer).  The
+    for the two-layer parallel TMs) and nconfig x length layer states of L
+    bits each (length + 1 for the full two-layer TM, whose dumper writes the
+    first layer, the partner layer of every step and the last layer).  The
     eigenvectors are checked against the oracle's operator: T q = lambda q."""
-    from cases import DUMP_CASES
+    from cases import DUMP_CASES, TWO_LAYER_DUMP
 
     for name, model, ax, ec, bj, k, k2, h, size, nconf, length, seed in DUMP_CASES:
         f = fixture(name)
@@ -91,11 +91,11 @@ def test_dump_fixtures_are_well_formed():
         tq = o.perform_op(q)
         lam = float(q @ tq)
         assert np.linalg.norm(tq - lam * q) < 1e-8 * abs(lam)
-        two_layer = (model, ax) == ("A", 2)
+        two_layer = (model, ax) in TWO_LAYER_DUMP
         if two_layer:
             ql = f["vecl"]
             assert ql.shape == (o.n,) and abs(np.linalg.norm(ql) - 1.0) < 1e-12
             tl = o.perform_op_t(ql)
             assert np.linalg.norm(tl - float(ql @ tl) * ql) < 1e-8 * abs(lam)
-        assert f["configs"].shape == (nconf, length + 1 if two_layer else length)
+        assert f["configs"].shape == (nconf, length + 1 if (model, ax) == ("A", 2) else length)
         assert int(f["configs"].max()) < (1 << size)
