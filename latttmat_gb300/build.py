@@ -1,4 +1,4 @@
-"""Build liblatttmat_gb300.so (CUDA, sm_103a) and the tmat CLI in-tree.
+"""Build liblatttmat_gb300.so (CUDA, sm_103a) and the tmat and dumpconfig CLIs in-tree.
 
 nvcc compiles each translation unit in parallel with
 ``-gencode arch=compute_103a,code=sm_103a``; objects go to
@@ -19,6 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblatttmat_gb300.so")
 CLI = os.path.join(HERE, "tmat")
+DUMP_CLI = os.path.join(HERE, "dumpconfig")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -78,12 +79,14 @@ def build(verbose: bool = False, extra_flags=None) -> str:
                     print(o)
     if jobs or _stale(LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcuda"])
-    cli_src = os.path.join(HERE, "host", "tmat_main.cpp")
-    if os.path.exists(cli_src):
-        host_deps = [cli_src, LIB] + [os.path.join(HERE, "host", f) for f in os.listdir(os.path.join(HERE, "host"))]
-        if _stale(CLI, host_deps):
-            _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(HERE, "host"),
-                  cli_src, "-o", CLI, "-L", HERE, "-llatttmat_gb300", "-Wl,-rpath,$ORIGIN"])
+    host_dir = os.path.join(HERE, "host")
+    if os.path.isdir(host_dir):
+        host_hdrs = [os.path.join(host_dir, f) for f in os.listdir(host_dir) if f.endswith(".hpp")]
+        for exe, main in ((CLI, "tmat_main.cpp"), (DUMP_CLI, "dumpconfig_main.cpp")):
+            src = os.path.join(host_dir, main)
+            if os.path.exists(src) and _stale(exe, [src, LIB] + host_hdrs):
+                _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", host_dir,
+                      src, "-o", exe, "-L", HERE, "-llatttmat_gb300", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
