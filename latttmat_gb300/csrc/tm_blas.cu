@@ -1,8 +1,10 @@
 // Krylov-solver vector kernels (FP64 Gram-Schmidt, norms, basis rotation) and
 // the small dense symmetric eigensolver, all on the device.
 #include <cmath>
+#include <mutex>
 
 #include "tm_blas.cuh"
+#include "tm_stage.cuh"
 
 namespace ltm {
 
@@ -753,6 +755,138 @@ __global__ void __launch_bounds__(BT) axpy_dot_f32v_kernel(const float* __restri
   block_reduce_store<NVT>(acc, nv, part);
 }
 
+// ---- staged forms (columns streamed through shared memory by bulk copies)
+// A chunk is kChunk floats of every column: 256 threads x one float4.  The
+// chunks cover the first 4 * (n / 4) elements; block 0 takes the n % 4 tail
+// with plain loads after the sweep.
+constexpr int kChunk = 4 * BT;
+
+// wout = win - V h ; part <- V . wout, for wide bases (9..16 columns): the
+// update reads V and win from the stage, the dots read V again from there
+template <int NVT>
+__global__ void __launch_bounds__(BT, 1) axpy_dot_f32_staged(const float* __restrict__ V, int64_t ldv, int nv,
+                                                             const double* __restrict__ h,
+                                                             const float* __restrict__ win,
+                                                             float* __restrict__ wout, int64_t n,
+                                                             double* __restrict__ part, int nstage, int* err) {
+  extern __shared__ __align__(128) float stg[];
+  __shared__ __align__(8) uint64_t full[kStageMax];
+  __shared__ float hs[NVT];
+  if (threadIdx.x < NVT) hs[threadIdx.x] = (threadIdx.x < nv) ? (float)h[threadIdx.x] : 0.f;
+  float acc[NVT];
+#pragma unroll
+  for (int k = 0; k < NVT; ++k) acc[k] = 0.f;
+  const int ncol = nv + 1;  // V columns, then win
+  const int64_t nf = (n >> 2) << 2;
+  const int64_t nch = (nf + kChunk - 1) / kChunk;
+  staged_sweep(
+      full, nstage, nch, err,
+      [&](int64_t c, int st, uint64_t* bar) {
+        const int64_t e0 = c * kChunk;
+        const uint32_t bytes = (uint32_t)(min((int64_t)kChunk, nf - e0) * 4);
+        mbar_arrive_expect_tx(bar, bytes * ncol);
+        float* d = stg + (int64_t)st * ncol * kChunk;
+        for (int k = 0; k < nv; ++k) bulk_g2s(d + k * kChunk, V + (int64_t)k * ldv + e0, bytes, bar);
+        bulk_g2s(d + nv * kChunk, win + e0, bytes, bar);
+      },
+      [&](int64_t c, int st) {
+        const int64_t e0 = c * kChunk;
+        const int t4 = threadIdx.x * 4;
+        if (e0 + t4 >= nf) return;
+        const float* d = stg + (int64_t)st * ncol * kChunk + t4;
+        float4 x = *reinterpret_cast<const float4*>(d + nv * kChunk);
+#pragma unroll
+        for (int k = 0; k < NVT; ++k)
+          if (k < nv) sub4(x, *reinterpret_cast<const float4*>(d + k * kChunk), hs[k]);
+        __stcs(reinterpret_cast<float4*>(wout + e0 + t4), x);
+#pragma unroll
+        for (int k = 0; k < NVT; ++k)
+          if (k < nv) acc[k] = dot4(*reinterpret_cast<const float4*>(d + k * kChunk), x, acc[k]);
+      });
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = nf + threadIdx.x;
+    float x = win[t];
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) x = fmaf(-V[(int64_t)k * ldv + t], hs[k], x);
+    wout[t] = x;
+#pragma unroll
+    for (int k = 0; k < NVT; ++k)
+      if (k < nv) acc[k] = fmaf(V[(int64_t)k * ldv + t], x, acc[k]);
+  }
+  block_reduce_store<NVT>(acc, nv, part);
+}
+
+// part[b][k*NW + j] = partial sums of V[k] . W[j] (kv <= KV, nw <= NW), the
+// kv + nw columns staged together
+template <int KV, int NW>
+__global__ void __launch_bounds__(BT, 1) mdot_block_f32_staged(const float* __restrict__ V, int64_t ldv, int kv,
+                                                               F32Cols W, int nw, int64_t n,
+                                                               double* __restrict__ part, int nstage, int* err) {
+  extern __shared__ __align__(128) float stg[];
+  __shared__ __align__(8) uint64_t full[kStageMax];
+  float acc[KV][NW];
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) acc[k][j] = 0.f;
+  const int ncol = kv + nw;  // V columns, then W columns
+  const int64_t nf = (n >> 2) << 2;
+  const int64_t nch = (nf + kChunk - 1) / kChunk;
+  staged_sweep(
+      full, nstage, nch, err,
+      [&](int64_t c, int st, uint64_t* bar) {
+        const int64_t e0 = c * kChunk;
+        const uint32_t bytes = (uint32_t)(min((int64_t)kChunk, nf - e0) * 4);
+        mbar_arrive_expect_tx(bar, bytes * ncol);
+        float* d = stg + (int64_t)st * ncol * kChunk;
+        for (int k = 0; k < kv; ++k) bulk_g2s(d + k * kChunk, V + (int64_t)k * ldv + e0, bytes, bar);
+        for (int j = 0; j < nw; ++j) bulk_g2s(d + (kv + j) * kChunk, W.c[j] + e0, bytes, bar);
+      },
+      [&](int64_t c, int st) {
+        const int t4 = threadIdx.x * 4;
+        if (c * kChunk + t4 >= nf) return;
+        const float* d = stg + (int64_t)st * ncol * kChunk + t4;
+        float4 wv[NW];
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+          wv[j] = (j < nw) ? *reinterpret_cast<const float4*>(d + (kv + j) * kChunk) : make_float4(0, 0, 0, 0);
+#pragma unroll
+        for (int k = 0; k < KV; ++k)
+          if (k < kv) {
+            const float4 v = *reinterpret_cast<const float4*>(d + k * kChunk);
+#pragma unroll
+            for (int j = 0; j < NW; ++j) acc[k][j] = dot4(v, wv[j], acc[k][j]);
+          }
+      });
+  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
+    const int64_t t = nf + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+      if (k < kv) {
+        const float v = V[(int64_t)k * ldv + t];
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+          if (j < nw) acc[k][j] = fmaf(v, W.c[j][t], acc[k][j]);
+      }
+  }
+  __shared__ double sh[BT / 32][KV * NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      double v = warp_sum((double)acc[k][j]);
+      if (lane == 0) sh[wid][k * NW + j] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < KV * NW; t += BT) {
+    double a = 0.0;
+    for (int q = 0; q < BT / 32; ++q) a += sh[q][t];
+    part[(int64_t)blockIdx.x * (KV * NW) + t] = a;
+  }
+}
+
 // w -= V h in place; with NRM, part <- ||w||^2
 template <int NVT, int U, bool NRM>
 __global__ void __launch_bounds__(BT) axpy_f32v_kernel(const float* __restrict__ V, int64_t ldv, int nv,
@@ -801,58 +935,6 @@ __global__ void __launch_bounds__(BT) axpy_f32v_kernel(const float* __restrict__
     if (NRM) acc[0] = fmaf(x, x, acc[0]);
   }
   if (NRM) block_reduce_store<1>(acc, 1, part);
-}
-
-// part[b][k*NW + j] = partial sums of V[k] . W[j]
-template <int KV, int NW>
-__global__ void __launch_bounds__(BT) mdot_block_f32v_kernel(const float* __restrict__ V, int64_t ldv, int kv,
-                                                             F32Cols W, int nw, int64_t n,
-                                                             double* __restrict__ part) {
-  float acc[KV][NW];
-#pragma unroll
-  for (int k = 0; k < KV; ++k)
-#pragma unroll
-    for (int j = 0; j < NW; ++j) acc[k][j] = 0.f;
-  const int64_t n4 = n >> 2;
-  const int64_t st = (int64_t)gridDim.x * BT;
-  for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n4; i += st) {
-    float4 wv[NW];
-#pragma unroll
-    for (int j = 0; j < NW; ++j) wv[j] = (j < nw) ? reinterpret_cast<const float4*>(W.c[j])[i] : make_float4(0, 0, 0, 0);
-#pragma unroll
-    for (int k = 0; k < KV; ++k)
-      if (k < kv) {
-        const float4 v = col4(V, ldv, k)[i];
-#pragma unroll
-        for (int j = 0; j < NW; ++j) acc[k][j] = dot4(v, wv[j], acc[k][j]);
-      }
-  }
-  if (blockIdx.x == 0 && threadIdx.x < (int)(n & 3)) {
-    const int64_t t = (n4 << 2) + threadIdx.x;
-#pragma unroll
-    for (int k = 0; k < KV; ++k)
-      if (k < kv) {
-        const float v = V[(int64_t)k * ldv + t];
-#pragma unroll
-        for (int j = 0; j < NW; ++j)
-          if (j < nw) acc[k][j] = fmaf(v, W.c[j][t], acc[k][j]);
-      }
-  }
-  __shared__ double sh[BT / 32][KV * NW];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < KV; ++k)
-#pragma unroll
-    for (int j = 0; j < NW; ++j) {
-      double v = warp_sum((double)acc[k][j]);
-      if (lane == 0) sh[wid][k * NW + j] = v;
-    }
-  __syncthreads();
-  for (int t = threadIdx.x; t < KV * NW; t += BT) {
-    double a = 0.0;
-    for (int q = 0; q < BT / 32; ++q) a += sh[q][t];
-    part[(int64_t)blockIdx.x * (KV * NW) + t] = a;
-  }
 }
 
 // W[j] -= sum_k V[k] H[k0 + k, j]
@@ -1246,6 +1328,49 @@ inline bool cols2(const double* V, int64_t ldv) { return al16(V) && (ldv & 1) ==
 
 }  // namespace
 
+int* stage_err_word() {
+  static std::mutex mu;
+  static int* words[64] = {};
+  int dev = 0;
+  TM_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) fail(TM_ERR_CUDA, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!words[dev]) {
+    int* p = nullptr;
+    TM_CK(cudaMalloc(&p, sizeof(int)));
+    TM_CK(cudaMemset(p, 0, sizeof(int)));
+    words[dev] = p;
+  }
+  return words[dev];
+}
+
+void stage_err_check(cudaStream_t s) {
+  int* w = stage_err_word();
+  int h = 0;
+  TM_CK(cudaMemcpyAsync(&h, w, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TM_CK(cudaStreamSynchronize(s));
+  if (h) {
+    TM_CK(cudaMemsetAsync(w, 0, sizeof(int), s));
+    fail(TM_ERR_CUDA, "a shared-memory stage of a Krylov sweep was not filled in time");
+  }
+}
+
+int stage_count(int64_t chunk_bytes) {
+  return (int)std::max<int64_t>(2, std::min<int64_t>(kStageMax, kStageBytes / chunk_bytes));
+}
+
+namespace {
+// Grid of a staged launch: as many CTAs per SM as the stages' shared memory
+// lets reside (at most kRedBlocksPerSM, the partial-sum buffers' bound).
+template <class K>
+int staged_grid(K kernel, size_t shm) {
+  raise_smem_limit((const void*)kernel, shm);
+  int occ = 0;
+  TM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, BT, shm));
+  return num_sms() * std::max(1, std::min(occ, kRedBlocksPerSM));
+}
+}  // namespace
+
 void mdot_f32(const float* V, int64_t ldv, int nv, const float* w, int64_t n, double* h, double* part,
               cudaStream_t s) {
   const bool vec = cols4(V, ldv) && al16(w);
@@ -1294,18 +1419,23 @@ void mdot_block_f32(const float* V, int64_t ldv, int nv, const F32Cols& W, int n
   for (int k0 = 0; k0 < nv; k0 += KV) {
     const int kv = std::min(KV, nv - k0);
     const float* Vk = V + (int64_t)k0 * ldv;
-    if (nw <= 4) {  // half the accumulators when the block is narrow
-      if (vec)
-        mdot_block_f32v_kernel<KV, 4><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
-      else
-        mdot_block_f32_kernel<KV, 4><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
+    if (vec) {
+      // the kv + nw columns staged together (the accumulators halve when the
+      // block is narrow)
+      const int nst = stage_count((int64_t)(kv + nw) * kChunk * 4);
+      const size_t shm = (size_t)nst * (kv + nw) * kChunk * 4;
+      const int nws = (nw <= 4) ? 4 : kMaxBlockW;
+      auto kfn = (nw <= 4) ? mdot_block_f32_staged<KV, 4> : mdot_block_f32_staged<KV, kMaxBlockW>;
+      const int gs = staged_grid(kfn, shm);
+      kfn<<<gs, BT, shm, s>>>(Vk, ldv, kv, W, nw, n, part, nst, stage_err_word());
+      TM_CKK("mdot_block_f32");
+      mdot_block_final<<<kv * nw, 256, 0, s>>>(part, gs, kv, nw, KV * nws, nws, H, ldh, k0);
+    } else if (nw <= 4) {  // half the accumulators when the block is narrow
+      mdot_block_f32_kernel<KV, 4><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
       TM_CKK("mdot_block_f32");
       mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * 4, 4, H, ldh, k0);
     } else {
-      if (vec)
-        mdot_block_f32v_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
-      else
-        mdot_block_f32_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
+      mdot_block_f32_kernel<KV, kMaxBlockW><<<nb, BT, 0, s>>>(Vk, ldv, kv, W, nw, n, part);
       TM_CKK("mdot_block_f32");
       mdot_block_final<<<kv * nw, 256, 0, s>>>(part, nb, kv, nw, KV * kMaxBlockW, kMaxBlockW, H, ldh, k0);
     }
@@ -1381,7 +1511,7 @@ void maxpy_f32(const float* V, int64_t ldv, int nv, const double* h, float* w, i
 void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const float* win, float* wout, int64_t n,
                   double* h2, double* part, cudaStream_t s) {
   if (nv > NV32) fail(TM_ERR_LIMIT, "axpy_dot_f32: too many vectors");
-  const int nb = red_blocks(n);
+  int nb = red_blocks(n);
   int stride = NV32;
   if (!(cols4(V, ldv) && al16(win) && al16(wout))) {
     axpy_dot_f32_kernel<<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
@@ -1391,11 +1521,15 @@ void axpy_dot_f32(const float* V, int64_t ldv, int nv, const double* h, const fl
   } else if (nv <= 8) {
     axpy_dot_f32v_kernel<8><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
     stride = 8;
-  } else if (nv <= 12) {
-    axpy_dot_f32v_kernel<12><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
-    stride = 12;
   } else {
-    axpy_dot_f32v_kernel<16><<<nb, BT, 0, s>>>(V, ldv, nv, h, win, wout, n, part);
+    // wide bases: staged, so the sweep is not limited by the registers that
+    // hold one vector of every column
+    const int nst = stage_count((int64_t)(nv + 1) * kChunk * 4);
+    const size_t shm = (size_t)nst * (nv + 1) * kChunk * 4;
+    auto kfn = axpy_dot_f32_staged<NV32>;
+    const int gs = staged_grid(kfn, shm);
+    kfn<<<gs, BT, shm, s>>>(V, ldv, nv, h, win, wout, n, part, nst, stage_err_word());
+    nb = gs;
   }
   TM_CKK("axpy_dot_f32");
   mdot_final<<<nv, 256, 0, s>>>(part, nb, nv, stride, h2);

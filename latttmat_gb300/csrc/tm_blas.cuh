@@ -5,6 +5,7 @@
 #pragma once
 #include "tm_df.cuh"
 #include "tm_internal.h"
+#include "tm_stage.cuh"
 
 namespace ltm {
 

@@ -1337,6 +1337,7 @@ tm_status lanczos_solve(const Op& op, int nev, int ncv, double tol, uint64_t see
   }
   info.nconv = done ? nev : 0;
   info.max_resid = max_resid;
+  stage_err_check(s);  // the staged Krylov sweeps' bounded waits all completed
   for (int i = 0; i < nev && i < (int)theta.size(); ++i) vals[i] = theta[i];
   if (vecs_host && Lz) {
     // eigenvectors in the reference's order.  Host memory the device can
