@@ -389,23 +389,68 @@ __global__ void block_final_df_kernel(const double* __restrict__ part, int nb, i
   }
 }
 
+// Conversions, two elements (16 bytes of double-float or FP64) per access and
+// four accesses per thread in flight; the odd tail element goes to block 0.
+// Every column starts on a 16-byte boundary.
+constexpr int kConvU = 4;
+
 __global__ void df_to_f32_kernel(const dfloat* __restrict__ x, float* __restrict__ out, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const dfloat v = x[i];
-    out[i] = v.hi + v.lo;
+  const int64_t n2 = n >> 1, st = (int64_t)gridDim.x * blockDim.x;
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  float2* o2 = reinterpret_cast<float2*>(out);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (kConvU - 1) * st < n2; i += kConvU * st) {
+    float4 v[kConvU];
+#pragma unroll
+    for (int u = 0; u < kConvU; ++u) v[u] = __ldcs(x4 + i + u * st);
+#pragma unroll
+    for (int u = 0; u < kConvU; ++u) o2[i + u * st] = make_float2(v[u].x + v[u].y, v[u].z + v[u].w);
   }
+  for (; i < n2; i += st) {
+    const float4 v = __ldcs(x4 + i);
+    o2[i] = make_float2(v.x + v.y, v.z + v.w);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) out[n - 1] = x[n - 1].hi + x[n - 1].lo;
 }
 
 __global__ void df_to_f64_kernel(const dfloat* __restrict__ x, double scale, double* __restrict__ out, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const dfloat v = x[i];
-    out[i] = ((double)v.hi + (double)v.lo) * scale;
+  const int64_t n2 = n >> 1, st = (int64_t)gridDim.x * blockDim.x;
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  double2* o2 = reinterpret_cast<double2*>(out);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  auto cv = [&](const float4& v) {
+    return make_double2(((double)v.x + (double)v.y) * scale, ((double)v.z + (double)v.w) * scale);
+  };
+  for (; i + (kConvU - 1) * st < n2; i += kConvU * st) {
+    float4 v[kConvU];
+#pragma unroll
+    for (int u = 0; u < kConvU; ++u) v[u] = __ldcs(x4 + i + u * st);
+#pragma unroll
+    for (int u = 0; u < kConvU; ++u) o2[i + u * st] = cv(v[u]);
   }
+  for (; i < n2; i += st) o2[i] = cv(__ldcs(x4 + i));
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+    out[n - 1] = ((double)x[n - 1].hi + (double)x[n - 1].lo) * scale;
 }
 
 __global__ void f64_to_df_kernel(const double* __restrict__ x, double scale, dfloat* __restrict__ out, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = dfloat(x[i] * scale);
+  const int64_t n2 = n >> 1, st = (int64_t)gridDim.x * blockDim.x;
+  const double2* x2 = reinterpret_cast<const double2*>(x);
+  float4* o4 = reinterpret_cast<float4*>(out);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  auto cv = [&](const double2& v) {
+    const dfloat a(v.x * scale), b(v.y * scale);
+    return make_float4(a.hi, a.lo, b.hi, b.lo);
+  };
+  for (; i + (kConvU - 1) * st < n2; i += kConvU * st) {
+    double2 v[kConvU];
+#pragma unroll
+    for (int u = 0; u < kConvU; ++u) v[u] = __ldcs(x2 + i + u * st);
+#pragma unroll
+    for (int u = 0; u < kConvU; ++u) o4[i + u * st] = cv(v[u]);
+  }
+  for (; i < n2; i += st) o4[i] = cv(__ldcs(x2 + i));
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) out[n - 1] = dfloat(x[n - 1] * scale);
 }
 
 }  // namespace

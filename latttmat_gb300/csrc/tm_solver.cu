@@ -567,25 +567,17 @@ constexpr int kMaxRefineNev = 8;
 // the X0 part in double-float, the B32 part in FP32 (its weights are at the
 // FP32 noise level).  Writes r / S as FP32 into R32 (column c), x into Xo
 // (double-float), and the block partial sums of ||r/S||^2 (FP32 per thread)
-// into part[block * NVW + c].
-//
-// The columns are staged through shared memory (tm_stage.cuh): one thread
-// posts a chunk of ce elements of every column (X0 and AX0 double-float, then
-// B32 and AB32 FP32) as bulk copies; each thread then forms one element of
-// every wanted Ritz vector and residual.  Chunks cover the first 4 * (n / 4)
-// elements; block 0 takes the rest.
+// into part[block * NVW + c].  All column blocks have an even leading
+// dimension ld and 16-byte aligned columns; a thread takes two elements.
 template <int NVW>
-__global__ void __launch_bounds__(256, 1) ritz_resid_staged(const dfloat* __restrict__ X0,
-                                                            const dfloat* __restrict__ AX0, int nx,
-                                                            const float* __restrict__ B32,
-                                                            const float* __restrict__ AB32, int nb,
-                                                            const double* __restrict__ Y, int nv,
-                                                            const double* __restrict__ theta_s,
-                                                            float* __restrict__ R32, dfloat* __restrict__ Xo,
-                                                            int64_t n, int64_t ld, double* __restrict__ part,
-                                                            int ce, int nstage, int* err) {
-  extern __shared__ __align__(128) unsigned char stg_raw[];
-  __shared__ __align__(8) uint64_t full[kStageMax];
+__global__ void __launch_bounds__(256) ritz_resid_kernel(const dfloat* __restrict__ X0,
+                                                         const dfloat* __restrict__ AX0, int nx,
+                                                         const float* __restrict__ B32,
+                                                         const float* __restrict__ AB32, int nb,
+                                                         const double* __restrict__ Y, int nv,
+                                                         const double* __restrict__ theta_s,
+                                                         float* __restrict__ R32, dfloat* __restrict__ Xo,
+                                                         int64_t n, int64_t ld, double* __restrict__ part) {
   __shared__ dfloat Yd[48 * NVW];
   __shared__ float Yf[48 * NVW];
   __shared__ dfloat th[NVW];
@@ -594,83 +586,87 @@ __global__ void __launch_bounds__(256, 1) ritz_resid_staged(const dfloat* __rest
     Yf[t] = (float)Y[t];
   }
   if (threadIdx.x < nv) th[threadIdx.x] = dfloat(-theta_s[threadIdx.x]);
+  __syncthreads();
   float acc[NVW];
 #pragma unroll
   for (int c = 0; c < NVW; ++c) acc[c] = 0.f;
-  const int nc = nb - nx;
-  // stage layout: X0 (nx x ce dfloat), AX0 (nx x ce), B32 (nc x ce float), AB32 (nc x ce)
-  const int64_t stage_bytes = (int64_t)ce * (16 * nx + 8 * nc);
-  const int64_t nf = (n >> 2) << 2;
-  const int64_t nch = (nf + ce - 1) / ce;
-  auto one = [&](int64_t i, const dfloat* xs0, const dfloat* as0, const float* bs, const float* abs_, int64_t sd,
-                 int64_t sf) {
-    dfloat x[NVW], a[NVW];
-    float xf[NVW], af[NVW];
+  auto ld2 = [](const dfloat* p, int64_t i, dfloat& a, dfloat& b) {
+    const float4 v = reinterpret_cast<const float4*>(p)[i];
+    a = dfloat(v.x, v.y);
+    b = dfloat(v.z, v.w);
+  };
+  const int64_t n2 = n >> 1;
+  const int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += st) {
+    dfloat x0[NVW], x1[NVW], a0[NVW], a1[NVW];
+    float2 xs[NVW], axs[NVW];
 #pragma unroll
     for (int c = 0; c < NVW; ++c) {
-      x[c] = a[c] = dfloat(0.f, 0.f);
-      xf[c] = af[c] = 0.f;
+      x0[c] = x1[c] = a0[c] = a1[c] = dfloat(0.f, 0.f);
+      xs[c] = axs[c] = make_float2(0.f, 0.f);
     }
+    // unrolled so that several columns' loads are in flight per thread
+#pragma unroll 4
     for (int j = 0; j < nx; ++j) {
-      const dfloat xa = xs0[j * sd], aa = as0[j * sd];
+      dfloat xa, xb, aa, ab;
+      ld2(X0 + (int64_t)j * ld, i, xa, xb);
+      ld2(AX0 + (int64_t)j * ld, i, aa, ab);
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
           const dfloat y = Yd[c * nb + j];
-          x[c] = df_fma(xa, y, x[c]);
-          a[c] = df_fma(aa, y, a[c]);
+          x0[c] = df_fma(xa, y, x0[c]);
+          x1[c] = df_fma(xb, y, x1[c]);
+          a0[c] = df_fma(aa, y, a0[c]);
+          a1[c] = df_fma(ab, y, a1[c]);
         }
     }
 #pragma unroll 4
-    for (int j = 0; j < nc; ++j) {
-      const float bv = bs[j * sf], abv = abs_[j * sf];
+    for (int j = nx; j < nb; ++j) {
+      const float2 bv = reinterpret_cast<const float2*>(B32 + (int64_t)j * ld)[i];
+      const float2 abv = reinterpret_cast<const float2*>(AB32 + (int64_t)j * ld)[i];
 #pragma unroll
       for (int c = 0; c < NVW; ++c)
         if (c < nv) {
-          const float y = Yf[c * nb + nx + j];
-          xf[c] = fmaf(bv, y, xf[c]);
-          af[c] = fmaf(abv, y, af[c]);
+          const float y = Yf[c * nb + j];
+          xs[c].x = fmaf(bv.x, y, xs[c].x);
+          xs[c].y = fmaf(bv.y, y, xs[c].y);
+          axs[c].x = fmaf(abv.x, y, axs[c].x);
+          axs[c].y = fmaf(abv.y, y, axs[c].y);
         }
     }
 #pragma unroll
     for (int c = 0; c < NVW; ++c)
       if (c < nv) {
-        const dfloat xx = x[c] + dfloat(xf[c], 0.f);
-        const dfloat r = df_fma(th[c], xx, a[c] + dfloat(af[c], 0.f));
-        const float f = r.hi + r.lo;
-        __stcs(R32 + (int64_t)c * ld + i, f);
-        __stcs(reinterpret_cast<float2*>(Xo + (int64_t)c * ld + i), make_float2(xx.hi, xx.lo));
-        acc[c] = fmaf(f, f, acc[c]);
+        const dfloat xx0 = x0[c] + dfloat(xs[c].x, 0.f), xx1 = x1[c] + dfloat(xs[c].y, 0.f);
+        const dfloat r0 = df_fma(th[c], xx0, a0[c] + dfloat(axs[c].x, 0.f));
+        const dfloat r1 = df_fma(th[c], xx1, a1[c] + dfloat(axs[c].y, 0.f));
+        const float f0 = r0.hi + r0.lo, f1 = r1.hi + r1.lo;
+        reinterpret_cast<float2*>(R32 + (int64_t)c * ld)[i] = make_float2(f0, f1);
+        reinterpret_cast<float4*>(Xo + (int64_t)c * ld)[i] = make_float4(xx0.hi, xx0.lo, xx1.hi, xx1.lo);
+        acc[c] = fmaf(f0, f0, fmaf(f1, f1, acc[c]));
       }
-  };
-  staged_sweep(
-      full, nstage, nch, err,
-      [&](int64_t c, int st, uint64_t* bar) {
-        const int64_t e0 = c * ce;
-        const int cnt = (int)min((int64_t)ce, nf - e0);
-        mbar_arrive_expect_tx(bar, (uint32_t)((int64_t)cnt * (16 * nx + 8 * nc)));
-        unsigned char* d = stg_raw + (int64_t)st * stage_bytes;
-        dfloat* dx = reinterpret_cast<dfloat*>(d);
-        for (int j = 0; j < nx; ++j) {
-          bulk_g2s(dx + (int64_t)j * ce, X0 + (int64_t)j * ld + e0, (uint32_t)cnt * 8, bar);
-          bulk_g2s(dx + (int64_t)(nx + j) * ce, AX0 + (int64_t)j * ld + e0, (uint32_t)cnt * 8, bar);
-        }
-        float* df = reinterpret_cast<float*>(dx + (int64_t)2 * nx * ce);
-        for (int j = 0; j < nc; ++j) {
-          bulk_g2s(df + (int64_t)j * ce, B32 + (int64_t)(nx + j) * ld + e0, (uint32_t)cnt * 4, bar);
-          bulk_g2s(df + (int64_t)(nc + j) * ce, AB32 + (int64_t)(nx + j) * ld + e0, (uint32_t)cnt * 4, bar);
-        }
-      },
-      [&](int64_t c, int st) {
-        const int t = threadIdx.x;
-        if (t >= ce || c * ce + t >= nf) return;
-        const dfloat* dx = reinterpret_cast<const dfloat*>(stg_raw + (int64_t)st * stage_bytes);
-        const float* df = reinterpret_cast<const float*>(dx + (int64_t)2 * nx * ce);
-        one(c * ce + t, dx + t, dx + (int64_t)nx * ce + t, df + t, df + (int64_t)nc * ce + t, ce, ce);
-      });
-  if (blockIdx.x == 0 && threadIdx.x < (int)(n - nf)) {
-    const int64_t i = nf + threadIdx.x;
-    one(i, X0 + i, AX0 + i, B32 + (int64_t)nx * ld + i, AB32 + (int64_t)nx * ld + i, ld, ld);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int64_t i = n - 1;
+    for (int c = 0; c < nv; ++c) {
+      dfloat x(0.f, 0.f), ax(0.f, 0.f);
+      float xs = 0.f, axs = 0.f;
+      for (int j = 0; j < nx; ++j) {
+        x = df_fma(X0[(int64_t)j * ld + i], Yd[c * nb + j], x);
+        ax = df_fma(AX0[(int64_t)j * ld + i], Yd[c * nb + j], ax);
+      }
+      for (int j = nx; j < nb; ++j) {
+        xs = fmaf(B32[(int64_t)j * ld + i], Yf[c * nb + j], xs);
+        axs = fmaf(AB32[(int64_t)j * ld + i], Yf[c * nb + j], axs);
+      }
+      const dfloat xx = x + dfloat(xs, 0.f);
+      const dfloat r = df_fma(th[c], xx, ax + dfloat(axs, 0.f));
+      const float f = r.hi + r.lo;
+      R32[(int64_t)c * ld + i] = f;
+      Xo[(int64_t)c * ld + i] = xx;
+      acc[c] = fmaf(f, f, acc[c]);
+    }
   }
   __shared__ double sh[8][NVW];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -776,7 +772,7 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
   Wd.alloc((size_t)ld * 8);
   Yd.alloc((size_t)48 * kMaxRefineNev * 8);
   thd.alloc(kMaxRefineNev * 8);
-  part.alloc((size_t)std::max(gblocks, num_sms()) * kMaxRefineNev * 8);  // ritz_resid_staged: one CTA per SM
+  part.alloc((size_t)gblocks * kMaxRefineNev * 8);
   auto f32col = [&](const DBuf& b, int j) { return b.as<float>() + (int64_t)j * ld; };
   auto x0 = [&](int j) { return XA.as<dfloat>() + (int64_t)j * ld; };          // X0 column j
   auto ax0 = [&](int j) { return XA.as<dfloat>() + (int64_t)(nev + j) * ld; };  // A X0 / S column j
@@ -940,25 +936,17 @@ bool refine_mixed(const Op& op, Lanczos& lz, int nev, int nx, double tol, std::v
     TM_CK(cudaMemcpyAsync(Yd.p, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, s));
     TM_CK(cudaMemcpyAsync(thd.p, ths.data(), nev * 8, cudaMemcpyHostToDevice, s));
     // wanted Ritz vectors (double-float) and residuals (FP32 copy and norms)
-    // (staged: every column's chunk arrives by bulk copy, 3-4 stages in flight)
-    auto ritz_kernel = (nev <= 4) ? ritz_resid_staged<4> : ritz_resid_staged<kMaxRefineNev>;
+    auto ritz_kernel = (nev <= 4) ? ritz_resid_kernel<4> : ritz_resid_kernel<kMaxRefineNev>;
     const int pstride = (nev <= 4) ? 4 : kMaxRefineNev;  // the kernel's per-block stride
-    int ce = 256;
-    if (2 * (int64_t)ce * (16 * nev + 8 * (nb - nev)) > kStageBytes) ce = 128;
-    const int64_t sbytes = (int64_t)ce * (16 * nev + 8 * (nb - nev));
-    const int nst = stage_count(sbytes);
-    const size_t shm = (size_t)nst * sbytes;
-    raise_smem_limit((const void*)ritz_kernel, shm);
-    const int rblocks = num_sms();  // one CTA per SM: the stages fill its shared memory
-    ritz_kernel<<<rblocks, 256, shm, s>>>(x0(0), ax0(0), nev, B32.as<float>(), AB32.as<float>(), nb,
-                                          Yd.as<double>(), nev, thd.as<double>(), R32.as<float>(), Xo.as<dfloat>(),
-                                          n, ld, part.as<double>(), ce, nst, stage_err_word());
+    ritz_kernel<<<gblocks, 256, 0, s>>>(x0(0), ax0(0), nev, B32.as<float>(), AB32.as<float>(), nb, Yd.as<double>(),
+                                        nev, thd.as<double>(), R32.as<float>(), Xo.as<dfloat>(), n, ld,
+                                        part.as<double>());
     TM_CKK("ritz_resid");
-    std::vector<double> ph((size_t)rblocks * kMaxRefineNev), rn(nev, 0.0);
+    std::vector<double> ph((size_t)gblocks * kMaxRefineNev), rn(nev, 0.0);
     TM_CK(cudaMemcpyAsync(ph.data(), part.p, ph.size() * 8, cudaMemcpyDeviceToHost, s));
     host_sync();
     have_x = true;
-    for (int b = 0; b < rblocks; ++b)
+    for (int b = 0; b < gblocks; ++b)
       for (int c = 0; c < nev; ++c) rn[c] += ph[(size_t)b * pstride + c];
     // The estimate differs from the true residual of x only through the
     // FP32 products in the C block: |r - r_est| <= eps32 ||A|| ||y_c||, with
